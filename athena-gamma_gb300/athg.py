@@ -1,0 +1,283 @@
+"""ctypes binding of the C ABI in include/athena_gb300.h.
+
+`Sim` holds one device context: a uniform periodic mesh of MeshBlocks in the block pool,
+with helpers that move global interior arrays (reference AthenaArray layout, i fastest)
+in and out. There is no CPU fallback: if the CUDA library cannot be loaded, or no GPU is
+present, construction raises.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libathena_gb300.so")
+
+HLLE, HLLC, HLLD, LHLLC, LHLLD = 0, 1, 2, 3, 4
+SOLVERS = {"hlle": HLLE, "hllc": HLLC, "hlld": HLLD, "lhllc": LHLLC, "lhlld": LHLLD}
+INTEGRATORS = {"vl2": 0, "rk1": 1, "rk2": 2, "rk3": 3}
+PRECISIONS = {"fp64": 0, "mixed": 1}
+VAR_CONS, VAR_B1F, VAR_B2F, VAR_B3F, VAR_PRIM, VAR_BCC, VAR_PHI = range(7)
+# default density/pressure floors of the reference EOS: sqrt(1024*FLT_MIN)
+FLOOR = float(np.sqrt(1024 * np.finfo(np.float32).tiny))
+# 3-D CFL limits of the integrators (reference task_list/time_integrator.cpp:216-218 etc.)
+CFL_LIMIT = {"vl2": 0.5, "rk1": 1.0, "rk2": 1.0, "rk3": 1.0}
+
+# names the C ABI exports (checked by the CPU tests against include/athena_gb300.h)
+EXPORTS = [
+    "athg_create", "athg_destroy", "athg_set_blocks", "athg_set_uniform_mesh",
+    "athg_num_blocks", "athg_block_location", "athg_var_size", "athg_upload",
+    "athg_download", "athg_initialize", "athg_stage", "athg_end_cycle", "athg_cycles",
+    "athg_get_time", "athg_set_time", "athg_synchronize", "athg_stream",
+    "athg_launches_per_cycle", "athg_calculate_fluxes", "athg_compute_corner_e",
+    "athg_integrate", "athg_exchange_ghosts", "athg_conserved_to_primitive",
+    "athg_new_block_dt", "athg_max_div_b", "athg_sum_conserved", "athg_last_error",
+]
+
+
+class Config(C.Structure):
+    _fields_ = [("nx1", C.c_int), ("nx2", C.c_int), ("nx3", C.c_int), ("nghost", C.c_int),
+                ("magnetic", C.c_int), ("rsolver", C.c_int), ("xorder", C.c_int),
+                ("integrator", C.c_int), ("precision", C.c_int),
+                ("gamma", C.c_double), ("dfloor", C.c_double), ("pfloor", C.c_double),
+                ("cfl_number", C.c_double), ("tlim", C.c_double)]
+
+
+class Mesh(C.Structure):
+    _fields_ = [("nx1", C.c_int), ("nx2", C.c_int), ("nx3", C.c_int),
+                ("x1min", C.c_double), ("x1max", C.c_double), ("x2min", C.c_double),
+                ("x2max", C.c_double), ("x3min", C.c_double), ("x3max", C.c_double),
+                ("periodic", C.c_int * 3)]
+
+
+class AthgError(RuntimeError):
+    pass
+
+
+_lib = None
+
+
+def lib():
+    """Load the CUDA library (built in-tree by __graft_entry__.build())."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise AthgError("CUDA library not built: %s (run __graft_entry__.build())" % LIB_PATH)
+    L = C.CDLL(LIB_PATH)
+    vp, i, d, sz = C.c_void_p, C.c_int, C.c_double, C.c_size_t
+    L.athg_last_error.restype = C.c_char_p
+    sig = {
+        "athg_create": [C.POINTER(Config), C.POINTER(vp)],
+        "athg_destroy": [vp],
+        "athg_set_uniform_mesh": [vp, C.POINTER(Mesh)],
+        "athg_num_blocks": [vp, C.POINTER(i)],
+        "athg_block_location": [vp, i, C.POINTER(C.c_int64)],
+        "athg_var_size": [vp, i, C.POINTER(sz)],
+        "athg_upload": [vp, i, i, C.POINTER(d), sz],
+        "athg_download": [vp, i, i, C.POINTER(d), sz],
+        "athg_initialize": [vp],
+        "athg_stage": [vp, i],
+        "athg_end_cycle": [vp],
+        "athg_cycles": [vp, i],
+        "athg_get_time": [vp, C.POINTER(d), C.POINTER(d), C.POINTER(C.c_int64)],
+        "athg_set_time": [vp, d, d, C.c_int64],
+        "athg_synchronize": [vp],
+        "athg_stream": [vp, C.POINTER(vp)],
+        "athg_launches_per_cycle": [vp, C.POINTER(i)],
+        "athg_calculate_fluxes": [vp, i],
+        "athg_compute_corner_e": [vp],
+        "athg_integrate": [vp, i],
+        "athg_exchange_ghosts": [vp],
+        "athg_conserved_to_primitive": [vp],
+        "athg_new_block_dt": [vp, C.POINTER(d)],
+        "athg_max_div_b": [vp, C.POINTER(d)],
+        "athg_sum_conserved": [vp, C.POINTER(d)],
+    }
+    for name, args in sig.items():
+        f = getattr(L, name)
+        f.argtypes = args
+        f.restype = C.c_int
+    _lib = L
+    return L
+
+
+def check(rc):
+    if rc != 0:
+        msg = lib().athg_last_error().decode(errors="replace")
+        raise AthgError("athg error %d: %s" % (rc, msg))
+
+
+def _dptr(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+class Sim:
+    """A uniform periodic mesh of MeshBlocks on the GPU."""
+
+    def __init__(self, mesh_nx, block_nx, mhd, solver, precision="fp64", xorder=2,
+                 integrator="vl2", gamma=5.0 / 3.0, cfl=0.4, tlim=1.0, ng=2,
+                 domain=((0.0, 1.0), (0.0, 1.0), (0.0, 1.0)), dfloor=FLOOR, pfloor=FLOOR,
+                 periodic=(1, 1, 1)):
+        L = lib()
+        c = Config()
+        c.nx1, c.nx2, c.nx3 = block_nx
+        c.nghost = ng
+        c.magnetic = int(mhd)
+        c.rsolver = SOLVERS[solver]
+        c.xorder = xorder
+        c.integrator = INTEGRATORS[integrator]
+        c.precision = PRECISIONS[precision]
+        c.gamma, c.dfloor, c.pfloor = gamma, dfloor, pfloor
+        c.cfl_number = min(cfl, CFL_LIMIT[integrator])
+        c.tlim = tlim
+        self.cfg = c
+        h = C.c_void_p()
+        check(L.athg_create(C.byref(c), C.byref(h)))
+        self.h = h
+        m = Mesh()
+        m.nx1, m.nx2, m.nx3 = mesh_nx
+        (m.x1min, m.x1max), (m.x2min, m.x2max), (m.x3min, m.x3max) = domain
+        for q in range(3):
+            m.periodic[q] = int(periodic[q])
+        check(L.athg_set_uniform_mesh(h, C.byref(m)))
+        self.mesh_nx, self.block_nx, self.ng, self.mhd = tuple(mesh_nx), tuple(block_nx), ng, mhd
+        nb = C.c_int()
+        check(L.athg_num_blocks(h, C.byref(nb)))
+        self.nb = nb.value
+        self.locs = []
+        loc = (C.c_int64 * 4)()
+        for b in range(self.nb):
+            check(L.athg_block_location(h, b, loc))
+            self.locs.append((loc[0], loc[1], loc[2]))
+        self.nc = tuple(n + 2 * ng for n in block_nx)
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().athg_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # ---------------------------------------------------------------- layout ----
+    def _shape(self, var):
+        n1, n2, n3 = self.nc
+        return {VAR_CONS: (5, n3, n2, n1), VAR_PRIM: (5, n3, n2, n1), VAR_BCC: (3, n3, n2, n1),
+                VAR_B1F: (n3, n2, n1 + 1), VAR_B2F: (n3, n2 + 1, n1),
+                VAR_B3F: (n3 + 1, n2, n1), VAR_PHI: (n3, n2, n1)}[var]
+
+    def upload(self, var, blocks_array):
+        a = np.ascontiguousarray(blocks_array, dtype=np.float64)
+        check(lib().athg_upload(self.h, -1, var, _dptr(a), a.size))
+
+    def download(self, var):
+        shp = (self.nb,) + self._shape(var)
+        a = np.empty(shp, dtype=np.float64)
+        check(lib().athg_download(self.h, -1, var, _dptr(a), a.size))
+        return a
+
+    def load_interior(self, u, b1=None, b2=None, b3=None):
+        """Scatter global interior arrays into the blocks (ghosts zero, filled later)."""
+        g = self.ng
+        nx1, nx2, nx3 = self.block_nx
+        U = np.zeros((self.nb,) + self._shape(VAR_CONS))
+        for b, (l1, l2, l3) in enumerate(self.locs):
+            U[b, :, g:g + nx3, g:g + nx2, g:g + nx1] = \
+                u[:, l3 * nx3:(l3 + 1) * nx3, l2 * nx2:(l2 + 1) * nx2, l1 * nx1:(l1 + 1) * nx1]
+        self.upload(VAR_CONS, U)
+        if self.mhd:
+            B = [np.zeros((self.nb,) + self._shape(v)) for v in (VAR_B1F, VAR_B2F, VAR_B3F)]
+            for b, (l1, l2, l3) in enumerate(self.locs):
+                o1, o2, o3 = l1 * nx1, l2 * nx2, l3 * nx3
+                B[0][b, g:g + nx3, g:g + nx2, g:g + nx1 + 1] = \
+                    b1[o3:o3 + nx3, o2:o2 + nx2, o1:o1 + nx1 + 1]
+                B[1][b, g:g + nx3, g:g + nx2 + 1, g:g + nx1] = \
+                    b2[o3:o3 + nx3, o2:o2 + nx2 + 1, o1:o1 + nx1]
+                B[2][b, g:g + nx3 + 1, g:g + nx2, g:g + nx1] = \
+                    b3[o3:o3 + nx3 + 1, o2:o2 + nx2, o1:o1 + nx1]
+            for v, arr in zip((VAR_B1F, VAR_B2F, VAR_B3F), B):
+                self.upload(v, arr)
+
+    def interior(self, prim=False):
+        """Gather global interior arrays (u, and b1/b2/b3 for MHD)."""
+        g = self.ng
+        nx1, nx2, nx3 = self.block_nx
+        N1, N2, N3 = self.mesh_nx
+        U = self.download(VAR_PRIM if prim else VAR_CONS)
+        u = np.empty((5, N3, N2, N1))
+        for b, (l1, l2, l3) in enumerate(self.locs):
+            u[:, l3 * nx3:(l3 + 1) * nx3, l2 * nx2:(l2 + 1) * nx2, l1 * nx1:(l1 + 1) * nx1] = \
+                U[b, :, g:g + nx3, g:g + nx2, g:g + nx1]
+        out = {"w" if prim else "u": u}
+        if self.mhd and not prim:
+            b1 = np.empty((N3, N2, N1 + 1))
+            b2 = np.empty((N3, N2 + 1, N1))
+            b3 = np.empty((N3 + 1, N2, N1))
+            B1, B2, B3 = (self.download(v) for v in (VAR_B1F, VAR_B2F, VAR_B3F))
+            for b, (l1, l2, l3) in enumerate(self.locs):
+                o1, o2, o3 = l1 * nx1, l2 * nx2, l3 * nx3
+                b1[o3:o3 + nx3, o2:o2 + nx2, o1:o1 + nx1 + 1] = B1[b, g:g + nx3, g:g + nx2, g:g + nx1 + 1]
+                b2[o3:o3 + nx3, o2:o2 + nx2 + 1, o1:o1 + nx1] = B2[b, g:g + nx3, g:g + nx2 + 1, g:g + nx1]
+                b3[o3:o3 + nx3 + 1, o2:o2 + nx2, o1:o1 + nx1] = B3[b, g:g + nx3 + 1, g:g + nx2, g:g + nx1]
+            out.update(b1=b1, b2=b2, b3=b3)
+        return out
+
+    # ------------------------------------------------------------------ driver ----
+    def initialize(self):
+        check(lib().athg_initialize(self.h))
+
+    def stage(self, s):
+        check(lib().athg_stage(self.h, s))
+
+    def end_cycle(self):
+        check(lib().athg_end_cycle(self.h))
+
+    def cycles(self, n):
+        check(lib().athg_cycles(self.h, n))
+
+    def synchronize(self):
+        check(lib().athg_synchronize(self.h))
+
+    def get_time(self):
+        t, dt, n = C.c_double(), C.c_double(), C.c_int64()
+        check(lib().athg_get_time(self.h, C.byref(t), C.byref(dt), C.byref(n)))
+        return t.value, dt.value, n.value
+
+    def run(self, tlim, nlim=-1, chunk=1):
+        """Whole cycles until time >= tlim (main.cpp:430 loop condition)."""
+        n = 0
+        t, _, _ = self.get_time()
+        while t < tlim and (nlim < 0 or n < nlim):
+            self.cycles(1)
+            n += 1
+            t, _, _ = self.get_time()
+        return n
+
+    def stream(self):
+        s = C.c_void_p()
+        check(lib().athg_stream(self.h, C.byref(s)))
+        return s.value
+
+    def launches_per_cycle(self):
+        n = C.c_int()
+        check(lib().athg_launches_per_cycle(self.h, C.byref(n)))
+        return n.value
+
+    def max_div_b(self):
+        v = C.c_double()
+        check(lib().athg_max_div_b(self.h, C.byref(v)))
+        return v.value
+
+    def sum_conserved(self):
+        a = np.zeros(5)
+        check(lib().athg_sum_conserved(self.h, _dptr(a)))
+        return a
+
+    def new_block_dt(self):
+        v = C.c_double()
+        check(lib().athg_new_block_dt(self.h, C.byref(v)))
+        return v.value

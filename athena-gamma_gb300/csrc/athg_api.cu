@@ -1,0 +1,784 @@
+// athg_api.cu -- the C ABI: context, device block pool, stage sequencing and the
+// CUDA-graph cycle. Declarations and reference interfaces: include/athena_gb300.h.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "athena_gb300.h"
+#include "athg_bvals.cuh"
+#include "athg_launch.cuh"
+
+using namespace athg;
+
+namespace {
+thread_local std::string g_err;
+
+int fail(int code, const std::string& msg) {
+  g_err = msg;
+  return code;
+}
+
+#define CK(call)                                                                        \
+  do {                                                                                  \
+    cudaError_t e_ = (call);                                                            \
+    if (e_ != cudaSuccess)                                                              \
+      return fail(ATHG_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));  \
+  } while (0)
+
+#define CKL()                                                                           \
+  do {                                                                                  \
+    cudaError_t e_ = cudaGetLastError();                                                \
+    if (e_ != cudaSuccess)                                                              \
+      return fail(ATHG_ERR_CUDA, std::string("kernel launch: ") + cudaGetErrorString(e_)); \
+  } while (0)
+
+constexpr double kDblMax = 1.79769313486231570815e308;
+
+// time += dt, ncycle++ (when advancing), then Mesh::NewTimeStep
+// (reference src/mesh/mesh.cpp:1078-1118). The block minimum is read and reset.
+__global__ void k_end_cycle(double* time, double* dt, long long* ncycle,
+                            unsigned long long* dtmin, double cfl, double tlim, int advance) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double t = *time, d = *dt;
+  if (advance) {
+    t += d;
+    *ncycle += 1;
+  }
+  double bdt = __longlong_as_double((long long)*dtmin) * cfl;
+  d = 2.0 * d;
+  d = (bdt < d) ? bdt : d;
+  if (t < tlim && (tlim - t) < d) d = tlim - t;
+  *time = t;
+  *dt = d;
+  *dtmin = (unsigned long long)__double_as_longlong(kDblMax);
+}
+
+// max |div B| * dx over interior cells (the quantity CT keeps at round-off)
+__global__ void k_divb(Geom g, const double* b1, const double* b2, const double* b3,
+                       const BlockGeo* geo, unsigned long long* out) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  double v = 0.0;
+  if (t < g.nx1 * g.nx2) {
+    const int jj = t / g.nx1, i = g.is + t - jj * g.nx1, j = g.js + jj;
+    const int k = g.ks + blockIdx.y, b = blockIdx.z;
+    const double* p1 = b1 + (int64_t)b * g.nf1;
+    const double* p2 = b2 + (int64_t)b * g.nf2;
+    const double* p3 = b3 + (int64_t)b * g.nf3;
+    const BlockGeo ge = geo[b];
+    double d = (p1[f1idx(g, k, j, i + 1)] - p1[f1idx(g, k, j, i)]) / ge.dx[0] +
+               (p2[f2idx(g, k, j + 1, i)] - p2[f2idx(g, k, j, i)]) / ge.dx[1] +
+               (p3[f3idx(g, k + 1, j, i)] - p3[f3idx(g, k, j, i)]) / ge.dx[2];
+    double h = fmin(ge.dx[0], fmin(ge.dx[1], ge.dx[2]));
+    v = fabs(d) * h;
+  }
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(out, (unsigned long long)__double_as_longlong(v));
+}
+
+// volume integral of the conserved variables (history output, src/outputs/history.cpp)
+__global__ void k_sum_cons(Geom g, const double* u, const BlockGeo* geo, double* out) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  double s[5] = {0, 0, 0, 0, 0};
+  if (t < g.nx1 * g.nx2) {
+    const int jj = t / g.nx1, i = g.is + t - jj * g.nx1, j = g.js + jj;
+    const int k = g.ks + blockIdx.y, b = blockIdx.z;
+    const BlockGeo ge = geo[b];
+    const double vol = ge.dx[0] * ge.dx[1] * ge.dx[2];
+    const double* ub = u + (int64_t)b * NHYD * g.ncell;
+    for (int n = 0; n < 5; ++n) s[n] = ub[n * g.ncell + cidx(g, k, j, i)] * vol;
+  }
+  for (int n = 0; n < 5; ++n) {
+    double v = s[n];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) atomicAdd(out + n, v);
+  }
+}
+
+// Stage weights of the low-storage integrators without orbital advection
+// (reference src/task_list/time_integrator.cpp:100-600).
+struct Integrator {
+  int nstages;
+  double delta[3], g1[3], g2[3], beta[3];
+};
+bool make_integrator(int id, Integrator* it) {
+  std::memset(it, 0, sizeof(*it));
+  switch (id) {
+    case ATHG_VL2:
+      *it = {2, {1.0, 0.0, 0}, {0.0, 0.0, 0}, {1.0, 1.0, 0}, {0.5, 1.0, 0}};
+      return true;
+    case ATHG_RK1:
+      *it = {1, {1.0, 0, 0}, {0.0, 0, 0}, {1.0, 0, 0}, {1.0, 0, 0}};
+      return true;
+    case ATHG_RK2:
+      *it = {2, {1.0, 0.0, 0}, {0.0, 0.5, 0}, {1.0, 0.5, 0}, {1.0, 0.5, 0}};
+      return true;
+    case ATHG_RK3:
+      *it = {3, {1.0, 0.0, 0.0}, {0.0, 0.25, 0.66666666666666667},
+             {1.0, 0.75, 0.33333333333333333}, {1.0, 0.25, 0.66666666666666667}};
+      return true;
+    default:
+      return false;
+  }
+}
+
+}  // namespace
+
+struct athg_ctx {
+  athg_config cfg{};
+  Integrator integ{};
+  Geom g{};
+  int nb = 0;
+  cudaStream_t st = nullptr;
+  // pool
+  double *u = nullptr, *u1 = nullptr, *b1 = nullptr, *b2 = nullptr, *b3 = nullptr;
+  double *r1 = nullptr, *r2 = nullptr, *r3 = nullptr, *edge = nullptr;
+  void *w = nullptr, *bcc = nullptr, *flx[3] = {nullptr, nullptr, nullptr};
+  BlockGeo* geo = nullptr;
+  double* coef = nullptr;
+  int* nbr = nullptr;
+  double* scal = nullptr;  // [0] time, [1] dt, [2] ncycle (as long long), [3] dtmin bits,
+                           // [4..8] sums, [9] div-b bits
+  std::vector<athg_block> blocks;
+  std::vector<double> coords;  // host copies of x?f arrays owned by the context
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t gexec = nullptr;
+  int launches_per_cycle = 0;
+  int counting = 0;
+  bool mixed() const { return cfg.precision == ATHG_MIXED; }
+};
+
+namespace {
+
+template <typename T>
+StagePtrs<T> ptrs(athg_ctx* c) {
+  StagePtrs<T> p;
+  p.u = c->u; p.u1 = c->u1;
+  p.b1 = c->b1; p.b2 = c->b2; p.b3 = c->b3;
+  p.r1 = c->r1; p.r2 = c->r2; p.r3 = c->r3;
+  p.w = (T*)c->w; p.bcc = (T*)c->bcc;
+  for (int d = 0; d < 3; ++d) p.flx[d] = (T*)c->flx[d];
+  p.edge = c->edge;
+  p.geo = c->geo;
+  p.coef = c->coef;
+  p.dt = c->scal + 1;
+  return p;
+}
+
+Phys phys(const athg_ctx* c) { return Phys{c->cfg.gamma, c->cfg.dfloor, c->cfg.pfloor}; }
+
+void free_pool(athg_ctx* c) {
+  void* ps[] = {c->u, c->u1, c->b1, c->b2, c->b3, c->r1, c->r2, c->r3, c->edge, c->w,
+                c->bcc, c->flx[0], c->flx[1], c->flx[2], c->geo, c->coef, c->nbr, c->scal};
+  for (void* p : ps)
+    if (p) cudaFree(p);
+  c->u = c->u1 = c->b1 = c->b2 = c->b3 = c->r1 = c->r2 = c->r3 = c->edge = nullptr;
+  c->w = c->bcc = c->flx[0] = c->flx[1] = c->flx[2] = nullptr;
+  c->geo = nullptr; c->coef = nullptr; c->nbr = nullptr; c->scal = nullptr;
+  if (c->gexec) cudaGraphExecDestroy(c->gexec);
+  if (c->graph) cudaGraphDestroy(c->graph);
+  c->gexec = nullptr; c->graph = nullptr;
+  c->nb = 0;
+}
+
+int launch_ghosts(athg_ctx* c) {
+  GhostPtrs gp{c->u, c->b1, c->b2, c->b3, c->nbr, NHYD, c->cfg.magnetic};
+  const Geom& g = c->g;
+  dim3 grid((unsigned)(((g.nc1 + 1) * (g.nc2 + 1) + 255) / 256), (unsigned)(g.nc3 + 1),
+            (unsigned)c->nb);
+  k_ghost_same_level<<<grid, 256, 0, c->st>>>(g, gp);
+  c->counting += 1;
+  CKL();
+  return ATHG_OK;
+}
+
+int launch_fluxes(athg_ctx* c, int order) {
+  bool mhd = c->cfg.magnetic != 0;
+  if (c->mixed())
+    Launcher<float>::fluxes(c->g, ptrs<float>(c), mhd, c->cfg.rsolver, order, phys(c), c->st);
+  else
+    Launcher<double>::fluxes(c->g, ptrs<double>(c), mhd, c->cfg.rsolver, order, phys(c), c->st);
+  c->counting += 3;
+  CKL();
+  return ATHG_OK;
+}
+
+int launch_corner(athg_ctx* c) {
+  if (!c->cfg.magnetic) return ATHG_OK;
+  if (c->mixed()) Launcher<float>::corner_emf(c->g, ptrs<float>(c), c->st);
+  else Launcher<double>::corner_emf(c->g, ptrs<double>(c), c->st);
+  c->counting += 1;
+  CKL();
+  return ATHG_OK;
+}
+
+int launch_update(athg_ctx* c, int l) {
+  const Integrator& it = c->integ;
+  StageW sw;
+  sw.delta = it.delta[l];
+  sw.g1 = it.g1[l];
+  sw.g2 = it.g2[l];
+  sw.beta = it.beta[l];
+  sw.swap = (it.g1[l] == 0.0 && it.g2[l] == 1.0) ? 1 : 0;
+  sw.zero_reg = (l == 0) ? 1 : 0;
+  bool mhd = c->cfg.magnetic != 0;
+  if (c->mixed()) Launcher<float>::update(c->g, ptrs<float>(c), mhd, sw, c->st);
+  else Launcher<double>::update(c->g, ptrs<double>(c), mhd, sw, c->st);
+  c->counting += 1;
+  CKL();
+  return ATHG_OK;
+}
+
+int launch_c2p(athg_ctx* c) {
+  bool mhd = c->cfg.magnetic != 0;
+  if (c->mixed()) Launcher<float>::c2p(c->g, ptrs<float>(c), mhd, phys(c), c->st);
+  else Launcher<double>::c2p(c->g, ptrs<double>(c), mhd, phys(c), c->st);
+  c->counting += 1;
+  CKL();
+  return ATHG_OK;
+}
+
+int launch_block_dt(athg_ctx* c) {
+  bool mhd = c->cfg.magnetic != 0;
+  unsigned long long* dm = (unsigned long long*)(c->scal + 3);
+  if (c->mixed()) Launcher<float>::block_dt(c->g, ptrs<float>(c), mhd, phys(c), dm, c->st);
+  else Launcher<double>::block_dt(c->g, ptrs<double>(c), mhd, phys(c), dm, c->st);
+  c->counting += 1;
+  CKL();
+  return ATHG_OK;
+}
+
+int launch_end(athg_ctx* c, int advance) {
+  k_end_cycle<<<1, 32, 0, c->st>>>(c->scal, c->scal + 1, (long long*)(c->scal + 2),
+                                   (unsigned long long*)(c->scal + 3), c->cfg.cfl_number,
+                                   c->cfg.tlim, advance);
+  c->counting += 1;
+  CKL();
+  return ATHG_OK;
+}
+
+int do_stage(athg_ctx* c, int stage) {
+  const int l = stage - 1;
+  int order = (c->cfg.integrator == ATHG_VL2 && l == 0) ? 1 : c->cfg.xorder;
+  int rc;
+  if ((rc = launch_fluxes(c, order))) return rc;
+  if ((rc = launch_corner(c))) return rc;
+  if ((rc = launch_update(c, l))) return rc;
+  if ((rc = launch_ghosts(c))) return rc;
+  if ((rc = launch_c2p(c))) return rc;
+  if (stage == c->integ.nstages)
+    if ((rc = launch_block_dt(c))) return rc;
+  return ATHG_OK;
+}
+
+int do_cycle(athg_ctx* c) {
+  for (int s = 1; s <= c->integ.nstages; ++s) {
+    int rc = do_stage(c, s);
+    if (rc) return rc;
+  }
+  return launch_end(c, 1);
+}
+
+int need_pool(const athg_ctx* c) {
+  if (!c) return fail(ATHG_ERR_ARG, "null context");
+  if (c->nb <= 0) return fail(ATHG_ERR_STATE, "no blocks: call athg_set_blocks first");
+  return ATHG_OK;
+}
+
+// Captures one whole cycle on the context stream into a CUDA graph (once); the
+// graph reads dt/time from device memory, so the same graph serves every cycle.
+int build_graph(athg_ctx* c) {
+  if (c->gexec) return ATHG_OK;
+  CK(cudaStreamBeginCapture(c->st, cudaStreamCaptureModeThreadLocal));
+  c->counting = 0;
+  int rc = do_cycle(c);
+  cudaGraph_t gr = nullptr;
+  cudaError_t e = cudaStreamEndCapture(c->st, &gr);
+  if (rc) {
+    if (gr) cudaGraphDestroy(gr);
+    return rc;
+  }
+  if (e != cudaSuccess)
+    return fail(ATHG_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+  c->graph = gr;
+  c->launches_per_cycle = c->counting;
+  CK(cudaGraphInstantiate(&c->gexec, c->graph, 0));
+  return ATHG_OK;
+}
+
+// mesh/mesh.hpp:389-405 and :467-488: symmetric logical position, uniform generator
+double gen_rx(int64_t index, int64_t nrange) {
+  int64_t noffset = index - nrange / 2;
+  int64_t noffset_ceil = index - (nrange + 1) / 2;
+  return static_cast<double>(noffset + noffset_ceil) / (2.0 * nrange);
+}
+double gen_x(double rx, double xmin, double xmax) {
+  return 0.5 * (xmin + xmax) + (rx * xmax - rx * xmin);
+}
+
+}  // namespace
+
+// =================================================================== C ABI ==========
+extern "C" {
+
+const char* athg_last_error(void) { return g_err.c_str(); }
+
+int athg_create(const athg_config* cfg, athg_ctx** out) {
+  if (!cfg || !out) return fail(ATHG_ERR_ARG, "null argument");
+  *out = nullptr;
+  if (cfg->nx1 < 2 || cfg->nx2 < 2 || cfg->nx3 < 2)
+    return fail(ATHG_ERR_ARG, "only 3-D MeshBlocks are supported");
+  if (cfg->xorder < 1 || cfg->xorder > 2)
+    return fail(ATHG_ERR_ARG, "xorder must be 1 or 2");
+  if (cfg->nghost < 2) return fail(ATHG_ERR_ARG, "nghost must be >= 2");
+  if (cfg->magnetic && !(cfg->rsolver == ATHG_HLLD || cfg->rsolver == ATHG_HLLE))
+    return fail(ATHG_ERR_ARG, "MHD needs the HLLD or HLLE solver");
+  if (!cfg->magnetic && !(cfg->rsolver == ATHG_HLLC || cfg->rsolver == ATHG_HLLE))
+    return fail(ATHG_ERR_ARG, "hydro needs the HLLC or HLLE solver");
+  if (cfg->precision != ATHG_FP64 && cfg->precision != ATHG_MIXED)
+    return fail(ATHG_ERR_ARG, "precision must be ATHG_FP64 or ATHG_MIXED");
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+    return fail(ATHG_ERR_CUDA, "no CUDA device available");
+  athg_ctx* c = new athg_ctx();
+  c->cfg = *cfg;
+  if (!make_integrator(cfg->integrator, &c->integ)) {
+    delete c;
+    return fail(ATHG_ERR_ARG, "unknown integrator");
+  }
+  if (cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking) != cudaSuccess) {
+    delete c;
+    return fail(ATHG_ERR_CUDA, "cudaStreamCreate failed");
+  }
+  Geom& g = c->g;
+  g.nx1 = cfg->nx1; g.nx2 = cfg->nx2; g.nx3 = cfg->nx3; g.ng = cfg->nghost;
+  g.nc1 = g.nx1 + 2 * g.ng; g.nc2 = g.nx2 + 2 * g.ng; g.nc3 = g.nx3 + 2 * g.ng;
+  g.is = g.ng; g.ie = g.ng + g.nx1 - 1;
+  g.js = g.ng; g.je = g.ng + g.nx2 - 1;
+  g.ks = g.ng; g.ke = g.ng + g.nx3 - 1;
+  g.ncell = (int64_t)g.nc1 * g.nc2 * g.nc3;
+  g.nf1 = (int64_t)g.nc3 * g.nc2 * (g.nc1 + 1);
+  g.nf2 = (int64_t)g.nc3 * (g.nc2 + 1) * g.nc1;
+  g.nf3 = (int64_t)(g.nc3 + 1) * g.nc2 * g.nc1;
+  g.ne = (int64_t)(g.nc3 + 1) * (g.nc2 + 1) * (g.nc1 + 1);
+  g.ncmax = std::max(g.nc1, std::max(g.nc2, g.nc3));
+  *out = c;
+  return ATHG_OK;
+}
+
+int athg_destroy(athg_ctx* c) {
+  if (!c) return ATHG_OK;
+  free_pool(c);
+  if (c->st) cudaStreamDestroy(c->st);
+  delete c;
+  return ATHG_OK;
+}
+
+int athg_set_blocks(athg_ctx* c, int nblocks, const athg_block* blocks) {
+  if (!c || nblocks <= 0 || !blocks) return fail(ATHG_ERR_ARG, "bad block list");
+  if (nblocks > 65535) return fail(ATHG_ERR_ARG, "at most 65535 blocks per context");
+  for (int b = 0; b < nblocks; ++b) {
+    if (!blocks[b].x1f || !blocks[b].x2f || !blocks[b].x3f)
+      return fail(ATHG_ERR_ARG, "block coordinates missing");
+    for (int n = 0; n < 27; ++n)
+      if (blocks[b].neighbor[n] < -1 || blocks[b].neighbor[n] >= nblocks)
+        return fail(ATHG_ERR_ARG, "neighbour id out of range");
+  }
+  free_pool(c);
+  const Geom& g0 = c->g;
+  c->g.nb = nblocks;
+  const Geom& g = c->g;
+  (void)g0;
+  const int64_t nb = nblocks;
+  const size_t tsz = c->mixed() ? sizeof(float) : sizeof(double);
+  const bool mhd = c->cfg.magnetic != 0;
+  const int NF = mhd ? 8 : 5;
+  CK(cudaMalloc(&c->u, sizeof(double) * NHYD * g.ncell * nb));
+  CK(cudaMalloc(&c->u1, sizeof(double) * NHYD * g.ncell * nb));
+  CK(cudaMalloc(&c->w, tsz * NHYD * g.ncell * nb));
+  CK(cudaMalloc(&c->flx[0], tsz * NF * g.nf1 * nb));
+  CK(cudaMalloc(&c->flx[1], tsz * NF * g.nf2 * nb));
+  CK(cudaMalloc(&c->flx[2], tsz * NF * g.nf3 * nb));
+  if (mhd) {
+    CK(cudaMalloc(&c->bcc, tsz * 3 * g.ncell * nb));
+    CK(cudaMalloc(&c->b1, sizeof(double) * g.nf1 * nb));
+    CK(cudaMalloc(&c->b2, sizeof(double) * g.nf2 * nb));
+    CK(cudaMalloc(&c->b3, sizeof(double) * g.nf3 * nb));
+    CK(cudaMalloc(&c->r1, sizeof(double) * g.nf1 * nb));
+    CK(cudaMalloc(&c->r2, sizeof(double) * g.nf2 * nb));
+    CK(cudaMalloc(&c->r3, sizeof(double) * g.nf3 * nb));
+    CK(cudaMalloc(&c->edge, sizeof(double) * 3 * g.ne * nb));
+    CK(cudaMemsetAsync(c->b1, 0, sizeof(double) * g.nf1 * nb, c->st));
+    CK(cudaMemsetAsync(c->b2, 0, sizeof(double) * g.nf2 * nb, c->st));
+    CK(cudaMemsetAsync(c->b3, 0, sizeof(double) * g.nf3 * nb, c->st));
+    CK(cudaMemsetAsync(c->edge, 0, sizeof(double) * 3 * g.ne * nb, c->st));
+  }
+  CK(cudaMemsetAsync(c->u, 0, sizeof(double) * NHYD * g.ncell * nb, c->st));
+  CK(cudaMemsetAsync(c->u1, 0, sizeof(double) * NHYD * g.ncell * nb, c->st));
+  CK(cudaMalloc(&c->geo, sizeof(BlockGeo) * nb));
+  CK(cudaMalloc(&c->coef, sizeof(double) * nb * 3 * 2 * g.ncmax));
+  CK(cudaMalloc(&c->nbr, sizeof(int) * 27 * nb));
+  CK(cudaMalloc(&c->scal, sizeof(double) * 16));
+  // host-side per-block tables
+  std::vector<BlockGeo> hgeo(nb);
+  std::vector<double> hcoef(nb * 3 * 2 * g.ncmax, 0.0);
+  std::vector<int> hnbr(27 * nb);
+  c->blocks.assign(blocks, blocks + nblocks);
+  const int ncs[3] = {g.nc1, g.nc2, g.nc3};
+  for (int b = 0; b < nblocks; ++b) {
+    const athg_block& B = blocks[b];
+    hgeo[b].dx[0] = B.dx1; hgeo[b].dx[1] = B.dx2; hgeo[b].dx[2] = B.dx3;
+    const double* xf[3] = {B.x1f, B.x2f, B.x3f};
+    for (int d = 0; d < 3; ++d) {
+      double* cp = &hcoef[((size_t)b * 3 + d) * 2 * g.ncmax];
+      double* cm = cp + g.ncmax;
+      const double dx = hgeo[b].dx[d];
+      for (int i = 0; i < ncs[d]; ++i) {
+        // Cartesian x_v (coordinates/cartesian.cpp:29) and the PLM interface
+        // coefficients of reconstruct/plm.cpp:113-119 (x1), :226-227 (x2), :332-333 (x3)
+        double xv = 0.5 * (xf[d][i + 1] + xf[d][i]);
+        cp[i] = (xf[d][i + 1] - xv) / dx;
+        cm[i] = (xv - xf[d][i]) / dx;
+      }
+    }
+    for (int n = 0; n < 27; ++n) hnbr[27 * b + n] = B.neighbor[n];
+  }
+  CK(cudaMemcpyAsync(c->geo, hgeo.data(), sizeof(BlockGeo) * nb, cudaMemcpyHostToDevice, c->st));
+  CK(cudaMemcpyAsync(c->coef, hcoef.data(), sizeof(double) * hcoef.size(), cudaMemcpyHostToDevice,
+                     c->st));
+  CK(cudaMemcpyAsync(c->nbr, hnbr.data(), sizeof(int) * hnbr.size(), cudaMemcpyHostToDevice,
+                     c->st));
+  double hs[16] = {0};
+  hs[1] = kDblMax;
+  unsigned long long big;
+  std::memcpy(&big, &kDblMax, 8);
+  std::memcpy(&hs[3], &big, 8);
+  CK(cudaMemcpyAsync(c->scal, hs, sizeof(hs), cudaMemcpyHostToDevice, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  // the host copies of the coordinate pointers are not kept
+  for (auto& B : c->blocks) B.x1f = B.x2f = B.x3f = nullptr;
+  c->nb = nblocks;
+  return ATHG_OK;
+}
+
+int athg_set_uniform_mesh(athg_ctx* c, const athg_mesh* m) {
+  if (!c || !m) return fail(ATHG_ERR_ARG, "null argument");
+  const Geom& g = c->g;
+  const int nmx[3] = {m->nx1, m->nx2, m->nx3};
+  const int nbx[3] = {g.nx1, g.nx2, g.nx3};
+  const double lo[3] = {m->x1min, m->x2min, m->x3min}, hi[3] = {m->x1max, m->x2max, m->x3max};
+  int nrb[3];
+  for (int d = 0; d < 3; ++d) {
+    if (nmx[d] % nbx[d] != 0)
+      return fail(ATHG_ERR_ARG, "mesh size must be a multiple of the MeshBlock size");
+    nrb[d] = nmx[d] / nbx[d];
+  }
+  const int nblocks = nrb[0] * nrb[1] * nrb[2];
+  std::vector<athg_block> bl(nblocks);
+  const int ncs[3] = {g.nc1, g.nc2, g.nc3};
+  c->coords.assign((size_t)nblocks * (ncs[0] + ncs[1] + ncs[2] + 3), 0.0);
+  size_t off = 0;
+  for (int b3 = 0; b3 < nrb[2]; ++b3)
+    for (int b2 = 0; b2 < nrb[1]; ++b2)
+      for (int b1 = 0; b1 < nrb[0]; ++b1) {
+        const int id = (b3 * nrb[1] + b2) * nrb[0] + b1;
+        athg_block& B = bl[id];
+        const int lx[3] = {b1, b2, b3};
+        B.lx1 = b1; B.lx2 = b2; B.lx3 = b3; B.level = 0;
+        double* xfs[3];
+        double dxs[3];
+        for (int d = 0; d < 3; ++d) {
+          // block_size (mesh/mesh.cpp:1675-1690): exact mesh bounds at the edges
+          double bmin = (lx[d] == 0) ? lo[d] : gen_x(gen_rx(lx[d], nrb[d]), lo[d], hi[d]);
+          double bmax = (lx[d] == nrb[d] - 1) ? hi[d]
+                                               : gen_x(gen_rx(lx[d] + 1, nrb[d]), lo[d], hi[d]);
+          // face positions (coordinates/coordinates.cpp:127-145, uniform branch)
+          const int il = g.ng, iu = g.ng + nbx[d] - 1;
+          double* xf = &c->coords[off];
+          off += ncs[d] + 1;
+          dxs[d] = (bmax - bmin) / (iu - il + 1);
+          for (int i = il - g.ng; i <= iu + g.ng + 1; ++i) {
+            int64_t noff = (int64_t)(i - il) + (int64_t)lx[d] * nbx[d];
+            xf[i] = gen_x(gen_rx(noff, nmx[d]), lo[d], hi[d]);
+          }
+          xf[il] = bmin;
+          xf[iu + 1] = bmax;
+          xfs[d] = xf;
+        }
+        B.x1f = xfs[0]; B.x2f = xfs[1]; B.x3f = xfs[2];
+        B.dx1 = dxs[0]; B.dx2 = dxs[1]; B.dx3 = dxs[2];
+        for (int o3 = -1; o3 <= 1; ++o3)
+          for (int o2 = -1; o2 <= 1; ++o2)
+            for (int o1 = -1; o1 <= 1; ++o1) {
+              int n[3] = {b1 + o1, b2 + o2, b3 + o3};
+              bool ok = true;
+              for (int d = 0; d < 3; ++d) {
+                if (n[d] < 0 || n[d] >= nrb[d]) {
+                  if (m->periodic[d]) n[d] = (n[d] + nrb[d]) % nrb[d];
+                  else ok = false;
+                }
+              }
+              B.neighbor[(o3 + 1) * 9 + (o2 + 1) * 3 + (o1 + 1)] =
+                  ok ? (n[2] * nrb[1] + n[1]) * nrb[0] + n[0] : -1;
+            }
+      }
+  return athg_set_blocks(c, nblocks, bl.data());
+}
+
+int athg_num_blocks(const athg_ctx* c, int* nblocks) {
+  if (!c || !nblocks) return fail(ATHG_ERR_ARG, "null argument");
+  *nblocks = c->nb;
+  return ATHG_OK;
+}
+
+int athg_block_location(const athg_ctx* c, int block, int64_t* out) {
+  if (!c || !out || block < 0 || block >= c->nb) return fail(ATHG_ERR_ARG, "bad block");
+  const athg_block& B = c->blocks[block];
+  out[0] = B.lx1; out[1] = B.lx2; out[2] = B.lx3; out[3] = B.level;
+  return ATHG_OK;
+}
+
+int athg_var_size(const athg_ctx* c, int var, size_t* count) {
+  if (!c || !count) return fail(ATHG_ERR_ARG, "null argument");
+  const Geom& g = c->g;
+  switch (var) {
+    case ATHG_VAR_CONS: case ATHG_VAR_PRIM: *count = (size_t)NHYD * g.ncell; break;
+    case ATHG_VAR_B1F: *count = (size_t)g.nf1; break;
+    case ATHG_VAR_B2F: *count = (size_t)g.nf2; break;
+    case ATHG_VAR_B3F: *count = (size_t)g.nf3; break;
+    case ATHG_VAR_BCC: *count = (size_t)3 * g.ncell; break;
+    case ATHG_VAR_PHI: *count = (size_t)g.ncell; break;
+    default: return fail(ATHG_ERR_ARG, "unknown variable");
+  }
+  return ATHG_OK;
+}
+
+namespace {
+// device array of var and whether it is stored in the flux precision (float when mixed)
+int var_ptr(athg_ctx* c, int var, void** p, bool* narrow) {
+  *narrow = false;
+  switch (var) {
+    case ATHG_VAR_CONS: *p = c->u; return ATHG_OK;
+    case ATHG_VAR_B1F: *p = c->b1; break;
+    case ATHG_VAR_B2F: *p = c->b2; break;
+    case ATHG_VAR_B3F: *p = c->b3; break;
+    case ATHG_VAR_PRIM: *p = c->w; *narrow = c->mixed(); return ATHG_OK;
+    case ATHG_VAR_BCC: *p = c->bcc; *narrow = c->mixed(); break;
+    default: return fail(ATHG_ERR_ARG, "variable not available");
+  }
+  if (!c->cfg.magnetic) return fail(ATHG_ERR_ARG, "no magnetic field in a hydro context");
+  return ATHG_OK;
+}
+}  // namespace
+
+int athg_upload(athg_ctx* c, int block, int var, const double* host, size_t count) {
+  int rc = need_pool(c);
+  if (rc) return rc;
+  size_t per;
+  if ((rc = athg_var_size(c, var, &per))) return rc;
+  void* d;
+  bool narrow;
+  if ((rc = var_ptr(c, var, &d, &narrow))) return rc;
+  if (narrow) return fail(ATHG_ERR_ARG, "derived variables cannot be uploaded");
+  if (block < -1 || block >= c->nb) return fail(ATHG_ERR_ARG, "bad block index");
+  size_t n = (block < 0) ? per * c->nb : per;
+  if (!host || count != n) return fail(ATHG_ERR_ARG, "host buffer size mismatch");
+  double* dst = (double*)d + (block < 0 ? 0 : per * block);
+  CK(cudaMemcpyAsync(dst, host, n * sizeof(double), cudaMemcpyHostToDevice, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  return ATHG_OK;
+}
+
+int athg_download(athg_ctx* c, int block, int var, double* host, size_t count) {
+  int rc = need_pool(c);
+  if (rc) return rc;
+  size_t per;
+  if ((rc = athg_var_size(c, var, &per))) return rc;
+  void* d;
+  bool narrow;
+  if ((rc = var_ptr(c, var, &d, &narrow))) return rc;
+  if (block < -1 || block >= c->nb) return fail(ATHG_ERR_ARG, "bad block index");
+  size_t n = (block < 0) ? per * c->nb : per;
+  if (!host || count != n) return fail(ATHG_ERR_ARG, "host buffer size mismatch");
+  size_t off = (block < 0 ? 0 : per * block);
+  if (!narrow) {
+    CK(cudaMemcpyAsync(host, (double*)d + off, n * sizeof(double), cudaMemcpyDeviceToHost,
+                       c->st));
+    CK(cudaStreamSynchronize(c->st));
+  } else {
+    std::vector<float> tmp(n);
+    CK(cudaMemcpyAsync(tmp.data(), (float*)d + off, n * sizeof(float), cudaMemcpyDeviceToHost,
+                       c->st));
+    CK(cudaStreamSynchronize(c->st));
+    for (size_t q = 0; q < n; ++q) host[q] = tmp[q];
+  }
+  return ATHG_OK;
+}
+
+int athg_initialize(athg_ctx* c) {
+  int rc = need_pool(c);
+  if (rc) return rc;
+  double hs[4];
+  hs[0] = 0.0; hs[1] = kDblMax; hs[2] = 0.0;
+  unsigned long long big;
+  std::memcpy(&big, &kDblMax, 8);
+  std::memcpy(&hs[3], &big, 8);
+  CK(cudaMemcpyAsync(c->scal, hs, sizeof(hs), cudaMemcpyHostToDevice, c->st));
+  if ((rc = launch_ghosts(c))) return rc;
+  if ((rc = launch_c2p(c))) return rc;
+  if ((rc = launch_block_dt(c))) return rc;
+  if ((rc = launch_end(c, 0))) return rc;
+  CK(cudaStreamSynchronize(c->st));
+  return ATHG_OK;
+}
+
+int athg_stage(athg_ctx* c, int stage) {
+  int rc = need_pool(c);
+  if (rc) return rc;
+  if (stage < 1 || stage > c->integ.nstages) return fail(ATHG_ERR_ARG, "stage out of range");
+  return do_stage(c, stage);
+}
+
+int athg_end_cycle(athg_ctx* c) {
+  int rc = need_pool(c);
+  if (rc) return rc;
+  return launch_end(c, 1);
+}
+
+int athg_cycles(athg_ctx* c, int n) {
+  int rc = need_pool(c);
+  if (rc) return rc;
+  if (n <= 0) return ATHG_OK;
+  if ((rc = build_graph(c))) return rc;
+  for (int q = 0; q < n; ++q) CK(cudaGraphLaunch(c->gexec, c->st));
+  return ATHG_OK;
+}
+
+int athg_launches_per_cycle(athg_ctx* c, int* n) {
+  int rc = need_pool(c);
+  if (rc) return rc;
+  if (!n) return fail(ATHG_ERR_ARG, "null argument");
+  if ((rc = build_graph(c))) return rc;
+  *n = c->launches_per_cycle;
+  return ATHG_OK;
+}
+
+int athg_get_time(athg_ctx* c, double* time, double* dt, int64_t* ncycle) {
+  int rc = need_pool(c);
+  if (rc) return rc;
+  double hs[3];
+  CK(cudaMemcpyAsync(hs, c->scal, sizeof(hs), cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  if (time) *time = hs[0];
+  if (dt) *dt = hs[1];
+  long long nc;
+  std::memcpy(&nc, &hs[2], 8);
+  if (ncycle) *ncycle = nc;
+  return ATHG_OK;
+}
+
+int athg_set_time(athg_ctx* c, double time, double dt, int64_t ncycle) {
+  int rc = need_pool(c);
+  if (rc) return rc;
+  double hs[3];
+  hs[0] = time; hs[1] = dt;
+  long long nc = ncycle;
+  std::memcpy(&hs[2], &nc, 8);
+  CK(cudaMemcpyAsync(c->scal, hs, sizeof(hs), cudaMemcpyHostToDevice, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  return ATHG_OK;
+}
+
+int athg_synchronize(athg_ctx* c) {
+  if (!c) return fail(ATHG_ERR_ARG, "null context");
+  CK(cudaStreamSynchronize(c->st));
+  return ATHG_OK;
+}
+
+int athg_stream(athg_ctx* c, void** stream) {
+  if (!c || !stream) return fail(ATHG_ERR_ARG, "null argument");
+  *stream = (void*)c->st;
+  return ATHG_OK;
+}
+
+int athg_calculate_fluxes(athg_ctx* c, int order) {
+  int rc = need_pool(c);
+  if (rc) return rc;
+  if (order < 1 || order > 2) return fail(ATHG_ERR_ARG, "order must be 1 or 2");
+  return launch_fluxes(c, order);
+}
+
+int athg_compute_corner_e(athg_ctx* c) {
+  int rc = need_pool(c);
+  if (rc) return rc;
+  return launch_corner(c);
+}
+
+int athg_integrate(athg_ctx* c, int stage) {
+  int rc = need_pool(c);
+  if (rc) return rc;
+  if (stage < 1 || stage > c->integ.nstages) return fail(ATHG_ERR_ARG, "stage out of range");
+  return launch_update(c, stage - 1);
+}
+
+int athg_exchange_ghosts(athg_ctx* c) {
+  int rc = need_pool(c);
+  if (rc) return rc;
+  return launch_ghosts(c);
+}
+
+int athg_conserved_to_primitive(athg_ctx* c) {
+  int rc = need_pool(c);
+  if (rc) return rc;
+  return launch_c2p(c);
+}
+
+int athg_new_block_dt(athg_ctx* c, double* dt_out) {
+  int rc = need_pool(c);
+  if (rc) return rc;
+  unsigned long long big;
+  std::memcpy(&big, &kDblMax, 8);
+  CK(cudaMemcpyAsync(c->scal + 3, &big, 8, cudaMemcpyHostToDevice, c->st));
+  if ((rc = launch_block_dt(c))) return rc;
+  unsigned long long bits;
+  CK(cudaMemcpyAsync(&bits, c->scal + 3, 8, cudaMemcpyDeviceToHost, c->st));
+  CK(cudaMemcpyAsync(c->scal + 3, &big, 8, cudaMemcpyHostToDevice, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  double v;
+  std::memcpy(&v, &bits, 8);
+  if (dt_out) *dt_out = v * c->cfg.cfl_number;
+  return ATHG_OK;
+}
+
+int athg_max_div_b(athg_ctx* c, double* out) {
+  int rc = need_pool(c);
+  if (rc) return rc;
+  if (!c->cfg.magnetic) return fail(ATHG_ERR_ARG, "no magnetic field in a hydro context");
+  const Geom& g = c->g;
+  CK(cudaMemsetAsync(c->scal + 9, 0, 8, c->st));
+  dim3 grid((unsigned)((g.nx1 * g.nx2 + 255) / 256), (unsigned)g.nx3, (unsigned)c->nb);
+  k_divb<<<grid, 256, 0, c->st>>>(g, c->b1, c->b2, c->b3, c->geo,
+                                  (unsigned long long*)(c->scal + 9));
+  CKL();
+  double v;
+  CK(cudaMemcpyAsync(&v, c->scal + 9, 8, cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  *out = v;
+  return ATHG_OK;
+}
+
+int athg_sum_conserved(athg_ctx* c, double* out5) {
+  int rc = need_pool(c);
+  if (rc) return rc;
+  const Geom& g = c->g;
+  CK(cudaMemsetAsync(c->scal + 4, 0, 5 * 8, c->st));
+  dim3 grid((unsigned)((g.nx1 * g.nx2 + 255) / 256), (unsigned)g.nx3, (unsigned)c->nb);
+  k_sum_cons<<<grid, 256, 0, c->st>>>(g, c->u, c->geo, c->scal + 4);
+  CKL();
+  CK(cudaMemcpyAsync(out5, c->scal + 4, 5 * 8, cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  return ATHG_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,81 @@
+// athg_bvals.cuh -- on-device ghost-zone exchange between MeshBlocks of the same level.
+//
+// The reference packs each neighbour's ghost region into a buffer, copies it
+// (std::memcpy on one rank, MPI otherwise) and unpacks it (src/bvals/bvals_var.cpp:108-330,
+// src/bvals/cc/bvals_cc.cpp:201-342, src/bvals/fc/bvals_fc.cpp:344-397). Here all blocks
+// live in one device pool, so one launch gathers every ghost value straight from the
+// owning neighbour's interior: no buffers, no pack/unpack.
+//
+// Ownership rule (same as the reference's pack ranges): along a cell axis a block owns
+// indices [s, e]; along the normal axis of a face field it owns [s, e+1] (the shared
+// face is never exchanged, bvals_fc.cpp:351-353). A ghost location takes the value of
+// the neighbour in direction (ox1,ox2,ox3) at the index shifted by -ox*nx.
+#pragma once
+#include "athg_device.cuh"
+
+namespace athg {
+
+struct GhostPtrs {
+  double *u, *b1, *b2, *b3;
+  const int* nbr;  // [nb][27], same-level neighbour block id, -1 = none
+  int nvar;        // cell variables in u (5)
+  int mhd;
+};
+
+__device__ __forceinline__ int ghost_dir(int i, int s, int e) {
+  return i < s ? -1 : (i > e ? 1 : 0);
+}
+
+// One thread per (k,j,i) of the largest (edge-sized) box of every block; each thread
+// handles the cell and the three faces that share this index, when they are ghosts.
+__global__ void __launch_bounds__(256) k_ghost_same_level(Geom g, GhostPtrs p) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int n1 = g.nc1 + 1, n2 = g.nc2 + 1;
+  if (t >= n1 * n2) return;
+  const int j = t / n1, i = t - j * n1, k = blockIdx.y, b = blockIdx.z;
+  const int* nb = p.nbr + (int64_t)b * 27;
+  // cell-centred variables
+  if (i < g.nc1 && j < g.nc2 && k < g.nc3) {
+    int o1 = ghost_dir(i, g.is, g.ie), o2 = ghost_dir(j, g.js, g.je), o3 = ghost_dir(k, g.ks, g.ke);
+    if (o1 | o2 | o3) {
+      int src = nb[(o3 + 1) * 9 + (o2 + 1) * 3 + (o1 + 1)];
+      if (src >= 0) {
+        int64_t d = cidx(g, k, j, i);
+        int64_t s = cidx(g, k - o3 * g.nx3, j - o2 * g.nx2, i - o1 * g.nx1);
+        const double* us = p.u + (int64_t)src * p.nvar * g.ncell;
+        double* ud = p.u + (int64_t)b * p.nvar * g.ncell;
+        for (int n = 0; n < p.nvar; ++n) ud[n * g.ncell + d] = us[n * g.ncell + s];
+      }
+    }
+  }
+  if (!p.mhd) return;
+  if (i <= g.nc1 && j < g.nc2 && k < g.nc3) {  // x1 faces
+    int o1 = ghost_dir(i, g.is, g.ie + 1), o2 = ghost_dir(j, g.js, g.je), o3 = ghost_dir(k, g.ks, g.ke);
+    if (o1 | o2 | o3) {
+      int src = nb[(o3 + 1) * 9 + (o2 + 1) * 3 + (o1 + 1)];
+      if (src >= 0)
+        p.b1[(int64_t)b * g.nf1 + f1idx(g, k, j, i)] =
+            p.b1[(int64_t)src * g.nf1 + f1idx(g, k - o3 * g.nx3, j - o2 * g.nx2, i - o1 * g.nx1)];
+    }
+  }
+  if (i < g.nc1 && j <= g.nc2 && k < g.nc3) {  // x2 faces
+    int o1 = ghost_dir(i, g.is, g.ie), o2 = ghost_dir(j, g.js, g.je + 1), o3 = ghost_dir(k, g.ks, g.ke);
+    if (o1 | o2 | o3) {
+      int src = nb[(o3 + 1) * 9 + (o2 + 1) * 3 + (o1 + 1)];
+      if (src >= 0)
+        p.b2[(int64_t)b * g.nf2 + f2idx(g, k, j, i)] =
+            p.b2[(int64_t)src * g.nf2 + f2idx(g, k - o3 * g.nx3, j - o2 * g.nx2, i - o1 * g.nx1)];
+    }
+  }
+  if (i < g.nc1 && j < g.nc2 && k <= g.nc3) {  // x3 faces
+    int o1 = ghost_dir(i, g.is, g.ie), o2 = ghost_dir(j, g.js, g.je), o3 = ghost_dir(k, g.ks, g.ke + 1);
+    if (o1 | o2 | o3) {
+      int src = nb[(o3 + 1) * 9 + (o2 + 1) * 3 + (o1 + 1)];
+      if (src >= 0)
+        p.b3[(int64_t)b * g.nf3 + f3idx(g, k, j, i)] =
+            p.b3[(int64_t)src * g.nf3 + f3idx(g, k - o3 * g.nx3, j - o2 * g.nx2, i - o1 * g.nx1)];
+    }
+  }
+}
+
+}  // namespace athg

@@ -1,0 +1,391 @@
+// athg_device.cuh -- device-side layout, EOS helpers and Riemann solvers.
+//
+// Block-pool layout (one pool for all MeshBlocks, every block the same interior size):
+//   cell arrays   [block][var][k][j][i]   nc = nx + 2*ng per axis, i fastest
+//                 (the AthenaArray (n,k,j,i) layout of one block, reference
+//                  src/athena_arrays.hpp:140, so upload/download is one memcpy per block)
+//   x1-face       [block][k][j][i]  (nc3, nc2, nc1+1)   src/athena.hpp:95-102
+//   x2-face       [block][k][j][i]  (nc3, nc2+1, nc1)
+//   x3-face       [block][k][j][i]  (nc3+1, nc2, nc1)
+//   edges         [block][comp][k][j][i] (nc3+1, nc2+1, nc1+1)
+// Conserved variables and face fields are always FP64. Primitives, reconstructed
+// states, Riemann fluxes and face EMFs use the template type T: double for the plain
+// FP64 path, float for the mixed path.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace athg {
+
+constexpr int NHYD = 5;
+constexpr int IDN = 0, IVX = 1, IVY = 2, IVZ = 3, IPR = 4, IEN = 4, IBY = 5, IBZ = 6;
+enum Solver { HLLE = 0, HLLC = 1, HLLD = 2, LHLLC = 3, LHLLD = 4 };
+
+// Sizes shared by every block of the pool.
+struct Geom {
+  int nx1, nx2, nx3, ng;
+  int nc1, nc2, nc3;
+  int is, ie, js, je, ks, ke;
+  int64_t ncell, nf1, nf2, nf3, ne;
+  int nb;
+  int ncmax;  // max(nc1, nc2, nc3), stride of the per-block coefficient arrays
+};
+
+__host__ __device__ inline int64_t cidx(const Geom& g, int k, int j, int i) {
+  return ((int64_t)k * g.nc2 + j) * g.nc1 + i;
+}
+__host__ __device__ inline int64_t f1idx(const Geom& g, int k, int j, int i) {
+  return ((int64_t)k * g.nc2 + j) * (g.nc1 + 1) + i;
+}
+__host__ __device__ inline int64_t f2idx(const Geom& g, int k, int j, int i) {
+  return ((int64_t)k * (g.nc2 + 1) + j) * g.nc1 + i;
+}
+__host__ __device__ inline int64_t f3idx(const Geom& g, int k, int j, int i) {
+  return cidx(g, k, j, i);
+}
+__host__ __device__ inline int64_t eidx(const Geom& g, int k, int j, int i) {
+  return ((int64_t)k * (g.nc2 + 1) + j) * (g.nc1 + 1) + i;
+}
+template <int DIR>
+__host__ __device__ inline int64_t fidx(const Geom& g, int k, int j, int i) {
+  return DIR == 0 ? f1idx(g, k, j, i) : (DIR == 1 ? f2idx(g, k, j, i) : f3idx(g, k, j, i));
+}
+template <int DIR>
+__host__ __device__ inline int64_t fsize(const Geom& g) {
+  return DIR == 0 ? g.nf1 : (DIR == 1 ? g.nf2 : g.nf3);
+}
+
+// Per-block geometry (uniform Cartesian: one width per axis).
+struct BlockGeo {
+  double dx[3];
+};
+
+// Physics constants of a run.
+struct Phys {
+  double gamma, dfloor, pfloor;
+};
+
+// Stage weights of the low-storage integrator (reference
+// src/task_list/time_integrator.cpp:100-600, applied as in :1563-1653).
+struct StageW {
+  double delta, g1, g2, beta;
+  int swap;  // g1==0 && g2==1 && g3==0: the reference swaps registers
+  int zero_reg;  // first stage: the register starts from zero
+};
+
+// std::min / std::max semantics (first argument wins ties)
+template <typename T> __device__ __forceinline__ T mn(T a, T b) { return (b < a) ? b : a; }
+template <typename T> __device__ __forceinline__ T mx(T a, T b) { return (a < b) ? b : a; }
+template <typename T> __device__ __forceinline__ T sq(T x) { return x * x; }
+
+// eos/adiabatic_mhd.cpp:149-156 (fast magnetosonic speed)
+template <typename T>
+__device__ __forceinline__ T fast_speed(T d, T p, T by, T bz, T bx, T gamma) {
+  T asq = gamma * p;
+  T vaxsq = bx * bx;
+  T ct2 = (by * by + bz * bz);
+  T qsq = vaxsq + ct2 + asq;
+  T tmp = vaxsq + ct2 - asq;
+  return sqrt(T(0.5) * (qsq + sqrt(tmp * tmp + T(4.0) * asq * ct2)) / d);
+}
+
+// hydro/hydro.cpp:154-158 (upwind weight for the corner EMF)
+template <typename T>
+__device__ __forceinline__ T ct_weight(T dflx, T rhol, T rhor, T dx, T dt) {
+  T v_over_c = (T(1024.0)) * dt * dflx / (dx * (rhol + rhor));
+  T tmp_min = mn(T(0.5), v_over_c);
+  return T(0.5) + mx(T(-0.5), tmp_min);
+}
+
+// ------------------------------------------------------------------------------------
+// Riemann solvers. Input states are in the rotated order (d, vn, vt1, vt2, p[, by, bz]);
+// the flux comes back in the same order.
+
+// HLLC, Toro PVRS wave speeds (reference hydro/rsolvers/hydro/hllc.cpp:54-168)
+template <typename T>
+__device__ __forceinline__ void rs_hllc(const T* wli, const T* wri, T gamma, T* flxi) {
+  const T gm1 = gamma - T(1.0), igm1 = T(1.0) / gm1;
+  T cl = sqrt(gamma * wli[IPR] / wli[IDN]);
+  T cr = sqrt(gamma * wri[IPR] / wri[IDN]);
+  T el = wli[IPR] * igm1 + T(0.5) * wli[IDN] * (sq(wli[IVX]) + sq(wli[IVY]) + sq(wli[IVZ]));
+  T er = wri[IPR] * igm1 + T(0.5) * wri[IDN] * (sq(wri[IVX]) + sq(wri[IVY]) + sq(wri[IVZ]));
+  T rhoa = T(.5) * (wli[IDN] + wri[IDN]);
+  T ca = T(.5) * (cl + cr);
+  T pmid = T(.5) * (wli[IPR] + wri[IPR] + (wli[IVX] - wri[IVX]) * rhoa * ca);
+  T ql = (pmid <= wli[IPR]) ? T(1.0)
+         : sqrt(T(1.0) + (gamma + T(1)) / (T(2) * gamma) * (pmid / wli[IPR] - T(1.0)));
+  T qr = (pmid <= wri[IPR]) ? T(1.0)
+         : sqrt(T(1.0) + (gamma + T(1)) / (T(2) * gamma) * (pmid / wri[IPR] - T(1.0)));
+  T al = wli[IVX] - cl * ql;
+  T ar = wri[IVX] + cr * qr;
+  T bp = ar > T(0.0) ? ar : T(1.0e-20);
+  T bm = al < T(0.0) ? al : -T(1.0e-20);
+  T vxl = wli[IVX] - al;
+  T vxr = wri[IVX] - ar;
+  T tl = wli[IPR] + vxl * wli[IDN] * wli[IVX];
+  T tr = wri[IPR] + vxr * wri[IDN] * wri[IVX];
+  T ml = wli[IDN] * vxl;
+  T mr = -(wri[IDN] * vxr);
+  T am = (tl - tr) / (ml + mr);
+  T cp = (ml * tr + mr * tl) / (ml + mr);
+  cp = cp > T(0.0) ? cp : T(0.0);
+  vxl = wli[IVX] - bm;
+  vxr = wri[IVX] - bp;
+  T fl0 = wli[IDN] * vxl, fr0 = wri[IDN] * vxr;
+  T fl1 = wli[IDN] * wli[IVX] * vxl + wli[IPR], fr1 = wri[IDN] * wri[IVX] * vxr + wri[IPR];
+  T fl2 = wli[IDN] * wli[IVY] * vxl, fr2 = wri[IDN] * wri[IVY] * vxr;
+  T fl3 = wli[IDN] * wli[IVZ] * vxl, fr3 = wri[IDN] * wri[IVZ] * vxr;
+  T fl4 = el * vxl + wli[IPR] * wli[IVX], fr4 = er * vxr + wri[IPR] * wri[IVX];
+  T sl, sr, sm;
+  if (am >= T(0.0)) {
+    sl = am / (am - bm); sr = T(0.0); sm = -bm / (am - bm);
+  } else {
+    sl = T(0.0); sr = -am / (bp - am); sm = bp / (bp - am);
+  }
+  flxi[IDN] = sl * fl0 + sr * fr0;
+  flxi[IVX] = sl * fl1 + sr * fr1 + sm * cp;
+  flxi[IVY] = sl * fl2 + sr * fr2;
+  flxi[IVZ] = sl * fl3 + sr * fr3;
+  flxi[IEN] = sl * fl4 + sr * fr4 + sm * cp * am;
+}
+
+// HLLE with Roe-averaged speeds, adiabatic hydro (hydro/rsolvers/hydro/hlle.cpp:64-151)
+template <typename T>
+__device__ __forceinline__ void rs_hlle_hydro(const T* wli, const T* wri, T gamma, T* flxi) {
+  const T gm1 = gamma - T(1.0), igm1 = T(1.0) / gm1;
+  T sqrtdl = sqrt(wli[IDN]), sqrtdr = sqrt(wri[IDN]);
+  T isdlpdr = T(1.0) / (sqrtdl + sqrtdr);
+  T rvx = (sqrtdl * wli[IVX] + sqrtdr * wri[IVX]) * isdlpdr;
+  T rvy = (sqrtdl * wli[IVY] + sqrtdr * wri[IVY]) * isdlpdr;
+  T rvz = (sqrtdl * wli[IVZ] + sqrtdr * wri[IVZ]) * isdlpdr;
+  T el = wli[IPR] * igm1 + T(0.5) * wli[IDN] * (sq(wli[IVX]) + sq(wli[IVY]) + sq(wli[IVZ]));
+  T er = wri[IPR] * igm1 + T(0.5) * wri[IDN] * (sq(wri[IVX]) + sq(wri[IVY]) + sq(wri[IVZ]));
+  T hroe = ((el + wli[IPR]) / sqrtdl + (er + wri[IPR]) / sqrtdr) * isdlpdr;
+  T cl = sqrt(gamma * wli[IPR] / wli[IDN]);
+  T cr = sqrt(gamma * wri[IPR] / wri[IDN]);
+  T q = hroe - T(0.5) * (sq(rvx) + sq(rvy) + sq(rvz));
+  T a = (q < T(0.0)) ? T(0.0) : sqrt(gm1 * q);
+  T al = mn(rvx - a, wli[IVX] - cl);
+  T ar = mx(rvx + a, wri[IVX] + cr);
+  T bp = ar > T(0.0) ? ar : T(0.0);
+  T bm = al < T(0.0) ? al : T(0.0);
+  T vxl = wli[IVX] - bm, vxr = wri[IVX] - bp;
+  T fl[5], fr[5];
+  fl[IDN] = wli[IDN] * vxl; fr[IDN] = wri[IDN] * vxr;
+  fl[IVX] = wli[IDN] * wli[IVX] * vxl; fr[IVX] = wri[IDN] * wri[IVX] * vxr;
+  fl[IVY] = wli[IDN] * wli[IVY] * vxl; fr[IVY] = wri[IDN] * wri[IVY] * vxr;
+  fl[IVZ] = wli[IDN] * wli[IVZ] * vxl; fr[IVZ] = wri[IDN] * wri[IVZ] * vxr;
+  fl[IVX] += wli[IPR]; fr[IVX] += wri[IPR];
+  fl[IEN] = el * vxl + wli[IPR] * wli[IVX];
+  fr[IEN] = er * vxr + wri[IPR] * wri[IVX];
+  T tmp = T(0.0);
+  if (bp != bm) tmp = T(0.5) * (bp + bm) / (bp - bm);
+#pragma unroll
+  for (int n = 0; n < 5; ++n) flxi[n] = T(0.5) * (fl[n] + fr[n]) + (fl[n] - fr[n]) * tmp;
+}
+
+// HLLE for adiabatic MHD (hydro/rsolvers/mhd/hlle_mhd.cpp:60-163)
+template <typename T>
+__device__ __forceinline__ void rs_hlle_mhd(const T* wli, const T* wri, T bxi, T gamma,
+                                            T* flxi) {
+  const T gm1 = gamma - T(1.0);
+  T sqrtdl = sqrt(wli[IDN]), sqrtdr = sqrt(wri[IDN]);
+  T isdlpdr = T(1.0) / (sqrtdl + sqrtdr);
+  T rd = sqrtdl * sqrtdr;
+  T rvx = (sqrtdl * wli[IVX] + sqrtdr * wri[IVX]) * isdlpdr;
+  T rvy = (sqrtdl * wli[IVY] + sqrtdr * wri[IVY]) * isdlpdr;
+  T rvz = (sqrtdl * wli[IVZ] + sqrtdr * wri[IVZ]) * isdlpdr;
+  T rby = (sqrtdr * wli[IBY] + sqrtdl * wri[IBY]) * isdlpdr;
+  T rbz = (sqrtdr * wli[IBZ] + sqrtdl * wri[IBZ]) * isdlpdr;
+  T x = T(0.5) * (sq(wli[IBY] - wri[IBY]) + sq(wli[IBZ] - wri[IBZ])) / (sq(sqrtdl + sqrtdr));
+  T y = T(0.5) * (wli[IDN] + wri[IDN]) / rd;
+  T pbl = T(0.5) * (bxi * bxi + sq(wli[IBY]) + sq(wli[IBZ]));
+  T pbr = T(0.5) * (bxi * bxi + sq(wri[IBY]) + sq(wri[IBZ]));
+  T el = wli[IPR] / gm1 + T(0.5) * wli[IDN] * (sq(wli[IVX]) + sq(wli[IVY]) + sq(wli[IVZ])) + pbl;
+  T er = wri[IPR] / gm1 + T(0.5) * wri[IDN] * (sq(wri[IVX]) + sq(wri[IVY]) + sq(wri[IVZ])) + pbr;
+  T hroe = ((el + wli[IPR] + pbl) / sqrtdl + (er + wri[IPR] + pbr) / sqrtdr) * isdlpdr;
+  T cl = fast_speed(wli[IDN], wli[IPR], wli[IBY], wli[IBZ], bxi, gamma);
+  T cr = fast_speed(wri[IDN], wri[IPR], wri[IBY], wri[IBZ], bxi, gamma);
+  T btsq = sq(rby) + sq(rbz);
+  T vaxsq = bxi * bxi / rd;
+  T bt_starsq = (gm1 - (gm1 - T(1.0)) * y) * btsq;
+  T hp = hroe - (vaxsq + btsq / rd);
+  T vsq = sq(rvx) + sq(rvy) + sq(rvz);
+  T twid_asq = mx((gm1 * (hp - T(0.5) * vsq) - (gm1 - T(1.0)) * x), T(0.0));
+  T ct2 = bt_starsq / rd;
+  T tsum = vaxsq + ct2 + twid_asq;
+  T tdif = vaxsq + ct2 - twid_asq;
+  T cf2_cs2 = sqrt(tdif * tdif + T(4.0) * twid_asq * ct2);
+  T cfsq = T(0.5) * (tsum + cf2_cs2);
+  T a = sqrt(cfsq);
+  T al = mn((rvx - a), (wli[IVX] - cl));
+  T ar = mx((rvx + a), (wri[IVX] + cr));
+  T bp = ar > T(0.0) ? ar : T(0.0);
+  T bm = al < T(0.0) ? al : T(0.0);
+  T vxl = wli[IVX] - bm, vxr = wri[IVX] - bp;
+  T fl[7], fr[7];
+  fl[IDN] = wli[IDN] * vxl; fr[IDN] = wri[IDN] * vxr;
+  fl[IVX] = wli[IDN] * wli[IVX] * vxl + pbl - sq(bxi);
+  fr[IVX] = wri[IDN] * wri[IVX] * vxr + pbr - sq(bxi);
+  fl[IVY] = wli[IDN] * wli[IVY] * vxl - bxi * wli[IBY];
+  fr[IVY] = wri[IDN] * wri[IVY] * vxr - bxi * wri[IBY];
+  fl[IVZ] = wli[IDN] * wli[IVZ] * vxl - bxi * wli[IBZ];
+  fr[IVZ] = wri[IDN] * wri[IVZ] * vxr - bxi * wri[IBZ];
+  fl[IVX] += wli[IPR]; fr[IVX] += wri[IPR];
+  fl[IEN] = el * vxl + wli[IVX] * (wli[IPR] + pbl - bxi * bxi);
+  fr[IEN] = er * vxr + wri[IVX] * (wri[IPR] + pbr - bxi * bxi);
+  fl[IEN] -= bxi * (wli[IBY] * wli[IVY] + wli[IBZ] * wli[IVZ]);
+  fr[IEN] -= bxi * (wri[IBY] * wri[IVY] + wri[IBZ] * wri[IVZ]);
+  fl[IBY] = wli[IBY] * vxl - bxi * wli[IVY];
+  fr[IBY] = wri[IBY] * vxr - bxi * wri[IVY];
+  fl[IBZ] = wli[IBZ] * vxl - bxi * wli[IVZ];
+  fr[IBZ] = wri[IBZ] * vxr - bxi * wri[IVZ];
+  T tmp = T(0.0);
+  if (bp != bm) tmp = T(0.5) * (bp + bm) / (bp - bm);
+#pragma unroll
+  for (int n = 0; n < 7; ++n) flxi[n] = T(0.5) * (fl[n] + fr[n]) + (fl[n] - fr[n]) * tmp;
+}
+
+template <typename T> struct C1D { T d, mx, my, mz, e, by, bz; };
+
+// HLLD, Miyoshi & Kusano (2005) five-wave solver (hydro/rsolvers/mhd/hlld.cpp:56-371)
+template <typename T>
+__device__ __forceinline__ void rs_hlld(const T* wli, const T* wri, T bxi, T gamma, T* flxi) {
+  const T SMALLN = T(1.0e-8);
+  const T igm1 = T(1.0) / (gamma - T(1.0));
+  C1D<T> ul, ur, ulst, uldst, urdst, urst, fl, fr;
+  T spd[5];
+  T bxsq = bxi * bxi;
+  T pbl = T(0.5) * (bxsq + (sq(wli[IBY]) + sq(wli[IBZ])));
+  T pbr = T(0.5) * (bxsq + (sq(wri[IBY]) + sq(wri[IBZ])));
+  T kel = T(0.5) * wli[IDN] * (sq(wli[IVX]) + (sq(wli[IVY]) + sq(wli[IVZ])));
+  T ker = T(0.5) * wri[IDN] * (sq(wri[IVX]) + (sq(wri[IVY]) + sq(wri[IVZ])));
+  ul.d = wli[IDN]; ul.mx = wli[IVX] * ul.d; ul.my = wli[IVY] * ul.d; ul.mz = wli[IVZ] * ul.d;
+  ul.e = wli[IPR] * igm1 + kel + pbl; ul.by = wli[IBY]; ul.bz = wli[IBZ];
+  ur.d = wri[IDN]; ur.mx = wri[IVX] * ur.d; ur.my = wri[IVY] * ur.d; ur.mz = wri[IVZ] * ur.d;
+  ur.e = wri[IPR] * igm1 + ker + pbr; ur.by = wri[IBY]; ur.bz = wri[IBZ];
+  T cfl = fast_speed(wli[IDN], wli[IPR], wli[IBY], wli[IBZ], bxi, gamma);
+  T cfr = fast_speed(wri[IDN], wri[IPR], wri[IBY], wri[IBZ], bxi, gamma);
+  spd[0] = mn(wli[IVX] - cfl, wri[IVX] - cfr);
+  spd[4] = mx(wli[IVX] + cfl, wri[IVX] + cfr);
+  T ptl = wli[IPR] + pbl, ptr = wri[IPR] + pbr;
+  fl.d = ul.mx;
+  fl.mx = ul.mx * wli[IVX] + ptl - bxsq;
+  fl.my = ul.my * wli[IVX] - bxi * ul.by;
+  fl.mz = ul.mz * wli[IVX] - bxi * ul.bz;
+  fl.e = wli[IVX] * (ul.e + ptl - bxsq) - bxi * (wli[IVY] * ul.by + wli[IVZ] * ul.bz);
+  fl.by = ul.by * wli[IVX] - bxi * wli[IVY];
+  fl.bz = ul.bz * wli[IVX] - bxi * wli[IVZ];
+  fr.d = ur.mx;
+  fr.mx = ur.mx * wri[IVX] + ptr - bxsq;
+  fr.my = ur.my * wri[IVX] - bxi * ur.by;
+  fr.mz = ur.mz * wri[IVX] - bxi * ur.bz;
+  fr.e = wri[IVX] * (ur.e + ptr - bxsq) - bxi * (wri[IVY] * ur.by + wri[IVZ] * ur.bz);
+  fr.by = ur.by * wri[IVX] - bxi * wri[IVY];
+  fr.bz = ur.bz * wri[IVX] - bxi * wri[IVZ];
+  T sdl = spd[0] - wli[IVX], sdr = spd[4] - wri[IVX];
+  spd[2] = (sdr * ur.mx - sdl * ul.mx + (ptl - ptr)) / (sdr * ur.d - sdl * ul.d);
+  T sdml = spd[0] - spd[2], sdmr = spd[4] - spd[2];
+  T sdml_inv = T(1.0) / sdml, sdmr_inv = T(1.0) / sdmr;
+  ulst.d = ul.d * sdl * sdml_inv;
+  urst.d = ur.d * sdr * sdmr_inv;
+  T ulst_d_inv = T(1.0) / ulst.d, urst_d_inv = T(1.0) / urst.d;
+  T sqrtdl = sqrt(ulst.d), sqrtdr = sqrt(urst.d);
+  spd[1] = spd[2] - fabs(bxi) / sqrtdl;
+  spd[3] = spd[2] + fabs(bxi) / sqrtdr;
+  T ptstl = ptl + ul.d * sdl * (spd[2] - wli[IVX]);
+  T ptstr = ptr + ur.d * sdr * (spd[2] - wri[IVX]);
+  T ptst = T(0.5) * (ptstr + ptstl);
+  ulst.mx = ulst.d * spd[2];
+  if (fabs(ul.d * sdl * sdml - bxsq) < (SMALLN) * ptst) {
+    ulst.my = ulst.d * wli[IVY]; ulst.mz = ulst.d * wli[IVZ];
+    ulst.by = ul.by; ulst.bz = ul.bz;
+  } else {
+    T tmp = bxi * (sdl - sdml) / (ul.d * sdl * sdml - bxsq);
+    ulst.my = ulst.d * (wli[IVY] - ul.by * tmp);
+    ulst.mz = ulst.d * (wli[IVZ] - ul.bz * tmp);
+    tmp = (ul.d * sq(sdl) - bxsq) / (ul.d * sdl * sdml - bxsq);
+    ulst.by = ul.by * tmp; ulst.bz = ul.bz * tmp;
+  }
+  T vbstl = (ulst.mx * bxi + (ulst.my * ulst.by + ulst.mz * ulst.bz)) * ulst_d_inv;
+  ulst.e = (sdl * ul.e - ptl * wli[IVX] + ptst * spd[2] +
+            bxi * (wli[IVX] * bxi + (wli[IVY] * ul.by + wli[IVZ] * ul.bz) - vbstl)) * sdml_inv;
+  urst.mx = urst.d * spd[2];
+  if (fabs(ur.d * sdr * sdmr - bxsq) < (SMALLN) * ptst) {
+    urst.my = urst.d * wri[IVY]; urst.mz = urst.d * wri[IVZ];
+    urst.by = ur.by; urst.bz = ur.bz;
+  } else {
+    T tmp = bxi * (sdr - sdmr) / (ur.d * sdr * sdmr - bxsq);
+    urst.my = urst.d * (wri[IVY] - ur.by * tmp);
+    urst.mz = urst.d * (wri[IVZ] - ur.bz * tmp);
+    tmp = (ur.d * sq(sdr) - bxsq) / (ur.d * sdr * sdmr - bxsq);
+    urst.by = ur.by * tmp; urst.bz = ur.bz * tmp;
+  }
+  T vbstr = (urst.mx * bxi + (urst.my * urst.by + urst.mz * urst.bz)) * urst_d_inv;
+  urst.e = (sdr * ur.e - ptr * wri[IVX] + ptst * spd[2] +
+            bxi * (wri[IVX] * bxi + (wri[IVY] * ur.by + wri[IVZ] * ur.bz) - vbstr)) * sdmr_inv;
+  if (T(0.5) * bxsq < (SMALLN) * ptst) {
+    uldst = ulst; urdst = urst;
+  } else {
+    T invsumd = T(1.0) / (sqrtdl + sqrtdr);
+    T bxsig = (bxi > T(0.0) ? T(1.0) : T(-1.0));
+    uldst.d = ulst.d; urdst.d = urst.d;
+    uldst.mx = ulst.mx; urdst.mx = urst.mx;
+    T tmp = invsumd * (sqrtdl * (ulst.my * ulst_d_inv) + sqrtdr * (urst.my * urst_d_inv) +
+                       bxsig * (urst.by - ulst.by));
+    uldst.my = uldst.d * tmp; urdst.my = urdst.d * tmp;
+    tmp = invsumd * (sqrtdl * (ulst.mz * ulst_d_inv) + sqrtdr * (urst.mz * urst_d_inv) +
+                     bxsig * (urst.bz - ulst.bz));
+    uldst.mz = uldst.d * tmp; urdst.mz = urdst.d * tmp;
+    tmp = invsumd * (sqrtdl * urst.by + sqrtdr * ulst.by +
+                     bxsig * sqrtdl * sqrtdr * ((urst.my * urst_d_inv) - (ulst.my * ulst_d_inv)));
+    uldst.by = urdst.by = tmp;
+    tmp = invsumd * (sqrtdl * urst.bz + sqrtdr * ulst.bz +
+                     bxsig * sqrtdl * sqrtdr * ((urst.mz * urst_d_inv) - (ulst.mz * ulst_d_inv)));
+    uldst.bz = urdst.bz = tmp;
+    tmp = spd[2] * bxi + (uldst.my * uldst.by + uldst.mz * uldst.bz) / uldst.d;
+    uldst.e = ulst.e - sqrtdl * bxsig * (vbstl - tmp);
+    urdst.e = urst.e + sqrtdr * bxsig * (vbstr - tmp);
+  }
+  // Select the region of the fan that contains x/t = 0; differences of the
+  // intermediate states scaled by the wave speeds are only formed where needed.
+  auto dif = [](const C1D<T>& a, const C1D<T>& b, T s, T* o) {
+    o[0] = s * (a.d - b.d); o[1] = s * (a.mx - b.mx); o[2] = s * (a.my - b.my);
+    o[3] = s * (a.mz - b.mz); o[4] = s * (a.e - b.e); o[5] = s * (a.by - b.by);
+    o[6] = s * (a.bz - b.bz);
+  };
+  T t0[7], t1[7];
+  if (spd[0] >= T(0.0)) {
+    flxi[IDN] = fl.d; flxi[IVX] = fl.mx; flxi[IVY] = fl.my; flxi[IVZ] = fl.mz;
+    flxi[IEN] = fl.e; flxi[IBY] = fl.by; flxi[IBZ] = fl.bz;
+  } else if (spd[4] <= T(0.0)) {
+    flxi[IDN] = fr.d; flxi[IVX] = fr.mx; flxi[IVY] = fr.my; flxi[IVZ] = fr.mz;
+    flxi[IEN] = fr.e; flxi[IBY] = fr.by; flxi[IBZ] = fr.bz;
+  } else if (spd[1] >= T(0.0)) {
+    dif(ulst, ul, spd[0], t0);
+    flxi[IDN] = fl.d + t0[0]; flxi[IVX] = fl.mx + t0[1]; flxi[IVY] = fl.my + t0[2];
+    flxi[IVZ] = fl.mz + t0[3]; flxi[IEN] = fl.e + t0[4]; flxi[IBY] = fl.by + t0[5];
+    flxi[IBZ] = fl.bz + t0[6];
+  } else if (spd[2] >= T(0.0)) {
+    dif(ulst, ul, spd[0], t0);
+    dif(uldst, ulst, spd[1], t1);
+    flxi[IDN] = fl.d + t0[0] + t1[0]; flxi[IVX] = fl.mx + t0[1] + t1[1];
+    flxi[IVY] = fl.my + t0[2] + t1[2]; flxi[IVZ] = fl.mz + t0[3] + t1[3];
+    flxi[IEN] = fl.e + t0[4] + t1[4]; flxi[IBY] = fl.by + t0[5] + t1[5];
+    flxi[IBZ] = fl.bz + t0[6] + t1[6];
+  } else if (spd[3] > T(0.0)) {
+    dif(urst, ur, spd[4], t0);
+    dif(urdst, urst, spd[3], t1);
+    flxi[IDN] = fr.d + t0[0] + t1[0]; flxi[IVX] = fr.mx + t0[1] + t1[1];
+    flxi[IVY] = fr.my + t0[2] + t1[2]; flxi[IVZ] = fr.mz + t0[3] + t1[3];
+    flxi[IEN] = fr.e + t0[4] + t1[4]; flxi[IBY] = fr.by + t0[5] + t1[5];
+    flxi[IBZ] = fr.bz + t0[6] + t1[6];
+  } else {
+    dif(urst, ur, spd[4], t0);
+    flxi[IDN] = fr.d + t0[0]; flxi[IVX] = fr.mx + t0[1]; flxi[IVY] = fr.my + t0[2];
+    flxi[IVZ] = fr.mz + t0[3]; flxi[IEN] = fr.e + t0[4]; flxi[IBY] = fr.by + t0[5];
+    flxi[IBZ] = fr.bz + t0[6];
+  }
+}
+
+}  // namespace athg

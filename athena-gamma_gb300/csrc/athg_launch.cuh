@@ -1,0 +1,113 @@
+// athg_launch.cuh -- host-side launch sequences for one precision (T = double: plain
+// FP64 path, T = float: mixed path). Instantiated once per precision in
+// kernels_f64.cu (built without FMA contraction, so the FP64 path reproduces the
+// reference's arithmetic bit for bit) and kernels_f32.cu.
+#pragma once
+#include "athg_stage.cuh"
+
+namespace athg {
+
+inline Box make_box(int il, int iu, int jl, int ju, int kl, int ku) {
+  Box b;
+  b.il = il; b.jl = jl; b.kl = kl;
+  b.ni = iu - il + 1; b.nj = ju - jl + 1; b.nk = ku - kl + 1;
+  return b;
+}
+inline dim3 box_grid(const Box& b, int nblocks, int tpb) {
+  return dim3((unsigned)((b.ni * b.nj + tpb - 1) / tpb), (unsigned)b.nk, (unsigned)nblocks);
+}
+
+template <typename T>
+struct Launcher {
+  // Hydro::CalculateFluxes over every block: three directional sweeps.
+  static void fluxes(const Geom& g, const StagePtrs<T>& p, bool mhd, int solver, int order,
+                     const Phys& ph, cudaStream_t st);
+  // Field::ComputeCornerE over every block.
+  static void corner_emf(const Geom& g, const StagePtrs<T>& p, cudaStream_t st);
+  // IntegrateHydro + IntegrateField (register average, flux divergence, CT).
+  static void update(const Geom& g, const StagePtrs<T>& p, bool mhd, const StageW& sw,
+                     cudaStream_t st);
+  // EquationOfState::ConservedToPrimitive over interior and ghost cells.
+  static void c2p(const Geom& g, const StagePtrs<T>& p, bool mhd, const Phys& ph,
+                  cudaStream_t st);
+  // Hydro::NewBlockTimeStep over every block, reduced to one minimum.
+  static void block_dt(const Geom& g, const StagePtrs<T>& p, bool mhd, const Phys& ph,
+                       unsigned long long* dtmin, cudaStream_t st);
+};
+
+#ifdef ATHG_LAUNCH_IMPL
+template <typename T, int DIR, int ORDER>
+static void flux_dir(const Geom& g, const StagePtrs<T>& p, bool mhd, int solver,
+                     const Phys& ph, cudaStream_t st) {
+  int il = g.is, iu = g.ie, jl = g.js, ju = g.je, kl = g.ks, ku = g.ke;
+  if (DIR == 0) {
+    iu = g.ie + 1;
+    if (mhd) { jl = g.js - 1; ju = g.je + 1; kl = g.ks - 1; ku = g.ke + 1; }
+  } else if (DIR == 1) {
+    ju = g.je + 1; il = g.is - 1; iu = g.ie + 1;
+    if (mhd) { kl = g.ks - 1; ku = g.ke + 1; }
+  } else {
+    ku = g.ke + 1;
+    if (mhd) { il = g.is - 1; iu = g.ie + 1; jl = g.js - 1; ju = g.je + 1; }
+  }
+  Box b = make_box(il, iu, jl, ju, kl, ku);
+  dim3 grid = box_grid(b, g.nb, 128);
+  if (mhd) {
+    if (solver == HLLD) k_flux<T, DIR, ORDER, HLLD, true><<<grid, 128, 0, st>>>(g, p, b, ph);
+    else k_flux<T, DIR, ORDER, HLLE, true><<<grid, 128, 0, st>>>(g, p, b, ph);
+  } else {
+    if (solver == HLLC) k_flux<T, DIR, ORDER, HLLC, false><<<grid, 128, 0, st>>>(g, p, b, ph);
+    else k_flux<T, DIR, ORDER, HLLE, false><<<grid, 128, 0, st>>>(g, p, b, ph);
+  }
+}
+
+template <typename T>
+void Launcher<T>::fluxes(const Geom& g, const StagePtrs<T>& p, bool mhd, int solver,
+                         int order, const Phys& ph, cudaStream_t st) {
+  if (order == 1) {
+    flux_dir<T, 0, 1>(g, p, mhd, solver, ph, st);
+    flux_dir<T, 1, 1>(g, p, mhd, solver, ph, st);
+    flux_dir<T, 2, 1>(g, p, mhd, solver, ph, st);
+  } else {
+    flux_dir<T, 0, 2>(g, p, mhd, solver, ph, st);
+    flux_dir<T, 1, 2>(g, p, mhd, solver, ph, st);
+    flux_dir<T, 2, 2>(g, p, mhd, solver, ph, st);
+  }
+}
+
+template <typename T>
+void Launcher<T>::corner_emf(const Geom& g, const StagePtrs<T>& p, cudaStream_t st) {
+  Box b = make_box(g.is, g.ie + 1, g.js, g.je + 1, g.ks, g.ke + 1);
+  k_corner_emf<T><<<box_grid(b, g.nb, 128), 128, 0, st>>>(g, p, b);
+}
+
+template <typename T>
+void Launcher<T>::update(const Geom& g, const StagePtrs<T>& p, bool mhd, const StageW& sw,
+                         cudaStream_t st) {
+  Box b = mhd ? make_box(g.is, g.ie + 1, g.js, g.je + 1, g.ks, g.ke + 1)
+              : make_box(g.is, g.ie, g.js, g.je, g.ks, g.ke);
+  if (mhd) k_update<T, true><<<box_grid(b, g.nb, 128), 128, 0, st>>>(g, p, b, sw);
+  else k_update<T, false><<<box_grid(b, g.nb, 128), 128, 0, st>>>(g, p, b, sw);
+}
+
+template <typename T>
+void Launcher<T>::c2p(const Geom& g, const StagePtrs<T>& p, bool mhd, const Phys& ph,
+                      cudaStream_t st) {
+  Box b = make_box(0, g.nc1 - 1, 0, g.nc2 - 1, 0, g.nc3 - 1);
+  if (mhd) k_c2p<T, true><<<box_grid(b, g.nb, 256), 256, 0, st>>>(g, p, b, ph);
+  else k_c2p<T, false><<<box_grid(b, g.nb, 256), 256, 0, st>>>(g, p, b, ph);
+}
+
+template <typename T>
+void Launcher<T>::block_dt(const Geom& g, const StagePtrs<T>& p, bool mhd, const Phys& ph,
+                           unsigned long long* dtmin, cudaStream_t st) {
+  Box b = make_box(g.is, g.ie, g.js, g.je, g.ks, g.ke);
+  if (mhd) k_block_dt<T, true><<<box_grid(b, g.nb, 256), 256, 0, st>>>(g, p, b, ph, dtmin);
+  else k_block_dt<T, false><<<box_grid(b, g.nb, 256), 256, 0, st>>>(g, p, b, ph, dtmin);
+}
+#endif  // ATHG_LAUNCH_IMPL
+
+extern template struct Launcher<double>;
+extern template struct Launcher<float>;
+
+}  // namespace athg

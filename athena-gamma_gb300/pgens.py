@@ -1,0 +1,234 @@
+"""Problem generators (initial states on a uniform mesh, interior cells and faces).
+
+Host-side counterparts of the reference's MeshBlock::ProblemGenerator hooks for the
+workloads of this path:
+  LinearWave    src/pgen/linear_wave.cpp (InitUserMeshData :76-186, ProblemGenerator
+                :464-575, eigenvectors of Stone et al. 2008 as coded at :626-1010, L1 error
+                of UserWorkAfterLoop :191-420)
+  orszag_tang   src/pgen/orszag_tang.cpp:42-115
+The arrays follow the reference layout (var, k, j, i) with i fastest; face fields are
+(nx3, nx2, nx1+1), (nx3, nx2+1, nx1), (nx3+1, nx2, nx1).
+"""
+import math
+
+import numpy as np
+
+TINY = 1.0e-20
+
+
+def _gen_rx(index, nrange):
+    noffset = index - nrange // 2
+    noffset_ceil = index - (nrange + 1) // 2
+    return (noffset + noffset_ceil) / (2.0 * nrange)
+
+
+def axis(nx, lo, hi):
+    """Face and centre positions of a single-block axis (mesh/mesh.hpp:389-488,
+    coordinates/coordinates.cpp:127-145, cartesian.cpp:29)."""
+    xf = np.array([0.5 * (lo + hi) + (_gen_rx(i, nx) * hi - _gen_rx(i, nx) * lo)
+                   for i in range(nx + 1)])
+    xf[0], xf[-1] = lo, hi
+    xv = 0.5 * (xf[1:] + xf[:-1])
+    dx = (hi - lo) / nx
+    return xf, xv, dx
+
+
+class LinearWave:
+    def __init__(self, nx, domain, mhd, gamma=1.666666666666667, amp=1.0e-6, wave_flag=0):
+        self.nx, self.domain, self.mhd, self.amp, self.wf = nx, domain, mhd, amp, wave_flag
+        self.gam = gamma
+        gm1 = gamma - 1.0
+        (x1a, x1b), (x2a, x2b), (x3a, x3b) = domain
+        x1size, x2size, x3size = x1b - x1a, x2b - x2a, x3b - x3a
+        ang_3 = math.atan(x1size / x2size)
+        self.sin_a3, self.cos_a3 = math.sin(ang_3), math.cos(ang_3)
+        ang_2 = math.atan(0.5 * (x1size * self.cos_a3 + x2size * self.sin_a3) / x3size)
+        self.sin_a2, self.cos_a2 = math.sin(ang_2), math.cos(ang_2)
+        x1 = x1size * self.cos_a2 * self.cos_a3
+        x2 = x2size * self.cos_a2 * self.sin_a3
+        x3 = x3size * self.sin_a2
+        lam = x1
+        if ang_3 != 0.0:
+            lam = min(lam, x2)
+        if ang_2 != 0.0:
+            lam = min(lam, x3)
+        self.k_par = 2.0 * math.pi / lam
+        self.lam = lam
+        d0, u0 = 1.0, 0.0
+        self.d0, self.u0 = d0, u0
+        self.bx0, self.by0, self.bz0 = 1.0, math.sqrt(2.0), 0.5
+        self.p0 = 1.0 / gamma
+        h0 = ((self.p0 / gm1 + 0.5 * d0 * (u0 * u0)) + self.p0) / d0
+        if mhd:
+            h0 += (self.bx0 ** 2 + self.by0 ** 2 + self.bz0 ** 2) / d0
+        self.rem, self.ev = self._right_eigvec(d0, u0, h0, gm1)
+
+    def _right_eigvec(self, d, v1, h, gm1):
+        """Column wave_flag(=0) of the right eigenmatrix (eq. B3 hydro, B21 MHD)."""
+        v2 = v3 = 0.0
+        vsq = v1 * v1 + v2 * v2 + v3 * v3
+        if not self.mhd:
+            asq = gm1 * max((h - 0.5 * vsq), TINY)
+            a = math.sqrt(asq)
+            return [1.0, v1 - a, v2, v3, h - v1 * a], v1 - a
+        x, y = 0.0, 1.0
+        b1, b2, b3 = self.bx0, self.by0, self.bz0
+        btsq = b2 * b2 + b3 * b3
+        bt_starsq = (gm1 - (gm1 - 1.0) * y) * btsq
+        vaxsq = b1 * b1 / d
+        hp = h - (vaxsq + btsq / d)
+        twid_asq = max((gm1 * (hp - 0.5 * vsq) - (gm1 - 1.0) * x), TINY)
+        ct2 = bt_starsq / d
+        tsum = vaxsq + ct2 + twid_asq
+        tdif = vaxsq + ct2 - twid_asq
+        cf2_cs2 = math.sqrt(tdif * tdif + 4.0 * twid_asq * ct2)
+        cfsq = 0.5 * (tsum + cf2_cs2)
+        cf = math.sqrt(cfsq)
+        cssq = twid_asq * vaxsq / cfsq
+        bt = math.sqrt(btsq)
+        bt_star = math.sqrt(bt_starsq)
+        bet2, bet3 = (1.0, 0.0) if bt == 0.0 else (b2 / bt, b3 / bt)
+        bet2_star = bet2 / math.sqrt(gm1 - (gm1 - 1.0) * y)
+        bet3_star = bet3 / math.sqrt(gm1 - (gm1 - 1.0) * y)
+        bet_starsq = bet2_star * bet2_star + bet3_star * bet3_star
+        vbet = v2 * bet2_star + v3 * bet3_star
+        if (cfsq - cssq) == 0.0:
+            alpha_f, alpha_s = 1.0, 0.0
+        elif (twid_asq - cssq) <= 0.0:
+            alpha_f, alpha_s = 0.0, 1.0
+        elif (cfsq - twid_asq) <= 0.0:
+            alpha_f, alpha_s = 1.0, 0.0
+        else:
+            alpha_f = math.sqrt((twid_asq - cssq) / (cfsq - cssq))
+            alpha_s = math.sqrt((cfsq - twid_asq) / (cfsq - cssq))
+        sqrtd = math.sqrt(d)
+        isqrtd = 1.0 / sqrtd
+        s = -1.0 if b1 < 0.0 else 1.0
+        twid_a = math.sqrt(twid_asq)
+        cs = math.sqrt(cssq)
+        qs = cs * alpha_s * s
+        as_prime = twid_a * alpha_s * isqrtd
+        aspbb = as_prime * bt_star * bet_starsq
+        ev0 = v1 - cf
+        col = [alpha_f, alpha_f * ev0, alpha_f * v2 + qs * bet2_star, alpha_f * v3 + qs * bet3_star,
+               alpha_f * (hp - v1 * cf) + qs * vbet + aspbb, as_prime * bet2_star,
+               as_prime * bet3_star]
+        return col, ev0
+
+    # ---------------------------------------------------------------------------------
+    def _axes(self):
+        nx1, nx2, nx3 = self.nx
+        (x1a, x1b), (x2a, x2b), (x3a, x3b) = self.domain
+        return axis(nx1, x1a, x1b), axis(nx2, x2a, x2b), axis(nx3, x3a, x3b)
+
+    def _cons_analytic(self):
+        """Cell-centre conserved state (and cell-centred B for MHD), :219-257."""
+        (x1f, x1v, dx1), (x2f, x2v, dx2), (x3f, x3v, dx3) = self._axes()
+        Z, Y, X = np.meshgrid(x3v, x2v, x1v, indexing="ij")
+        x = self.cos_a2 * (X * self.cos_a3 + Y * self.sin_a3) + Z * self.sin_a2
+        sn = np.sin(self.k_par * x)
+        amp, r = self.amp, self.rem
+        ca2, sa2, ca3, sa3 = self.cos_a2, self.sin_a2, self.cos_a3, self.sin_a3
+        d1 = self.d0 + amp * sn * r[0]
+        mx = self.d0 * 0.0 + amp * sn * r[1]
+        my = amp * sn * r[2]
+        mz = amp * sn * r[3]
+        u = np.empty((5,) + X.shape)
+        u[0] = d1
+        u[1] = mx * ca2 * ca3 - my * sa3 - mz * sa2 * ca3
+        u[2] = mx * ca2 * sa3 + my * ca3 - mz * sa2 * sa3
+        u[3] = mx * sa2 + mz * ca2
+        gm1 = self.gam - 1.0
+        e0 = self.p0 / gm1 + 0.5 * self.d0 * self.u0 * self.u0 + amp * sn * r[4]
+        bcc = None
+        if self.mhd:
+            e0 = e0 + 0.5 * (self.bx0 ** 2 + self.by0 ** 2 + self.bz0 ** 2)
+            bx = self.bx0
+            by = self.by0 + amp * sn * r[5]
+            bz = self.bz0 + amp * sn * r[6]
+            bcc = np.empty((3,) + X.shape)
+            bcc[0] = bx * ca2 * ca3 - by * sa3 - bz * sa2 * ca3
+            bcc[1] = bx * ca2 * sa3 + by * ca3 - bz * sa2 * sa3
+            bcc[2] = bx * sa2 + bz * ca2
+        u[4] = e0
+        return u, bcc
+
+    def _A(self, comp, x1, x2, x3):
+        """Vector potential components A1, A2, A3 (:588-624)."""
+        ca2, sa2, ca3, sa3 = self.cos_a2, self.sin_a2, self.cos_a3, self.sin_a3
+        kp = self.k_par
+        dby = self.amp * self.rem[5]
+        dbz = self.amp * self.rem[6]
+        x = x1 * ca2 * ca3 + x2 * ca2 * sa3 + x3 * sa2
+        y = -x1 * sa3 + x2 * ca3
+        Az = -self.by0 * x + (dby / kp) * np.cos(kp * (x)) + self.bx0 * y
+        if comp == 3:
+            return Az * ca2
+        Ay = self.bz0 * x - (dbz / kp) * np.cos(kp * (x))
+        if comp == 1:
+            return -Ay * sa3 - Az * sa2 * ca3
+        return Ay * ca3 - Az * sa2 * sa3
+
+    def initial_state(self):
+        """Interior conserved state and face fields as the reference pgen sets them."""
+        u, _ = self._cons_analytic()
+        if not self.mhd:
+            return u, None, None, None
+        (x1f, x1v, dx1), (x2f, x2v, dx2), (x3f, x3v, dx3) = self._axes()
+        # a1 on (x1v, x2f, x3f), a2 on (x1f, x2v, x3f), a3 on (x1f, x2f, x3v)
+        Z, Y, X = np.meshgrid(x3f, x2f, x1v, indexing="ij")
+        a1 = self._A(1, X, Y, Z)
+        Z, Y, X = np.meshgrid(x3f, x2v, x1f, indexing="ij")
+        a2 = self._A(2, X, Y, Z)
+        Z, Y, X = np.meshgrid(x3v, x2f, x1f, indexing="ij")
+        a3 = self._A(3, X, Y, Z)
+        b1 = (a3[:, 1:, :] - a3[:, :-1, :]) / dx2 - (a2[1:, :, :] - a2[:-1, :, :]) / dx3
+        b2 = (a1[1:, :, :] - a1[:-1, :, :]) / dx3 - (a3[:, :, 1:] - a3[:, :, :-1]) / dx1
+        b3 = (a2[:, :, 1:] - a2[:, :, :-1]) / dx1 - (a1[:, 1:, :] - a1[:, :-1, :]) / dx2
+        return u, np.ascontiguousarray(b1), np.ascontiguousarray(b2), np.ascontiguousarray(b3)
+
+    def l1_errors(self, u, b1=None, b2=None, b3=None):
+        """RMS of the per-variable L1 errors against the initial state (:298-372)."""
+        ua, bcca = self._cons_analytic()
+        (x1f, x1v, dx1), (x2f, x2v, dx2), (x3f, x3v, dx3) = self._axes()
+        vol = dx1 * dx2 * dx3
+        (x1a, x1b), (x2a, x2b), (x3a, x3b) = self.domain
+        vdom = (x1b - x1a) * (x2b - x2a) * (x3b - x3a)
+        l1 = [np.sum(np.abs(ua[n] - u[n]) * vol) / vdom for n in range(5)]
+        if self.mhd:
+            bc = [0.5 * b1[:, :, :-1] + 0.5 * b1[:, :, 1:], 0.5 * b2[:, :-1, :] + 0.5 * b2[:, 1:, :],
+                  0.5 * b3[:-1, :, :] + 0.5 * b3[1:, :, :]]
+            l1 += [np.sum(np.abs(bcca[n] - bc[n]) * vol) / vdom for n in range(3)]
+        rms = math.sqrt(sum(e * e for e in l1))
+        return rms, l1
+
+
+def orszag_tang(nx, domain=((-0.5, 0.5), (-0.5, 0.5), (-0.5, 0.5)), gamma=5.0 / 3.0):
+    """3-D (z-invariant) Orszag-Tang vortex from the vector potential
+    A_z = B0/(4 pi) (cos 4 pi x - 2 cos 2 pi y), src/pgen/orszag_tang.cpp:42-115."""
+    nx1, nx2, nx3 = nx
+    (x1f, x1v, dx1), (x2f, x2v, dx2), (x3f, x3v, dx3) = (
+        axis(nx1, *domain[0]), axis(nx2, *domain[1]), axis(nx3, *domain[2]))
+    PI = 3.1415926535897932
+    TWO_PI = 6.2831853071795862
+    gm1 = gamma - 1.0
+    B0 = 1.0 / math.sqrt(4.0 * PI)
+    d0 = 25.0 / (36.0 * PI)
+    v0 = 1.0
+    p0 = 5.0 / (12.0 * PI)
+    az = B0 / (4.0 * PI) * (np.cos(4.0 * PI * x1f)[None, :] - 2.0 * np.cos(TWO_PI * x2f)[:, None])
+    u = np.zeros((5, nx3, nx2, nx1))
+    u[0] = d0
+    u[1] = (d0 * v0 * np.sin(TWO_PI * x2v))[None, :, None]
+    u[2] = (-d0 * v0 * np.sin(TWO_PI * x1v))[None, None, :]
+    b1 = np.empty((nx3, nx2, nx1 + 1))
+    b1[:] = ((az[1:, :] - az[:-1, :]) / dx2)[None]
+    b2 = np.empty((nx3, nx2 + 1, nx1))
+    b2[:] = ((az[:, :-1] - az[:, 1:]) / dx1)[None]
+    b3 = np.zeros((nx3 + 1, nx2, nx1))
+    bc1 = 0.5 * (b1[:, :, :-1] + b1[:, :, 1:])
+    bc2 = 0.5 * (b2[:, :-1, :] + b2[:, 1:, :])
+    bc3 = 0.5 * (b3[:-1, :, :] + b3[1:, :, :])
+    u[4] = (p0 / gm1 + 0.5 * (bc1 ** 2 + bc2 ** 2 + bc3 ** 2)
+            + 0.5 * (u[1] ** 2 + u[2] ** 2 + u[3] ** 2) / u[0])
+    return u, b1, b2, b3

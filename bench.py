@@ -1,0 +1,295 @@
+#!/usr/bin/env python3
+"""Zone-cycles/s of the GB300 MHD stage update on the 256^3 Orszag-Tang vortex.
+
+Workload (the reference's C2 configuration): 3-D ideal MHD, 256^3 periodic cells on
+[-0.5,0.5]^3 as 64 MeshBlocks of 64^3, PLM + HLLD + constrained transport, VL2, CFL 0.4,
+gamma 5/3, Orszag-Tang initial state (z-invariant). One step = one full VL2 cycle (two
+stages + new dt). The headline is the mixed path (FP32 reconstruction/Riemann, FP64
+conserved state, face field and CT); the plain FP64 path is timed in the same run.
+
+    python bench.py [--steps K] [--warmup W] [--impl ours|reference]
+
+Rank 0 prints one JSON line. `--impl reference` times the CPU restatement of the
+reference's algorithm (the oracle port) on this host's cores on the same workload.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "athena-gamma_gb300"))
+
+NX = (256, 256, 256)
+MB = (64, 64, 64)
+CFL = 0.4
+BYTES_PER_ZC = 384  # VL2 MHD: 2 stages x (read 2 + write 1) x (40 B U + 24 B face B)
+METRIC = "zone-cycles/s"
+WORKLOAD = "orszag_tang_256^3_mhd_plm_hlld_vl2"
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """Samples nvidia-smi SM clocks and throttle reasons while the timed region runs."""
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index, self.rows, self.stop = index, [], threading.Event()
+        self.t = threading.Thread(target=self._run, daemon=True)
+
+    def _run(self):
+        while not self.stop.is_set():
+            try:
+                r = subprocess.run(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                    "--format=csv,noheader,nounits"], capture_output=True,
+                                   text=True, timeout=5)
+                if r.returncode == 0:
+                    self.rows.append([x.strip() for x in r.stdout.strip().split(",")])
+            except Exception:
+                pass
+            self.stop.wait(0.2)
+
+    def __enter__(self):
+        self.t.start()
+        return self
+
+    def __exit__(self, *a):
+        self.stop.set()
+        self.t.join(timeout=10)
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[q] for r in self.rows for q in range(4)
+                          if len(r) > 3 + q and r[3 + q].lower().startswith("active")})
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(self.rows)}
+
+
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), \
+        int(os.environ.get("LOCAL_RANK", 0))
+
+
+def cpu_reference(steps_cells, sample_cycles):
+    """Times the oracle port (FP64 CPU restatement) on this host's cores."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_lib as ol
+    import pgens
+    nx = steps_cells
+    u, b1, b2, b3 = pgens.orszag_tang(nx)
+    o = ol.Oracle(nx, True, "hlld", cfl=CFL, domain=((-0.5, 0.5),) * 3)
+    o.load_interior(u, b1, b2, b3)
+    o.initialize(100.0)
+    t0 = time.perf_counter()
+    o.cycle(sample_cycles, 100.0)
+    el = time.perf_counter() - t0
+    zc = float(np.prod(nx)) * sample_cycles
+    return zc / el, ol.lib().orc_num_threads(), el
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    cycles = max(1, args.cpu_cycles)
+    vals = []
+    for _ in range(max(1, args.steps if args.steps <= 3 else 3)):
+        v, cores, _ = cpu_reference(NX, cycles)
+        vals.append(v)
+    v = float(np.median(vals))
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": METRIC, "n_gpus": args.gpus,
+            "steps": len(vals), "warmup": 0, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (Orszag-Tang initial state)",
+            "config": {"workload": WORKLOAD, "cells": list(NX), "meshblock": list(MB)},
+            "cpu_baseline": {"value": v, "unit": METRIC, "cores": cores, "kind": "port",
+                             "sample": "%d VL2 cycle(s) of the 256^3 Orszag-Tang update per "
+                                       "step, FP64 oracle port, OpenMP" % cycles},
+            "e2e": {"value": v, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def make_sim(athg, precision):
+    return athg.Sim(NX, MB, mhd=True, solver="hlld", precision=precision, cfl=CFL, tlim=1e30,
+                    domain=((-0.5, 0.5),) * 3)
+
+
+def timed_cycles(sim, torch, steps):
+    ext = torch.cuda.ExternalStream(sim.stream())
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    with torch.cuda.stream(ext):
+        s.record(ext)
+        sim.cycles(steps)
+        e.record(ext)
+    e.synchronize()
+    return s.elapsed_time(e) / 1e3
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-cycles", type=int, default=2)
+    ap.add_argument("--fp64-steps", type=int, default=6)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+    import athg
+    import pgens
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    u, b1, b2, b3 = pgens.orszag_tang(NX)
+    zones = float(np.prod(NX))
+
+    # ---------------- device-resident throughput, mixed (headline) and FP64 -------------
+    res = {}
+    for prec, steps in (("mixed", args.steps), ("fp64", args.fp64_steps)):
+        sim = make_sim(athg, prec)
+        sim.load_interior(u, b1, b2, b3)
+        sim.initialize()
+        sim.cycles(args.warmup)
+        sim.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+        clk = None
+        if prec == "mixed":
+            with ClockSampler(local) as cs:
+                el = timed_cycles(sim, torch, steps)
+            clk = cs.summary()
+        else:
+            el = timed_cycles(sim, torch, steps)
+        if world > 1:
+            t = torch.tensor([el], device="cuda")
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            el = float(t.item())
+        res[prec] = {"el": el, "steps": steps, "zcps": zones * steps * world / el,
+                     "launches": sim.launches_per_cycle(), "clocks": clk,
+                     "t": sim.get_time(), "divb": sim.max_div_b()}
+        sim.close()
+        del sim
+
+    # L1 deviation of the mixed path from the FP64 path after the same number of cycles
+    n_cmp = 4
+    devs = {}
+    for prec in ("mixed", "fp64"):
+        sim = make_sim(athg, prec)
+        sim.load_interior(u, b1, b2, b3)
+        sim.initialize()
+        sim.cycles(n_cmp)
+        devs[prec] = sim.interior()
+        sim.close()
+    l1_dev = float(np.mean(np.abs(devs["mixed"]["u"][0] - devs["fp64"]["u"][0])))
+    l1_rel = l1_dev / float(np.mean(np.abs(devs["fp64"]["u"][0])))
+
+    # ---------------- end to end through the C ABI with host buffers ----------------
+    sim = make_sim(athg, "mixed")
+    sim.load_interior(u, b1, b2, b3)
+    blocks = {v: sim.download(v) for v in (athg.VAR_CONS, athg.VAR_B1F, athg.VAR_B2F, athg.VAR_B3F)}
+    pinned = {v: torch.from_numpy(a).pin_memory() for v, a in blocks.items()}
+    outbuf = {v: torch.empty_like(t).pin_memory() for v, t in pinned.items()}
+    import ctypes as C
+    L = athg.lib()
+
+    def e2e_run(k):
+        for v, t in pinned.items():
+            athg.check(L.athg_upload(sim.h, -1, v, C.cast(t.data_ptr(), C.POINTER(C.c_double)),
+                                     t.numel()))
+        sim.initialize()
+        tt, dd, nn = C.c_double(), C.c_double(), C.c_int64()
+        for _ in range(k):
+            sim.cycles(1)
+            athg.check(L.athg_get_time(sim.h, C.byref(tt), C.byref(dd), C.byref(nn)))
+        for v, t in outbuf.items():
+            athg.check(L.athg_download(sim.h, -1, v, C.cast(t.data_ptr(), C.POINTER(C.c_double)),
+                                       t.numel()))
+
+    e2e_run(1)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    e2e_run(args.steps)
+    torch.cuda.synchronize()
+    e2e_el = time.perf_counter() - t0
+    state_bytes = sum(t.numel() * 8 for t in pinned.values())
+    sim.close()
+
+    # ---------------- CPU baseline (oracle port) ----------------
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        v, cores, el = cpu_reference(NX, args.cpu_cycles)
+        cpu = {"value": v, "unit": METRIC, "cores": cores, "kind": "port",
+               "sample": "%d VL2 cycles of the 256^3 Orszag-Tang update, FP64 oracle port "
+                         "(OpenMP), %.1f s" % (args.cpu_cycles, el)}
+
+    peak, peak_kind = peaks()
+    m = res["mixed"]
+    sec_per_cycle = m["el"] / m["steps"]
+    achieved = BYTES_PER_ZC * zones / sec_per_cycle / 1e9
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "traffic_ot256_mhd.json")
+    if os.path.exists(tpath):
+        with open(tpath) as f:
+            traffic = json.load(f).get("mixed_bytes_per_cycle")
+    line = {
+        "metric": METRIC, "value": m["zcps"], "unit": METRIC, "n_gpus": world,
+        "steps": m["steps"], "warmup": args.warmup, "ms_per_step": 1e3 * sec_per_cycle,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
+        "data": "synthetic (Orszag-Tang initial state, 256^3)",
+        "config": {"workload": WORKLOAD, "cells": list(NX), "meshblock": list(MB),
+                   "blocks": int(np.prod([a // b for a, b in zip(NX, MB)])),
+                   "precision": "mixed: FP32 reconstruction+Riemann, FP64 U/B/CT",
+                   "l2": "working set (~2.9 GB) far larger than L2; no flush needed",
+                   "parallelism": "replicas" if world > 1 else "1 GPU"},
+        "fp64": {"value": res["fp64"]["zcps"], "ms_per_step": 1e3 * res["fp64"]["el"] / res["fp64"]["steps"],
+                 "steps": res["fp64"]["steps"]},
+        "mixed_over_fp64": m["zcps"] / res["fp64"]["zcps"],
+        "l1_rho_mixed_vs_fp64": {"cycles": n_cmp, "abs": l1_dev, "rel": l1_rel},
+        "div_b_max": {"mixed": m["divb"], "fp64": res["fp64"]["divb"]},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": traffic,
+                     "note": "one launch = one captured VL2 cycle (graph); algorithmic bytes "
+                             "384 B/zone-cycle; peak %s" % peak_kind},
+        "cpu_baseline": cpu,
+        "e2e": {"value": zones * args.steps / e2e_el, "unit": METRIC,
+                "h2d_bytes_per_step": state_bytes / args.steps,
+                "d2h_bytes_per_step": state_bytes / args.steps + 24},
+        "gpu_launches": m["launches"] * m["steps"],
+        "clocks": m["clocks"],
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,152 @@
+/* athena_gb300.h -- C ABI of the GB300-native finite-volume (M)HD stage update and
+ * multigrid Poisson solve.
+ *
+ * Plain C: opaque handles, plain pointers and sizes, int status codes (0 = ok, <0 =
+ * error, message from athg_last_error()). No exceptions cross this boundary. All
+ * MeshBlock state lives in one device pool owned by the context; host code holds
+ * handles and exchanges arrays in the reference's AthenaArray layout (n,k,j,i), i
+ * fastest, ghosts included, so problem generators and outputs keep working.
+ *
+ * Every entry point names the reference interface it replaces (paths are relative to
+ * the reference's src/). The reference calls these per MeshBlock from its TaskList;
+ * here one call covers every block of the pool, stream-ordered on the context's CUDA
+ * stream. One host thread per context.
+ */
+#ifndef ATHENA_GB300_H_
+#define ATHENA_GB300_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ATHG_OK 0
+#define ATHG_ERR_ARG (-1)    /* invalid argument or unsupported configuration */
+#define ATHG_ERR_CUDA (-2)   /* CUDA runtime error */
+#define ATHG_ERR_STATE (-3)  /* call out of order (e.g. no blocks yet) */
+#define ATHG_ERR_DEVICE (-4) /* a kernel reported an error through the device error word */
+
+/* Riemann solvers (configure.py --flux) */
+enum { ATHG_HLLE = 0, ATHG_HLLC = 1, ATHG_HLLD = 2, ATHG_LHLLC = 3, ATHG_LHLLD = 4 };
+/* time integrators (<time> integrator) */
+enum { ATHG_VL2 = 0, ATHG_RK1 = 1, ATHG_RK2 = 2, ATHG_RK3 = 3 };
+/* arithmetic of reconstruction/Riemann fluxes: FP64, or FP32 with FP64 state + CT */
+enum { ATHG_FP64 = 0, ATHG_MIXED = 1 };
+/* arrays exchanged with the host, per block, AthenaArray layout with ghosts:
+ * CONS (5,nc3,nc2,nc1)  B1F (nc3,nc2,nc1+1)  B2F (nc3,nc2+1,nc1)  B3F (nc3+1,nc2,nc1)
+ * PRIM (5,nc3,nc2,nc1)  BCC (3,nc3,nc2,nc1)  PHI (nc3,nc2,nc1)   nc = nx + 2*nghost */
+enum {
+  ATHG_VAR_CONS = 0, ATHG_VAR_B1F = 1, ATHG_VAR_B2F = 2, ATHG_VAR_B3F = 3,
+  ATHG_VAR_PRIM = 4, ATHG_VAR_BCC = 5, ATHG_VAR_PHI = 6
+};
+
+typedef struct athg_ctx athg_ctx;
+
+/* Compile-time physics of the reference (configure.py, src/defs.hpp.in) plus the
+ * runtime keys of <time>/<hydro> the stage needs. */
+typedef struct {
+  int nx1, nx2, nx3;  /* MeshBlock interior size (<meshblock> nx1..nx3); same for all blocks */
+  int nghost;         /* NGHOST (2 for PLM, >= 3 for PPM) */
+  int magnetic;       /* MAGNETIC_FIELDS_ENABLED */
+  int rsolver;        /* ATHG_HLLE / ATHG_HLLC (hydro) / ATHG_HLLD (MHD) */
+  int xorder;         /* <time> xorder: 1 donor cell, 2 PLM, 3 PPM */
+  int integrator;     /* ATHG_VL2 / ATHG_RK1 / ATHG_RK2 / ATHG_RK3 */
+  int precision;      /* ATHG_FP64 or ATHG_MIXED */
+  double gamma;       /* <hydro> gamma */
+  double dfloor, pfloor; /* <hydro> dfloor, pfloor (default sqrt(1024*FLT_MIN)) */
+  double cfl_number;  /* <time> cfl_number, already limited to the integrator's limit */
+  double tlim;        /* <time> tlim: the last dt is clamped to reach it */
+} athg_config;
+
+/* One MeshBlock: reference MeshBlock::loc, block_size and the neighbour table of
+ * BoundaryBase (src/bvals/bvals_base.cpp). */
+typedef struct {
+  int64_t lx1, lx2, lx3;
+  int32_t level;
+  double dx1, dx2, dx3;          /* uniform cell widths (coordinates.cpp:127-145) */
+  const double *x1f, *x2f, *x3f; /* host arrays of face positions incl. ghosts, nc+1 each */
+  int32_t neighbor[27];          /* same-level neighbour block id, -1 if none; index
+                                    (ox3+1)*9 + (ox2+1)*3 + (ox1+1) */
+} athg_block;
+
+/* A uniform single-level mesh (<mesh> and <meshblock>), built the way the reference's
+ * Mesh constructor lays out a root grid (src/mesh/mesh.cpp:1664-1760 block sizes,
+ * src/coordinates/coordinates.cpp:88-150 face positions). */
+typedef struct {
+  int nx1, nx2, nx3;                         /* <mesh> nx1..nx3 */
+  double x1min, x1max, x2min, x2max, x3min, x3max;
+  int periodic[3];                           /* 1 if ix/ox bc are periodic on this axis */
+} athg_mesh;
+
+/* ---- context and pool ---------------------------------------------------------- */
+int athg_create(const athg_config* cfg, athg_ctx** out);
+int athg_destroy(athg_ctx* ctx);
+/* Replaces the per-block allocation of Hydro/Field/EOS (hydro/hydro.cpp:31,
+ * field/field.cpp, mesh/meshblock.cpp:47): allocates every block in one device pool. */
+int athg_set_blocks(athg_ctx* ctx, int nblocks, const athg_block* blocks);
+/* Builds the blocks of a uniform mesh (Mesh::Mesh block layout, SetBlockSizeAndBoundaries
+ * mesh/mesh.cpp:1668, Coordinates ctor) and calls athg_set_blocks. Blocks are ordered
+ * with lx1 fastest, then lx2, then lx3. */
+int athg_set_uniform_mesh(athg_ctx* ctx, const athg_mesh* mesh);
+int athg_num_blocks(const athg_ctx* ctx, int* nblocks);
+/* logical location of block b: out[0..3] = lx1, lx2, lx3, level */
+int athg_block_location(const athg_ctx* ctx, int block, int64_t* out);
+/* Number of doubles one block holds for var (see ATHG_VAR_*). */
+int athg_var_size(const athg_ctx* ctx, int var, size_t* count);
+/* Host <-> device copies of one block (block >= 0) or of all blocks back to back
+ * (block = -1). count is the number of doubles in host. */
+int athg_upload(athg_ctx* ctx, int block, int var, const double* host, size_t count);
+int athg_download(athg_ctx* ctx, int block, int var, double* host, size_t count);
+
+/* ---- the stage (TaskList) --------------------------------------------------------- */
+/* Tail of Mesh::Initialize (mesh/mesh.cpp:1405-1649): ghost exchange, W(U) over interior
+ * and ghosts, first NewBlockTimeStep and Mesh::NewTimeStep. */
+int athg_initialize(athg_ctx* ctx);
+/* One stage (1-based) of TimeIntegratorTaskList::DoTaskListOneStage
+ * (task_list/task_list.cpp:66) over every block: CalculateHydroFlux (donor cell on the
+ * first VL2 stage), CalculateEMF, IntegrateHydro, IntegrateField, ghost exchange,
+ * Primitives, and on the last stage NewBlockTimeStep (time_integrator.cpp:1460-2093). */
+int athg_stage(athg_ctx* ctx, int stage);
+/* main.cpp:478-485: time += dt, ncycle++, Mesh::NewTimeStep (mesh/mesh.cpp:1078). */
+int athg_end_cycle(athg_ctx* ctx);
+/* n whole cycles (all stages + athg_end_cycle) replayed from one captured CUDA graph;
+ * time, dt and ncycle stay on the device. */
+int athg_cycles(athg_ctx* ctx, int n);
+/* Current time, dt and cycle count (synchronises the context's stream). */
+int athg_get_time(athg_ctx* ctx, double* time, double* dt, int64_t* ncycle);
+int athg_set_time(athg_ctx* ctx, double time, double dt, int64_t ncycle);
+int athg_synchronize(athg_ctx* ctx);
+/* The context's CUDA stream (a cudaStream_t), for callers that time or order work. */
+int athg_stream(athg_ctx* ctx, void** stream);
+/* Kernel launches of one whole cycle (what athg_cycles replays per cycle). */
+int athg_launches_per_cycle(athg_ctx* ctx, int* n);
+
+/* ---- individual operators (each over every block) -------------------------------- */
+/* Hydro::CalculateFluxes(w, b, bcc, order) (hydro/hydro.hpp:72-73) */
+int athg_calculate_fluxes(athg_ctx* ctx, int order);
+/* Field::ComputeCornerE(w, bcc) (field/field.hpp:67) */
+int athg_compute_corner_e(athg_ctx* ctx);
+/* MeshBlock::WeightedAve + Hydro::AddFluxDivergence + Field::CT for stage `stage`
+ * (mesh/weighted_ave.cpp:33,238; hydro/hydro.hpp:67; field/field.hpp:65) */
+int athg_integrate(athg_ctx* ctx, int stage);
+/* BoundaryVariable::Send/ReceiveBoundaryBuffers for U and face B (bvals/bvals_var.cpp:212) */
+int athg_exchange_ghosts(athg_ctx* ctx);
+/* EquationOfState::ConservedToPrimitive (eos/eos.hpp:37-40) incl. cell-centred B */
+int athg_conserved_to_primitive(athg_ctx* ctx);
+/* Hydro::NewBlockTimeStep (hydro/hydro.hpp:66) reduced over all blocks: min CFL dt */
+int athg_new_block_dt(athg_ctx* ctx, double* dt_out);
+
+/* ---- diagnostics ------------------------------------------------------------------- */
+/* max over interior cells of |div B| * dx (the CT invariant) */
+int athg_max_div_b(athg_ctx* ctx, double* out);
+/* volume integrals of the 5 conserved variables over all interior cells (history) */
+int athg_sum_conserved(athg_ctx* ctx, double* out5);
+
+const char* athg_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* ATHENA_GB300_H_ */

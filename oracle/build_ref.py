@@ -56,6 +56,7 @@ CONFIGS = {
     "sphere_mg": ("harness:uniform_sphere.cpp", "hllc", False, 2, 2, False, None),
     "jeans_mg": ("jeans.cpp", "hllc", False, 2, 2, False, None),
     "sg_state_mhd_hlld": ("harness:load_state.cpp", "hlld", True, 2, 2, False, None),
+    "sg_state_hydro": ("harness:load_state.cpp", "hllc", False, 2, 2, False, None),
 }
 
 

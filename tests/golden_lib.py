@@ -1,0 +1,24 @@
+"""Loading of the golden fixtures made by tests/golden/make_golden.py."""
+import glob
+import json
+import os
+
+import numpy as np
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def cases():
+    return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "*.npz")))
+
+
+def load(name):
+    z = np.load(os.path.join(GOLDEN, name + ".npz"))
+    meta = json.loads(str(z["meta"]))
+    arr = {k: z[k] for k in z.files if k != "meta"}
+    return meta, arr
+
+
+def linear_wave_errors():
+    with open(os.path.join(GOLDEN, "linear_wave_errors.json")) as f:
+        return json.load(f)

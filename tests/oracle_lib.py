@@ -29,14 +29,26 @@ class OrcParams(C.Structure):
                 ("x2max", C.c_double), ("x3min", C.c_double), ("x3max", C.c_double)]
 
 
+class MgParams(C.Structure):
+    _fields_ = [("lmax", C.c_int), ("xmin", C.c_double * 3), ("xmax", C.c_double * 3),
+                ("bc", C.c_int * 6), ("mporder", C.c_int), ("autompo", C.c_int),
+                ("nodipole", C.c_int), ("mporigin", C.c_double * 3), ("fmg", C.c_int),
+                ("eps", C.c_double), ("niter", C.c_int), ("omega", C.c_double)]
+
+
+MG_BC = {"periodic": 0, "zerograd": 1, "zerofixed": 2, "multipole": 3}
+
+
 def build_oracle(force=False):
     """Compile the oracle with the flags that keep its FP64 arithmetic reproducible."""
     src = os.path.join(ORACLE_DIR, "athena_oracle.c")
     if (not force and os.path.exists(LIB_PATH)
-            and os.path.getmtime(LIB_PATH) > os.path.getmtime(src)):
+            and os.path.getmtime(LIB_PATH) > max(os.path.getmtime(src), os.path.getmtime(
+                os.path.join(ORACLE_DIR, "mg_oracle.c")))):
         return LIB_PATH
+    srcs = [src, os.path.join(ORACLE_DIR, "mg_oracle.c")]
     cmd = ["gcc", "-O3", "-std=c11", "-ffp-contract=off", "-fopenmp", "-fPIC", "-shared",
-           "-o", LIB_PATH, src, "-lm"]
+           "-o", LIB_PATH] + srcs + ["-lm"]
     subprocess.run(cmd, check=True)
     return LIB_PATH
 
@@ -65,6 +77,22 @@ def lib():
         L.orc_get_time.restype = C.c_double
         L.orc_get_time.argtypes = [C.c_void_p]
         L.orc_num_threads.restype = C.c_int
+        L.orc_mg_create.restype = C.c_void_p
+        L.orc_mg_create.argtypes = [C.POINTER(MgParams)]
+        L.orc_mg_destroy.argtypes = [C.c_void_p]
+        L.orc_mg_u.restype = C.POINTER(C.c_double)
+        L.orc_mg_u.argtypes = [C.c_void_p]
+        L.orc_mg_src.restype = C.POINTER(C.c_double)
+        L.orc_mg_src.argtypes = [C.c_void_p]
+        L.orc_mg_solve.argtypes = [C.c_void_p]
+        L.orc_mg_vcycles.argtypes = [C.c_void_p, C.c_int]
+        L.orc_mg_iterations.restype = C.c_int
+        L.orc_mg_iterations.argtypes = [C.c_void_p]
+        L.orc_mg_last_norm.restype = C.c_double
+        L.orc_mg_last_norm.argtypes = [C.c_void_p]
+        L.orc_mg_defect_norm.restype = C.c_double
+        L.orc_mg_defect_norm.argtypes = [C.c_void_p]
+        L.orc_mg_mpcoeff.argtypes = [C.c_void_p, C.POINTER(C.c_double)]
         _lib = L
     return _lib
 
@@ -174,6 +202,61 @@ class Oracle:
         return self.L.orc_get_time(self.s)
 
 
+class MgOracle:
+    """FP64 multigrid on a cubic N^3 mesh (N = 2^lmax), one ghost layer per level."""
+
+    def __init__(self, lmax, domain=((-0.5, 0.5),) * 3, bc="periodic", mporder=4, autompo=True,
+                 nodipole=False, mporigin=(0.0, 0.0, 0.0), fmg=True, eps=-1.0, niter=10):
+        self.L = lib()
+        p = MgParams()
+        p.lmax = lmax
+        for d in range(3):
+            p.xmin[d], p.xmax[d] = domain[d]
+            p.mporigin[d] = mporigin[d]
+        bcs = [bc] * 6 if isinstance(bc, str) else list(bc)
+        for f in range(6):
+            p.bc[f] = MG_BC[bcs[f]]
+        p.mporder, p.autompo, p.nodipole = mporder, int(autompo), int(nodipole)
+        p.fmg, p.eps, p.niter, p.omega = int(fmg), eps, niter, 1.15
+        self.p = p
+        self.m = self.L.orc_mg_create(C.byref(p))
+        self.n = 1 << lmax
+
+    def __del__(self):
+        try:
+            self.L.orc_mg_destroy(self.m)
+        except Exception:
+            pass
+
+    def _view(self, ptr):
+        nt = self.n + 2
+        return np.ctypeslib.as_array(ptr, shape=(nt, nt, nt))
+
+    @property
+    def u(self):
+        return self._view(self.L.orc_mg_u(self.m))
+
+    @property
+    def src(self):
+        return self._view(self.L.orc_mg_src(self.m))
+
+    def load_source(self, src_interior):
+        self.src[1:-1, 1:-1, 1:-1] = src_interior
+
+    def solve(self):
+        self.L.orc_mg_solve(self.m)
+        return self.L.orc_mg_iterations(self.m), self.L.orc_mg_last_norm(self.m)
+
+    def vcycles(self, n):
+        self.L.orc_mg_vcycles(self.m, n)
+
+    def defect_norm(self):
+        return self.L.orc_mg_defect_norm(self.m)
+
+    def phi(self):
+        return self.u[1:-1, 1:-1, 1:-1].copy()
+
+
 # ------------------------------------------------------------------ seeded states ----
 def smooth_random_state(nx, mhd, seed, amp=0.1, gamma=5.0 / 3.0):
     """A smooth, periodic, seeded state (a few random Fourier modes on a uniform
@@ -270,7 +353,8 @@ def read_state(path, nx, mhd, phi=False):
     return out
 
 
-def athinput_text(nx, mb, domain, cfl, tlim, nlim, gamma, xorder, integrator, extra=""):
+def athinput_text(nx, mb, domain, cfl, tlim, nlim, gamma, xorder, integrator, extra="",
+                  blocks="", mesh_bc="periodic"):
     (x1a, x1b), (x2a, x2b), (x3a, x3b) = domain
     return f"""<job>
 problem_id = st
@@ -285,18 +369,18 @@ ncycle_out = 100000
 nx1 = {nx[0]}
 x1min = {x1a!r}
 x1max = {x1b!r}
-ix1_bc = periodic
-ox1_bc = periodic
+ix1_bc = {mesh_bc}
+ox1_bc = {mesh_bc}
 nx2 = {nx[1]}
 x2min = {x2a!r}
 x2max = {x2b!r}
-ix2_bc = periodic
-ox2_bc = periodic
+ix2_bc = {mesh_bc}
+ox2_bc = {mesh_bc}
 nx3 = {nx[2]}
 x3min = {x3a!r}
 x3max = {x3b!r}
-ix3_bc = periodic
-ox3_bc = periodic
+ix3_bc = {mesh_bc}
+ox3_bc = {mesh_bc}
 <meshblock>
 nx1 = {mb[0]}
 nx2 = {mb[1]}
@@ -307,17 +391,20 @@ gamma = {gamma!r}
 state_in = state_in.bin
 state_out = state_out.bin
 {extra}
+{blocks}
 """
 
 
 def run_reference_state(exe, workdir, nx, mb, mhd, u, b1, b2, b3, cfl, tlim, nlim,
                         gamma=5.0 / 3.0, xorder=2, integrator="vl2",
-                        domain=((0.0, 1.0), (0.0, 1.0), (0.0, 1.0)), extra="", phi=False):
+                        domain=((0.0, 1.0), (0.0, 1.0), (0.0, 1.0)), extra="", phi=False,
+                        blocks="", mesh_bc="periodic"):
     """Run the reference binary built with the load_state harness pgen."""
     os.makedirs(workdir, exist_ok=True)
     write_state(os.path.join(workdir, "state_in.bin"), u, b1, b2, b3)
     with open(os.path.join(workdir, "athinput.st"), "w") as f:
-        f.write(athinput_text(nx, mb, domain, cfl, tlim, nlim, gamma, xorder, integrator, extra))
+        f.write(athinput_text(nx, mb, domain, cfl, tlim, nlim, gamma, xorder, integrator, extra,
+                              blocks, mesh_bc))
     r = subprocess.run([exe, "-i", "athinput.st"], cwd=workdir, capture_output=True, text=True)
     if r.returncode != 0 or "FATAL" in r.stdout:
         raise RuntimeError("reference run failed:\n" + r.stdout[-2000:] + r.stderr[-2000:])
