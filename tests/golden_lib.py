@@ -8,8 +8,18 @@ import numpy as np
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
 
-def cases():
+def _all():
     return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "*.npz")))
+
+
+def cases():
+    """Stage-update fixtures (hydro/MHD)."""
+    return [c for c in _all() if not c.startswith("mg_")]
+
+
+def mg_cases():
+    """Multigrid fixtures."""
+    return [c for c in _all() if c.startswith("mg_")]
 
 
 def load(name):

@@ -5,7 +5,7 @@ import pytest
 import golden_lib
 import oracle_lib as ol
 
-MG_CASES = [c for c in golden_lib.cases() if c.startswith("mg_")]
+MG_CASES = golden_lib.mg_cases()
 
 
 @pytest.mark.parametrize("name", MG_CASES)
