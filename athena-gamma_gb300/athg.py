@@ -32,7 +32,20 @@ EXPORTS = [
     "athg_launches_per_cycle", "athg_calculate_fluxes", "athg_compute_corner_e",
     "athg_integrate", "athg_exchange_ghosts", "athg_conserved_to_primitive",
     "athg_new_block_dt", "athg_max_div_b", "athg_sum_conserved", "athg_last_error",
+    "athg_mg_create", "athg_mg_destroy", "athg_mg_load_source", "athg_mg_set_phi",
+    "athg_mg_solve", "athg_mg_vcycles", "athg_mg_defect_norm", "athg_mg_get_phi",
+    "athg_mg_stream", "athg_mg_multipole",
 ]
+MG_BC = {"periodic": 0, "zerograd": 1, "zerofixed": 2, "multipole": 3}
+
+
+class MgConfig(C.Structure):
+    _fields_ = [("nx", C.c_int), ("x1min", C.c_double), ("x1max", C.c_double),
+                ("x2min", C.c_double), ("x2max", C.c_double), ("x3min", C.c_double),
+                ("x3max", C.c_double), ("bc", C.c_int * 6), ("mporder", C.c_int),
+                ("auto_mporigin", C.c_int), ("nodipole", C.c_int), ("mporigin", C.c_double * 3),
+                ("mode", C.c_int), ("threshold", C.c_double), ("niteration", C.c_int),
+                ("precision", C.c_int)]
 
 
 class Config(C.Structure):
@@ -93,6 +106,16 @@ def lib():
         "athg_new_block_dt": [vp, C.POINTER(d)],
         "athg_max_div_b": [vp, C.POINTER(d)],
         "athg_sum_conserved": [vp, C.POINTER(d)],
+        "athg_mg_create": [C.POINTER(MgConfig), C.POINTER(vp)],
+        "athg_mg_destroy": [vp],
+        "athg_mg_load_source": [vp, C.POINTER(d), sz, d],
+        "athg_mg_set_phi": [vp, C.POINTER(d), sz],
+        "athg_mg_solve": [vp, C.POINTER(i), C.POINTER(d)],
+        "athg_mg_vcycles": [vp, i],
+        "athg_mg_defect_norm": [vp, C.POINTER(d)],
+        "athg_mg_get_phi": [vp, C.POINTER(d), sz],
+        "athg_mg_stream": [vp, C.POINTER(vp)],
+        "athg_mg_multipole": [vp, C.POINTER(d)],
     }
     for name, args in sig.items():
         f = getattr(L, name)
@@ -281,3 +304,74 @@ class Sim:
         v = C.c_double()
         check(lib().athg_new_block_dt(self.h, C.byref(v)))
         return v.value
+
+
+class Multigrid:
+    """Multigrid Poisson solver (lap phi = src) on a cubic mesh of nx^3 cells."""
+
+    def __init__(self, nx, domain=((-0.5, 0.5),) * 3, bc="periodic", mporder=4,
+                 auto_mporigin=True, nodipole=False, mporigin=(0.0, 0.0, 0.0), mode="FMG",
+                 threshold=-1.0, niteration=10, precision="fp64"):
+        L = lib()
+        c = MgConfig()
+        c.nx = nx
+        (c.x1min, c.x1max), (c.x2min, c.x2max), (c.x3min, c.x3max) = domain
+        bcs = [bc] * 6 if isinstance(bc, str) else list(bc)
+        for f in range(6):
+            c.bc[f] = MG_BC[bcs[f]]
+        c.mporder, c.auto_mporigin, c.nodipole = mporder, int(auto_mporigin), int(nodipole)
+        for q in range(3):
+            c.mporigin[q] = mporigin[q]
+        c.mode = 0 if mode.upper() == "FMG" else 1
+        c.threshold, c.niteration = threshold, niteration
+        c.precision = PRECISIONS[precision]
+        h = C.c_void_p()
+        check(L.athg_mg_create(C.byref(c), C.byref(h)))
+        self.h, self.nx, self.cfg = h, nx, c
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().athg_mg_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def load_source(self, rho, fac=1.0):
+        a = np.ascontiguousarray(rho, dtype=np.float64)
+        check(lib().athg_mg_load_source(self.h, _dptr(a), a.size, fac))
+
+    def set_phi(self, phi):
+        a = np.ascontiguousarray(phi, dtype=np.float64)
+        check(lib().athg_mg_set_phi(self.h, _dptr(a), a.size))
+
+    def solve(self):
+        it, nrm = C.c_int(), C.c_double()
+        check(lib().athg_mg_solve(self.h, C.byref(it), C.byref(nrm)))
+        return it.value, nrm.value
+
+    def vcycles(self, n):
+        check(lib().athg_mg_vcycles(self.h, n))
+
+    def defect_norm(self):
+        v = C.c_double()
+        check(lib().athg_mg_defect_norm(self.h, C.byref(v)))
+        return v.value
+
+    def phi(self):
+        a = np.empty((self.nx,) * 3)
+        check(lib().athg_mg_get_phi(self.h, _dptr(a), a.size))
+        return a
+
+    def stream(self):
+        s = C.c_void_p()
+        check(lib().athg_mg_stream(self.h, C.byref(s)))
+        return s.value
+
+    def multipole(self):
+        a = np.zeros(28)
+        check(lib().athg_mg_multipole(self.h, _dptr(a)))
+        return a

@@ -125,6 +125,10 @@ bool make_integrator(int id, Integrator* it) {
 
 }  // namespace
 
+namespace athg {
+void set_last_error(const std::string& s) { g_err = s; }
+}  // namespace athg
+
 struct athg_ctx {
   athg_config cfg{};
   Integrator integ{};

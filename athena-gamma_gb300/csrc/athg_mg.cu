@@ -1,0 +1,955 @@
+// athg_mg.cu -- multigrid Poisson solver on the GPU (C ABI in include/athena_gb300.h).
+//
+// A cubic mesh of N = 2^L cells per side is held as one device grid per level with one
+// ghost layer; on such a mesh the reference's per-MeshBlock levels plus its root grid
+// visit exactly these uniform levels (same stencils, colour parity, boundary fills,
+// coarsest solve), so one launch covers a whole level. Reference routines:
+//   smoother      gravity/mg_gravity.cpp:220-273     defect     :283-314
+//   FAS rhs       gravity/mg_gravity.cpp:324-351     restrict   multigrid/multigrid.cpp:684-725
+//   prolongation  multigrid/multigrid.cpp:733-832    FMG        :838-1048
+//   cycles        multigrid/multigrid_driver.cpp:553-823, FAS with multipole faces :292-295
+//   boundaries    bvals/cc/mg/bvals_mg.cpp:321-368, multigrid/mgbval_*.cpp
+//   multipoles    multigrid/multigrid.cpp:1054-1300, multigrid_driver.cpp:1909-2018
+//
+// FP64 path: the reference's algorithm in FP64 (built without FMA contraction).
+// Mixed path: FP32 FMG, then iterative refinement -- the FP64 defect of the FP64 solution
+// drives an FP32 V(1,1) cycle on the correction equation (homogeneous boundaries), and
+// the correction is accumulated in FP64 until the FP64 defect norm meets the threshold.
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "athena_gb300.h"
+
+namespace athg {
+// the error channel of athg_last_error() (defined in athg_api.cu)
+void set_last_error(const std::string& s);
+}
+
+namespace {
+
+int mgfail(int code, const std::string& msg) {
+  athg::set_last_error(msg);
+  return code;
+}
+#define MCK(call)                                                                    \
+  do {                                                                               \
+    cudaError_t e_ = (call);                                                         \
+    if (e_ != cudaSuccess)                                                           \
+      return mgfail(ATHG_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+#define MCKL()                                                                       \
+  do {                                                                               \
+    cudaError_t e_ = cudaGetLastError();                                             \
+    if (e_ != cudaSuccess)                                                           \
+      return mgfail(ATHG_ERR_CUDA, std::string("kernel launch: ") + cudaGetErrorString(e_)); \
+  } while (0)
+
+constexpr int TPB = 256;
+inline unsigned nblk(long long n) { return (unsigned)((n + TPB - 1) / TPB); }
+
+__host__ __device__ inline long long ix(int nt, int k, int j, int i) {
+  return ((long long)k * nt + j) * nt + i;
+}
+
+// ------------------------------------------------------------------------- kernels --
+// Red-black Gauss-Seidel half sweep: cells with (color + k + j + i - 1) even in the
+// reference's local indexing (i = is + c, is + c + 2, ...), one thread per updated cell.
+template <typename T>
+__global__ void k_smooth(T* __restrict__ u, const T* __restrict__ src, int n, T dx2, T isix,
+                         int color) {
+  const int nh = (n + 1) / 2;
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long)nh * n * n) return;
+  int ip = (int)(t % nh);
+  long long r = t / nh;
+  int j = (int)(r % n) + 1, k = (int)(r / n) + 1;
+  int c = (color + k + j) & 1;
+  int i = 1 + c + 2 * ip;
+  if (i > n) return;
+  const int nt = n + 2;
+  const long long q = ix(nt, k, j, i), sk = (long long)nt * nt, sj = nt;
+  u[q] -= ((T(6.0) * u[q] - u[q + sk] - u[q + sj] - u[q + 1] - u[q - sk] - u[q - sj] - u[q - 1]) +
+           src[q] * dx2) * isix;
+}
+
+// defect of the fine level averaged onto the coarse cell (CalculateDefect + Restrict);
+// with FAS the fine solution is restricted too (RestrictBlock).
+template <typename T>
+__global__ void k_defect_restrict(const T* __restrict__ uf, const T* __restrict__ sf,
+                                  T* __restrict__ sc, T* __restrict__ uc, int nc, T idx2, int fas) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long)nc * nc * nc) return;
+  int i = (int)(t % nc) + 1;
+  long long r = t / nc;
+  int j = (int)(r % nc) + 1, k = (int)(r / nc) + 1;
+  const int nf = 2 * nc, ntf = nf + 2, ntc = nc + 2;
+  const long long sk = (long long)ntf * ntf, sj = ntf;
+  const int fk = 2 * k - 1, fj = 2 * j - 1, fi = 2 * i - 1;
+  T d[8];
+  int q8 = 0;
+  for (int dk = 0; dk < 2; ++dk)
+    for (int dj = 0; dj < 2; ++dj)
+      for (int di = 0; di < 2; ++di) {
+        long long q = ix(ntf, fk + dk, fj + dj, fi + di);
+        d[q8++] = (T(6.0) * uf[q] - uf[q + sk] - uf[q + sj] - uf[q + 1] - uf[q - sk] - uf[q - sj] -
+                   uf[q - 1]) * idx2 + sf[q];
+      }
+  const long long qc = ix(ntc, k, j, i);
+  sc[qc] = T(0.125) * (d[0] + d[1] + d[2] + d[3] + d[4] + d[5] + d[6] + d[7]);
+  if (fas) {
+    auto U = [&](int a, int b, int c) { return uf[ix(ntf, fk + a, fj + b, fi + c)]; };
+    uc[qc] = T(0.125) * (U(0, 0, 0) + U(0, 0, 1) + U(0, 1, 0) + U(0, 1, 1) + U(1, 0, 0) +
+                         U(1, 0, 1) + U(1, 1, 0) + U(1, 1, 1));
+  }
+}
+
+// plain 8-cell average (RestrictFMGSource)
+template <typename T>
+__global__ void k_restrict(const T* __restrict__ f, T* __restrict__ c, int nc) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long)nc * nc * nc) return;
+  int i = (int)(t % nc) + 1;
+  long long r = t / nc;
+  int j = (int)(r % nc) + 1, k = (int)(r / nc) + 1;
+  const int ntf = 2 * nc + 2;
+  const int fk = 2 * k - 1, fj = 2 * j - 1, fi = 2 * i - 1;
+  auto F = [&](int a, int b, int cc) { return f[ix(ntf, fk + a, fj + b, fi + cc)]; };
+  c[ix(nc + 2, k, j, i)] = T(0.125) * (F(0, 0, 0) + F(0, 0, 1) + F(0, 1, 0) + F(0, 1, 1) +
+                                       F(1, 0, 0) + F(1, 0, 1) + F(1, 1, 0) + F(1, 1, 1));
+}
+
+// src -= L'(u) on the interior (CalculateFASRHS)
+template <typename T>
+__global__ void k_fas_rhs(const T* __restrict__ u, T* __restrict__ src, int n, T idx2) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long)n * n * n) return;
+  int i = (int)(t % n) + 1;
+  long long r = t / n;
+  int j = (int)(r % n) + 1, k = (int)(r / n) + 1;
+  const int nt = n + 2;
+  const long long q = ix(nt, k, j, i), sk = (long long)nt * nt, sj = nt;
+  src[q] -= (T(6.0) * u[q] - u[q + sk] - u[q + sj] - u[q + 1] - u[q - sk] - u[q - sj] - u[q - 1]) *
+            idx2;
+}
+
+// trilinear prolongation of the coarse correction, added to the fine level
+// (ProlongateAndCorrect); with FAS the correction is u_c - u_old_c.
+template <typename T>
+__global__ void k_prolong_correct(const T* __restrict__ uc, const T* __restrict__ uold,
+                                  T* __restrict__ uf, int nc) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long)nc * nc * nc) return;
+  int i = (int)(t % nc) + 1;
+  long long r = t / nc;
+  int j = (int)(r % nc) + 1, k = (int)(r / nc) + 1;
+  const int ntc = nc + 2, ntf = 2 * nc + 2;
+  auto S = [&](int kk, int jj, int ii) -> T {
+    long long q = ix(ntc, kk, jj, ii);
+    return uold ? T(uc[q] - uold[q]) : uc[q];
+  };
+  const int fk = 2 * (k - 1) + 1, fj = 2 * (j - 1) + 1, fi = 2 * (i - 1) + 1;
+  const T c0 = S(k, j, i);
+  for (int oz = 0; oz < 2; ++oz)
+    for (int oy = 0; oy < 2; ++oy)
+      for (int ox = 0; ox < 2; ++ox) {
+        const int dz = oz ? 1 : -1, dy = oy ? 1 : -1, dx = ox ? 1 : -1;
+        uf[ix(ntf, fk + oz, fj + oy, fi + ox)] +=
+            T(0.015625) * (T(27.0) * c0 + S(k + dz, j + dy, i + dx) +
+                           T(9.0) * (S(k, j, i + dx) + S(k, j + dy, i) + S(k + dz, j, i)) +
+                           T(3.0) * (S(k + dz, j + dy, i) + S(k + dz, j, i + dx) + S(k, j + dy, i + dx)));
+      }
+}
+
+// FMG prolongation: separable 1-D weights (5,30,-3)/32 per axis, 27 products summed in
+// the reference's order, divided by 32768 (FMGProlongate)
+template <typename T>
+__global__ void k_fmg_prolong(const T* __restrict__ uc, T* __restrict__ uf, int nc) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long)nc * nc * nc) return;
+  int i = (int)(t % nc) + 1;
+  long long r = t / nc;
+  int j = (int)(r % nc) + 1, k = (int)(r / nc) + 1;
+  const int ntc = nc + 2, ntf = 2 * nc + 2;
+  T s[27];
+  for (int a = 0; a < 3; ++a)
+    for (int b = 0; b < 3; ++b)
+      for (int c = 0; c < 3; ++c) s[(a * 3 + b) * 3 + c] = uc[ix(ntc, k - 1 + a, j - 1 + b, i - 1 + c)];
+  const T w0[3] = {T(5.0), T(30.0), T(-3.0)}, w1[3] = {T(-3.0), T(30.0), T(5.0)};
+  const int fk = 2 * (k - 1) + 1, fj = 2 * (j - 1) + 1, fi = 2 * (i - 1) + 1;
+  for (int oz = 0; oz < 2; ++oz)
+    for (int oy = 0; oy < 2; ++oy)
+      for (int ox = 0; ox < 2; ++ox) {
+        const T *wz = oz ? w1 : w0, *wy = oy ? w1 : w0, *wx = ox ? w1 : w0;
+        T acc = (wz[0] * wy[0] * wx[0]) * s[0];
+        for (int q = 1; q < 27; ++q) {
+          int a = q / 9, b = (q / 3) % 3, c = q % 3;
+          acc = acc + (wz[a] * wy[b] * wx[c]) * s[q];
+        }
+        uf[ix(ntf, fk + oz, fj + oy, fi + ox)] = acc / T(32768.0);
+      }
+}
+
+// periodic wrap of every ghost cell of the listed axes (one launch over the shell)
+template <typename T>
+__global__ void k_bc_wrap(T* a, int n, int px, int py, int pz) {
+  const int nt = n + 2;
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= 6LL * nt * nt) return;
+  int face = (int)(t / ((long long)nt * nt));
+  long long r = t % ((long long)nt * nt);
+  int p = (int)(r % nt), q = (int)(r / nt);
+  int i, j, k;
+  int ax = face >> 1, side = face & 1;
+  int g = side ? n + 1 : 0;
+  if (ax == 0) { i = g; j = p; k = q; } else if (ax == 1) { j = g; i = p; k = q; } else { k = g; i = p; j = q; }
+  int ii = i, jj = j, kk = k;
+  if (px) ii = i == 0 ? n : (i == n + 1 ? 1 : i);
+  if (py) jj = j == 0 ? n : (j == n + 1 ? 1 : j);
+  if (pz) kk = k == 0 ? n : (k == n + 1 ? 1 : k);
+  if (ii == i && jj == j && kk == k) return;
+  if (ii < 1 || ii > n || jj < 1 || jj > n || kk < 1 || kk > n) {
+    // still a ghost along a non-periodic axis: that face pass fills it
+    return;
+  }
+  a[ix(nt, k, j, i)] = a[ix(nt, kk, jj, ii)];
+}
+
+struct MpCoef {
+  double c[25];
+  double o[3];
+  int order;
+};
+
+__device__ double mp_phi(const MpCoef& m, double x, double y, double z) {
+  const double* c = m.c;
+  double x2 = x * x, y2 = y * y, z2 = z * z, xy = x * y, yz = y * z, zx = z * x;
+  double r2 = x2 + y2 + z2;
+  double ir2 = 1.0 / r2, ir1 = sqrt(ir2);
+  double ir3 = ir2 * ir1, ir5 = ir3 * ir2;
+  if (m.order == 2)
+    return ir1 * c[0] + ir3 * (c[1] * y + c[2] * z + c[3] * x) +
+           ir5 * (c[4] * xy + c[5] * yz + (3.0 * z2 - r2) * c[6] + c[7] * zx + c[8] * 0.5 * (x2 - y2));
+  double ir7 = ir5 * ir2, ir9 = ir7 * ir2;
+  double hx2my2 = 0.5 * (x2 - y2), x2mty2 = x2 - 3.0 * y2, tx2my2 = 3.0 * x2 - y2;
+  return ir1 * c[0] + ir3 * (c[1] * y + c[2] * z + c[3] * x) +
+         ir5 * (c[4] * xy + c[5] * yz + (3.0 * z2 - r2) * c[6] + c[7] * zx + c[8] * 0.5 * (x2 - y2)) +
+         ir7 * (y * tx2my2 * c[9] + x * x2mty2 * c[15] + xy * z * c[10] + z * hx2my2 * c[14] +
+                (5.0 * z2 - r2) * (y * c[11] + x * c[13]) + z * (z2 - 3.0 * r2) * c[12]) +
+         ir9 * (xy * hx2my2 * c[16] + 0.125 * (x2 * x2mty2 - y2 * tx2my2) * c[24] +
+                yz * tx2my2 * c[17] + zx * x2mty2 * c[23] +
+                (7.0 * z2 - r2) * (xy * c[18] + hx2my2 * c[22]) +
+                (7.0 * z2 - 3.0 * r2) * (yz * c[19] + zx * c[21]) +
+                (35.0 * z2 * z2 - 30.0 * z2 * r2 + 3.0 * r2 * r2) * c[20]);
+}
+
+// level coordinates (multigrid/multigrid.cpp:1321-1346)
+__device__ inline double xface(int i, int n, double lo, double hi) {
+  if (i == 1) return lo;
+  if (i == n + 1) return hi;
+  return lo + (i - 1) * ((hi - lo) / n);
+}
+__device__ inline double xcen(int i, int n, double lo, double hi) {
+  return 0.5 * (xface(i, n, lo, hi) + xface(i + 1, n, lo, hi));
+}
+
+struct FaceBC {
+  int type[2];          // inner, outer
+  int lo1, hi1, lo2, hi2;
+  double lo[3], hi[3];  // domain
+  int homogeneous;      // correction equation: multipole faces become zero-fixed
+};
+
+// one axis' two faces (bvals_mg.cpp:339-366 extents); a1 runs over the first
+// transverse axis (j for x1, i for x2 and x3), a2 over the second.
+template <typename T>
+__global__ void k_bc_face(T* a, int n, int dir, FaceBC f, MpCoef mp) {
+  const int n1 = f.hi1 - f.lo1 + 1, n2 = f.hi2 - f.lo2 + 1;
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= 2LL * n1 * n2) return;
+  int side = (int)(t / ((long long)n1 * n2));
+  long long r = t % ((long long)n1 * n2);
+  int a1 = f.lo1 + (int)(r % n1), a2 = f.lo2 + (int)(r / n1);
+  const int nt = n + 2;
+  int gi = side ? n + 1 : 0, si = side ? n : 1;
+  long long g, s;
+  double px, py, pz;
+  if (dir == 0) {
+    g = ix(nt, a2, a1, gi); s = ix(nt, a2, a1, si);
+    px = xface(side ? n + 1 : 1, n, f.lo[0], f.hi[0]);
+    py = xcen(a1, n, f.lo[1], f.hi[1]); pz = xcen(a2, n, f.lo[2], f.hi[2]);
+  } else if (dir == 1) {
+    g = ix(nt, a2, gi, a1); s = ix(nt, a2, si, a1);
+    px = xcen(a1, n, f.lo[0], f.hi[0]);
+    py = xface(side ? n + 1 : 1, n, f.lo[1], f.hi[1]); pz = xcen(a2, n, f.lo[2], f.hi[2]);
+  } else {
+    g = ix(nt, gi, a2, a1); s = ix(nt, si, a2, a1);
+    px = xcen(a1, n, f.lo[0], f.hi[0]); py = xcen(a2, n, f.lo[1], f.hi[1]);
+    pz = xface(side ? n + 1 : 1, n, f.lo[2], f.hi[2]);
+  }
+  const int bc = f.type[side];
+  if (bc == ATHG_MG_ZEROGRAD) a[g] = a[s];
+  else if (bc == ATHG_MG_ZEROFIXED || (bc == ATHG_MG_MULTIPOLE && f.homogeneous)) a[g] = -a[s];
+  else if (bc == ATHG_MG_MULTIPOLE)
+    a[g] = (T)(2.0 * mp_phi(mp, px - mp.o[0], py - mp.o[1], pz - mp.o[2]) - (double)a[s]);
+}
+
+// ---- reductions (FP64 accumulation) ----
+__device__ inline double warp_sum(double v) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+template <int NV>
+__device__ void block_add(double (&v)[NV], double* out) {
+  __shared__ double sh[NV][TPB / 32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (int q = 0; q < NV; ++q) {
+    double s = warp_sum(v[q]);
+    if (lane == 0) sh[q][w] = s;
+  }
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    for (int q = 0; q < NV; ++q) {
+      double s = (lane < TPB / 32) ? sh[q][lane] : 0.0;
+      s = warp_sum(s);
+      if (lane == 0) atomicAdd(out + q, s);
+    }
+  }
+}
+
+template <typename T>
+__global__ void k_sum(const T* a, int n, double* out) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  double v[1] = {0.0};
+  if (t < (long long)n * n * n) {
+    int i = (int)(t % n) + 1;
+    long long r = t / n;
+    int j = (int)(r % n) + 1, k = (int)(r / n) + 1;
+    v[0] = (double)a[ix(n + 2, k, j, i)];
+  }
+  block_add<1>(v, out);
+}
+
+template <typename T>
+__global__ void k_sub_const(T* a, long long cnt, const double* tot, double scale) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= cnt) return;
+  const double ave = (*tot) * scale;
+  a[t] -= (T)ave;
+}
+
+// sum of squared FP64 defects of the finest level
+__global__ void k_defect_sq(const double* u, const double* src, int n, double idx2, double* out) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  double v[1] = {0.0};
+  if (t < (long long)n * n * n) {
+    int i = (int)(t % n) + 1;
+    long long r = t / n;
+    int j = (int)(r % n) + 1, k = (int)(r / n) + 1;
+    const int nt = n + 2;
+    const long long q = ix(nt, k, j, i), sk = (long long)nt * nt, sj = nt;
+    double d = (6.0 * u[q] - u[q + sk] - u[q + sj] - u[q + 1] - u[q - sk] - u[q - sj] - u[q - 1]) *
+                   idx2 + src[q];
+    v[0] = d * d;
+  }
+  block_add<1>(v, out);
+}
+
+// FP64 defect of the FP64 solution, narrowed to the FP32 correction source
+__global__ void k_defect_to32(const double* u, const double* src, int n, double idx2, float* r32) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long)n * n * n) return;
+  int i = (int)(t % n) + 1;
+  long long r = t / n;
+  int j = (int)(r % n) + 1, k = (int)(r / n) + 1;
+  const int nt = n + 2;
+  const long long q = ix(nt, k, j, i), sk = (long long)nt * nt, sj = nt;
+  double d = (6.0 * u[q] - u[q + sk] - u[q + sj] - u[q + 1] - u[q - sk] - u[q - sj] - u[q - 1]) *
+                 idx2 + src[q];
+  r32[q] = (float)d;
+}
+
+__global__ void k_add_correction(double* u, const float* e, long long cnt) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < cnt) u[t] += (double)e[t];
+}
+__global__ void k_widen(const float* a, double* b, long long cnt) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < cnt) b[t] = (double)a[t];
+}
+__global__ void k_narrow(const double* a, float* b, long long cnt) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < cnt) b[t] = (float)a[t];
+}
+
+// multipole moments (and the centre of mass) of the finest source, FP64
+__global__ void k_com(const double* src, int n, double lo0, double hi0, double lo1, double hi1,
+                      double lo2, double hi2, double vol, double* out) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  double v[4] = {0, 0, 0, 0};
+  if (t < (long long)n * n * n) {
+    int i = (int)(t % n) + 1;
+    long long r = t / n;
+    int j = (int)(r % n) + 1, k = (int)(r / n) + 1;
+    double s = src[ix(n + 2, k, j, i)] * vol;
+    v[0] = s; v[1] = s * xcen(j, n, lo1, hi1); v[2] = s * xcen(k, n, lo2, hi2);
+    v[3] = s * xcen(i, n, lo0, hi0);
+  }
+  block_add<4>(v, out);
+}
+
+__global__ void k_moments(const double* src, int n, double lo0, double hi0, double lo1, double hi1,
+                          double lo2, double hi2, double vol, const double* origin, int order,
+                          int nodipole, double* out) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  double m[25];
+  for (int q = 0; q < 25; ++q) m[q] = 0.0;
+  if (t < (long long)n * n * n) {
+    int i = (int)(t % n) + 1;
+    long long r = t / n;
+    int j = (int)(r % n) + 1, k = (int)(r / n) + 1;
+    double z = xcen(k, n, lo2, hi2) - origin[2], z2 = z * z;
+    double y = xcen(j, n, lo1, hi1) - origin[1], y2 = y * y, yz = y * z;
+    double x = xcen(i, n, lo0, hi0) - origin[0];
+    double x2 = x * x, xy = x * y, zx = z * x;
+    double r2 = x2 + y2 + z2;
+    double s = src[ix(n + 2, k, j, i)] * vol;
+    m[0] = s;
+    if (!nodipole) { m[1] = s * y; m[2] = s * z; m[3] = s * x; }
+    m[4] = s * xy; m[5] = s * yz; m[6] = s * (3.0 * z2 - r2); m[7] = s * zx;
+    if (order == 4) {
+      double hx2my2 = 0.5 * (x2 - y2), x2mty2 = x2 - 3.0 * y2, tx2my2 = 3.0 * x2 - y2;
+      double fz2mr2 = 5.0 * z2 - r2, sz2mr2 = 7.0 * z2 - r2, sz2mtr2 = 7.0 * z2 - 3.0 * r2;
+      m[8] = s * hx2my2;
+      m[9] = s * y * tx2my2; m[10] = s * xy * z; m[11] = s * y * fz2mr2;
+      m[12] = s * z * (z2 - 3.0 * r2); m[13] = s * x * fz2mr2; m[14] = s * z * hx2my2;
+      m[15] = s * x * x2mty2; m[16] = s * xy * hx2my2; m[17] = s * yz * tx2my2;
+      m[18] = s * xy * sz2mr2; m[19] = s * yz * sz2mtr2;
+      m[20] = s * (35.0 * z2 * z2 - 30.0 * z2 * r2 + 3.0 * r2 * r2);
+      m[21] = s * zx * sz2mtr2; m[22] = s * hx2my2 * sz2mr2; m[23] = s * zx * x2mty2;
+      m[24] = s * 0.125 * (x2 * x2mty2 - y2 * tx2my2);
+    } else {
+      m[8] = s * 0.5 * (x2 - y2);
+    }
+  }
+  block_add<25>(m, out);
+}
+
+// --------------------------------------------------------------------- hierarchy --
+template <typename T>
+struct Hier {
+  int nl = 0;
+  std::vector<T*> u, src, uold;
+  std::vector<int> n;
+  std::vector<double> dx;
+  size_t cells(int L) const { return (size_t)(n[L] + 2) * (n[L] + 2) * (n[L] + 2); }
+};
+
+template <typename T>
+int alloc_hier(Hier<T>& h, int lmax, double rdx, bool with_old) {
+  h.nl = lmax + 1;
+  h.u.assign(h.nl, nullptr); h.src.assign(h.nl, nullptr); h.uold.assign(h.nl, nullptr);
+  h.n.resize(h.nl); h.dx.resize(h.nl);
+  for (int L = 0; L < h.nl; ++L) {
+    h.n[L] = 1 << L;
+    // finest width scaled by powers of two, as the reference does for coarser levels
+    h.dx[L] = rdx * (double)(1 << (lmax - L));
+    size_t c = h.cells(L);
+    MCK(cudaMalloc(&h.u[L], c * sizeof(T)));
+    MCK(cudaMalloc(&h.src[L], c * sizeof(T)));
+    MCK(cudaMemset(h.u[L], 0, c * sizeof(T)));
+    MCK(cudaMemset(h.src[L], 0, c * sizeof(T)));
+    if (with_old) {
+      MCK(cudaMalloc(&h.uold[L], c * sizeof(T)));
+      MCK(cudaMemset(h.uold[L], 0, c * sizeof(T)));
+    }
+  }
+  return ATHG_OK;
+}
+// only the finest level's u and src are allocated
+int alloc_top(Hier<double>& h, int lmax, double rdx) {
+  h.nl = lmax + 1;
+  h.u.assign(h.nl, nullptr); h.src.assign(h.nl, nullptr); h.uold.assign(h.nl, nullptr);
+  h.n.resize(h.nl); h.dx.resize(h.nl);
+  for (int L = 0; L < h.nl; ++L) {
+    h.n[L] = 1 << L;
+    h.dx[L] = rdx * (double)(1 << (lmax - L));
+  }
+  size_t c = h.cells(lmax);
+  MCK(cudaMalloc(&h.u[lmax], c * sizeof(double)));
+  MCK(cudaMalloc(&h.src[lmax], c * sizeof(double)));
+  MCK(cudaMemset(h.u[lmax], 0, c * sizeof(double)));
+  MCK(cudaMemset(h.src[lmax], 0, c * sizeof(double)));
+  return ATHG_OK;
+}
+
+template <typename T>
+void free_hier(Hier<T>& h) {
+  for (auto* p : h.u) if (p) cudaFree(p);
+  for (auto* p : h.src) if (p) cudaFree(p);
+  for (auto* p : h.uold) if (p) cudaFree(p);
+  h.u.clear(); h.src.clear(); h.uold.clear();
+}
+
+}  // namespace
+
+struct athg_mg {
+  athg_mg_config cfg{};
+  int lmax = 0;
+  bool periodic = true, subtract = true, fas = false, any_mp = false;
+  double rdx = 0.0, vol = 0.0;
+  cudaStream_t st = nullptr;
+  Hier<double> h64;      // FP64 path: all levels; mixed path: finest level only
+  Hier<float> h32;       // mixed path: FP32 hierarchy
+  double* red = nullptr; // reduction scratch [0..31]
+  double* mpo_d = nullptr;
+  MpCoef mp{};
+  int coffset = 0;       // colour offset, flipped at every V-cycle (multigrid_driver.cpp:686)
+  int coffset32 = 0;
+  int iterations = 0;
+  double last_norm = 0.0;
+};
+
+namespace {
+
+template <typename T>
+int apply_bc(athg_mg* m, Hier<T>& h, int L, bool homogeneous) {
+  const int n = h.n[L];
+  T* a = h.u[L];
+  const int* bc = m->cfg.bc;
+  int px = bc[0] == ATHG_MG_PERIODIC, py = bc[2] == ATHG_MG_PERIODIC, pz = bc[4] == ATHG_MG_PERIODIC;
+  const int nt = n + 2;
+  if (px || py || pz) {
+    k_bc_wrap<T><<<nblk(6LL * nt * nt), TPB, 0, m->st>>>(a, n, px, py, pz);
+    MCKL();
+  }
+  if (m->periodic) return ATHG_OK;
+  FaceBC f;
+  f.lo[0] = m->cfg.x1min; f.hi[0] = m->cfg.x1max;
+  f.lo[1] = m->cfg.x2min; f.hi[1] = m->cfg.x2max;
+  f.lo[2] = m->cfg.x3min; f.hi[2] = m->cfg.x3max;
+  f.homogeneous = homogeneous ? 1 : 0;
+  const int bjs = py ? 0 : 1, bje = py ? n + 1 : n, bks = pz ? 0 : 1, bke = pz ? n + 1 : n;
+  if (!px) {
+    f.type[0] = bc[0]; f.type[1] = bc[1];
+    f.lo1 = bjs; f.hi1 = bje; f.lo2 = bks; f.hi2 = bke;
+    k_bc_face<T><<<nblk(2LL * (bje - bjs + 1) * (bke - bks + 1)), TPB, 0, m->st>>>(a, n, 0, f, m->mp);
+    MCKL();
+  }
+  if (!py) {
+    f.type[0] = bc[2]; f.type[1] = bc[3];
+    f.lo1 = 0; f.hi1 = n + 1; f.lo2 = bks; f.hi2 = bke;
+    k_bc_face<T><<<nblk(2LL * (n + 2) * (bke - bks + 1)), TPB, 0, m->st>>>(a, n, 1, f, m->mp);
+    MCKL();
+  }
+  if (!pz) {
+    f.type[0] = bc[4]; f.type[1] = bc[5];
+    f.lo1 = 0; f.hi1 = n + 1; f.lo2 = 0; f.hi2 = n + 1;
+    k_bc_face<T><<<nblk(2LL * (n + 2) * (n + 2)), TPB, 0, m->st>>>(a, n, 2, f, m->mp);
+    MCKL();
+  }
+  return ATHG_OK;
+}
+
+template <typename T>
+int smooth(athg_mg* m, Hier<T>& h, int L, int color, int coff) {
+  const int n = h.n[L];
+  const double dx = h.dx[L];
+  const double isix = 1.15 / 6.0;
+  long long nth = (long long)((n + 1) / 2) * n * n;
+  k_smooth<T><<<nblk(nth), TPB, 0, m->st>>>(h.u[L], h.src[L], n, (T)(dx * dx), (T)isix,
+                                            color ^ coff);
+  MCKL();
+  return ATHG_OK;
+}
+
+template <typename T>
+int fas_rhs(athg_mg* m, Hier<T>& h, int L) {
+  const int n = h.n[L];
+  const double dx = h.dx[L];
+  k_fas_rhs<T><<<nblk((long long)n * n * n), TPB, 0, m->st>>>(h.u[L], h.src[L], n,
+                                                              (T)(1.0 / (dx * dx)));
+  MCKL();
+  return ATHG_OK;
+}
+
+template <typename T>
+int store_old(athg_mg* m, Hier<T>& h, int L) {
+  MCK(cudaMemcpyAsync(h.uold[L], h.u[L], h.cells(L) * sizeof(T), cudaMemcpyDeviceToDevice, m->st));
+  return ATHG_OK;
+}
+
+#define RC(x) do { int r_ = (x); if (r_) return r_; } while (0)
+
+// coarsest level (multigrid_driver.cpp:778-823, ni = 1 on a cubic power-of-two mesh)
+template <typename T>
+int coarsest(athg_mg* m, Hier<T>& h, bool fas, bool homog, bool subtract, int coff) {
+  if (subtract) {
+    if (fas) { RC(apply_bc(m, h, 0, homog)); RC(store_old(m, h, 0)); }
+    MCK(cudaMemsetAsync(h.u[0], 0, h.cells(0) * sizeof(T), m->st));
+    return ATHG_OK;
+  }
+  RC(apply_bc(m, h, 0, homog));
+  if (fas) { RC(store_old(m, h, 0)); RC(fas_rhs(m, h, 0)); }
+  RC(smooth(m, h, 0, 0, coff));
+  RC(apply_bc(m, h, 0, homog));
+  RC(smooth(m, h, 0, 1, coff));
+  RC(apply_bc(m, h, 0, homog));
+  return ATHG_OK;
+}
+
+// V(1,1) from level `top` (the current FMG level), multigrid_driver.cpp:684-694
+template <typename T>
+int vcycle(athg_mg* m, Hier<T>& h, int top, bool fas, bool homog, bool subtract, int& coffset) {
+  coffset ^= 1;
+  const int coff = coffset;
+  for (int L = top; L > 0; --L) {
+    RC(apply_bc(m, h, L, homog));
+    if (fas && L < top) { RC(store_old(m, h, L)); RC(fas_rhs(m, h, L)); }
+    RC(smooth(m, h, L, 0, coff));
+    RC(apply_bc(m, h, L, homog));
+    RC(smooth(m, h, L, 1, coff));
+    RC(apply_bc(m, h, L, homog));
+    const int nc = h.n[L - 1];
+    const double dx = h.dx[L];
+    k_defect_restrict<T><<<nblk((long long)nc * nc * nc), TPB, 0, m->st>>>(
+        h.u[L], h.src[L], h.src[L - 1], h.u[L - 1], nc, (T)(1.0 / (dx * dx)), fas ? 1 : 0);
+    MCKL();
+    if (!fas) MCK(cudaMemsetAsync(h.u[L - 1], 0, h.cells(L - 1) * sizeof(T), m->st));
+  }
+  RC(coarsest(m, h, fas, homog, subtract, coff));
+  for (int L = 0; L < top; ++L) {
+    RC(apply_bc(m, h, L, homog));
+    const int nc = h.n[L];
+    k_prolong_correct<T><<<nblk((long long)nc * nc * nc), TPB, 0, m->st>>>(
+        h.u[L], fas ? h.uold[L] : nullptr, h.u[L + 1], nc);
+    MCKL();
+    RC(apply_bc(m, h, L + 1, homog));
+    RC(smooth(m, h, L + 1, 0, coff));
+    RC(apply_bc(m, h, L + 1, homog));
+    RC(smooth(m, h, L + 1, 1, coff));
+  }
+  RC(apply_bc(m, h, top, homog));
+  return ATHG_OK;
+}
+
+template <typename T>
+int subtract_mean(athg_mg* m, Hier<T>& h, T* a, int L) {
+  const int n = h.n[L];
+  MCK(cudaMemsetAsync(m->red, 0, sizeof(double), m->st));
+  k_sum<T><<<nblk((long long)n * n * n), TPB, 0, m->st>>>(a, n, m->red);
+  MCKL();
+  const double dxl = h.dx[L];
+  // total = sum * dx^3 (Multigrid::CalculateTotal), average = total / volume
+  const double scale = dxl * dxl * dxl / m->vol;
+  k_sub_const<T><<<nblk((long long)h.cells(L)), TPB, 0, m->st>>>(a, (long long)h.cells(L), m->red,
+                                                                scale);
+  MCKL();
+  return ATHG_OK;
+}
+
+// FMG: source restriction through all levels, then V(1,1) at each level followed by
+// FMG prolongation (MultigridDriver::SolveFMGCycle)
+template <typename T>
+int fmg(athg_mg* m, Hier<T>& h, bool fas, bool subtract, int& coffset) {
+  const int top = h.nl - 1;
+  for (int L = top; L > 0; --L) {
+    const int nc = h.n[L - 1];
+    k_restrict<T><<<nblk((long long)nc * nc * nc), TPB, 0, m->st>>>(h.src[L], h.src[L - 1], nc);
+    MCKL();
+  }
+  for (int f = 0; f <= top; ++f) {
+    RC(vcycle(m, h, f, fas, false, subtract, coffset));
+    if (f != top) {
+      RC(apply_bc(m, h, f, false));
+      const int nc = h.n[f];
+      k_fmg_prolong<T><<<nblk((long long)nc * nc * nc), TPB, 0, m->st>>>(h.u[f], h.u[f + 1], nc);
+      MCKL();
+    }
+  }
+  return ATHG_OK;
+}
+
+int defect_norm64(athg_mg* m, double* out) {
+  Hier<double>& h = m->h64;
+  const int L = h.nl - 1, n = h.n[L];
+  RC(apply_bc(m, h, L, false));
+  MCK(cudaMemsetAsync(m->red, 0, sizeof(double), m->st));
+  const double dx = h.dx[L];
+  k_defect_sq<<<nblk((long long)n * n * n), TPB, 0, m->st>>>(h.u[L], h.src[L], n, 1.0 / (dx * dx),
+                                                             m->red);
+  MCKL();
+  double s;
+  MCK(cudaMemcpyAsync(&s, m->red, sizeof(double), cudaMemcpyDeviceToHost, m->st));
+  MCK(cudaStreamSynchronize(m->st));
+  // multigrid.cpp:594 (sum * dV), multigrid_driver.cpp:849-856 (/ volume, sqrt)
+  *out = std::sqrt(s * dx * dx * dx / m->vol);
+  return ATHG_OK;
+}
+
+int multipole_setup(athg_mg* m) {
+  Hier<double>& h = m->h64;
+  const int L = h.nl - 1, n = h.n[L];
+  const athg_mg_config& c = m->cfg;
+  // cell volume from the level's face positions (multigrid.cpp:1063-1064)
+  auto xf = [&](int i, double lo, double hi) {
+    return i == 1 ? lo : (i == n + 1 ? hi : lo + (i - 1) * ((hi - lo) / n));
+  };
+  double vol = (xf(2, c.x1min, c.x1max) - xf(1, c.x1min, c.x1max)) *
+               (xf(2, c.x2min, c.x2max) - xf(1, c.x2min, c.x2max)) *
+               (xf(2, c.x3min, c.x3max) - xf(1, c.x3min, c.x3max));
+  double origin[3] = {c.mporigin[0], c.mporigin[1], c.mporigin[2]};
+  if (c.auto_mporigin) {
+    MCK(cudaMemsetAsync(m->red, 0, 4 * sizeof(double), m->st));
+    k_com<<<nblk((long long)n * n * n), TPB, 0, m->st>>>(h.src[L], n, c.x1min, c.x1max, c.x2min,
+                                                         c.x2max, c.x3min, c.x3max, vol, m->red);
+    MCKL();
+    double s[4];
+    MCK(cudaMemcpyAsync(s, m->red, sizeof(s), cudaMemcpyDeviceToHost, m->st));
+    MCK(cudaStreamSynchronize(m->st));
+    double im = 1.0 / s[0];
+    origin[0] = im * s[3]; origin[1] = im * s[1]; origin[2] = im * s[2];
+  }
+  MCK(cudaMemcpyAsync(m->mpo_d, origin, sizeof(origin), cudaMemcpyHostToDevice, m->st));
+  MCK(cudaMemsetAsync(m->red, 0, 25 * sizeof(double), m->st));
+  k_moments<<<nblk((long long)n * n * n), TPB, 0, m->st>>>(h.src[L], n, c.x1min, c.x1max, c.x2min,
+                                                           c.x2max, c.x3min, c.x3max, vol, m->mpo_d,
+                                                           c.mporder, c.nodipole, m->red);
+  MCKL();
+  double mm[25];
+  MCK(cudaMemcpyAsync(mm, m->red, sizeof(mm), cudaMemcpyDeviceToHost, m->st));
+  MCK(cudaStreamSynchronize(m->st));
+  const double PI = 3.1415926535897932;
+  const double c0 = -0.25 / PI, c1 = -0.25 / PI, c2 = -0.0625 / PI, c2a = -0.75 / PI;
+  const double c30 = -0.0625 / PI, c31 = -0.0625 * 1.5 / PI, c32 = -0.25 * 15.0 / PI,
+               c33 = -0.0625 * 2.5 / PI;
+  const double c40 = -0.0625 * 0.0625 / PI, c41 = -0.0625 * 2.5 / PI, c42 = -0.0625 * 5.0 / PI,
+               c43 = -0.0625 * 17.5 / PI, c44 = -0.25 * 35.0 / PI;
+  const double sc[25] = {c0, c1, c1, c1, c2a, c2a, c2, c2a, c2a, c33, c32, c31, c30,
+                         c31, c32, c33, c44, c43, c42, c41, c40, c41, c42, c43, c44};
+  const int nc = c.mporder == 4 ? 25 : 9;
+  for (int q = 0; q < 25; ++q) m->mp.c[q] = q < nc ? mm[q] * sc[q] : 0.0;
+  for (int d = 0; d < 3; ++d) m->mp.o[d] = origin[d];
+  m->mp.order = c.mporder;
+  return ATHG_OK;
+}
+
+// mixed path: FP32 V-cycle on the correction equation for the current FP64 defect,
+// correction accumulated into the FP64 solution
+int refine_once(athg_mg* m) {
+  Hier<double>& H = m->h64;
+  Hier<float>& h = m->h32;
+  const int top = h.nl - 1, n = h.n[top];
+  RC(apply_bc(m, H, top, false));
+  const double dx = H.dx[top];
+  k_defect_to32<<<nblk((long long)n * n * n), TPB, 0, m->st>>>(H.u[top], H.src[top], n,
+                                                               1.0 / (dx * dx), h.src[top]);
+  MCKL();
+  MCK(cudaMemsetAsync(h.u[top], 0, h.cells(top) * sizeof(float), m->st));
+  RC(vcycle(m, h, top, false, true, m->subtract, m->coffset32));
+  k_add_correction<<<nblk((long long)h.cells(top)), TPB, 0, m->st>>>(H.u[top], h.u[top],
+                                                                     (long long)h.cells(top));
+  MCKL();
+  return ATHG_OK;
+}
+
+int one_cycle(athg_mg* m) {
+  const int top = m->lmax;
+  if (m->cfg.precision == ATHG_MIXED) return refine_once(m);
+  return vcycle(m, m->h64, top, m->fas, false, m->subtract, m->coffset);
+}
+
+}  // namespace
+
+extern "C" {
+
+int athg_mg_create(const athg_mg_config* cfg, athg_mg** out) {
+  if (!cfg || !out) return mgfail(ATHG_ERR_ARG, "null argument");
+  *out = nullptr;
+  int n = cfg->nx, lmax = 0;
+  if (n < 2 || (n & (n - 1)) != 0) return mgfail(ATHG_ERR_ARG, "nx must be a power of two >= 2");
+  if (n > 4096) return mgfail(ATHG_ERR_ARG, "nx too large");
+  while ((1 << lmax) < n) ++lmax;
+  for (int f = 0; f < 6; ++f)
+    if (cfg->bc[f] < ATHG_MG_PERIODIC || cfg->bc[f] > ATHG_MG_MULTIPOLE)
+      return mgfail(ATHG_ERR_ARG, "unknown multigrid boundary type");
+  for (int d = 0; d < 3; ++d)
+    if ((cfg->bc[2 * d] == ATHG_MG_PERIODIC) != (cfg->bc[2 * d + 1] == ATHG_MG_PERIODIC))
+      return mgfail(ATHG_ERR_ARG, "periodic boundaries must be set on both faces of an axis");
+  if (cfg->precision != ATHG_FP64 && cfg->precision != ATHG_MIXED)
+    return mgfail(ATHG_ERR_ARG, "precision must be ATHG_FP64 or ATHG_MIXED");
+  if (cfg->threshold < 0.0 && cfg->niteration < 0)
+    return mgfail(ATHG_ERR_ARG, "set a threshold >= 0 or niteration >= 0");
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+    return mgfail(ATHG_ERR_CUDA, "no CUDA device available");
+  athg_mg* m = new athg_mg();
+  m->cfg = *cfg;
+  m->lmax = lmax;
+  for (int f = 0; f < 6; ++f) {
+    if (cfg->bc[f] != ATHG_MG_PERIODIC) m->periodic = false;
+    if (cfg->bc[f] == ATHG_MG_MULTIPOLE) m->any_mp = true;
+  }
+  if (m->any_mp && cfg->mporder != 2 && cfg->mporder != 4) {
+    delete m;
+    return mgfail(ATHG_ERR_ARG, "mporder must be 2 or 4 with multipole boundaries");
+  }
+  // multigrid_driver.cpp:139-300: the mean source is removed unless a face is multipole,
+  // which switches on the full approximation scheme instead
+  m->subtract = !m->any_mp;
+  m->fas = m->any_mp;
+  m->rdx = (cfg->x1max - cfg->x1min) / (double)n;
+  m->vol = (cfg->x1max - cfg->x1min) * (cfg->x2max - cfg->x2min) * (cfg->x3max - cfg->x3min);
+  int rc;
+  if (cudaStreamCreateWithFlags(&m->st, cudaStreamNonBlocking) != cudaSuccess) {
+    delete m;
+    return mgfail(ATHG_ERR_CUDA, "cudaStreamCreate failed");
+  }
+  if (cfg->precision == ATHG_MIXED) {
+    // FP64 solution and source on the finest level only; FP32 hierarchy for the cycles
+    rc = alloc_top(m->h64, lmax, m->rdx);
+    if (!rc) rc = alloc_hier(m->h32, lmax, m->rdx, m->fas);
+  } else {
+    rc = alloc_hier(m->h64, lmax, m->rdx, m->fas);
+  }
+  if (!rc && cudaMalloc(&m->red, 32 * sizeof(double)) != cudaSuccess) rc = ATHG_ERR_CUDA;
+  if (!rc && cudaMalloc(&m->mpo_d, 4 * sizeof(double)) != cudaSuccess) rc = ATHG_ERR_CUDA;
+  if (rc) {
+    athg_mg_destroy(m);
+    return mgfail(ATHG_ERR_CUDA, "multigrid allocation failed");
+  }
+  *out = m;
+  return ATHG_OK;
+}
+
+int athg_mg_destroy(athg_mg* m) {
+  if (!m) return ATHG_OK;
+  free_hier(m->h64);
+  free_hier(m->h32);
+  if (m->red) cudaFree(m->red);
+  if (m->mpo_d) cudaFree(m->mpo_d);
+  if (m->st) cudaStreamDestroy(m->st);
+  delete m;
+  return ATHG_OK;
+}
+
+int athg_mg_load_source(athg_mg* m, const double* rho, size_t count, double fac) {
+  if (!m || !rho) return mgfail(ATHG_ERR_ARG, "null argument");
+  const int n = 1 << m->lmax, nt = n + 2;
+  if (count != (size_t)n * n * n) return mgfail(ATHG_ERR_ARG, "source size mismatch");
+  std::vector<double> full((size_t)nt * nt * nt, 0.0);
+  for (int k = 0; k < n; ++k)
+    for (int j = 0; j < n; ++j)
+      for (int i = 0; i < n; ++i)
+        full[ix(nt, k + 1, j + 1, i + 1)] =
+            (fac == 1.0) ? rho[((size_t)k * n + j) * n + i] : rho[((size_t)k * n + j) * n + i] * fac;
+  MCK(cudaMemcpyAsync(m->h64.src[m->lmax], full.data(), full.size() * 8, cudaMemcpyHostToDevice,
+                      m->st));
+  MCK(cudaStreamSynchronize(m->st));
+  return ATHG_OK;
+}
+
+int athg_mg_set_phi(athg_mg* m, const double* phi, size_t count) {
+  if (!m || !phi) return mgfail(ATHG_ERR_ARG, "null argument");
+  const int n = 1 << m->lmax, nt = n + 2;
+  if (count != (size_t)n * n * n) return mgfail(ATHG_ERR_ARG, "phi size mismatch");
+  std::vector<double> full((size_t)nt * nt * nt, 0.0);
+  for (int k = 0; k < n; ++k)
+    for (int j = 0; j < n; ++j)
+      for (int i = 0; i < n; ++i) full[ix(nt, k + 1, j + 1, i + 1)] = phi[((size_t)k * n + j) * n + i];
+  MCK(cudaMemcpyAsync(m->h64.u[m->lmax], full.data(), full.size() * 8, cudaMemcpyHostToDevice,
+                      m->st));
+  MCK(cudaStreamSynchronize(m->st));
+  return ATHG_OK;
+}
+
+int athg_mg_get_phi(athg_mg* m, double* phi, size_t count) {
+  if (!m || !phi) return mgfail(ATHG_ERR_ARG, "null argument");
+  const int n = 1 << m->lmax, nt = n + 2;
+  if (count != (size_t)n * n * n) return mgfail(ATHG_ERR_ARG, "phi size mismatch");
+  std::vector<double> full((size_t)nt * nt * nt);
+  MCK(cudaMemcpyAsync(full.data(), m->h64.u[m->lmax], full.size() * 8, cudaMemcpyDeviceToHost,
+                      m->st));
+  MCK(cudaStreamSynchronize(m->st));
+  for (int k = 0; k < n; ++k)
+    for (int j = 0; j < n; ++j)
+      for (int i = 0; i < n; ++i) phi[((size_t)k * n + j) * n + i] = full[ix(nt, k + 1, j + 1, i + 1)];
+  return ATHG_OK;
+}
+
+int athg_mg_solve(athg_mg* m, int* iterations, double* defect_norm) {
+  if (!m) return mgfail(ATHG_ERR_ARG, "null argument");
+  const int top = m->lmax;
+  Hier<double>& H = m->h64;
+  m->iterations = 0;
+  if (m->subtract) RC(subtract_mean(m, H, H.src[top], top));
+  if (m->any_mp) RC(multipole_setup(m));
+  if (m->cfg.mode == ATHG_MG_FMG) {
+    if (m->cfg.precision == ATHG_MIXED) {
+      Hier<float>& h = m->h32;
+      const long long c = (long long)h.cells(top);
+      k_narrow<<<nblk(c), TPB, 0, m->st>>>(H.src[top], h.src[top], c);
+      MCKL();
+      RC(fmg(m, h, m->fas, m->subtract, m->coffset32));
+      k_widen<<<nblk(c), TPB, 0, m->st>>>(h.u[top], H.u[top], c);
+      MCKL();
+    } else {
+      RC(fmg(m, H, m->fas, m->subtract, m->coffset));
+    }
+    if (m->subtract) RC(subtract_mean(m, H, H.u[top], top));
+  }
+  double def = 0.0;
+  if (m->cfg.threshold >= 0.0) {  // SolveIterative (multigrid_driver.cpp:721-760)
+    RC(defect_norm64(m, &def));
+    int nit = 0;
+    while (def > m->cfg.threshold) {
+      RC(one_cycle(m));
+      m->iterations++;
+      double old = def;
+      RC(defect_norm64(m, &def));
+      if (def / old > 0.8 && m->cfg.threshold == 0.0) break;
+      if (nit > 100) break;
+      nit++;
+    }
+  } else {
+    for (int q = 0; q < m->cfg.niteration; ++q) {
+      RC(one_cycle(m));
+      m->iterations++;
+    }
+    RC(defect_norm64(m, &def));
+  }
+  if (m->subtract) RC(subtract_mean(m, H, H.u[top], top));
+  RC(apply_bc(m, H, top, false));
+  MCK(cudaStreamSynchronize(m->st));
+  m->last_norm = def;
+  if (iterations) *iterations = m->iterations;
+  if (defect_norm) *defect_norm = def;
+  return ATHG_OK;
+}
+
+int athg_mg_vcycles(athg_mg* m, int n) {
+  if (!m) return mgfail(ATHG_ERR_ARG, "null argument");
+  for (int q = 0; q < n; ++q) RC(one_cycle(m));
+  return ATHG_OK;
+}
+
+int athg_mg_defect_norm(athg_mg* m, double* out) {
+  if (!m || !out) return mgfail(ATHG_ERR_ARG, "null argument");
+  return defect_norm64(m, out);
+}
+
+int athg_mg_stream(athg_mg* m, void** stream) {
+  if (!m || !stream) return mgfail(ATHG_ERR_ARG, "null argument");
+  *stream = (void*)m->st;
+  return ATHG_OK;
+}
+
+int athg_mg_multipole(athg_mg* m, double* out28) {
+  if (!m || !out28) return mgfail(ATHG_ERR_ARG, "null argument");
+  for (int q = 0; q < 25; ++q) out28[q] = m->mp.c[q];
+  for (int d = 0; d < 3; ++d) out28[25 + d] = m->mp.o[d];
+  return ATHG_OK;
+}
+
+}  // extern "C"

@@ -144,6 +144,55 @@ int athg_max_div_b(athg_ctx* ctx, double* out);
 /* volume integrals of the 5 conserved variables over all interior cells (history) */
 int athg_sum_conserved(athg_ctx* ctx, double* out5);
 
+/* ---- multigrid Poisson solver (self-gravity) ----------------------------------------
+ * Replaces MGGravityDriver::Solve (gravity/mg_gravity.cpp:166-211) and the Multigrid
+ * primitives it drives (multigrid/multigrid.hpp:120-129): red-black Gauss-Seidel smoother
+ * (omega = 1.15), defect, restriction, trilinear prolongation, FMG prolongation, V(1,1)
+ * and FMG cycles, defect norms, periodic / zero-gradient / zero-fixed / multipole
+ * (l <= 4) boundaries. The mesh is cubic with 2^L cells per side; each level is one
+ * device grid with one ghost layer (the reference's per-MeshBlock levels plus root grid
+ * visit the same uniform levels on such a mesh). Solves  lap(phi) = src. */
+enum { ATHG_MG_PERIODIC = 0, ATHG_MG_ZEROGRAD = 1, ATHG_MG_ZEROFIXED = 2, ATHG_MG_MULTIPOLE = 3 };
+enum { ATHG_MG_FMG = 0, ATHG_MG_MGI = 1 };
+
+typedef struct athg_mg athg_mg;
+
+typedef struct {
+  int nx;                 /* cells per side, a power of two (<mesh> nx1 = nx2 = nx3) */
+  double x1min, x1max, x2min, x2max, x3min, x3max;
+  int bc[6];              /* <gravity> ix1_bc, ox1_bc, ix2_bc, ox2_bc, ix3_bc, ox3_bc */
+  int mporder;            /* <gravity> mporder: 2 or 4 (multipole boundaries only) */
+  int auto_mporigin;      /* <gravity> auto_mporigin: expand about the centre of mass */
+  int nodipole;           /* <gravity> nodipole */
+  double mporigin[3];     /* <gravity> mporigin_x1..x3 when auto_mporigin = 0 */
+  int mode;               /* <gravity> mgmode: ATHG_MG_FMG or ATHG_MG_MGI */
+  double threshold;       /* <gravity> threshold: >= 0 iterate until the L2 defect <= it
+                             (0: until convergence stalls); < 0: niteration cycles */
+  int niteration;         /* <gravity> niteration */
+  int precision;          /* ATHG_FP64: the reference's FP64 cycle; ATHG_MIXED: FP32 V-cycles
+                             on the FP64 defect, corrections accumulated in FP64 */
+} athg_mg_config;
+
+int athg_mg_create(const athg_mg_config* cfg, athg_mg** out);
+int athg_mg_destroy(athg_mg* mg);
+/* Multigrid::LoadSource (multigrid/multigrid.cpp:194): src = fac * rho on the finest
+ * level; rho is the nx^3 interior, i fastest. */
+int athg_mg_load_source(athg_mg* mg, const double* rho, size_t count, double fac);
+/* Multigrid::LoadFinestData: initial guess for ATHG_MG_MGI (nx^3 interior). */
+int athg_mg_set_phi(athg_mg* mg, const double* phi, size_t count);
+/* MGGravityDriver::Solve after LoadSource: SetupMultigrid, FMG and/or iterations,
+ * average subtraction; returns V-cycles done and the final L2 defect norm. */
+int athg_mg_solve(athg_mg* mg, int* iterations, double* defect_norm);
+/* n V(1,1) cycles on the finest level (MultigridDriver::SolveVCycle). */
+int athg_mg_vcycles(athg_mg* mg, int n);
+/* MultigridDriver::CalculateDefectNorm(l2) of the current solution. */
+int athg_mg_defect_norm(athg_mg* mg, double* out);
+/* Multigrid::RetrieveResult: the nx^3 interior of phi. */
+int athg_mg_get_phi(athg_mg* mg, double* phi, size_t count);
+int athg_mg_stream(athg_mg* mg, void** stream);
+/* Multipole coefficients (25) and expansion origin (3), after a solve. */
+int athg_mg_multipole(athg_mg* mg, double* out28);
+
 const char* athg_last_error(void);
 
 #ifdef __cplusplus
