@@ -146,6 +146,44 @@ def timed_cycles(sim, torch, steps):
     return s.elapsed_time(e) / 1e3
 
 
+def run_e2e(athg, torch, u, b1, b2, b3, steps, zones):
+    """The same cycles through the C ABI with host (pinned) buffers: upload of the state,
+    initialisation, `steps` cycles each followed by the time read-back the driver loop
+    does, and download of the final state, all inside the timed region."""
+    import ctypes as C
+    sim = make_sim(athg, "mixed")
+    sim.load_interior(u, b1, b2, b3)
+    blocks = {v: sim.download(v) for v in (athg.VAR_CONS, athg.VAR_B1F, athg.VAR_B2F, athg.VAR_B3F)}
+    pinned = {v: torch.from_numpy(a).pin_memory() for v, a in blocks.items()}
+    outbuf = {v: torch.empty_like(t).pin_memory() for v, t in pinned.items()}
+    L = athg.lib()
+
+    def e2e_run(k):
+        for v, t in pinned.items():
+            athg.check(L.athg_upload(sim.h, -1, v, C.cast(t.data_ptr(), C.POINTER(C.c_double)),
+                                     t.numel()))
+        sim.initialize()
+        tt, dd, nn = C.c_double(), C.c_double(), C.c_int64()
+        for _ in range(k):
+            sim.cycles(1)
+            athg.check(L.athg_get_time(sim.h, C.byref(tt), C.byref(dd), C.byref(nn)))
+        for v, t in outbuf.items():
+            athg.check(L.athg_download(sim.h, -1, v, C.cast(t.data_ptr(), C.POINTER(C.c_double)),
+                                       t.numel()))
+
+    e2e_run(1)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    e2e_run(steps)
+    torch.cuda.synchronize()
+    el = time.perf_counter() - t0
+    state_bytes = sum(t.numel() * 8 for t in pinned.values())
+    sim.close()
+    return {"value": zones * steps / el, "unit": METRIC,
+            "h2d_bytes_per_step": state_bytes / steps,
+            "d2h_bytes_per_step": state_bytes / steps + 24}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -155,7 +193,12 @@ def main():
     ap.add_argument("--cpu-cycles", type=int, default=2)
     ap.add_argument("--fp64-steps", type=int, default=6)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--nx", type=int, default=256, help="cells per side (profiling: 128)")
+    ap.add_argument("--no-e2e", action="store_true")
     args = ap.parse_args()
+    global NX, WORKLOAD
+    NX = (args.nx,) * 3
+    WORKLOAD = "orszag_tang_%d^3_mhd_plm_hlld_vl2" % args.nx
     if args.impl == "reference":
         return run_reference(args)
 
@@ -212,35 +255,9 @@ def main():
     l1_rel = l1_dev / float(np.mean(np.abs(devs["fp64"]["u"][0])))
 
     # ---------------- end to end through the C ABI with host buffers ----------------
-    sim = make_sim(athg, "mixed")
-    sim.load_interior(u, b1, b2, b3)
-    blocks = {v: sim.download(v) for v in (athg.VAR_CONS, athg.VAR_B1F, athg.VAR_B2F, athg.VAR_B3F)}
-    pinned = {v: torch.from_numpy(a).pin_memory() for v, a in blocks.items()}
-    outbuf = {v: torch.empty_like(t).pin_memory() for v, t in pinned.items()}
-    import ctypes as C
-    L = athg.lib()
-
-    def e2e_run(k):
-        for v, t in pinned.items():
-            athg.check(L.athg_upload(sim.h, -1, v, C.cast(t.data_ptr(), C.POINTER(C.c_double)),
-                                     t.numel()))
-        sim.initialize()
-        tt, dd, nn = C.c_double(), C.c_double(), C.c_int64()
-        for _ in range(k):
-            sim.cycles(1)
-            athg.check(L.athg_get_time(sim.h, C.byref(tt), C.byref(dd), C.byref(nn)))
-        for v, t in outbuf.items():
-            athg.check(L.athg_download(sim.h, -1, v, C.cast(t.data_ptr(), C.POINTER(C.c_double)),
-                                       t.numel()))
-
-    e2e_run(1)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    e2e_run(args.steps)
-    torch.cuda.synchronize()
-    e2e_el = time.perf_counter() - t0
-    state_bytes = sum(t.numel() * 8 for t in pinned.values())
-    sim.close()
+    e2e = None
+    if not args.no_e2e:
+        e2e = run_e2e(athg, torch, u, b1, b2, b3, args.steps, zones)
 
     # ---------------- CPU baseline (oracle port) ----------------
     cpu = None
@@ -279,9 +296,7 @@ def main():
                      "note": "one launch = one captured VL2 cycle (graph); algorithmic bytes "
                              "384 B/zone-cycle; peak %s" % peak_kind},
         "cpu_baseline": cpu,
-        "e2e": {"value": zones * args.steps / e2e_el, "unit": METRIC,
-                "h2d_bytes_per_step": state_bytes / args.steps,
-                "d2h_bytes_per_step": state_bytes / args.steps + 24},
+        "e2e": e2e,
         "gpu_launches": m["launches"] * m["steps"],
         "clocks": m["clocks"],
     }
