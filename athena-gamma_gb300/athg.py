@@ -34,7 +34,7 @@ EXPORTS = [
     "athg_new_block_dt", "athg_max_div_b", "athg_sum_conserved", "athg_last_error",
     "athg_mg_create", "athg_mg_destroy", "athg_mg_load_source", "athg_mg_set_phi",
     "athg_mg_solve", "athg_mg_vcycles", "athg_mg_defect_norm", "athg_mg_get_phi",
-    "athg_mg_stream", "athg_mg_multipole",
+    "athg_mg_stream", "athg_mg_multipole", "athg_block_cfl_dt_noalloc",
 ]
 MG_BC = {"periodic": 0, "zerograd": 1, "zerofixed": 2, "multipole": 3}
 
@@ -116,6 +116,7 @@ def lib():
         "athg_mg_get_phi": [vp, C.POINTER(d), sz],
         "athg_mg_stream": [vp, C.POINTER(vp)],
         "athg_mg_multipole": [vp, C.POINTER(d)],
+        "athg_block_cfl_dt_noalloc": [C.POINTER(Config), vp, vp, vp, vp, vp, d, d, d, vp, vp],
     }
     for name, args in sig.items():
         f = getattr(L, name)

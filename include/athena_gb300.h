@@ -193,6 +193,26 @@ int athg_mg_stream(athg_mg* mg, void** stream);
 /* Multipole coefficients (25) and expansion origin (3), after a solve. */
 int athg_mg_multipole(athg_mg* mg, double* out28);
 
+/* ---- CFL time step of one caller-owned block, with no device allocation ------------
+ * No counterpart in the reference: an addition for callers that cannot allocate device
+ * memory (a stream being captured into a CUDA graph, a host whose device memory belongs
+ * to its own pool, a fixed memory budget). Computes the same minimum as
+ * athg_new_block_dt (dx / (|v| + c_f) over the interior, times cfg->cfl_number) for ONE
+ * block whose device arrays the caller owns, in the AthenaArray layout with ghosts, FP64:
+ *   w (5,nc3,nc2,nc1) primitives; for MHD also bcc (3,nc3,nc2,nc1) and the face fields
+ *   b1f (nc3,nc2,nc1+1), b2f (nc3,nc2+1,nc1), b3f (nc3+1,nc2,nc1); nc = nx + 2*nghost.
+ * The result is written to dt_out, a device pointer, on `stream` (a cudaStream_t, NULL
+ * for the default stream); nothing is synchronised.
+ * Only cfg->nx1..nx3, nghost, magnetic, gamma and cfl_number are read.
+ * Scratch is a fixed file-scope device array of 8192 doubles (64 KiB) that every GPU
+ * loading this library keeps until exit; blocks of more than 16,777,216 interior cells
+ * are rejected with ATHG_ERR_ARG. The first call on a device looks up the array's device
+ * address (cudaGetSymbolAddress), so make that first call before any stream capture.
+ * All calls share the array: calls that overlap on the GPU (e.g. on two streams) race. */
+int athg_block_cfl_dt_noalloc(const athg_config* cfg, const double* w, const double* bcc,
+                              const double* b1f, const double* b2f, const double* b3f,
+                              double dx1, double dx2, double dx3, double* dt_out, void* stream);
+
 const char* athg_last_error(void);
 
 #ifdef __cplusplus
