@@ -85,7 +85,19 @@ typedef struct {
   double dt, time;
   int nstages;
   double delta[4], g1[4], g2[4], g3[4], beta[4];
+  /* self-gravity (SELF_GRAVITY_ENABLED == 2): potential with one ghost layer, the
+   * attached multigrid solver (mg_oracle.c) and 4 pi G */
+  double *phi;
+  struct orc_mg_s *mg;
+  double four_pi_G;
 } orc_sim;
+
+/* mg_oracle.c */
+struct orc_mg_s;
+double *orc_mg_u(struct orc_mg_s *m);
+double *orc_mg_src(struct orc_mg_s *m);
+void orc_mg_solve(struct orc_mg_s *m);
+int orc_mg_size(const struct orc_mg_s *m);
 
 /* ---------------------------------------------------------------- indexing ---- */
 #define C3(s, k, j, i) ((((size_t)(k)) * (s)->n2 + (size_t)(j)) * (s)->n1 + (size_t)(i))
@@ -193,7 +205,7 @@ void orc_destroy(orc_sim *s) {
   double *ptrs[] = {s->u, s->u1, s->w, s->w1, s->bcc, s->b1, s->b2, s->b3, s->r1, s->r2,
                     s->r3, s->f1, s->f2, s->f3, s->e3x1, s->e2x1, s->wx1, s->e1x2, s->e3x2,
                     s->wx2, s->e1x3, s->e2x3, s->wx3, s->e1, s->e2, s->e3, s->cce, s->x1f,
-                    s->x2f, s->x3f, s->x1v, s->x2v, s->x3v};
+                    s->x2f, s->x3f, s->x1v, s->x2v, s->x3v, s->phi};
   for (size_t n = 0; n < sizeof(ptrs) / sizeof(ptrs[0]); ++n) free(ptrs[n]);
   free(s);
 }
@@ -630,6 +642,69 @@ static inline double wave_var(const orc_sim *s, int dir, int n, int k, int j, in
   return s->bcc[(size_t)comp * s->ncell + c];
 }
 
+/* PPM of one cell on a uniform Cartesian axis (reconstruct/ppm.cpp:44-342 with the
+ * uniform weights of reconstruct/reconstruction.cpp:420-431): from the five values
+ * q[-2..2] returns qminus (state at the lower face) and qplus (upper face). */
+static inline double sgn(double x) { return (x < 0.0) ? -1.0 : 1.0; }
+static void ppm_cell(double q_im2, double q_im1, double q, double q_ip1, double q_ip2,
+                     double *qminus_out, double *qplus_out) {
+  const double C2 = 1.25;
+  const double c1 = 0.5, c2 = 0.5, c3 = 0.5, c4 = 0.5, c5 = 1.0 / 6.0, c6 = -1.0 / 6.0;
+  double qa = (q - q_im1);
+  double qb = (q_ip1 - q);
+  double dd_im1 = c1 * qa + c2 * (q_im1 - q_im2);
+  double dd = c1 * qb + c2 * qa;
+  double dd_ip1 = c1 * (q_ip2 - q_ip1) + c2 * qb;
+  double dph = (c3 * q_im1 + c4 * q) + (c5 * dd_im1 + c6 * dd);
+  double dph_ip1 = (c3 * q + c4 * q_ip1) + (c5 * dd + c6 * dd_ip1);
+  double d2qc_im1 = q_im2 + q - 2.0 * q_im1;
+  double d2qc = q_im1 + q_ip1 - 2.0 * q;
+  double d2qc_ip1 = q + q_ip2 - 2.0 * q_ip1;
+  {
+    double qa_tmp = dph - q_im1, qb_tmp = q - dph;
+    double a = 3.0 * (q_im1 + q - 2.0 * dph), b = d2qc_im1, c = d2qc;
+    double qd = 0.0;
+    if (sgn(a) == sgn(b) && sgn(a) == sgn(c))
+      qd = sgn(a) * fmin_ref(C2 * fabs(b), fmin_ref(C2 * fabs(c), fabs(a)));
+    double dph_tmp = 0.5 * (q_im1 + q) - qd / 6.0;
+    if (qa_tmp * qb_tmp < 0.0) dph = dph_tmp;
+  }
+  {
+    double qa_tmp = dph_ip1 - q, qb_tmp = q_ip1 - dph_ip1;
+    double a = 3.0 * (q + q_ip1 - 2.0 * dph_ip1), b = d2qc, c = d2qc_ip1;
+    double qd = 0.0;
+    if (sgn(a) == sgn(b) && sgn(a) == sgn(c))
+      qd = sgn(a) * fmin_ref(C2 * fabs(b), fmin_ref(C2 * fabs(c), fabs(a)));
+    double dphip1_tmp = 0.5 * (q + q_ip1) - qd / 6.0;
+    if (qa_tmp * qb_tmp < 0.0) dph_ip1 = dphip1_tmp;
+  }
+  double d2qf = 6.0 * (dph + dph_ip1 - 2.0 * q);
+  double qminus = dph, qplus = dph_ip1;
+  double dqf_minus = q - qminus, dqf_plus = qplus - q;
+  double qa_tmp = dqf_minus * dqf_plus;
+  double qb_tmp = (q_ip1 - q) * (q - q_im1);
+  double a = d2qc_im1, b = d2qc, c = d2qc_ip1, d = d2qf, qe = 0.0;
+  if (sgn(a) == sgn(b) && sgn(a) == sgn(c) && sgn(a) == sgn(d))
+    qe = sgn(d) * fmin_ref(fmin_ref(C2 * fabs(a), C2 * fabs(b)), fmin_ref(C2 * fabs(c), fabs(d)));
+  a = fmax_ref(fabs(q_im1), fabs(q_im2));
+  b = fmax_ref(fmax_ref(fabs(q), fabs(q_ip1)), fabs(q_ip2));
+  double rho = 0.0;
+  if (fabs(d) > (1.0e-12) * fmax_ref(a, b)) rho = qe / d;
+  double tmp_m = q - rho * dqf_minus, tmp_p = q + rho * dqf_plus;
+  double tmp2_m = q - 2.0 * dqf_plus, tmp2_p = q + 2.0 * dqf_minus;
+  if ((qa_tmp <= 0.0 || qb_tmp <= 0.0)) {
+    if (rho <= (1.0 - (1.0e-12))) {
+      qminus = tmp_m;
+      qplus = tmp_p;
+    }
+  } else {
+    if (fabs(dqf_minus) >= 2.0 * fabs(dqf_plus)) qminus = tmp2_m;
+    if (fabs(dqf_plus) >= 2.0 * fabs(dqf_minus)) qplus = tmp2_p;
+  }
+  *qminus_out = qminus;
+  *qplus_out = qplus;
+}
+
 /* left/right states at the face with face index (k,j,i) in direction dir
  * (face between the cell at index-1 and the cell at index along dir). */
 static void recon_face(const orc_sim *s, int dir, int order, int k, int j, int i,
@@ -641,6 +716,24 @@ static void recon_face(const orc_sim *s, int dir, int order, int k, int j, int i
       wl[n] = wave_var(s, dir, n, k - dk, j - dj, i - di);
       wr[n] = wave_var(s, dir, n, k, j, i);
     }
+    return;
+  }
+  if (order == 3) { /* PPM: wl from cell f-1 (qplus), wr from cell f (qminus), then floors */
+    for (int n = 0; n < nw; ++n) {
+      double v[6];
+      for (int q = 0; q < 6; ++q)
+        v[q] = wave_var(s, dir, n, k + (q - 3) * dk, j + (q - 3) * dj, i + (q - 3) * di);
+      double qm, qp, dummy;
+      ppm_cell(v[0], v[1], v[2], v[3], v[4], &dummy, &qp);
+      ppm_cell(v[1], v[2], v[3], v[4], v[5], &qm, &dummy);
+      wl[n] = qp;
+      wr[n] = qm;
+    }
+    /* eos ApplyPrimitiveFloors (ppm.cpp:326-332) */
+    wl[IDN] = (wl[IDN] > s->p.dfloor) ? wl[IDN] : s->p.dfloor;
+    wl[IPR] = (wl[IPR] > s->p.pfloor) ? wl[IPR] : s->p.pfloor;
+    wr[IDN] = (wr[IDN] > s->p.dfloor) ? wr[IDN] : s->p.dfloor;
+    wr[IPR] = (wr[IPR] > s->p.pfloor) ? wr[IPR] : s->p.pfloor;
     return;
   }
   /* reconstruct/plm.cpp uniform VL branch: cell c gives wl(c+1) and wr(c) */
@@ -930,7 +1023,73 @@ static void boundaries(orc_sim *s) {
 }
 
 /* Mesh::Initialize tail (mesh/mesh.cpp:1405-1649): ghosts, W(U), first dt. */
+/* ---------------------------------------------------------- self-gravity ---- */
+/* Couple a multigrid solver covering the same cubic mesh (one block). */
+int orc_attach_gravity(orc_sim *s, struct orc_mg_s *mg, double four_pi_G) {
+  const int n = orc_mg_size(mg);
+  if (n != s->p.nx1 || n != s->p.nx2 || n != s->p.nx3) return -1;
+  s->mg = mg;
+  s->four_pi_G = four_pi_G;
+  if (!s->phi) s->phi = calloc(s->ncell, 8);
+  return 0;
+}
+double *orc_phi(orc_sim *s) { return s->phi; }
+
+/* MGGravityDriver::Solve (gravity/mg_gravity.cpp:166-211): LoadSource of u(IDN) times
+ * 4 pi G (multigrid/multigrid.cpp:194-233), the solve, and RetrieveResult with one ghost
+ * layer (multigrid.cpp:269-286) */
+static void gravity_solve(orc_sim *s) {
+  const int n = s->p.nx1, nt = n + 2;
+  double *src = orc_mg_src(s->mg);
+  const double fac = s->four_pi_G;
+  for (int k = 0; k < n; ++k)
+    for (int j = 0; j < n; ++j)
+      for (int i = 0; i < n; ++i) {
+        double d = s->u[C3(s, k + s->ks, j + s->js, i + s->is)];
+        src[((size_t)(k + 1) * nt + (j + 1)) * nt + (i + 1)] = (fac == 1.0) ? d : d * fac;
+      }
+  orc_mg_solve(s->mg);
+  const double *u = orc_mg_u(s->mg);
+  for (int k = -1; k <= n; ++k)
+    for (int j = -1; j <= n; ++j)
+      for (int i = -1; i <= n; ++i)
+        s->phi[C3(s, k + s->ks, j + s->js, i + s->is)] =
+            u[((size_t)(k + 1) * nt + (j + 1)) * nt + (i + 1)];
+}
+
+/* HydroSourceTerms::SelfGravity (hydro/srcterms/self_gravity.cpp:35-125): momentum from
+ * the face potentials, energy from the mass fluxes; three passes in the reference's
+ * order, each its own read-modify-write of U */
+static void self_gravity(orc_sim *s, double dt) {
+  const size_t nc = s->ncell, n1f = f1n(s), n2f = f2n(s), n3f = f3n(s);
+  const double *phi = s->phi, *w = s->w;
+  double *u = s->u;
+  for (int dir = 0; dir < 3; ++dir) {
+    const double dx = dir == 0 ? s->dx1 : (dir == 1 ? s->dx2 : s->dx3);
+    const size_t st = dir == 0 ? 1 : (dir == 1 ? (size_t)s->n1 : (size_t)s->n1 * s->n2);
+    const double *fl = dir == 0 ? s->f1 : (dir == 1 ? s->f2 : s->f3);
+    (void)n1f; (void)n2f; (void)n3f;
+#pragma omp parallel for collapse(2)
+    for (int k = s->ks; k <= s->ke; ++k)
+      for (int j = s->js; j <= s->je; ++j)
+        for (int i = s->is; i <= s->ie; ++i) {
+          const size_t c = C3(s, k, j, i);
+          const double dtodx = dt / dx;
+          const double phic = phi[c];
+          const double phil = 0.5 * (phi[c - st] + phi[c]);
+          const double phir = 0.5 * (phi[c] + phi[c + st]);
+          u[(1 + dir) * nc + c] -= dtodx * w[c] * (phir - phil);
+          size_t fl_l, fl_r;
+          if (dir == 0) { fl_l = F1I(s, k, j, i); fl_r = F1I(s, k, j, i + 1); }
+          else if (dir == 1) { fl_l = F2I(s, k, j, i); fl_r = F2I(s, k, j + 1, i); }
+          else { fl_l = F3I(s, k, j, i); fl_r = F3I(s, k + 1, j, i); }
+          u[4 * nc + c] -= dtodx * (fl[fl_l] * (phic - phil) + fl[fl_r] * (phir - phic));
+        }
+  }
+}
+
 void orc_initialize(orc_sim *s, double tlim) {
+  if (s->mg) gravity_solve(s); /* mesh/mesh.cpp:1398-1402 */
   boundaries(s);
   c2p(s);
   s->time = 0.0;
@@ -958,6 +1117,8 @@ void orc_stage(orc_sim *s, int l) {
   if (do_swap) swapp(&s->u, &s->u1);
   else ave_cc(s, s->u, s->u1, s->g1[l], s->g2[l]);
   flux_divergence(s, s->beta[l] * s->dt);
+  /* AddSourceTerms (:1655-1676); every stage of these integrators is a main stage */
+  if (s->mg) self_gravity(s, s->beta[l] * s->dt);
   if (s->p.mhd) { /* IntegrateField (:1618-1653) */
     double *bo[3] = {s->r1, s->r2, s->r3}, *bi[3] = {s->b1, s->b2, s->b3};
     if (s->delta[l] != 0.0) ave_fc(s, bo, bi, 1.0, s->delta[l]);
@@ -971,6 +1132,7 @@ void orc_stage(orc_sim *s, int l) {
   }
   boundaries(s);
   c2p(s);
+  if (s->mg) gravity_solve(s); /* main.cpp:461-466 */
 }
 
 /* One cycle (main.cpp:459-485): all stages, time advance, new dt. */

@@ -50,7 +50,7 @@ typedef struct {
   double omega;
 } orc_mg_params;
 
-typedef struct {
+typedef struct orc_mg_s {
   orc_mg_params p;
   int nl;                   /* number of levels = lmax + 1 */
   double **u, **src, **def, **uold;
@@ -132,6 +132,7 @@ void orc_mg_destroy(orc_mg *m) {
 double *orc_mg_u(orc_mg *m) { return m->u[m->nl - 1]; }
 double *orc_mg_src(orc_mg *m) { return m->src[m->nl - 1]; }
 int orc_mg_iterations(const orc_mg *m) { return m->iterations; }
+int orc_mg_size(const orc_mg *m) { return 1 << m->p.lmax; }
 double orc_mg_last_norm(const orc_mg *m) { return m->last_norm; }
 int orc_mg_coffset(const orc_mg *m) { return m->coffset; }
 void orc_mg_set_coffset(orc_mg *m, int c) { m->coffset = c; }

@@ -37,7 +37,11 @@ CASES = {
     "mhd_hlle_plm_vl2": ("state_mhd_hlle", True, "hlle", (16, 8, 8), (16, 8, 8), "vl2", 2, 3, 9, 0.4),
     "mhd_hlld_plm_rk2": ("state_mhd_hlld", True, "hlld", (16, 8, 8), (16, 8, 8), "rk2", 2, 3, 13, 0.8),
     "mhd_hlld_plm_vl2_4blocks": ("state_mhd_hlld", True, "hlld", (16, 16, 8), (8, 8, 8), "vl2", 2, 3, 21, 0.4),
+    "hydro_hllc_ppm_rk3": ("state_hydro_hllc_ng4", False, "hllc", (16, 8, 8), (16, 8, 8), "rk3", 3, 3, 31, 0.8),
+    "mhd_hlld_ppm_rk3": ("state_mhd_hlld_ng4", True, "hlld", (16, 8, 8), (16, 8, 8), "rk3", 3, 3, 32, 0.8),
+    "mhd_hlld_ppm_vl2": ("state_mhd_hlld_ng4", True, "hlld", (16, 8, 8), (16, 8, 8), "vl2", 3, 3, 33, 0.4),
 }
+NGHOST = {"state_hydro_hllc_ng4": 4, "state_mhd_hlld_ng4": 4}
 
 
 def make_case(name, spec):
@@ -52,7 +56,8 @@ def make_case(name, spec):
                       b3_out=out["b3"])
     meta = dict(mhd=mhd, solver=solver, nx=list(nx), meshblock=list(mb), integrator=integ,
                 xorder=xorder, ncycles=ncyc, seed=seed, cfl=cfl, gamma=5.0 / 3.0,
-                time=out["time"], dt=out["dt"], ncycle=out["ncycle"])
+                time=out["time"], dt=out["dt"], ncycle=out["ncycle"],
+                nghost=NGHOST.get(exe_cfg, 2))
     np.savez_compressed(os.path.join(HERE, name + ".npz"), meta=json.dumps(meta), **arrays)
     print("wrote", name, "t=%.6g ncycle=%d" % (out["time"], out["ncycle"]))
 
@@ -110,6 +115,42 @@ def make_mg_case(name, spec):
     print("wrote", name)
 
 
+# self-gravity evolution: name -> (exe config, mhd, solver, N, meshblock, integrator,
+# ncycles, seed, cfl, four_pi_G, MG mode, niteration)
+SG_CASES = {
+    "sg_hydro_hllc_plm_vl2": ("sg_state_hydro", False, "hllc", 32, 32, "vl2", 3, 51, 0.4,
+                              2.0 * np.pi, "FMG", 2),
+    "sg_hydro_hllc_plm_vl2_8blocks": ("sg_state_hydro", False, "hllc", 32, 16, "vl2", 3, 52,
+                                      0.4, 2.0 * np.pi, "FMG", 2),
+    "sg_mhd_hlld_plm_vl2": ("sg_state_mhd_hlld", True, "hlld", 32, 32, "vl2", 3, 53, 0.4,
+                            2.0 * np.pi, "FMG", 2),
+}
+
+
+def make_sg_case(name, spec):
+    exe_cfg, mhd, solver, n, mb, integ, ncyc, seed, cfl, fpg, mode, niter = spec
+    exe = build_ref.build(exe_cfg)
+    nx = (n, n, n)
+    u, b1, b2, b3 = ol.smooth_random_state(nx, mhd, seed=seed)
+    extra = "four_pi_G = %r" % fpg
+    blocks = ("<gravity>\nmgmode = %s\nniteration = %d\n" % (mode, niter) +
+              "".join("%s = periodic\n" % f for f in
+                      ("ix1_bc", "ox1_bc", "ix2_bc", "ox2_bc", "ix3_bc", "ox3_bc")))
+    out = ol.run_reference_state(exe, os.path.join(WORK, name), nx, (mb, mb, mb), mhd, u, b1,
+                                 b2, b3, cfl=cfl, tlim=100.0, nlim=ncyc, integrator=integ,
+                                 extra=extra, phi=True, blocks=blocks)
+    arrays = {"u_in": u, "u_out": out["u"], "phi_out": out["phi"]}
+    if mhd:
+        arrays.update(b1_in=b1, b2_in=b2, b3_in=b3, b1_out=out["b1"], b2_out=out["b2"],
+                      b3_out=out["b3"])
+    meta = dict(mhd=mhd, solver=solver, nx=list(nx), meshblock=[mb] * 3, integrator=integ,
+                xorder=2, ncycles=ncyc, seed=seed, cfl=cfl, gamma=5.0 / 3.0,
+                time=out["time"], dt=out["dt"], ncycle=out["ncycle"], nghost=2,
+                four_pi_G=fpg, mgmode=mode, niteration=niter, self_gravity=True)
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), meta=json.dumps(meta), **arrays)
+    print("wrote", name, "t=%.6g ncycle=%d" % (out["time"], out["ncycle"]))
+
+
 def linear_wave_errors():
     """Reference's own linear-wave L1 errors (C1 hydro; MHD fast wave)."""
     res = {}
@@ -140,12 +181,14 @@ def linear_wave_errors():
 if __name__ == "__main__":
     if not build_ref.available():
         sys.exit("reference tree not found")
-    names = sys.argv[1:] or (list(CASES) + list(MG_CASES))
+    names = sys.argv[1:] or (list(CASES) + list(MG_CASES) + list(SG_CASES))
     for n in names:
         if n == "lw":
             continue
         if n in MG_CASES:
             make_mg_case(n, MG_CASES[n])
+        elif n in SG_CASES:
+            make_sg_case(n, SG_CASES[n])
         else:
             make_case(n, CASES[n])
     if not sys.argv[1:] or "lw" in sys.argv[1:]:

@@ -13,8 +13,13 @@ def _all():
 
 
 def cases():
-    """Stage-update fixtures (hydro/MHD)."""
-    return [c for c in _all() if not c.startswith("mg_")]
+    """Stage-update fixtures (hydro/MHD, no gravity)."""
+    return [c for c in _all() if not c.startswith(("mg_", "sg_"))]
+
+
+def sg_cases():
+    """Stage-update fixtures with multigrid self-gravity."""
+    return [c for c in _all() if c.startswith("sg_")]
 
 
 def mg_cases():

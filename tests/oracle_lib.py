@@ -93,6 +93,10 @@ def lib():
         L.orc_mg_defect_norm.restype = C.c_double
         L.orc_mg_defect_norm.argtypes = [C.c_void_p]
         L.orc_mg_mpcoeff.argtypes = [C.c_void_p, C.POINTER(C.c_double)]
+        L.orc_attach_gravity.restype = C.c_int
+        L.orc_attach_gravity.argtypes = [C.c_void_p, C.c_void_p, C.c_double]
+        L.orc_phi.restype = C.POINTER(C.c_double)
+        L.orc_phi.argtypes = [C.c_void_p]
         _lib = L
     return _lib
 
@@ -183,6 +187,16 @@ class Oracle:
             out["b2"] = self.b2[g:g + nx3, g:g + nx2 + 1, g:g + nx1].copy()
             out["b3"] = self.b3[g:g + nx3 + 1, g:g + nx2, g:g + nx1].copy()
         return out
+
+    def attach_gravity(self, mg, four_pi_G):
+        """Self-gravity through a multigrid oracle covering the same cubic mesh."""
+        self._mg = mg  # keep the solver alive as long as the block uses it
+        if self.L.orc_attach_gravity(self.s, mg.m, four_pi_G) != 0:
+            raise ValueError("multigrid size differs from the mesh")
+
+    @property
+    def phi(self):
+        return np.ctypeslib.as_array(self.L.orc_phi(self.s), shape=(self.n3, self.n2, self.n1))
 
     def initialize(self, tlim):
         self.L.orc_initialize(self.s, tlim)

@@ -11,7 +11,8 @@ def test_oracle_matches_reference(name):
     meta, a = golden_lib.load(name)
     mhd = meta["mhd"]
     o = ol.Oracle(tuple(meta["nx"]), mhd, meta["solver"], xorder=meta["xorder"],
-                  integrator=meta["integrator"], cfl=meta["cfl"], gamma=meta["gamma"])
+                  integrator=meta["integrator"], cfl=meta["cfl"], gamma=meta["gamma"],
+                  ng=meta.get("nghost", 2))
     o.load_interior(a["u_in"], a.get("b1_in"), a.get("b2_in"), a.get("b3_in"))
     o.initialize(100.0)
     o.cycle(meta["ncycles"], 100.0)
