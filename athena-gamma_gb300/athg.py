@@ -34,7 +34,7 @@ EXPORTS = [
     "athg_new_block_dt", "athg_max_div_b", "athg_sum_conserved", "athg_last_error",
     "athg_mg_create", "athg_mg_destroy", "athg_mg_load_source", "athg_mg_set_phi",
     "athg_mg_solve", "athg_mg_vcycles", "athg_mg_defect_norm", "athg_mg_get_phi",
-    "athg_mg_stream", "athg_mg_multipole", "athg_block_cfl_dt_noalloc",
+    "athg_mg_stream", "athg_mg_multipole", "athg_attach_gravity", "athg_block_cfl_dt_noalloc",
 ]
 MG_BC = {"periodic": 0, "zerograd": 1, "zerofixed": 2, "multipole": 3}
 
@@ -116,6 +116,7 @@ def lib():
         "athg_mg_get_phi": [vp, C.POINTER(d), sz],
         "athg_mg_stream": [vp, C.POINTER(vp)],
         "athg_mg_multipole": [vp, C.POINTER(d)],
+        "athg_attach_gravity": [vp, vp, d],
         "athg_block_cfl_dt_noalloc": [C.POINTER(Config), vp, vp, vp, vp, vp, d, d, d, vp, vp],
     }
     for name, args in sig.items():
@@ -305,6 +306,24 @@ class Sim:
         v = C.c_double()
         check(lib().athg_new_block_dt(self.h, C.byref(v)))
         return v.value
+
+    def attach_gravity(self, mg, four_pi_G):
+        """Self-gravity through a Multigrid on the same mesh (None detaches)."""
+        check(lib().athg_attach_gravity(self.h, mg.h if mg is not None else None, four_pi_G))
+        self._grav = mg  # the solver must outlive the coupling
+
+    def phi(self):
+        """Global potential with one ghost layer around the mesh: (N3+2, N2+2, N1+2)."""
+        g = self.ng
+        nx1, nx2, nx3 = self.block_nx
+        N1, N2, N3 = self.mesh_nx
+        P = self.download(VAR_PHI)
+        out = np.zeros((N3 + 2, N2 + 2, N1 + 2))
+        for b, (l1, l2, l3) in enumerate(self.locs):
+            out[l3 * nx3:(l3 + 1) * nx3 + 2, l2 * nx2:(l2 + 1) * nx2 + 2,
+                l1 * nx1:(l1 + 1) * nx1 + 2] = \
+                P[b, g - 1:g + nx3 + 1, g - 1:g + nx2 + 1, g - 1:g + nx1 + 1]
+        return out
 
 
 class Multigrid:

@@ -1,6 +1,7 @@
 // athg_api.cu -- the C ABI: context, device block pool, stage sequencing and the
 // CUDA-graph cycle. Declarations and reference interfaces: include/athena_gb300.h.
 #include <cmath>
+#include <type_traits>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -9,6 +10,7 @@
 #include "athena_gb300.h"
 #include "athg_bvals.cuh"
 #include "athg_launch.cuh"
+#include "athg_internal.h"
 
 using namespace athg;
 
@@ -39,7 +41,8 @@ constexpr double kDblMax = 1.79769313486231570815e308;
 // time += dt, ncycle++ (when advancing), then Mesh::NewTimeStep
 // (reference src/mesh/mesh.cpp:1078-1118). The block minimum is read and reset.
 __global__ void k_end_cycle(double* time, double* dt, long long* ncycle,
-                            unsigned long long* dtmin, double cfl, double tlim, int advance) {
+                            unsigned long long* dtmin, double cfl, double tlim, int advance,
+                            float* dtf) {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
   double t = *time, d = *dt;
   if (advance) {
@@ -52,6 +55,7 @@ __global__ void k_end_cycle(double* time, double* dt, long long* ncycle,
   if (t < tlim && (tlim - t) < d) d = tlim - t;
   *time = t;
   *dt = d;
+  if (dtf) *dtf = (float)d;  // the flux kernels of the mixed path read dt in FP32
   *dtmin = (unsigned long long)__double_as_longlong(kDblMax);
 }
 
@@ -137,10 +141,14 @@ struct athg_ctx {
   cudaStream_t st = nullptr;
   // pool
   double *u = nullptr, *u1 = nullptr, *b1 = nullptr, *b2 = nullptr, *b3 = nullptr;
-  double *r1 = nullptr, *r2 = nullptr, *r3 = nullptr, *edge = nullptr;
-  void *w = nullptr, *bcc = nullptr, *flx[3] = {nullptr, nullptr, nullptr};
+  double *r1 = nullptr, *r2 = nullptr, *r3 = nullptr;
+  void *w = nullptr, *bcc = nullptr, *flx[3] = {nullptr, nullptr, nullptr}, *edge = nullptr;
   BlockGeo* geo = nullptr;
-  double* coef = nullptr;
+  void* coef = nullptr;        // PLM coefficients in the flux precision
+  void* dxT = nullptr;         // cell widths in the flux precision
+  MixedGeo* mg = nullptr;      // per-block widths of the mixed-path update
+  float* dtf = nullptr;        // dt in FP32 (mixed path)
+  float* bf32[3] = {nullptr, nullptr, nullptr};  // FP32 face-field copies (mixed MHD)
   int* nbr = nullptr;
   double* scal = nullptr;  // [0] time, [1] dt, [2] ncycle (as long long), [3] dtmin bits,
                            // [4..8] sums, [9] div-b bits
@@ -150,6 +158,12 @@ struct athg_ctx {
   cudaGraphExec_t gexec = nullptr;
   int launches_per_cycle = 0;
   int counting = 0;
+  // self-gravity (SELF_GRAVITY_ENABLED == 2): coupled multigrid solver, 4 pi G, the
+  // potential of every block [nb][cells] and each block's offset in the root grid
+  athg_mg* grav = nullptr;
+  double four_pi_G = 0.0;
+  double* phi = nullptr;
+  int* boff = nullptr;
   bool mixed() const { return cfg.precision == ATHG_MIXED; }
 };
 
@@ -163,26 +177,46 @@ StagePtrs<T> ptrs(athg_ctx* c) {
   p.r1 = c->r1; p.r2 = c->r2; p.r3 = c->r3;
   p.w = (T*)c->w; p.bcc = (T*)c->bcc;
   for (int d = 0; d < 3; ++d) p.flx[d] = (T*)c->flx[d];
-  p.edge = c->edge;
+  p.edge = (T*)c->edge;
   p.geo = c->geo;
-  p.coef = c->coef;
+  p.coef = (const T*)c->coef;
+  p.dxT = (const T*)c->dxT;
+  p.mg = c->mg;
   p.dt = c->scal + 1;
+  if constexpr (std::is_same<T, float>::value) {
+    p.dtT = (const T*)c->dtf;
+    for (int d = 0; d < 3; ++d) { p.bf[d] = (const T*)c->bf32[d]; p.bfw[d] = (T*)c->bf32[d]; }
+  } else {
+    p.dtT = (const T*)(c->scal + 1);
+    p.bf[0] = (const T*)c->b1; p.bf[1] = (const T*)c->b2; p.bf[2] = (const T*)c->b3;
+    for (int d = 0; d < 3; ++d) p.bfw[d] = nullptr;
+  }
   return p;
 }
 
-Phys phys(const athg_ctx* c) { return Phys{c->cfg.gamma, c->cfg.dfloor, c->cfg.pfloor}; }
+Phys phys(const athg_ctx* c) {
+  return Phys{c->cfg.gamma, c->cfg.dfloor, c->cfg.pfloor, c->cfg.gamma - 1.0};
+}
 
 void free_pool(athg_ctx* c) {
   void* ps[] = {c->u, c->u1, c->b1, c->b2, c->b3, c->r1, c->r2, c->r3, c->edge, c->w,
-                c->bcc, c->flx[0], c->flx[1], c->flx[2], c->geo, c->coef, c->nbr, c->scal};
+                c->bcc, c->flx[0], c->flx[1], c->flx[2], c->geo, c->coef, c->nbr, c->scal,
+                c->dxT, c->mg, c->dtf, c->bf32[0], c->bf32[1], c->bf32[2]};
   for (void* p : ps)
     if (p) cudaFree(p);
-  c->u = c->u1 = c->b1 = c->b2 = c->b3 = c->r1 = c->r2 = c->r3 = c->edge = nullptr;
-  c->w = c->bcc = c->flx[0] = c->flx[1] = c->flx[2] = nullptr;
+  c->u = c->u1 = c->b1 = c->b2 = c->b3 = c->r1 = c->r2 = c->r3 = nullptr;
+  c->w = c->bcc = c->flx[0] = c->flx[1] = c->flx[2] = c->edge = nullptr;
   c->geo = nullptr; c->coef = nullptr; c->nbr = nullptr; c->scal = nullptr;
+  c->dxT = nullptr; c->mg = nullptr; c->dtf = nullptr;
+  c->bf32[0] = c->bf32[1] = c->bf32[2] = nullptr;
   if (c->gexec) cudaGraphExecDestroy(c->gexec);
   if (c->graph) cudaGraphDestroy(c->graph);
   c->gexec = nullptr; c->graph = nullptr;
+  if (c->phi) cudaFree(c->phi);
+  if (c->boff) cudaFree(c->boff);
+  c->phi = nullptr; c->boff = nullptr;
+  if (c->grav) athg::mg_bind_stream(c->grav, nullptr);
+  c->grav = nullptr;
   c->nb = 0;
 }
 
@@ -217,7 +251,7 @@ int launch_corner(athg_ctx* c) {
   return ATHG_OK;
 }
 
-int launch_update(athg_ctx* c, int l) {
+StageW stage_weights(const athg_ctx* c, int l) {
   const Integrator& it = c->integ;
   StageW sw;
   sw.delta = it.delta[l];
@@ -226,6 +260,14 @@ int launch_update(athg_ctx* c, int l) {
   sw.beta = it.beta[l];
   sw.swap = (it.g1[l] == 0.0 && it.g2[l] == 1.0) ? 1 : 0;
   sw.zero_reg = (l == 0) ? 1 : 0;
+  sw.copy_reg = (sw.zero_reg && sw.delta == 1.0) ? 1 : 0;
+  sw.has_delta = (sw.delta != 0.0) ? 1 : 0;
+  sw.betaf = (float)sw.beta;
+  return sw;
+}
+
+int launch_update(athg_ctx* c, int l) {
+  StageW sw = stage_weights(c, l);
   bool mhd = c->cfg.magnetic != 0;
   if (c->mixed()) Launcher<float>::update(c->g, ptrs<float>(c), mhd, sw, c->st);
   else Launcher<double>::update(c->g, ptrs<double>(c), mhd, sw, c->st);
@@ -256,7 +298,65 @@ int launch_block_dt(athg_ctx* c) {
 int launch_end(athg_ctx* c, int advance) {
   k_end_cycle<<<1, 32, 0, c->st>>>(c->scal, c->scal + 1, (long long*)(c->scal + 2),
                                    (unsigned long long*)(c->scal + 3), c->cfg.cfl_number,
-                                   c->cfg.tlim, advance);
+                                   c->cfg.tlim, advance, c->dtf);
+  c->counting += 1;
+  CKL();
+  return ATHG_OK;
+}
+
+// Multigrid::LoadSource (multigrid/multigrid.cpp:194-233): u(IDN) of every block, times
+// 4 pi G, into the interior of the solver's finest level
+__global__ void k_gather_rho(Geom g, const double* __restrict__ u, const int* __restrict__ boff,
+                             double* __restrict__ src, int n, double fac) {
+  const int b = blockIdx.z, k = blockIdx.y;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= g.nx1 * g.nx2) return;
+  const int j = t / g.nx1, i = t - j * g.nx1;
+  const double d = u[(int64_t)b * NHYD * g.ncell + cidx(g, k + g.ks, j + g.js, i + g.is)];
+  const int64_t nt = n + 2;
+  const int I = boff[3 * b] + i + 1, J = boff[3 * b + 1] + j + 1, K = boff[3 * b + 2] + k + 1;
+  src[((int64_t)K * nt + J) * nt + I] = (fac == 1.0) ? d : d * fac;
+}
+
+// Multigrid::RetrieveResult (multigrid.cpp:269-286) with one ghost layer: the solver's
+// finest level, whose ghost layer holds the final boundary fill, into every block's phi
+__global__ void k_scatter_phi(Geom g, double* __restrict__ phi, const int* __restrict__ boff,
+                              const double* __restrict__ um, int n) {
+  const int b = blockIdx.z, k = blockIdx.y;  // k over nx3 + 2
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int w1 = g.nx1 + 2, w2 = g.nx2 + 2;
+  if (t >= w1 * w2) return;
+  const int j = t / w1, i = t - j * w1;
+  const int64_t nt = n + 2;
+  const int I = boff[3 * b] + i, J = boff[3 * b + 1] + j, K = boff[3 * b + 2] + k;
+  phi[(int64_t)b * g.ncell + cidx(g, k + g.ks - 1, j + g.js - 1, i + g.is - 1)] =
+      um[((int64_t)K * nt + J) * nt + I];
+}
+
+// MGGravityDriver::Solve (gravity/mg_gravity.cpp:166-211) on the context's stream
+int gravity_solve(athg_ctx* c) {
+  double *um, *src;
+  int n;
+  int rc = athg::mg_finest(c->grav, &um, &src, &n);
+  if (rc) return rc;
+  const Geom& g = c->g;
+  dim3 gg((unsigned)((g.nx1 * g.nx2 + 255) / 256), (unsigned)g.nx3, (unsigned)c->nb);
+  k_gather_rho<<<gg, 256, 0, c->st>>>(g, c->u, c->boff, src, n, c->four_pi_G);
+  CKL();
+  if ((rc = athg::mg_solve(c->grav, false, nullptr, nullptr))) return rc;
+  dim3 gs((unsigned)(((g.nx1 + 2) * (g.nx2 + 2) + 255) / 256), (unsigned)(g.nx3 + 2),
+          (unsigned)c->nb);
+  k_scatter_phi<<<gs, 256, 0, c->st>>>(g, c->phi, c->boff, um, n);
+  CKL();
+  c->counting += 2;
+  return ATHG_OK;
+}
+
+int launch_self_gravity(athg_ctx* c, int l) {
+  StageW sw = stage_weights(c, l);
+  bool mhd = c->cfg.magnetic != 0;
+  if (c->mixed()) Launcher<float>::self_gravity(c->g, ptrs<float>(c), mhd, sw, c->phi, c->st);
+  else Launcher<double>::self_gravity(c->g, ptrs<double>(c), mhd, sw, c->phi, c->st);
   c->counting += 1;
   CKL();
   return ATHG_OK;
@@ -269,8 +369,11 @@ int do_stage(athg_ctx* c, int stage) {
   if ((rc = launch_fluxes(c, order))) return rc;
   if ((rc = launch_corner(c))) return rc;
   if ((rc = launch_update(c, l))) return rc;
+  // AddSourceTerms (time_integrator.cpp:1655-1676); every stage here is a main stage
+  if (c->grav && (rc = launch_self_gravity(c, l))) return rc;
   if ((rc = launch_ghosts(c))) return rc;
   if ((rc = launch_c2p(c))) return rc;
+  if (c->grav && (rc = gravity_solve(c))) return rc;  // main.cpp:461-466
   if (stage == c->integ.nstages)
     if ((rc = launch_block_dt(c))) return rc;
   return ATHG_OK;
@@ -333,9 +436,11 @@ int athg_create(const athg_config* cfg, athg_ctx** out) {
   *out = nullptr;
   if (cfg->nx1 < 2 || cfg->nx2 < 2 || cfg->nx3 < 2)
     return fail(ATHG_ERR_ARG, "only 3-D MeshBlocks are supported");
-  if (cfg->xorder < 1 || cfg->xorder > 2)
-    return fail(ATHG_ERR_ARG, "xorder must be 1 or 2");
+  if (cfg->xorder < 1 || cfg->xorder > 3)
+    return fail(ATHG_ERR_ARG, "xorder must be 1 (donor cell), 2 (PLM) or 3 (PPM)");
   if (cfg->nghost < 2) return fail(ATHG_ERR_ARG, "nghost must be >= 2");
+  // reconstruct/reconstruction.cpp:90-98: PPM needs three ghost layers
+  if (cfg->xorder == 3 && cfg->nghost < 3) return fail(ATHG_ERR_ARG, "PPM needs nghost >= 3");
   if (cfg->magnetic && !(cfg->rsolver == ATHG_HLLD || cfg->rsolver == ATHG_HLLE))
     return fail(ATHG_ERR_ARG, "MHD needs the HLLD or HLLE solver");
   if (!cfg->magnetic && !(cfg->rsolver == ATHG_HLLC || cfg->rsolver == ATHG_HLLE))
@@ -412,16 +517,27 @@ int athg_set_blocks(athg_ctx* c, int nblocks, const athg_block* blocks) {
     CK(cudaMalloc(&c->r1, sizeof(double) * g.nf1 * nb));
     CK(cudaMalloc(&c->r2, sizeof(double) * g.nf2 * nb));
     CK(cudaMalloc(&c->r3, sizeof(double) * g.nf3 * nb));
-    CK(cudaMalloc(&c->edge, sizeof(double) * 3 * g.ne * nb));
+    CK(cudaMalloc(&c->edge, tsz * 3 * g.ne * nb));
+    if (c->mixed()) {
+      CK(cudaMalloc(&c->bf32[0], sizeof(float) * g.nf1 * nb));
+      CK(cudaMalloc(&c->bf32[1], sizeof(float) * g.nf2 * nb));
+      CK(cudaMalloc(&c->bf32[2], sizeof(float) * g.nf3 * nb));
+      CK(cudaMemsetAsync(c->bf32[0], 0, sizeof(float) * g.nf1 * nb, c->st));
+      CK(cudaMemsetAsync(c->bf32[1], 0, sizeof(float) * g.nf2 * nb, c->st));
+      CK(cudaMemsetAsync(c->bf32[2], 0, sizeof(float) * g.nf3 * nb, c->st));
+    }
     CK(cudaMemsetAsync(c->b1, 0, sizeof(double) * g.nf1 * nb, c->st));
     CK(cudaMemsetAsync(c->b2, 0, sizeof(double) * g.nf2 * nb, c->st));
     CK(cudaMemsetAsync(c->b3, 0, sizeof(double) * g.nf3 * nb, c->st));
-    CK(cudaMemsetAsync(c->edge, 0, sizeof(double) * 3 * g.ne * nb, c->st));
+    CK(cudaMemsetAsync(c->edge, 0, tsz * 3 * g.ne * nb, c->st));
   }
   CK(cudaMemsetAsync(c->u, 0, sizeof(double) * NHYD * g.ncell * nb, c->st));
   CK(cudaMemsetAsync(c->u1, 0, sizeof(double) * NHYD * g.ncell * nb, c->st));
   CK(cudaMalloc(&c->geo, sizeof(BlockGeo) * nb));
-  CK(cudaMalloc(&c->coef, sizeof(double) * nb * 3 * 2 * g.ncmax));
+  CK(cudaMalloc(&c->coef, tsz * nb * 3 * 2 * g.ncmax));
+  CK(cudaMalloc(&c->dxT, tsz * nb * 3));
+  CK(cudaMalloc(&c->mg, sizeof(MixedGeo) * nb));
+  if (c->mixed()) CK(cudaMalloc(&c->dtf, sizeof(float)));
   CK(cudaMalloc(&c->nbr, sizeof(int) * 27 * nb));
   CK(cudaMalloc(&c->scal, sizeof(double) * 16));
   // host-side per-block tables
@@ -449,8 +565,39 @@ int athg_set_blocks(athg_ctx* c, int nblocks, const athg_block* blocks) {
     for (int n = 0; n < 27; ++n) hnbr[27 * b + n] = B.neighbor[n];
   }
   CK(cudaMemcpyAsync(c->geo, hgeo.data(), sizeof(BlockGeo) * nb, cudaMemcpyHostToDevice, c->st));
-  CK(cudaMemcpyAsync(c->coef, hcoef.data(), sizeof(double) * hcoef.size(), cudaMemcpyHostToDevice,
-                     c->st));
+  std::vector<double> hdx(nb * 3);
+  for (int b = 0; b < nblocks; ++b)
+    for (int d = 0; d < 3; ++d) hdx[b * 3 + d] = hgeo[b].dx[d];
+  // Mixed-path widths: blocks of one level whose widths agree to round-off share the
+  // first such block's values (uniform meshes), so shared faces and edges carry one weight
+  std::vector<MixedGeo> hmg(nb);
+  for (int b = 0; b < nblocks; ++b) {
+    const double* dx = hgeo[b].dx;
+    for (int a = 0; a < b; ++a) {
+      if (blocks[a].level != blocks[b].level) continue;
+      bool same = true;
+      for (int d = 0; d < 3; ++d)
+        same = same && std::fabs(hgeo[a].dx[d] - dx[d]) <= 1e-12 * std::fabs(dx[d]);
+      if (same) { dx = hgeo[a].dx; break; }
+    }
+    const double vol = dx[0] * dx[1] * dx[2];
+    for (int d = 0; d < 3; ++d) {
+      hmg[b].idx[d] = (float)(1.0 / dx[d]);
+      hmg[b].dx[d] = (float)dx[d];
+      hmg[b].ia[d] = dx[d] / vol;
+    }
+  }
+  if (c->mixed()) {
+    std::vector<float> fc(hcoef.begin(), hcoef.end()), fdx(hdx.begin(), hdx.end());
+    CK(cudaMemcpyAsync(c->coef, fc.data(), sizeof(float) * fc.size(), cudaMemcpyHostToDevice, c->st));
+    CK(cudaMemcpyAsync(c->dxT, fdx.data(), sizeof(float) * fdx.size(), cudaMemcpyHostToDevice, c->st));
+    CK(cudaStreamSynchronize(c->st));  // the host vectors above go out of scope
+  } else {
+    CK(cudaMemcpyAsync(c->coef, hcoef.data(), sizeof(double) * hcoef.size(), cudaMemcpyHostToDevice,
+                       c->st));
+    CK(cudaMemcpyAsync(c->dxT, hdx.data(), sizeof(double) * hdx.size(), cudaMemcpyHostToDevice, c->st));
+  }
+  CK(cudaMemcpyAsync(c->mg, hmg.data(), sizeof(MixedGeo) * nb, cudaMemcpyHostToDevice, c->st));
   CK(cudaMemcpyAsync(c->nbr, hnbr.data(), sizeof(int) * hnbr.size(), cudaMemcpyHostToDevice,
                      c->st));
   double hs[16] = {0};
@@ -569,6 +716,10 @@ int var_ptr(athg_ctx* c, int var, void** p, bool* narrow) {
     case ATHG_VAR_B3F: *p = c->b3; break;
     case ATHG_VAR_PRIM: *p = c->w; *narrow = c->mixed(); return ATHG_OK;
     case ATHG_VAR_BCC: *p = c->bcc; *narrow = c->mixed(); break;
+    case ATHG_VAR_PHI:
+      if (!c->phi) return fail(ATHG_ERR_ARG, "no self-gravity attached");
+      *p = c->phi;
+      return ATHG_OK;
     default: return fail(ATHG_ERR_ARG, "variable not available");
   }
   if (!c->cfg.magnetic) return fail(ATHG_ERR_ARG, "no magnetic field in a hydro context");
@@ -629,6 +780,7 @@ int athg_initialize(athg_ctx* c) {
   std::memcpy(&big, &kDblMax, 8);
   std::memcpy(&hs[3], &big, 8);
   CK(cudaMemcpyAsync(c->scal, hs, sizeof(hs), cudaMemcpyHostToDevice, c->st));
+  if (c->grav && (rc = gravity_solve(c))) return rc;  // mesh/mesh.cpp:1398-1402
   if ((rc = launch_ghosts(c))) return rc;
   if ((rc = launch_c2p(c))) return rc;
   if ((rc = launch_block_dt(c))) return rc;
@@ -654,6 +806,12 @@ int athg_cycles(athg_ctx* c, int n) {
   int rc = need_pool(c);
   if (rc) return rc;
   if (n <= 0) return ATHG_OK;
+  if (c->grav && !athg::mg_solve_capturable(c->grav)) {
+    // the solve iterates to a threshold or sets up multipole moments on the host
+    for (int q = 0; q < n; ++q)
+      if ((rc = do_cycle(c))) return rc;
+    return ATHG_OK;
+  }
   if ((rc = build_graph(c))) return rc;
   for (int q = 0; q < n; ++q) CK(cudaGraphLaunch(c->gexec, c->st));
   return ATHG_OK;
@@ -663,8 +821,56 @@ int athg_launches_per_cycle(athg_ctx* c, int* n) {
   int rc = need_pool(c);
   if (rc) return rc;
   if (!n) return fail(ATHG_ERR_ARG, "null argument");
+  if (c->grav && !athg::mg_solve_capturable(c->grav))
+    return fail(ATHG_ERR_STATE, "cycles with this multigrid mode are not captured as a graph");
   if ((rc = build_graph(c))) return rc;
   *n = c->launches_per_cycle;
+  return ATHG_OK;
+}
+
+int athg_attach_gravity(athg_ctx* c, athg_mg* mg, double four_pi_G) {
+  int rc = need_pool(c);
+  if (rc) return rc;
+  // drop any captured cycle: the stage sequence changes
+  if (c->gexec) cudaGraphExecDestroy(c->gexec);
+  if (c->graph) cudaGraphDestroy(c->graph);
+  c->gexec = nullptr; c->graph = nullptr;
+  if (c->grav) athg::mg_bind_stream(c->grav, nullptr);
+  c->grav = nullptr;
+  if (!mg) return ATHG_OK;
+  double *um, *src;
+  int n;
+  if ((rc = athg::mg_finest(mg, &um, &src, &n))) return rc;
+  // one uniform level tiling the solver's n^3 root grid
+  const Geom& g = c->g;
+  std::vector<int> hb(3 * c->nb);
+  std::vector<char> seen((size_t)(n / g.nx1 + 1) * (n / g.nx2 + 1) * (n / g.nx3 + 1), 0);
+  if (n % g.nx1 || n % g.nx2 || n % g.nx3)
+    return fail(ATHG_ERR_ARG, "multigrid size is not a multiple of the block size");
+  const int64_t nbx = n / g.nx1, nby = n / g.nx2, nbz = n / g.nx3;
+  if (nbx * nby * nbz != c->nb)
+    return fail(ATHG_ERR_ARG, "blocks do not tile the multigrid root grid");
+  for (int b = 0; b < c->nb; ++b) {
+    const athg_block& B = c->blocks[b];
+    if (B.level != c->blocks[0].level)
+      return fail(ATHG_ERR_ARG, "self-gravity needs blocks of one refinement level");
+    if (B.lx1 < 0 || B.lx1 >= nbx || B.lx2 < 0 || B.lx2 >= nby || B.lx3 < 0 || B.lx3 >= nbz)
+      return fail(ATHG_ERR_ARG, "block location outside the multigrid root grid");
+    char& f = seen[((size_t)B.lx3 * nby + B.lx2) * nbx + B.lx1];
+    if (f) return fail(ATHG_ERR_ARG, "two blocks at one location");
+    f = 1;
+    hb[3 * b] = (int)(B.lx1 * g.nx1);
+    hb[3 * b + 1] = (int)(B.lx2 * g.nx2);
+    hb[3 * b + 2] = (int)(B.lx3 * g.nx3);
+  }
+  if (!c->boff) CK(cudaMalloc(&c->boff, sizeof(int) * 3 * c->nb));
+  if (!c->phi) CK(cudaMalloc(&c->phi, sizeof(double) * g.ncell * c->nb));
+  CK(cudaMemsetAsync(c->phi, 0, sizeof(double) * g.ncell * c->nb, c->st));
+  CK(cudaMemcpyAsync(c->boff, hb.data(), sizeof(int) * hb.size(), cudaMemcpyHostToDevice, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  if ((rc = athg::mg_bind_stream(mg, c->st))) return rc;
+  c->grav = mg;
+  c->four_pi_G = four_pi_G;
   return ATHG_OK;
 }
 
@@ -690,6 +896,8 @@ int athg_set_time(athg_ctx* c, double time, double dt, int64_t ncycle) {
   long long nc = ncycle;
   std::memcpy(&hs[2], &nc, 8);
   CK(cudaMemcpyAsync(c->scal, hs, sizeof(hs), cudaMemcpyHostToDevice, c->st));
+  float df = (float)dt;
+  if (c->dtf) CK(cudaMemcpyAsync(c->dtf, &df, sizeof(float), cudaMemcpyHostToDevice, c->st));
   CK(cudaStreamSynchronize(c->st));
   return ATHG_OK;
 }
@@ -709,7 +917,8 @@ int athg_stream(athg_ctx* c, void** stream) {
 int athg_calculate_fluxes(athg_ctx* c, int order) {
   int rc = need_pool(c);
   if (rc) return rc;
-  if (order < 1 || order > 2) return fail(ATHG_ERR_ARG, "order must be 1 or 2");
+  if (order < 1 || order > 3) return fail(ATHG_ERR_ARG, "order must be 1, 2 or 3");
+  if (order == 3 && c->g.ng < 3) return fail(ATHG_ERR_ARG, "PPM needs nghost >= 3");
   return launch_fluxes(c, order);
 }
 

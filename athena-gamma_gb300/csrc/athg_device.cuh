@@ -14,6 +14,7 @@
 #pragma once
 #include <cstdint>
 #include <cuda_runtime.h>
+#include "athg_numeric.h"
 
 namespace athg {
 
@@ -63,6 +64,7 @@ struct BlockGeo {
 // Physics constants of a run.
 struct Phys {
   double gamma, dfloor, pfloor;
+  double gm1;  // gamma - 1
 };
 
 // Stage weights of the low-storage integrator (reference
@@ -71,6 +73,18 @@ struct StageW {
   double delta, g1, g2, beta;
   int swap;  // g1==0 && g2==1 && g3==0: the reference swaps registers
   int zero_reg;  // first stage: the register starts from zero
+  int copy_reg;  // zero_reg && delta == 1: the register becomes a copy of the state
+  int has_delta;  // delta != 0
+  float betaf;  // beta in FP32 (mixed path)
+};
+
+// Per-block widths of the mixed-path update. Same-level blocks of a uniform mesh share one
+// set of values, so a face flux or an edge EMF enters both neighbours with the same
+// FP32 weight and the sums telescope (conservation and div B stay at round-off).
+struct MixedGeo {
+  float idx[3];    // 1 / dx_d
+  float dx[3];     // dx_d
+  double ia[3];    // dx_d / (dx1 dx2 dx3): face-flux change -> face-field change
 };
 
 // std::min / std::max semantics (first argument wins ties)
@@ -95,6 +109,73 @@ __device__ __forceinline__ T ct_weight(T dflx, T rhol, T rhor, T dx, T dt) {
   T v_over_c = (T(1024.0)) * dt * dflx / (dx * (rhol + rhor));
   T tmp_min = mn(T(0.5), v_over_c);
   return T(0.5) + mx(T(-0.5), tmp_min);
+}
+
+template <typename T> __device__ __forceinline__ T sgn(T x) { return (x < T(0.0)) ? T(-1.0) : T(1.0); }
+
+// PPM of one cell on a uniform Cartesian axis: Colella-Woodward interface values with the
+// Colella-Sekora extremum-preserving limiter (reference src/reconstruct/ppm.cpp:44-342,
+// uniform weights 0.5 and +-1/6 of src/reconstruct/reconstruction.cpp:420-431). From the
+// five cell values q[-2..2] it returns the states at the cell's lower (qm) and upper (qp)
+// faces.
+template <typename T>
+__device__ __forceinline__ void ppm_cell(T q_im2, T q_im1, T q, T q_ip1, T q_ip2, T& qm, T& qp) {
+  const T C2 = T(1.25);
+  const T c1 = T(0.5), c2 = T(0.5), c3 = T(0.5), c4 = T(0.5);
+  const T c5 = T(1.0 / 6.0), c6 = T(-1.0 / 6.0);
+  T qa = (q - q_im1);
+  T qb = (q_ip1 - q);
+  T dd_im1 = c1 * qa + c2 * (q_im1 - q_im2);
+  T dd = c1 * qb + c2 * qa;
+  T dd_ip1 = c1 * (q_ip2 - q_ip1) + c2 * qb;
+  T dph = (c3 * q_im1 + c4 * q) + (c5 * dd_im1 + c6 * dd);
+  T dph_ip1 = (c3 * q + c4 * q_ip1) + (c5 * dd + c6 * dd_ip1);
+  T d2qc_im1 = q_im2 + q - T(2.0) * q_im1;
+  T d2qc = q_im1 + q_ip1 - T(2.0) * q;
+  T d2qc_ip1 = q + q_ip2 - T(2.0) * q_ip1;
+  {
+    T qa_tmp = dph - q_im1, qb_tmp = q - dph;
+    T a = T(3.0) * (q_im1 + q - T(2.0) * dph), b = d2qc_im1, c = d2qc;
+    T qd = T(0.0);
+    if (sgn(a) == sgn(b) && sgn(a) == sgn(c))
+      qd = sgn(a) * mn(C2 * fabs(b), mn(C2 * fabs(c), fabs(a)));
+    T dph_tmp = T(0.5) * (q_im1 + q) - qd / T(6.0);
+    if (qa_tmp * qb_tmp < T(0.0)) dph = dph_tmp;
+  }
+  {
+    T qa_tmp = dph_ip1 - q, qb_tmp = q_ip1 - dph_ip1;
+    T a = T(3.0) * (q + q_ip1 - T(2.0) * dph_ip1), b = d2qc, c = d2qc_ip1;
+    T qd = T(0.0);
+    if (sgn(a) == sgn(b) && sgn(a) == sgn(c))
+      qd = sgn(a) * mn(C2 * fabs(b), mn(C2 * fabs(c), fabs(a)));
+    T dphip1_tmp = T(0.5) * (q + q_ip1) - qd / T(6.0);
+    if (qa_tmp * qb_tmp < T(0.0)) dph_ip1 = dphip1_tmp;
+  }
+  T d2qf = T(6.0) * (dph + dph_ip1 - T(2.0) * q);
+  T qminus = dph, qplus = dph_ip1;
+  T dqf_minus = q - qminus, dqf_plus = qplus - q;
+  T qa_tmp = dqf_minus * dqf_plus;
+  T qb_tmp = (q_ip1 - q) * (q - q_im1);
+  T a = d2qc_im1, b = d2qc, c = d2qc_ip1, d = d2qf, qe = T(0.0);
+  if (sgn(a) == sgn(b) && sgn(a) == sgn(c) && sgn(a) == sgn(d))
+    qe = sgn(d) * mn(mn(C2 * fabs(a), C2 * fabs(b)), mn(C2 * fabs(c), fabs(d)));
+  a = mx(fabs(q_im1), fabs(q_im2));
+  b = mx(mx(fabs(q), fabs(q_ip1)), fabs(q_ip2));
+  T rho = T(0.0);
+  if (fabs(d) > T(1.0e-12) * mx(a, b)) rho = qe / d;
+  T tmp_m = q - rho * dqf_minus, tmp_p = q + rho * dqf_plus;
+  T tmp2_m = q - T(2.0) * dqf_plus, tmp2_p = q + T(2.0) * dqf_minus;
+  if ((qa_tmp <= T(0.0) || qb_tmp <= T(0.0))) {
+    if (rho <= (T(1.0) - T(1.0e-12))) {
+      qminus = tmp_m;
+      qplus = tmp_p;
+    }
+  } else {
+    if (fabs(dqf_minus) >= T(2.0) * fabs(dqf_plus)) qminus = tmp2_m;
+    if (fabs(dqf_plus) >= T(2.0) * fabs(dqf_minus)) qplus = tmp2_p;
+  }
+  qm = qminus;
+  qp = qplus;
 }
 
 // ------------------------------------------------------------------------------------

@@ -30,6 +30,9 @@ struct Launcher {
   // EquationOfState::ConservedToPrimitive over interior and ghost cells.
   static void c2p(const Geom& g, const StagePtrs<T>& p, bool mhd, const Phys& ph,
                   cudaStream_t st);
+  // HydroSourceTerms::SelfGravity over every block (phi: [nb][cells] potential).
+  static void self_gravity(const Geom& g, const StagePtrs<T>& p, bool mhd, const StageW& sw,
+                           const double* phi, cudaStream_t st);
   // Hydro::NewBlockTimeStep over every block, reduced to one minimum.
   static void block_dt(const Geom& g, const StagePtrs<T>& p, bool mhd, const Phys& ph,
                        unsigned long long* dtmin, cudaStream_t st);
@@ -50,6 +53,23 @@ static void flux_dir(const Geom& g, const StagePtrs<T>& p, bool mhd, int solver,
     ku = g.ke + 1;
     if (mhd) { il = g.is - 1; iu = g.ie + 1; jl = g.js - 1; ju = g.je + 1; }
   }
+  if constexpr (DIR != 0) {
+    // marching sweeps: pencils over (i, k) for DIR=1 and (i, j) for DIR=2
+    Box pb = DIR == 1 ? make_box(il, iu, kl, ku, 0, 0) : make_box(il, iu, jl, ju, 0, 0);
+    const int fs = DIR == 1 ? jl : kl, fe = DIR == 1 ? ju : ku;
+    dim3 grid((unsigned)((pb.ni * pb.nj + 127) / 128), 1, (unsigned)g.nb);
+    if (mhd) {
+      if (solver == HLLD)
+        k_flux_march<T, DIR, ORDER, HLLD, true><<<grid, 128, 0, st>>>(g, p, pb, ph, fs, fe);
+      else
+        k_flux_march<T, DIR, ORDER, HLLE, true><<<grid, 128, 0, st>>>(g, p, pb, ph, fs, fe);
+    } else {
+      if (solver == HLLC)
+        k_flux_march<T, DIR, ORDER, HLLC, false><<<grid, 128, 0, st>>>(g, p, pb, ph, fs, fe);
+      else
+        k_flux_march<T, DIR, ORDER, HLLE, false><<<grid, 128, 0, st>>>(g, p, pb, ph, fs, fe);
+    }
+  } else {
   Box b = make_box(il, iu, jl, ju, kl, ku);
   dim3 grid = box_grid(b, g.nb, 128);
   if (mhd) {
@@ -58,6 +78,7 @@ static void flux_dir(const Geom& g, const StagePtrs<T>& p, bool mhd, int solver,
   } else {
     if (solver == HLLC) k_flux<T, DIR, ORDER, HLLC, false><<<grid, 128, 0, st>>>(g, p, b, ph);
     else k_flux<T, DIR, ORDER, HLLE, false><<<grid, 128, 0, st>>>(g, p, b, ph);
+  }
   }
 }
 
@@ -68,6 +89,10 @@ void Launcher<T>::fluxes(const Geom& g, const StagePtrs<T>& p, bool mhd, int sol
     flux_dir<T, 0, 1>(g, p, mhd, solver, ph, st);
     flux_dir<T, 1, 1>(g, p, mhd, solver, ph, st);
     flux_dir<T, 2, 1>(g, p, mhd, solver, ph, st);
+  } else if (order == 3) {
+    flux_dir<T, 0, 3>(g, p, mhd, solver, ph, st);
+    flux_dir<T, 1, 3>(g, p, mhd, solver, ph, st);
+    flux_dir<T, 2, 3>(g, p, mhd, solver, ph, st);
   } else {
     flux_dir<T, 0, 2>(g, p, mhd, solver, ph, st);
     flux_dir<T, 1, 2>(g, p, mhd, solver, ph, st);
@@ -88,6 +113,14 @@ void Launcher<T>::update(const Geom& g, const StagePtrs<T>& p, bool mhd, const S
               : make_box(g.is, g.ie, g.js, g.je, g.ks, g.ke);
   if (mhd) k_update<T, true><<<box_grid(b, g.nb, 128), 128, 0, st>>>(g, p, b, sw);
   else k_update<T, false><<<box_grid(b, g.nb, 128), 128, 0, st>>>(g, p, b, sw);
+}
+
+template <typename T>
+void Launcher<T>::self_gravity(const Geom& g, const StagePtrs<T>& p, bool mhd, const StageW& sw,
+                               const double* phi, cudaStream_t st) {
+  Box b = make_box(g.is, g.ie, g.js, g.je, g.ks, g.ke);
+  if (mhd) k_self_gravity<T, true><<<box_grid(b, g.nb, 128), 128, 0, st>>>(g, p, b, sw, phi);
+  else k_self_gravity<T, false><<<box_grid(b, g.nb, 128), 128, 0, st>>>(g, p, b, sw, phi);
 }
 
 template <typename T>

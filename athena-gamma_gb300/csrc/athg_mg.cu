@@ -21,6 +21,7 @@
 #include <vector>
 
 #include "athena_gb300.h"
+#include "athg_internal.h"
 
 namespace athg {
 // the error channel of athg_last_error() (defined in athg_api.cu)
@@ -500,6 +501,7 @@ struct athg_mg {
   bool periodic = true, subtract = true, fas = false, any_mp = false;
   double rdx = 0.0, vol = 0.0;
   cudaStream_t st = nullptr;
+  cudaStream_t own_st = nullptr;  // the stream created with the solver
   Hier<double> h64;      // FP64 path: all levels; mixed path: finest level only
   Hier<float> h32;       // mixed path: FP32 hierarchy
   double* red = nullptr; // reduction scratch [0..31]
@@ -806,6 +808,7 @@ int athg_mg_create(const athg_mg_config* cfg, athg_mg** out) {
     delete m;
     return mgfail(ATHG_ERR_CUDA, "cudaStreamCreate failed");
   }
+  m->own_st = m->st;
   if (cfg->precision == ATHG_MIXED) {
     // FP64 solution and source on the finest level only; FP32 hierarchy for the cycles
     rc = alloc_top(m->h64, lmax, m->rdx);
@@ -829,7 +832,7 @@ int athg_mg_destroy(athg_mg* m) {
   free_hier(m->h32);
   if (m->red) cudaFree(m->red);
   if (m->mpo_d) cudaFree(m->mpo_d);
-  if (m->st) cudaStreamDestroy(m->st);
+  if (m->own_st) cudaStreamDestroy(m->own_st);
   delete m;
   return ATHG_OK;
 }
@@ -878,8 +881,29 @@ int athg_mg_get_phi(athg_mg* m, double* phi, size_t count) {
   return ATHG_OK;
 }
 
-int athg_mg_solve(athg_mg* m, int* iterations, double* defect_norm) {
-  if (!m) return mgfail(ATHG_ERR_ARG, "null argument");
+}  // extern "C"
+
+namespace athg {
+
+int mg_finest(athg_mg* m, double** u, double** src, int* n) {
+  if (!m) return mgfail(ATHG_ERR_ARG, "null multigrid");
+  *u = m->h64.u[m->lmax];
+  *src = m->h64.src[m->lmax];
+  *n = 1 << m->lmax;
+  return ATHG_OK;
+}
+
+int mg_bind_stream(athg_mg* m, cudaStream_t st) {
+  if (!m) return mgfail(ATHG_ERR_ARG, "null multigrid");
+  m->st = st ? st : m->own_st;
+  return ATHG_OK;
+}
+
+bool mg_solve_capturable(const athg_mg* m) {
+  return m && m->cfg.threshold < 0.0 && !m->any_mp;
+}
+
+int mg_solve(athg_mg* m, bool want_norm, int* iterations, double* defect_norm) {
   const int top = m->lmax;
   Hier<double>& H = m->h64;
   m->iterations = 0;
@@ -917,15 +941,24 @@ int athg_mg_solve(athg_mg* m, int* iterations, double* defect_norm) {
       RC(one_cycle(m));
       m->iterations++;
     }
-    RC(defect_norm64(m, &def));
+    if (want_norm) RC(defect_norm64(m, &def));
   }
   if (m->subtract) RC(subtract_mean(m, H, H.u[top], top));
   RC(apply_bc(m, H, top, false));
-  MCK(cudaStreamSynchronize(m->st));
+  if (want_norm) MCK(cudaStreamSynchronize(m->st));
   m->last_norm = def;
   if (iterations) *iterations = m->iterations;
   if (defect_norm) *defect_norm = def;
   return ATHG_OK;
+}
+
+}  // namespace athg
+
+extern "C" {
+
+int athg_mg_solve(athg_mg* m, int* iterations, double* defect_norm) {
+  if (!m) return mgfail(ATHG_ERR_ARG, "null argument");
+  return athg::mg_solve(m, true, iterations, defect_norm);
 }
 
 int athg_mg_vcycles(athg_mg* m, int n) {

@@ -1,0 +1,88 @@
+// athg_numeric.h -- format conversions and error-free sums of the mixed-precision path.
+//
+// FP64 instructions (conversions included) issue at a small fraction of the FP32 rate on
+// this GPU, so the mixed path converts between the IEEE 754 binary32 and binary64 formats
+// with integer operations and sums FP32 values with error-free transformations, leaving
+// only the few FP64 additions that touch the FP64 state. Everything here is plain C++
+// (host and device), so the CPU tests check it bit for bit against the host's own casts.
+#pragma once
+#include <cstdint>
+#include <cstring>
+
+#ifdef __CUDACC__
+#define ATHG_HD __host__ __device__ __forceinline__
+#else
+#define ATHG_HD inline
+#endif
+
+namespace athg {
+
+ATHG_HD uint32_t bits_f(float f) { uint32_t u; std::memcpy(&u, &f, 4); return u; }
+ATHG_HD uint64_t bits_d(double d) { uint64_t u; std::memcpy(&u, &d, 8); return u; }
+ATHG_HD float from_bits_f(uint32_t u) { float f; std::memcpy(&f, &u, 4); return f; }
+ATHG_HD double from_bits_d(uint64_t u) { double d; std::memcpy(&d, &u, 8); return d; }
+
+// binary32 -> binary64, exact for normal numbers; zero and subnormal inputs give a
+// signed zero (the FP32 kernels flush subnormals), infinities and NaNs keep their class.
+ATHG_HD double f2d_int(float f) {
+  const uint32_t x = bits_f(f);
+  const uint32_t a = x & 0x7fffffffu;
+  const uint64_t s = (uint64_t)(x & 0x80000000u) << 32;
+  uint64_t m = ((uint64_t)a << 29) + 0x3800000000000000ull;  // exponent bias 127 -> 1023
+  if (a < 0x00800000u) m = 0ull;
+  if (a >= 0x7f800000u) m = 0x7ff0000000000000ull | ((uint64_t)(a & 0x007fffffu) << 29);
+  return from_bits_d(s | m);
+}
+
+// binary64 -> binary32 rounded to nearest, ties to even; results that round below the
+// smallest normal binary32 flush to a signed zero, results above the largest become
+// infinity. Works on the two 32-bit halves: masking the sign off the whole 64-bit
+// pattern is the idiom compilers turn back into an FP64 absolute value.
+ATHG_HD float d2f_int(double d) {
+  const uint64_t x = bits_d(d);
+  const uint32_t hi = (uint32_t)(x >> 32), lo = (uint32_t)x;
+  const uint32_t s = hi & 0x80000000u;
+  const uint32_t ed = (hi >> 20) & 0x7ffu;                  // binary64 exponent
+  const uint32_t m23 = ((hi & 0x000fffffu) << 3) | (lo >> 29);  // kept mantissa bits
+  const uint32_t rb = lo & 0x1fffffffu;                      // the 29 dropped bits
+  const uint32_t up = (rb > 0x10000000u || (rb == 0x10000000u && (m23 & 1u))) ? 1u : 0u;
+  const int fe = (int)ed - 896;                              // binary32 exponent
+  uint32_t m;
+  if (ed == 0x7ffu) m = (m23 | (hi & 0x000fffffu) | lo) ? 0x7fc00000u : 0x7f800000u;
+  else if (fe >= 255) m = 0x7f800000u;
+  else if (fe <= 0) m = (fe == 0 && m23 == 0x7fffffu && up) ? 0x00800000u : 0u;
+  else m = (((uint32_t)fe << 23) | m23) + up;               // a carry moves into the exponent
+  return from_bits_f(s | m);
+}
+
+// Knuth's TwoSum: s + e == a + b exactly in round-to-nearest binary32 arithmetic (only
+// additions, so no contraction into FMA can change it)
+ATHG_HD void two_sum(float a, float b, float& s, float& e) {
+  s = a + b;
+  const float bp = s - a;
+  e = (a - (s - bp)) + (b - bp);
+}
+
+// (a - b) + (c - d) + (f - h) as an unevaluated pair hi + lo (cascaded TwoSum,
+// Ogita-Rump-Oishi Sum2): |hi + lo - exact| <= about 2^-44 (|a|+|b|+...+|h|)
+ATHG_HD void sum3diff(float a, float b, float c, float d, float f, float h, float& hi,
+                      float& lo) {
+  float s1, e1, s2, e2, s3, e3, t, e4, e5;
+  two_sum(a, -b, s1, e1);
+  two_sum(c, -d, s2, e2);
+  two_sum(f, -h, s3, e3);
+  two_sum(s1, s2, t, e4);
+  two_sum(t, s3, hi, e5);
+  lo = ((e1 + e2) + e3) + (e4 + e5);
+}
+
+// (a - b) + (c - d) as hi + lo: |hi + lo - exact| <= about 2^-45 (|a|+|b|+|c|+|d|)
+ATHG_HD void sum2diff(float a, float b, float c, float d, float& hi, float& lo) {
+  float s1, e1, s2, e2, e3;
+  two_sum(a, -b, s1, e1);
+  two_sum(c, -d, s2, e2);
+  two_sum(s1, s2, hi, e3);
+  lo = (e1 + e2) + e3;
+}
+
+}  // namespace athg

@@ -4,6 +4,8 @@
 //
 // Each launch covers every MeshBlock of the pool (grid.z runs over k and blocks).
 #pragma once
+#include <type_traits>
+
 #include "athg_device.cuh"
 
 namespace athg {
@@ -17,11 +19,21 @@ struct StagePtrs {
   T *w, *bcc;                // primitives [nb][5][cells], cell-centred B [nb][3][cells]
   T *flx[3];                 // per direction [nb][NF][faces]; NF = 5 (hydro) or 8 (MHD:
                              // 5 fluxes, ey, ez, CT weight)
-  double *edge;              // corner EMFs [nb][3][edges]
-  const BlockGeo *geo;       // [nb]
-  const double *coef;        // PLM interface coefficients [nb][3][2][ncmax]
+  T *edge;                   // corner EMFs [nb][3][edges]
+  const BlockGeo *geo;       // [nb] cell widths (FP64)
+  const T *coef;             // PLM interface coefficients [nb][3][2][ncmax]
+  const T *dxT;              // [nb][3] cell widths in T
   const double *dt;          // current time step (device scalar)
+  const T *dtT;              // the same time step in T
+  const T *bf[3];            // face field as read by the flux kernels: the FP64 field itself,
+                             // or its FP32 copy (written by k_c2p) in the mixed path
+  T *bfw[3];                 // where k_c2p writes that FP32 copy (mixed path only)
+  const MixedGeo *mg;        // [nb] widths of the mixed-path update
 };
+
+// The mixed path keeps FP64 work (which runs at a small fraction of the FP32 rate on this
+// GPU, conversions included) out of the FP32 kernels.
+template <typename T> constexpr bool kMixed = std::is_same<T, float>::value;
 
 // Index box of one launch: every (i,j) of the box is flattened onto grid.x (so ranges
 // like is..ie+1 do not leave idle half-warps), grid.y runs over k, grid.z over blocks.
@@ -74,10 +86,29 @@ k_flux(Geom g, StagePtrs<T> p, Box bx, Phys ph) {
       wl[n] = wave_var<T, DIR>(w, bcc, nc, n, c - st);
       wr[n] = wave_var<T, DIR>(w, bcc, nc, n, c);
     }
+  } else if (ORDER == 3) {
+#pragma unroll
+    for (int n = 0; n < NW; ++n) {
+      T v0 = wave_var<T, DIR>(w, bcc, nc, n, c - 3 * st);
+      T v1 = wave_var<T, DIR>(w, bcc, nc, n, c - 2 * st);
+      T v2 = wave_var<T, DIR>(w, bcc, nc, n, c - st);
+      T v3 = wave_var<T, DIR>(w, bcc, nc, n, c);
+      T v4 = wave_var<T, DIR>(w, bcc, nc, n, c + st);
+      T v5 = wave_var<T, DIR>(w, bcc, nc, n, c + 2 * st);
+      T qm, qp, unused;
+      ppm_cell<T>(v0, v1, v2, v3, v4, unused, qp);
+      ppm_cell<T>(v1, v2, v3, v4, v5, qm, unused);
+      wl[n] = qp;
+      wr[n] = qm;
+    }
+    // density and pressure floors on the PPM states (ppm.cpp:326-332)
+    const T df = (T)ph.dfloor, pf = (T)ph.pfloor;
+    wl[IDN] = (wl[IDN] > df) ? wl[IDN] : df; wl[IPR] = (wl[IPR] > pf) ? wl[IPR] : pf;
+    wr[IDN] = (wr[IDN] > df) ? wr[IDN] : df; wr[IPR] = (wr[IPR] > pf) ? wr[IPR] : pf;
   } else {
-    const double* cf = p.coef + ((int64_t)b * 3 + DIR) * 2 * g.ncmax;
-    const T cpL = (T)cf[f - 1];              // (x_f(c+1) - x_v(c)) / dx  for c = f-1
-    const T cmR = (T)cf[g.ncmax + f];        // (x_v(c) - x_f(c)) / dx    for c = f
+    const T* cf = p.coef + ((int64_t)b * 3 + DIR) * 2 * g.ncmax;
+    const T cpL = cf[f - 1];                 // (x_f(c+1) - x_v(c)) / dx  for c = f-1
+    const T cmR = cf[g.ncmax + f];           // (x_v(c) - x_f(c)) / dx    for c = f
 #pragma unroll
     for (int n = 0; n < NW; ++n) {
       T a0 = wave_var<T, DIR>(w, bcc, nc, n, c - 2 * st);
@@ -109,14 +140,12 @@ k_flux(Geom g, StagePtrs<T> p, Box bx, Phys ph) {
   if constexpr (MHD) {
     wli[IBY] = wl[IBY]; wli[IBZ] = wl[IBZ];
     wri[IBY] = wr[IBY]; wri[IBZ] = wr[IBZ];
-    const double* bn = DIR == 0 ? p.b1 + (int64_t)b * g.nf1
-                                : (DIR == 1 ? p.b2 + (int64_t)b * g.nf2 : p.b3 + (int64_t)b * g.nf3);
-    const T bxi = (T)bn[fi];
+    const T bxi = p.bf[DIR][(int64_t)b * nf + fi];
     if (SOLVER == HLLD) rs_hlld<T>(wli, wri, bxi, gam, fx);
     else rs_hlle_mhd<T>(wli, wri, bxi, gam, fx);
     out[5 * nf + fi] = -fx[IBY];
     out[6 * nf + fi] = fx[IBZ];
-    out[7 * nf + fi] = ct_weight<T>(fx[IDN], wli[IDN], wri[IDN], (T)p.geo[b].dx[DIR], (T)(*p.dt));
+    out[7 * nf + fi] = ct_weight<T>(fx[IDN], wli[IDN], wri[IDN], p.dxT[b * 3 + DIR], *p.dtT);
   } else {
     if (SOLVER == HLLC) rs_hllc<T>(wli, wri, gam, fx);
     else rs_hlle_hydro<T>(wli, wri, gam, fx);
@@ -126,6 +155,160 @@ k_flux(Geom g, StagePtrs<T> p, Box bx, Phys ph) {
   out[ivy * nf + fi] = fx[IVY];
   out[ivz * nf + fi] = fx[IVZ];
   out[IEN * nf + fi] = fx[IEN];
+}
+
+// Riemann solve of one face from reconstructed states in the unrotated order, storing the
+// flux (and for MHD the face EMFs and CT weight) like k_flux.
+template <typename T, int DIR, int SOLVER, bool MHD>
+__device__ __forceinline__ void face_solve(const Geom& g, const StagePtrs<T>& p, const Phys& ph,
+                                           int b, int64_t fi, const T* wl, const T* wr) {
+  constexpr int NF = MHD ? 8 : 5;
+  constexpr int ivx = IVX + DIR, ivy = IVX + (DIR + 1) % 3, ivz = IVX + (DIR + 2) % 3;
+  T wli[7], wri[7], fx[7];
+  wli[IDN] = wl[IDN]; wli[IVX] = wl[ivx]; wli[IVY] = wl[ivy]; wli[IVZ] = wl[ivz];
+  wli[IPR] = wl[IPR];
+  wri[IDN] = wr[IDN]; wri[IVX] = wr[ivx]; wri[IVY] = wr[ivy]; wri[IVZ] = wr[ivz];
+  wri[IPR] = wr[IPR];
+  const int64_t nf = fsize<DIR>(g);
+  T* __restrict__ out = p.flx[DIR] + (int64_t)b * NF * nf;
+  const T gam = (T)ph.gamma;
+  if constexpr (MHD) {
+    wli[IBY] = wl[IBY]; wli[IBZ] = wl[IBZ];
+    wri[IBY] = wr[IBY]; wri[IBZ] = wr[IBZ];
+    const T bxi = p.bf[DIR][(int64_t)b * nf + fi];
+    if (SOLVER == HLLD) rs_hlld<T>(wli, wri, bxi, gam, fx);
+    else rs_hlle_mhd<T>(wli, wri, bxi, gam, fx);
+    out[5 * nf + fi] = -fx[IBY];
+    out[6 * nf + fi] = fx[IBZ];
+    out[7 * nf + fi] = ct_weight<T>(fx[IDN], wli[IDN], wri[IDN], p.dxT[b * 3 + DIR], *p.dtT);
+  } else {
+    if (SOLVER == HLLC) rs_hllc<T>(wli, wri, gam, fx);
+    else rs_hlle_hydro<T>(wli, wri, gam, fx);
+  }
+  out[IDN * nf + fi] = fx[IDN];
+  out[ivx * nf + fi] = fx[IVX];
+  out[ivy * nf + fi] = fx[IVY];
+  out[ivz * nf + fi] = fx[IVZ];
+  out[IEN * nf + fi] = fx[IEN];
+}
+
+// Marching face-flux kernel for the j (DIR=1) and k (DIR=2) sweeps: one thread per
+// pencil along DIR (consecutive threads on consecutive i, so every load is coalesced),
+// walking faces fs..fe with a register window of three cells. Each cell is loaded once
+// and its limited slope computed once, giving the right state of its lower face and the
+// left state of its upper face -- the same row-by-row reuse as the reference's
+// wl_/wlb_ swap in hydro/calculate_fluxes.cpp:174-212 and :278-316.
+// The box describes the transverse pencil set (i, and k or j) and the face range (nk).
+template <typename T, int DIR, int ORDER, int SOLVER, bool MHD>
+__global__ void __launch_bounds__(128)
+k_flux_march(Geom g, StagePtrs<T> p, Box bx, Phys ph, int fs, int fe) {
+  static_assert(DIR == 1 || DIR == 2, "marching sweeps are transverse to i");
+  int i, a, unused, b;
+  {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= bx.ni * bx.nj) return;
+    int aa = t / bx.ni;
+    i = bx.il + (t - aa * bx.ni);
+    a = bx.jl + aa;  // the other transverse index: k for DIR=1, j for DIR=2
+    b = blockIdx.z;
+    (void)unused;
+  }
+  constexpr int NW = MHD ? 7 : 5;
+  const int64_t nc = g.ncell;
+  const T* __restrict__ w = p.w + (int64_t)b * NHYD * nc;
+  const T* __restrict__ bcc = MHD ? p.bcc + (int64_t)b * 3 * nc : nullptr;
+  const int64_t st = DIR == 1 ? (int64_t)g.nc1 : (int64_t)g.nc1 * g.nc2;
+  // cell index of pencil position f
+  auto cell_at = [&](int f) -> int64_t {
+    return DIR == 1 ? cidx(g, a, f, i) : cidx(g, f, a, i);
+  };
+  auto face_at = [&](int f) -> int64_t {
+    return DIR == 1 ? f2idx(g, a, f, i) : f3idx(g, f, a, i);
+  };
+  const T* cf = p.coef + ((int64_t)b * 3 + DIR) * 2 * g.ncmax;
+  T cm1[7], c0[7], cp1[7], wlnext[7], wr[7];
+  if (ORDER == 1) {
+    int64_t c = cell_at(fs - 1);
+#pragma unroll
+    for (int n = 0; n < NW; ++n) wlnext[n] = wave_var<T, DIR>(w, bcc, nc, n, c);
+    for (int f = fs; f <= fe; ++f) {
+      int64_t cc = c + st;
+#pragma unroll
+      for (int n = 0; n < NW; ++n) wr[n] = wave_var<T, DIR>(w, bcc, nc, n, cc);
+      face_solve<T, DIR, SOLVER, MHD>(g, p, ph, b, face_at(f), wlnext, wr);
+#pragma unroll
+      for (int n = 0; n < NW; ++n) wlnext[n] = wr[n];
+      c = cc;
+    }
+    return;
+  }
+  if (ORDER == 3) {
+    // PPM: window of five cells; cell f gives the right state of face f (qminus) and
+    // the left state of face f+1 (qplus)
+    const T df = (T)ph.dfloor, pf = (T)ph.pfloor;
+    T win[5][7];
+    int64_t c = cell_at(fs - 1);
+#pragma unroll
+    for (int n = 0; n < NW; ++n) {
+#pragma unroll
+      for (int q = 0; q < 5; ++q) win[q][n] = wave_var<T, DIR>(w, bcc, nc, n, c + (q - 2) * st);
+      T unused;
+      ppm_cell<T>(win[0][n], win[1][n], win[2][n], win[3][n], win[4][n], unused, wlnext[n]);
+    }
+    for (int f = fs; f <= fe; ++f) {
+      c += st;  // cell f
+#pragma unroll
+      for (int n = 0; n < NW; ++n) {
+        win[0][n] = win[1][n]; win[1][n] = win[2][n]; win[2][n] = win[3][n];
+        win[3][n] = win[4][n];
+        win[4][n] = wave_var<T, DIR>(w, bcc, nc, n, c + 2 * st);
+        T qm, qp;
+        ppm_cell<T>(win[0][n], win[1][n], win[2][n], win[3][n], win[4][n], qm, qp);
+        wr[n] = qm;
+        cm1[n] = wlnext[n];
+        wlnext[n] = qp;
+      }
+      cm1[IDN] = (cm1[IDN] > df) ? cm1[IDN] : df; cm1[IPR] = (cm1[IPR] > pf) ? cm1[IPR] : pf;
+      wr[IDN] = (wr[IDN] > df) ? wr[IDN] : df; wr[IPR] = (wr[IPR] > pf) ? wr[IPR] : pf;
+      face_solve<T, DIR, SOLVER, MHD>(g, p, ph, b, face_at(f), cm1, wr);
+    }
+    return;
+  }
+  // prologue: cells fs-2, fs-1, fs -> left state of face fs from the slope of cell fs-1
+  {
+    int64_t c = cell_at(fs - 1);
+    const T cp = cf[fs - 1];
+#pragma unroll
+    for (int n = 0; n < NW; ++n) {
+      cm1[n] = wave_var<T, DIR>(w, bcc, nc, n, c - st);
+      c0[n] = wave_var<T, DIR>(w, bcc, nc, n, c);
+      cp1[n] = wave_var<T, DIR>(w, bcc, nc, n, c + st);
+      T dwl = (c0[n] - cm1[n]), dwr = (cp1[n] - c0[n]);
+      T dw2 = dwl * dwr;
+      T dwm = T(2.0) * dw2 / (dwl + dwr);
+      if (dw2 <= T(0.0)) dwm = T(0.0);
+      wlnext[n] = c0[n] + cp * dwm;
+    }
+  }
+  int64_t c = cell_at(fs);  // c0 <- cell fs (window shifts at loop start)
+  for (int f = fs; f <= fe; ++f) {
+    const T cmR = cf[g.ncmax + f], cpR = cf[f];
+#pragma unroll
+    for (int n = 0; n < NW; ++n) {
+      cm1[n] = c0[n];
+      c0[n] = cp1[n];
+      cp1[n] = wave_var<T, DIR>(w, bcc, nc, n, c + st);
+      T dwl = (c0[n] - cm1[n]), dwr = (cp1[n] - c0[n]);
+      T dw2 = dwl * dwr;
+      T dwm = T(2.0) * dw2 / (dwl + dwr);
+      if (dw2 <= T(0.0)) dwm = T(0.0);
+      wr[n] = c0[n] - cmR * dwm;
+      cm1[n] = wlnext[n];                 // reuse the slot: left state of face f
+      wlnext[n] = c0[n] + cpR * dwm;      // left state of face f+1
+    }
+    face_solve<T, DIR, SOLVER, MHD>(g, p, ph, b, face_at(f), cm1, wr);
+    c += st;
+  }
 }
 
 // Corner EMFs (Gardiner & Stone upwind integration), one thread per corner location
@@ -162,7 +345,7 @@ __global__ void __launch_bounds__(128) k_corner_emf(Geom g, StagePtrs<T> p, Box 
   auto e1x3 = [&](int kk, int jj, int ii) { return F3[6 * n3 + f3idx(g, kk, jj, ii)]; };
   auto wx3 = [&](int kk, int jj, int ii) { return F3[7 * n3 + f3idx(g, kk, jj, ii)]; };
   const T one = T(1.0), q = T(0.25);
-  double* E = p.edge + (int64_t)b * 3 * g.ne;
+  T* E = p.edge + (int64_t)b * 3 * g.ne;
   const int64_t ei = eidx(g, k, j, i);
   {
     T de1_l3 = (one - wx2(k - 1, j, i)) * (e1x3(k, j, i) - cce(0, k - 1, j, i)) +
@@ -173,8 +356,8 @@ __global__ void __launch_bounds__(128) k_corner_emf(Geom g, StagePtrs<T> p, Box 
                (wx3(k, j - 1, i)) * (e1x2(k - 1, j, i) - cce(0, k - 1, j - 1, i));
     T de1_r2 = (one - wx3(k, j, i)) * (e1x2(k, j, i) - cce(0, k, j, i)) +
                (wx3(k, j, i)) * (e1x2(k - 1, j, i) - cce(0, k - 1, j, i));
-    E[ei] = (double)(q * (de1_l3 + de1_r3 + de1_l2 + de1_r2 + e1x2(k - 1, j, i) +
-                          e1x2(k, j, i) + e1x3(k, j - 1, i) + e1x3(k, j, i)));
+    E[ei] = q * (de1_l3 + de1_r3 + de1_l2 + de1_r2 + e1x2(k - 1, j, i) +
+                 e1x2(k, j, i) + e1x3(k, j - 1, i) + e1x3(k, j, i));
   }
   {
     T de2_l3 = (one - wx1(k - 1, j, i)) * (e2x3(k, j, i) - cce(1, k - 1, j, i)) +
@@ -185,8 +368,8 @@ __global__ void __launch_bounds__(128) k_corner_emf(Geom g, StagePtrs<T> p, Box 
                (wx3(k, j, i - 1)) * (e2x1(k - 1, j, i) - cce(1, k - 1, j, i - 1));
     T de2_r1 = (one - wx3(k, j, i)) * (e2x1(k, j, i) - cce(1, k, j, i)) +
                (wx3(k, j, i)) * (e2x1(k - 1, j, i) - cce(1, k - 1, j, i));
-    E[g.ne + ei] = (double)(q * (de2_l3 + de2_r3 + de2_l1 + de2_r1 + e2x3(k, j, i - 1) +
-                                 e2x3(k, j, i) + e2x1(k - 1, j, i) + e2x1(k, j, i)));
+    E[g.ne + ei] = q * (de2_l3 + de2_r3 + de2_l1 + de2_r1 + e2x3(k, j, i - 1) +
+                        e2x3(k, j, i) + e2x1(k - 1, j, i) + e2x1(k, j, i));
   }
   {
     T de3_l2 = (one - wx1(k, j - 1, i)) * (e3x2(k, j, i) - cce(2, k, j - 1, i)) +
@@ -197,8 +380,8 @@ __global__ void __launch_bounds__(128) k_corner_emf(Geom g, StagePtrs<T> p, Box 
                (wx2(k, j, i - 1)) * (e3x1(k, j - 1, i) - cce(2, k, j - 1, i - 1));
     T de3_r1 = (one - wx2(k, j, i)) * (e3x1(k, j, i) - cce(2, k, j, i)) +
                (wx2(k, j, i)) * (e3x1(k, j - 1, i) - cce(2, k, j - 1, i));
-    E[2 * g.ne + ei] = (double)(q * (de3_l1 + de3_r1 + de3_l2 + de3_r2 + e3x2(k, j, i - 1) +
-                                     e3x2(k, j, i) + e3x1(k, j - 1, i) + e3x1(k, j, i)));
+    E[2 * g.ne + ei] = q * (de3_l1 + de3_r1 + de3_l2 + de3_r2 + e3x2(k, j, i - 1) +
+                            e3x2(k, j, i) + e3x1(k, j - 1, i) + e3x1(k, j, i));
   }
 }
 
@@ -215,74 +398,164 @@ template <typename T, bool MHD>
 __global__ void __launch_bounds__(128) k_update(Geom g, StagePtrs<T> p, Box bx, StageW sw) {
   int i, j, k, b;
   if (!box_coords(bx, i, j, k, b)) return;
-  const double wght = sw.beta * (*p.dt);
-  const BlockGeo geo = p.geo[b];
-  const double dx1 = geo.dx[0], dx2 = geo.dx[1], dx3 = geo.dx[2];
-  if (i <= g.ie && j <= g.je && k <= g.ke) {
-    const int64_t nc = g.ncell;
-    double* u = p.u + (int64_t)b * NHYD * nc;
-    double* u1 = p.u1 + (int64_t)b * NHYD * nc;
-    constexpr int NF = MHD ? 8 : 5;
-    const T* F1 = p.flx[0] + (int64_t)b * NF * g.nf1;
-    const T* F2 = p.flx[1] + (int64_t)b * NF * g.nf2;
-    const T* F3 = p.flx[2] + (int64_t)b * NF * g.nf3;
-    const double a1 = dx2 * dx3, a2 = dx1 * dx3, a3 = dx1 * dx2;
-    const double vol = dx1 * dx2 * dx3;
-    const int64_t c = cidx(g, k, j, i);
-    const int64_t q1 = f1idx(g, k, j, i), q2 = f2idx(g, k, j, i), q3 = f3idx(g, k, j, i);
-    const int64_t s2 = g.nc1, s3 = (int64_t)g.nc1 * g.nc2;
+  if constexpr (kMixed<T>) {
+    // Mixed path. Every face flux enters the update pre-multiplied by the FP32 weight
+    // beta dt / dx (the same rounded value in both neighbouring cells), the six weighted
+    // fluxes of a cell are summed without rounding error into a pair hi + lo, and only
+    // the final U - (hi + lo) runs in FP64. The face fields take the same route with
+    // edge-integrated EMFs (beta dt dx_e E), so each face's flux change is an exact sum
+    // of shared edge values and div B stays at FP64 round-off.
+    const MixedGeo mg = p.mg[b];
+    const float wf = __fmul_rn(sw.betaf, *p.dtT);
+    if (i <= g.ie && j <= g.je && k <= g.ke) {
+      const float cw1 = __fmul_rn(wf, mg.idx[0]), cw2 = __fmul_rn(wf, mg.idx[1]),
+                  cw3 = __fmul_rn(wf, mg.idx[2]);
+      const int64_t nc = g.ncell;
+      double* u = p.u + (int64_t)b * NHYD * nc;
+      double* u1 = p.u1 + (int64_t)b * NHYD * nc;
+      constexpr int NF = MHD ? 8 : 5;
+      const T* F1 = p.flx[0] + (int64_t)b * NF * g.nf1;
+      const T* F2 = p.flx[1] + (int64_t)b * NF * g.nf2;
+      const T* F3 = p.flx[2] + (int64_t)b * NF * g.nf3;
+      const int64_t c = cidx(g, k, j, i);
+      const int64_t q1 = f1idx(g, k, j, i), q2 = f2idx(g, k, j, i), q3 = f3idx(g, k, j, i);
+      const int64_t s2 = g.nc1, s3 = (int64_t)g.nc1 * g.nc2;
 #pragma unroll
-    for (int n = 0; n < NHYD; ++n) {
-      double uo = u[n * nc + c];
-      double r = sw.zero_reg ? 0.0 : u1[n * nc + c];
-      if (sw.delta != 0.0) { r += sw.delta * uo; u1[n * nc + c] = r; }
-      double base = sw.swap ? r : sw.g1 * uo + sw.g2 * r;
-      double d = (a1 * (double)F1[n * g.nf1 + q1 + 1] - a1 * (double)F1[n * g.nf1 + q1]);
-      d += (a2 * (double)F2[n * g.nf2 + q2 + s2] - a2 * (double)F2[n * g.nf2 + q2]);
-      d += (a3 * (double)F3[n * g.nf3 + q3 + s3] - a3 * (double)F3[n * g.nf3 + q3]);
-      u[n * nc + c] = base - wght * d / vol;
-    }
-  }
-  if constexpr (MHD) {
-    const double* E1 = p.edge + (int64_t)b * 3 * g.ne;
-    const double* E2 = E1 + g.ne;
-    const double* E3 = E2 + g.ne;
-    const double ar1 = dx2 * dx3, ar2 = dx1 * dx3, ar3 = dx1 * dx2;
-    const double l1 = dx1, l2 = dx2, l3 = dx3;
-    const int64_t e = eidx(g, k, j, i);
-    const int64_t ej = (int64_t)g.nc1 + 1, ek = ((int64_t)g.nc1 + 1) * (g.nc2 + 1);
-    // applies "-= (w/a)*curl_m" and "+= (w/a)*curl_p" in the reference's order
-    auto face = [&](double* bb, double* rr, int64_t q, double curl_m, double curl_p,
-                    double ar, bool plus_first) {
-      double bo = bb[q];
-      double r = sw.zero_reg ? 0.0 : rr[q];
-      if (sw.delta != 0.0) { r += sw.delta * bo; rr[q] = r; }
-      double v = sw.swap ? r : sw.g1 * bo + sw.g2 * r;
-      if (plus_first) {
-        v += (wght / ar) * curl_p;
-        v -= (wght / ar) * curl_m;
-      } else {
-        v -= (wght / ar) * curl_m;
-        v += (wght / ar) * curl_p;
+      for (int n = 0; n < NHYD; ++n) {
+        const double uo = u[n * nc + c];
+        double base;
+        if (sw.copy_reg) {  // first stage: register = u exactly
+          u1[n * nc + c] = uo;
+          base = sw.swap ? uo : sw.g1 * uo + sw.g2 * uo;
+        } else {
+          double r = sw.zero_reg ? 0.0 : u1[n * nc + c];
+          if (sw.has_delta) { r += sw.delta * uo; u1[n * nc + c] = r; }
+          base = sw.swap ? r : sw.g1 * uo + sw.g2 * r;
+        }
+        float hi, lo;
+        sum3diff(__fmul_rn(cw1, F1[n * g.nf1 + q1 + 1]), __fmul_rn(cw1, F1[n * g.nf1 + q1]),
+                 __fmul_rn(cw2, F2[n * g.nf2 + q2 + s2]), __fmul_rn(cw2, F2[n * g.nf2 + q2]),
+                 __fmul_rn(cw3, F3[n * g.nf3 + q3 + s3]), __fmul_rn(cw3, F3[n * g.nf3 + q3]),
+                 hi, lo);
+        u[n * nc + c] = (base - f2d_int(hi)) - f2d_int(lo);
       }
-      bb[q] = v;
-    };
-    if (j <= g.je && k <= g.ke) {  // B1 at (k,j,i), i in [is, ie+1]
-      int64_t q = (int64_t)b * g.nf1 + f1idx(g, k, j, i);
-      face(p.b1, p.r1, q, (l3 * E3[e + ej] - l3 * E3[e]), (l2 * E2[e + ek] - l2 * E2[e]), ar1,
-           false);
     }
-    if (i <= g.ie && k <= g.ke) {  // B2 at (k,j,i), j in [js, je+1]
-      int64_t q = (int64_t)b * g.nf2 + f2idx(g, k, j, i);
-      // ct.cpp:80-93: b2 += (w/a)*(curl e3 along i) first, then b2 -= (w/a)*(curl e1 along k)
-      face(p.b2, p.r2, q, (l1 * E1[e + ek] - l1 * E1[e]), (l3 * E3[e + 1] - l3 * E3[e]), ar2,
-           true);
+    if constexpr (MHD) {
+      const T* E1 = p.edge + (int64_t)b * 3 * g.ne;
+      const T* E2 = E1 + g.ne;
+      const T* E3 = E2 + g.ne;
+      const float we1 = __fmul_rn(wf, mg.dx[0]), we2 = __fmul_rn(wf, mg.dx[1]),
+                  we3 = __fmul_rn(wf, mg.dx[2]);
+      const int64_t e = eidx(g, k, j, i);
+      const int64_t ej = (int64_t)g.nc1 + 1, ek = ((int64_t)g.nc1 + 1) * (g.nc2 + 1);
+      auto reg = [&](double* bb, double* rr, int64_t q) -> double {
+        const double bo = bb[q];
+        if (sw.copy_reg) {
+          rr[q] = bo;
+          return sw.swap ? bo : sw.g1 * bo + sw.g2 * bo;
+        }
+        double r = sw.zero_reg ? 0.0 : rr[q];
+        if (sw.has_delta) { r += sw.delta * bo; rr[q] = r; }
+        return sw.swap ? r : sw.g1 * bo + sw.g2 * r;
+      };
+      auto apply = [&](double v, float hi, float lo, double ia) {
+        v = fma(f2d_int(hi), ia, v);
+        return fma(f2d_int(lo), ia, v);
+      };
+      float hi, lo;
+      if (j <= g.je && k <= g.ke) {  // dPhi1 = -(eps3(j+1) - eps3(j)) + (eps2(k+1) - eps2(k))
+        int64_t q = (int64_t)b * g.nf1 + f1idx(g, k, j, i);
+        double v = reg(p.b1, p.r1, q);
+        sum2diff(__fmul_rn(we3, E3[e]), __fmul_rn(we3, E3[e + ej]),
+                 __fmul_rn(we2, E2[e + ek]), __fmul_rn(we2, E2[e]), hi, lo);
+        p.b1[q] = apply(v, hi, lo, mg.ia[0]);
+      }
+      if (i <= g.ie && k <= g.ke) {  // dPhi2 = (eps3(i+1) - eps3(i)) - (eps1(k+1) - eps1(k))
+        int64_t q = (int64_t)b * g.nf2 + f2idx(g, k, j, i);
+        double v = reg(p.b2, p.r2, q);
+        sum2diff(__fmul_rn(we3, E3[e + 1]), __fmul_rn(we3, E3[e]),
+                 __fmul_rn(we1, E1[e]), __fmul_rn(we1, E1[e + ek]), hi, lo);
+        p.b2[q] = apply(v, hi, lo, mg.ia[1]);
+      }
+      if (i <= g.ie && j <= g.je) {  // dPhi3 = -(eps2(i+1) - eps2(i)) + (eps1(j+1) - eps1(j))
+        int64_t q = (int64_t)b * g.nf3 + f3idx(g, k, j, i);
+        double v = reg(p.b3, p.r3, q);
+        sum2diff(__fmul_rn(we2, E2[e]), __fmul_rn(we2, E2[e + 1]),
+                 __fmul_rn(we1, E1[e + ej]), __fmul_rn(we1, E1[e]), hi, lo);
+        p.b3[q] = apply(v, hi, lo, mg.ia[2]);
+      }
     }
-    if (i <= g.ie && j <= g.je) {  // B3 at (k,j,i), k in [ks, ke+1]
-      int64_t q = (int64_t)b * g.nf3 + f3idx(g, k, j, i);
-      face(p.b3, p.r3, q, (l2 * E2[e + 1] - l2 * E2[e]), (l1 * E1[e + ej] - l1 * E1[e]), ar3,
-           false);
+  } else {
+    const double wght = sw.beta * (*p.dt);
+    const BlockGeo geo = p.geo[b];
+    const double dx1 = geo.dx[0], dx2 = geo.dx[1], dx3 = geo.dx[2];
+    if (i <= g.ie && j <= g.je && k <= g.ke) {
+      const int64_t nc = g.ncell;
+      double* u = p.u + (int64_t)b * NHYD * nc;
+      double* u1 = p.u1 + (int64_t)b * NHYD * nc;
+      constexpr int NF = MHD ? 8 : 5;
+      const T* F1 = p.flx[0] + (int64_t)b * NF * g.nf1;
+      const T* F2 = p.flx[1] + (int64_t)b * NF * g.nf2;
+      const T* F3 = p.flx[2] + (int64_t)b * NF * g.nf3;
+      const double a1 = dx2 * dx3, a2 = dx1 * dx3, a3 = dx1 * dx2;
+      const double vol = dx1 * dx2 * dx3;
+      const int64_t c = cidx(g, k, j, i);
+      const int64_t q1 = f1idx(g, k, j, i), q2 = f2idx(g, k, j, i), q3 = f3idx(g, k, j, i);
+      const int64_t s2 = g.nc1, s3 = (int64_t)g.nc1 * g.nc2;
+  #pragma unroll
+      for (int n = 0; n < NHYD; ++n) {
+        double uo = u[n * nc + c];
+        double r = sw.zero_reg ? 0.0 : u1[n * nc + c];
+        if (sw.delta != 0.0) { r += sw.delta * uo; u1[n * nc + c] = r; }
+        double base = sw.swap ? r : sw.g1 * uo + sw.g2 * r;
+        double d = (a1 * (double)F1[n * g.nf1 + q1 + 1] - a1 * (double)F1[n * g.nf1 + q1]);
+        d += (a2 * (double)F2[n * g.nf2 + q2 + s2] - a2 * (double)F2[n * g.nf2 + q2]);
+        d += (a3 * (double)F3[n * g.nf3 + q3 + s3] - a3 * (double)F3[n * g.nf3 + q3]);
+        u[n * nc + c] = base - wght * d / vol;
+      }
     }
+    if constexpr (MHD) {
+      const T* E1 = p.edge + (int64_t)b * 3 * g.ne;
+      const T* E2 = E1 + g.ne;
+      const T* E3 = E2 + g.ne;
+      const double ar1 = dx2 * dx3, ar2 = dx1 * dx3, ar3 = dx1 * dx2;
+      const double l1 = dx1, l2 = dx2, l3 = dx3;
+      const int64_t e = eidx(g, k, j, i);
+      const int64_t ej = (int64_t)g.nc1 + 1, ek = ((int64_t)g.nc1 + 1) * (g.nc2 + 1);
+      // applies "-= (w/a)*curl_m" and "+= (w/a)*curl_p" in the reference's order
+      auto face = [&](double* bb, double* rr, int64_t q, double curl_m, double curl_p,
+                      double ar, bool plus_first) {
+        double bo = bb[q];
+        double r = sw.zero_reg ? 0.0 : rr[q];
+        if (sw.delta != 0.0) { r += sw.delta * bo; rr[q] = r; }
+        double v = sw.swap ? r : sw.g1 * bo + sw.g2 * r;
+        if (plus_first) {
+          v += (wght / ar) * curl_p;
+          v -= (wght / ar) * curl_m;
+        } else {
+          v -= (wght / ar) * curl_m;
+          v += (wght / ar) * curl_p;
+        }
+        bb[q] = v;
+      };
+      if (j <= g.je && k <= g.ke) {  // B1 at (k,j,i), i in [is, ie+1]
+        int64_t q = (int64_t)b * g.nf1 + f1idx(g, k, j, i);
+        face(p.b1, p.r1, q, (l3 * E3[e + ej] - l3 * E3[e]), (l2 * E2[e + ek] - l2 * E2[e]), ar1,
+             false);
+      }
+      if (i <= g.ie && k <= g.ke) {  // B2 at (k,j,i), j in [js, je+1]
+        int64_t q = (int64_t)b * g.nf2 + f2idx(g, k, j, i);
+        // ct.cpp:80-93: b2 += (w/a)*(curl e3 along i) first, then b2 -= (w/a)*(curl e1 along k)
+        face(p.b2, p.r2, q, (l1 * E1[e + ek] - l1 * E1[e]), (l3 * E3[e + 1] - l3 * E3[e]), ar2,
+             true);
+      }
+      if (i <= g.ie && j <= g.je) {  // B3 at (k,j,i), k in [ks, ke+1]
+        int64_t q = (int64_t)b * g.nf3 + f3idx(g, k, j, i);
+        face(p.b3, p.r3, q, (l2 * E2[e + 1] - l2 * E2[e]), (l1 * E1[e + ej] - l1 * E1[e]), ar3,
+             false);
+      }
+    }
+
   }
 }
 
@@ -294,38 +567,145 @@ template <typename T, bool MHD>
 __global__ void __launch_bounds__(256) k_c2p(Geom g, StagePtrs<T> p, Box bx, Phys ph) {
   int i, j, k, b;
   if (!box_coords(bx, i, j, k, b)) return;
+  if constexpr (kMixed<T>) {
+    // Mixed path: the internal energy is still formed in FP64 (it is the small difference
+    // of large terms); everything that is only stored in FP32 is formed in FP32, and the
+    // conversions run on the integer pipe. Density is floored in place, energy only where
+    // the pressure floor acts (the reference writes the same values).
+    const int64_t nc = g.ncell;
+    const int64_t c = cidx(g, k, j, i);
+    double* u = p.u + (int64_t)b * NHYD * nc;
+    float* w = p.w + (int64_t)b * NHYD * nc;
+    double ss = 0.0;  // (2 Bcc)^2
+    if constexpr (MHD) {
+      const double* b1 = p.b1 + (int64_t)b * g.nf1;
+      const double* b2 = p.b2 + (int64_t)b * g.nf2;
+      const double* b3 = p.b3 + (int64_t)b * g.nf3;
+      const int64_t q1 = f1idx(g, k, j, i), q2 = f2idx(g, k, j, i), q3 = f3idx(g, k, j, i);
+      const double f1 = b1[q1], f2 = b2[q2], f3 = b3[q3];
+      const double s1 = f1 + b1[q1 + 1], s2 = f2 + b2[q2 + g.nc1],
+                   s3 = f3 + b3[q3 + (int64_t)g.nc1 * g.nc2];
+      float* bcc = p.bcc + (int64_t)b * 3 * nc;
+      bcc[c] = 0.5f * d2f_int(s1);
+      bcc[nc + c] = 0.5f * d2f_int(s2);
+      bcc[2 * nc + c] = 0.5f * d2f_int(s3);
+      // FP32 copy of the lower faces of this cell for the flux kernels; every face index
+      // the sweeps read (< nc along the normal) is the lower face of some cell
+      p.bfw[0][(int64_t)b * g.nf1 + q1] = d2f_int(f1);
+      p.bfw[1][(int64_t)b * g.nf2 + q2] = d2f_int(f2);
+      p.bfw[2][(int64_t)b * g.nf3 + q3] = d2f_int(f3);
+      ss = fma(s1, s1, fma(s2, s2, s3 * s3));
+    }
+    double ud = u[c];
+    const double m1 = u[nc + c], m2 = u[2 * nc + c], m3 = u[3 * nc + c], ue = u[4 * nc + c];
+    if (!(ud > ph.dfloor)) { ud = ph.dfloor; u[c] = ud; }
+    // FP32 reciprocal refined by one Newton step (relative error ~1e-14)
+    const float udf = d2f_int(ud);
+    const double r0 = f2d_int(1.0f / udf);
+    const double di = r0 * fma(-ud, r0, 2.0);
+    const double mm = fma(m1, m1, fma(m2, m2, m3 * m3));
+    const double x = MHD ? fma(mm, di, 0.25 * ss) : mm * di;  // 2 (e_k + p_B)
+    double wp = ph.gm1 * fma(-0.5, x, ue);
+    if (!(wp > ph.pfloor)) {
+      u[4 * nc + c] = (ph.pfloor / ph.gm1) + 0.5 * x;
+      wp = ph.pfloor;
+    }
+    const float dif = d2f_int(di);
+    w[c] = udf;
+    w[nc + c] = d2f_int(m1) * dif;
+    w[2 * nc + c] = d2f_int(m2) * dif;
+    w[3 * nc + c] = d2f_int(m3) * dif;
+    w[4 * nc + c] = d2f_int(wp);
+    return;
+  } else {
+    const int64_t nc = g.ncell;
+    const int64_t c = cidx(g, k, j, i);
+    double* u = p.u + (int64_t)b * NHYD * nc;
+    T* w = p.w + (int64_t)b * NHYD * nc;
+    const double gm1 = ph.gamma - 1.0;
+    double pb = 0.0;
+    if constexpr (MHD) {
+      const double* b1 = p.b1 + (int64_t)b * g.nf1;
+      const double* b2 = p.b2 + (int64_t)b * g.nf2;
+      const double* b3 = p.b3 + (int64_t)b * g.nf3;
+      const double f1 = b1[f1idx(g, k, j, i)], f2 = b2[f2idx(g, k, j, i)], f3 = b3[f3idx(g, k, j, i)];
+      double bc1 = 0.5 * f1 + 0.5 * b1[f1idx(g, k, j, i + 1)];
+      double bc2 = 0.5 * f2 + 0.5 * b2[f2idx(g, k, j + 1, i)];
+      double bc3 = 0.5 * f3 + 0.5 * b3[f3idx(g, k + 1, j, i)];
+      T* bcc = p.bcc + (int64_t)b * 3 * nc;
+      bcc[c] = (T)bc1; bcc[nc + c] = (T)bc2; bcc[2 * nc + c] = (T)bc3;
+      pb = 0.5 * (bc1 * bc1 + bc2 * bc2 + bc3 * bc3);
+    }
+    double ud = u[c], m1 = u[nc + c], m2 = u[2 * nc + c], m3 = u[3 * nc + c], ue = u[4 * nc + c];
+    ud = (ud > ph.dfloor) ? ud : ph.dfloor;
+    u[c] = ud;
+    double di = 1.0 / ud;
+    double e_k = 0.5 * di * (m1 * m1 + m2 * m2 + m3 * m3);
+    double wp = MHD ? gm1 * (ue - e_k - pb) : gm1 * (ue - e_k);
+    if (!(wp > ph.pfloor)) {
+      u[4 * nc + c] = MHD ? ((ph.pfloor / gm1) + e_k + pb) : ((ph.pfloor / gm1) + e_k);
+      wp = ph.pfloor;
+    }
+    w[c] = (T)ud;
+    w[nc + c] = (T)(m1 * di);
+    w[2 * nc + c] = (T)(m2 * di);
+    w[3 * nc + c] = (T)(m3 * di);
+    w[4 * nc + c] = (T)wp;
+  }
+}
+
+// Self-gravity source (hydro/srcterms/self_gravity.cpp:35-125): momentum from the face
+// potentials, energy from the mass fluxes of this stage, applied after the flux
+// divergence with the stage weight beta dt. phi is the block pool's potential (one ghost
+// layer filled from the multigrid solution). The FP64 path keeps the reference's order
+// (x1, x2, x3 passes, each a read-modify-write of U); the mixed path forms the potential
+// differences in FP64 and the products in FP32.
+template <typename T, bool MHD>
+__global__ void __launch_bounds__(128)
+k_self_gravity(Geom g, StagePtrs<T> p, Box bx, StageW sw, const double* __restrict__ phi_pool) {
+  constexpr int NF = MHD ? 8 : 5;
+  int i, j, k, b;
+  if (!box_coords(bx, i, j, k, b)) return;
   const int64_t nc = g.ncell;
   const int64_t c = cidx(g, k, j, i);
   double* u = p.u + (int64_t)b * NHYD * nc;
-  T* w = p.w + (int64_t)b * NHYD * nc;
-  const double gm1 = ph.gamma - 1.0;
-  double pb = 0.0;
-  if constexpr (MHD) {
-    const double* b1 = p.b1 + (int64_t)b * g.nf1;
-    const double* b2 = p.b2 + (int64_t)b * g.nf2;
-    const double* b3 = p.b3 + (int64_t)b * g.nf3;
-    double bc1 = 0.5 * b1[f1idx(g, k, j, i)] + 0.5 * b1[f1idx(g, k, j, i + 1)];
-    double bc2 = 0.5 * b2[f2idx(g, k, j, i)] + 0.5 * b2[f2idx(g, k, j + 1, i)];
-    double bc3 = 0.5 * b3[f3idx(g, k, j, i)] + 0.5 * b3[f3idx(g, k + 1, j, i)];
-    T* bcc = p.bcc + (int64_t)b * 3 * nc;
-    bcc[c] = (T)bc1; bcc[nc + c] = (T)bc2; bcc[2 * nc + c] = (T)bc3;
-    pb = 0.5 * (bc1 * bc1 + bc2 * bc2 + bc3 * bc3);
+  const T* w = p.w + (int64_t)b * NHYD * nc;
+  const double* phi = phi_pool + (int64_t)b * nc;
+  const T* F1 = p.flx[0] + (int64_t)b * NF * g.nf1;
+  const T* F2 = p.flx[1] + (int64_t)b * NF * g.nf2;
+  const T* F3 = p.flx[2] + (int64_t)b * NF * g.nf3;
+  const int64_t st[3] = {1, (int64_t)g.nc1, (int64_t)g.nc1 * g.nc2};
+  const int64_t fl[3] = {f1idx(g, k, j, i), f2idx(g, k, j, i), f3idx(g, k, j, i)};
+  const int64_t fr[3] = {f1idx(g, k, j, i + 1), f2idx(g, k, j + 1, i), f3idx(g, k + 1, j, i)};
+  const T* F[3] = {F1, F2, F3};
+  if constexpr (kMixed<T>) {
+    const MixedGeo mg = p.mg[b];
+    const float wf = __fmul_rn(sw.betaf, *p.dtT);
+    const float rho = w[c];
+    float de = 0.0f;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      const float dtodx = wf * mg.idx[d];
+      const float dl = d2f_int(phi[c] - phi[c - st[d]]);
+      const float dr = d2f_int(phi[c + st[d]] - phi[c]);
+      const float dm = dtodx * rho * (0.5f * (dl + dr));
+      u[(1 + d) * nc + c] -= f2d_int(dm);
+      de += dtodx * (0.5f * (F[d][fl[d]] * dl + F[d][fr[d]] * dr));
+    }
+    u[4 * nc + c] -= f2d_int(de);
+  } else {
+    const double dt = sw.beta * (*p.dt);
+    const BlockGeo geo = p.geo[b];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      const double dtodx = dt / geo.dx[d];
+      const double phic = phi[c];
+      const double phil = 0.5 * (phi[c - st[d]] + phi[c]);
+      const double phir = 0.5 * (phi[c] + phi[c + st[d]]);
+      u[(1 + d) * nc + c] -= dtodx * w[c] * (phir - phil);
+      u[4 * nc + c] -= dtodx * (F[d][fl[d]] * (phic - phil) + F[d][fr[d]] * (phir - phic));
+    }
   }
-  double ud = u[c], m1 = u[nc + c], m2 = u[2 * nc + c], m3 = u[3 * nc + c], ue = u[4 * nc + c];
-  ud = (ud > ph.dfloor) ? ud : ph.dfloor;
-  u[c] = ud;
-  double di = 1.0 / ud;
-  double e_k = 0.5 * di * (m1 * m1 + m2 * m2 + m3 * m3);
-  double wp = MHD ? gm1 * (ue - e_k - pb) : gm1 * (ue - e_k);
-  if (!(wp > ph.pfloor)) {
-    u[4 * nc + c] = MHD ? ((ph.pfloor / gm1) + e_k + pb) : ((ph.pfloor / gm1) + e_k);
-    wp = ph.pfloor;
-  }
-  w[c] = (T)ud;
-  w[nc + c] = (T)(m1 * di);
-  w[2 * nc + c] = (T)(m2 * di);
-  w[3 * nc + c] = (T)(m3 * di);
-  w[4 * nc + c] = (T)wp;
 }
 
 // Per-block CFL limit (src/hydro/new_blockdt.cpp:58-158) reduced over the whole pool
@@ -334,44 +714,56 @@ __global__ void __launch_bounds__(256) k_c2p(Geom g, StagePtrs<T> p, Box bx, Phy
 template <typename T, bool MHD>
 __global__ void __launch_bounds__(256)
 k_block_dt(Geom g, StagePtrs<T> p, Box bx, Phys ph, unsigned long long* dtmin) {
+  // the reduction runs in T: FP32 in the mixed path (relative change of dt ~1e-7)
   int i, j, k, b;
-  double mindt = 1.79769313486231570815e308;
+  const T kBig = kMixed<T> ? T(3.402823466e38f) : T(1.79769313486231570815e308);
+  T mindt = kBig;
   if (box_coords(bx, i, j, k, b)) {
     const int64_t nc = g.ncell, c = cidx(g, k, j, i);
     const T* w = p.w + (int64_t)b * NHYD * nc;
-    const BlockGeo geo = p.geo[b];
-    double d = w[c], vx = w[nc + c], vy = w[2 * nc + c], vz = w[3 * nc + c], pr = w[4 * nc + c];
-    double dt1, dt2, dt3;
+    T d = w[c], vx = w[nc + c], vy = w[2 * nc + c], vz = w[3 * nc + c], pr = w[4 * nc + c];
+    T dx1, dx2, dx3;
+    if constexpr (kMixed<T>) {
+      dx1 = p.dxT[b * 3]; dx2 = p.dxT[b * 3 + 1]; dx3 = p.dxT[b * 3 + 2];
+    } else {
+      const BlockGeo geo = p.geo[b];
+      dx1 = geo.dx[0]; dx2 = geo.dx[1]; dx3 = geo.dx[2];
+    }
+    const T gam = (T)ph.gamma;
+    T dt1, dt2, dt3;
     if constexpr (MHD) {
       const T* bcc = p.bcc + (int64_t)b * 3 * nc;
-      double bc1 = bcc[c], bc2 = bcc[nc + c], bc3 = bcc[2 * nc + c];
-      double bx1 = bc1 + fabs(p.b1[(int64_t)b * g.nf1 + f1idx(g, k, j, i)] - bc1);
-      double cf = fast_speed<double>(d, pr, bc2, bc3, bx1, ph.gamma);
-      dt1 = geo.dx[0] / (fabs(vx) + cf);
-      double bx2 = bc2 + fabs(p.b2[(int64_t)b * g.nf2 + f2idx(g, k, j, i)] - bc2);
-      cf = fast_speed<double>(d, pr, bc3, bc1, bx2, ph.gamma);
-      dt2 = geo.dx[1] / (fabs(vy) + cf);
-      double bx3 = bc3 + fabs(p.b3[(int64_t)b * g.nf3 + f3idx(g, k, j, i)] - bc3);
-      cf = fast_speed<double>(d, pr, bc1, bc2, bx3, ph.gamma);
-      dt3 = geo.dx[2] / (fabs(vz) + cf);
+      T bc1 = bcc[c], bc2 = bcc[nc + c], bc3 = bcc[2 * nc + c];
+      T bx1 = bc1 + fabs(p.bf[0][(int64_t)b * g.nf1 + f1idx(g, k, j, i)] - bc1);
+      T cf = fast_speed<T>(d, pr, bc2, bc3, bx1, gam);
+      dt1 = dx1 / (fabs(vx) + cf);
+      T bx2 = bc2 + fabs(p.bf[1][(int64_t)b * g.nf2 + f2idx(g, k, j, i)] - bc2);
+      cf = fast_speed<T>(d, pr, bc3, bc1, bx2, gam);
+      dt2 = dx2 / (fabs(vy) + cf);
+      T bx3 = bc3 + fabs(p.bf[2][(int64_t)b * g.nf3 + f3idx(g, k, j, i)] - bc3);
+      cf = fast_speed<T>(d, pr, bc1, bc2, bx3, gam);
+      dt3 = dx3 / (fabs(vz) + cf);
     } else {
-      double cs = sqrt(ph.gamma * pr / d);
-      dt1 = geo.dx[0] / (fabs(vx) + cs);
-      dt2 = geo.dx[1] / (fabs(vy) + cs);
-      dt3 = geo.dx[2] / (fabs(vz) + cs);
+      T cs = sqrt(gam * pr / d);
+      dt1 = dx1 / (fabs(vx) + cs);
+      dt2 = dx2 / (fabs(vy) + cs);
+      dt3 = dx3 / (fabs(vz) + cs);
     }
     mindt = mn(mn(mn(mindt, dt1), dt2), dt3);
   }
   for (int o = 16; o > 0; o >>= 1) mindt = mn(mindt, __shfl_xor_sync(0xffffffffu, mindt, o));
-  __shared__ double red[32];
+  __shared__ T red[32];
   const int tid = threadIdx.x + blockDim.x * threadIdx.y;
   const int nt = blockDim.x * blockDim.y;
   if ((tid & 31) == 0) red[tid >> 5] = mindt;
   __syncthreads();
   if (tid < 32) {
-    double v = (tid < (nt + 31) / 32) ? red[tid] : 1.79769313486231570815e308;
+    T v = (tid < (nt + 31) / 32) ? red[tid] : kBig;
     for (int o = 16; o > 0; o >>= 1) v = mn(v, __shfl_xor_sync(0xffffffffu, v, o));
-    if (tid == 0) atomicMin(dtmin, (unsigned long long)__double_as_longlong(v));
+    if (tid == 0) {
+      const double vd = (v == kBig) ? 1.79769313486231570815e308 : (double)v;
+      atomicMin(dtmin, (unsigned long long)__double_as_longlong(vd));
+    }
   }
 }
 

@@ -129,6 +129,72 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+MG_N = 256
+MG_WORKLOAD = "uniform_sphere_256^3_multipole4_fmg_vcycle11"
+# algorithmic bytes of one V(1,1) cycle per finest cell: ~11.7 element sizes (smoothing,
+# defect, restriction, prolongation over all levels, x 8/7 for the coarse levels); the
+# mixed refinement cycle adds an FP64 defect and correction (24 B)
+MG_BYTES_PER_CELL = {"fp64": 11.7 * 8, "mixed": 11.7 * 4 + 24}
+
+
+def sphere_density(n):
+    x = (np.arange(n) + 0.5) / n - 0.5
+    r2 = x[None, None, :] ** 2 + x[None, :, None] ** 2 + x[:, None, None] ** 2
+    return np.where(r2 < 0.0625, 1.0, 1.0e-6)
+
+
+def sphere_phi_exact(n, R=0.25):
+    """phi = -2 pi G rho (R^2 - r^2/3) inside, -G M / r outside (G = 1, rho = 1)."""
+    x = (np.arange(n) + 0.5) / n - 0.5
+    r = np.sqrt(x[None, None, :] ** 2 + x[None, :, None] ** 2 + x[:, None, None] ** 2)
+    M = 4.0 / 3.0 * np.pi * R ** 3
+    return np.where(r < R, -2.0 * np.pi * (R * R - r * r / 3.0), -M / np.maximum(r, 1e-30))
+
+
+def run_mg(athg, torch, vcycles=5):
+    """MG leg: FMG + V(1,1) to 1e-10 of the initial defect on the 256^3 uniform sphere
+    with l<=4 multipole boundaries, FP64 and mixed; V-cycle time by CUDA events."""
+    n = MG_N
+    rho = sphere_density(n)
+    fpg = 4.0 * np.pi
+    d0 = fpg * float(np.sqrt(np.mean(rho * rho)))  # L2 defect of phi = 0
+    exact = sphere_phi_exact(n)
+    peak, kind = peaks()
+    out = {"workload": MG_WORKLOAD, "threshold": 1e-10 * d0}
+    for prec in ("fp64", "mixed"):
+        mg = athg.Multigrid(n, bc="multipole", mporder=4, mode="FMG", threshold=1e-10 * d0,
+                            precision=prec)
+        mg.load_source(rho, fpg)
+        mg.solve()  # warm-up (allocations, module load)
+        mg.load_source(rho, fpg)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        it, nrm = mg.solve()
+        solve_s = time.perf_counter() - t0
+        phi = mg.phi()
+        l1 = float(np.mean(np.abs(phi - exact)) / np.mean(np.abs(exact)))
+        ext = torch.cuda.ExternalStream(mg.stream())
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(ext):
+            mg.vcycles(2)
+            s.record(ext)
+            mg.vcycles(vcycles)
+            e.record(ext)
+        e.synchronize()
+        vc_s = s.elapsed_time(e) / 1e3 / vcycles
+        achieved = MG_BYTES_PER_CELL[prec] * n ** 3 / vc_s / 1e9
+        out[prec] = {"solve_ms": 1e3 * solve_s, "vcycles_after_fmg": it,
+                     "defect_l2": nrm, "rel_defect": nrm / d0, "vcycle_ms": 1e3 * vc_s,
+                     "l1_vs_analytic": l1,
+                     "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak,
+                                  "unit": "GB/s", "frac": achieved / peak,
+                                  "bytes_per_cell": MG_BYTES_PER_CELL[prec],
+                                  "peak_kind": kind}}
+        mg.close()
+    out["mixed_over_fp64_vcycle"] = out["fp64"]["vcycle_ms"] / out["mixed"]["vcycle_ms"]
+    return out
+
+
 def make_sim(athg, precision):
     return athg.Sim(NX, MB, mhd=True, solver="hlld", precision=precision, cfl=CFL, tlim=1e30,
                     domain=((-0.5, 0.5),) * 3)
@@ -195,6 +261,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--nx", type=int, default=256, help="cells per side (profiling: 128)")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-mg", action="store_true")
     args = ap.parse_args()
     global NX, WORKLOAD
     NX = (args.nx,) * 3
@@ -259,6 +326,11 @@ def main():
     if not args.no_e2e:
         e2e = run_e2e(athg, torch, u, b1, b2, b3, args.steps, zones)
 
+    # ---------------- multigrid (uniform sphere, multipole boundaries) ----------------
+    mgres = None
+    if not args.no_mg:
+        mgres = run_mg(athg, torch)
+
     # ---------------- CPU baseline (oracle port) ----------------
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -299,6 +371,7 @@ def main():
         "e2e": e2e,
         "gpu_launches": m["launches"] * m["steps"],
         "clocks": m["clocks"],
+        "mg": mgres,
     }
     if rank == 0:
         print(json.dumps(line), flush=True)

@@ -193,6 +193,18 @@ int athg_mg_stream(athg_mg* mg, void** stream);
 /* Multipole coefficients (25) and expansion origin (3), after a solve. */
 int athg_mg_multipole(athg_mg* mg, double* out28);
 
+/* Self-gravity (SELF_GRAVITY_ENABLED == 2 with <problem> four_pi_G, Mesh::SetFourPiG).
+ * Couples mg to the hydro context: the solve of MGGravityDriver::Solve
+ * (gravity/mg_gravity.cpp:166) runs in athg_initialize (mesh/mesh.cpp:1398-1402) and
+ * after every stage (main.cpp:461-466), on u(IDN) * four_pi_G of all blocks, and
+ * HydroSourceTerms::SelfGravity (hydro/srcterms/self_gravity.cpp:35) adds the
+ * momentum and energy sources after each stage's flux divergence. The blocks must be
+ * one refinement level tiling mg's nx^3 root grid (the same mesh). The potential of
+ * each block, with one ghost layer, downloads as ATHG_VAR_PHI. mg must outlive the
+ * coupling; pass mg = NULL to detach. Solves with a threshold or a multipole boundary
+ * synchronise with the host, so athg_cycles then runs the stages without a graph. */
+int athg_attach_gravity(athg_ctx* ctx, athg_mg* mg, double four_pi_G);
+
 /* ---- CFL time step of one caller-owned block, with no device allocation ------------
  * No counterpart in the reference: an addition for callers that cannot allocate device
  * memory (a stream being captured into a CUDA graph, a host whose device memory belongs

@@ -1,0 +1,58 @@
+"""Self-gravity on the GPU (multigrid solve after every stage + the source term of
+hydro/srcterms/self_gravity.cpp) against reference runs with SELF_GRAVITY_ENABLED = 2."""
+import numpy as np
+import pytest
+
+import golden_lib
+
+athg = pytest.importorskip("athg")
+pytestmark = pytest.mark.gpu
+
+
+def run_gpu(meta, a, precision, mg_precision="fp64"):
+    n = meta["nx"][0]
+    mb = tuple(meta["meshblock"])
+    sim = athg.Sim(tuple(meta["nx"]), mb, meta["mhd"], meta["solver"], precision=precision,
+                   xorder=meta["xorder"], integrator=meta["integrator"], cfl=meta["cfl"],
+                   gamma=meta["gamma"], tlim=100.0)
+    mg = athg.Multigrid(n, domain=((0.0, 1.0),) * 3, bc="periodic",
+                        mode=meta["mgmode"], niteration=meta["niteration"], threshold=-1.0,
+                        precision=mg_precision)
+    sim.attach_gravity(mg, meta["four_pi_G"])
+    sim.load_interior(a["u_in"], a.get("b1_in"), a.get("b2_in"), a.get("b3_in"))
+    sim.initialize()
+    sim.cycles(meta["ncycles"])
+    out = sim.interior()
+    phi = sim.phi()[1:-1, 1:-1, 1:-1]
+    t, _, _ = sim.get_time()
+    sim.attach_gravity(None, 0.0)
+    sim.close()
+    mg.close()
+    return out, phi, t
+
+
+@pytest.mark.parametrize("name", golden_lib.sg_cases())
+def test_sg_fp64_matches_reference(name):
+    meta, a = golden_lib.load(name)
+    out, phi, t = run_gpu(meta, a, "fp64")
+    assert t == pytest.approx(meta["time"], rel=1e-13)
+    # the multigrid's sums (average subtraction, defect norms) run as parallel reductions,
+    # so the potential, and the state through it, agree to round-off, not bit for bit
+    for k in (["u"] + (["b1", "b2", "b3"] if meta["mhd"] else [])):
+        ref = a[k + "_out"]
+        np.testing.assert_allclose(out[k], ref, rtol=0, atol=1e-12 * np.abs(ref).max())
+    np.testing.assert_allclose(phi, a["phi_out"], rtol=0, atol=1e-11 * np.abs(a["phi_out"]).max())
+
+
+@pytest.mark.parametrize("name", golden_lib.sg_cases())
+def test_sg_mixed_close_to_reference(name):
+    meta, a = golden_lib.load(name)
+    # mixed hydro (FP32 fluxes and source products) with the FP64 multigrid cycle, whose
+    # iterates after a fixed number of V-cycles match the reference's
+    out, phi, _ = run_gpu(meta, a, "mixed", "fp64")
+    for k in (["u"] + (["b1", "b2", "b3"] if meta["mhd"] else [])):
+        ref = a[k + "_out"]
+        err = np.abs(out[k] - ref).max() / np.abs(ref).max()
+        assert err < 5e-6, (k, err)
+    err = np.abs(phi - a["phi_out"]).max() / np.abs(a["phi_out"]).max()
+    assert err < 2e-7, err

@@ -23,7 +23,7 @@ def _sim_for(meta, precision):
     return athg.Sim(tuple(meta["nx"]), tuple(meta["meshblock"]), mhd=meta["mhd"],
                     solver=meta["solver"], precision=precision, xorder=meta["xorder"],
                     integrator=meta["integrator"], cfl=meta["cfl"], gamma=meta["gamma"],
-                    tlim=100.0)
+                    tlim=100.0, ng=meta.get("nghost", 2))
 
 
 def _run_case(name, precision, use_graph=True):
@@ -67,12 +67,15 @@ def test_stage_by_stage_equals_graph(name):
 def test_mixed_close_to_reference(name):
     meta, a, out, _ = _run_case(name, "mixed")
     # FP32 fluxes: each stage perturbs U by ~1e-7 of the flux increment; after three
-    # cycles the state differs from the FP64 reference at the 1e-6 level.
+    # cycles the state differs from the FP64 reference at the 1e-6 level. PPM's limiter
+    # branches on the signs of second differences (reconstruct/ppm.cpp:150-230), which
+    # FP32 rounding of nearly flat data can flip, so PPM cases are held to 2e-5.
+    tol = 2e-5 if meta["xorder"] == 3 else 2e-6
     for k in (["u"] + (["b1", "b2", "b3"] if meta["mhd"] else [])):
         ref = a[k + "_out"]
         scale = np.abs(ref).max()
         err = np.abs(out[k] - ref).max() / scale
-        assert err < 2e-6, (k, err)
+        assert err < tol, (k, err)
 
 
 def test_multiblock_matches_single_block_oracle():
