@@ -143,6 +143,7 @@ struct athg_ctx {
   double *u = nullptr, *u1 = nullptr, *b1 = nullptr, *b2 = nullptr, *b3 = nullptr;
   double *r1 = nullptr, *r2 = nullptr, *r3 = nullptr;
   void *w = nullptr, *bcc = nullptr, *flx[3] = {nullptr, nullptr, nullptr}, *edge = nullptr;
+  float* cce = nullptr;  // mixed MHD: cell-centred EMF written by the primitive recovery
   BlockGeo* geo = nullptr;
   void* coef = nullptr;        // PLM coefficients in the flux precision
   void* dxT = nullptr;         // cell widths in the flux precision
@@ -178,6 +179,7 @@ StagePtrs<T> ptrs(athg_ctx* c) {
   p.w = (T*)c->w; p.bcc = (T*)c->bcc;
   for (int d = 0; d < 3; ++d) p.flx[d] = (T*)c->flx[d];
   p.edge = (T*)c->edge;
+  p.cce = std::is_same<T, float>::value ? (T*)c->cce : nullptr;
   p.geo = c->geo;
   p.coef = (const T*)c->coef;
   p.dxT = (const T*)c->dxT;
@@ -195,17 +197,19 @@ StagePtrs<T> ptrs(athg_ctx* c) {
 }
 
 Phys phys(const athg_ctx* c) {
-  return Phys{c->cfg.gamma, c->cfg.dfloor, c->cfg.pfloor, c->cfg.gamma - 1.0};
+  return Phys{c->cfg.gamma, c->cfg.dfloor, c->cfg.pfloor, c->cfg.gamma - 1.0,
+              split_ff(c->cfg.gamma - 1.0), split_ff(c->cfg.pfloor)};
 }
 
 void free_pool(athg_ctx* c) {
-  void* ps[] = {c->u, c->u1, c->b1, c->b2, c->b3, c->r1, c->r2, c->r3, c->edge, c->w,
+  void* ps[] = {c->u, c->u1, c->b1, c->b2, c->b3, c->r1, c->r2, c->r3, c->edge, c->cce, c->w,
                 c->bcc, c->flx[0], c->flx[1], c->flx[2], c->geo, c->coef, c->nbr, c->scal,
                 c->dxT, c->mg, c->dtf, c->bf32[0], c->bf32[1], c->bf32[2]};
   for (void* p : ps)
     if (p) cudaFree(p);
   c->u = c->u1 = c->b1 = c->b2 = c->b3 = c->r1 = c->r2 = c->r3 = nullptr;
   c->w = c->bcc = c->flx[0] = c->flx[1] = c->flx[2] = c->edge = nullptr;
+  c->cce = nullptr;
   c->geo = nullptr; c->coef = nullptr; c->nbr = nullptr; c->scal = nullptr;
   c->dxT = nullptr; c->mg = nullptr; c->dtf = nullptr;
   c->bf32[0] = c->bf32[1] = c->bf32[2] = nullptr;
@@ -441,10 +445,12 @@ int athg_create(const athg_config* cfg, athg_ctx** out) {
   if (cfg->nghost < 2) return fail(ATHG_ERR_ARG, "nghost must be >= 2");
   // reconstruct/reconstruction.cpp:90-98: PPM needs three ghost layers
   if (cfg->xorder == 3 && cfg->nghost < 3) return fail(ATHG_ERR_ARG, "PPM needs nghost >= 3");
-  if (cfg->magnetic && !(cfg->rsolver == ATHG_HLLD || cfg->rsolver == ATHG_HLLE))
-    return fail(ATHG_ERR_ARG, "MHD needs the HLLD or HLLE solver");
-  if (!cfg->magnetic && !(cfg->rsolver == ATHG_HLLC || cfg->rsolver == ATHG_HLLE))
-    return fail(ATHG_ERR_ARG, "hydro needs the HLLC or HLLE solver");
+  if (cfg->magnetic &&
+      !(cfg->rsolver == ATHG_HLLD || cfg->rsolver == ATHG_HLLE || cfg->rsolver == ATHG_LHLLD))
+    return fail(ATHG_ERR_ARG, "MHD needs the HLLD, LHLLD or HLLE solver");
+  if (!cfg->magnetic &&
+      !(cfg->rsolver == ATHG_HLLC || cfg->rsolver == ATHG_HLLE || cfg->rsolver == ATHG_LHLLC))
+    return fail(ATHG_ERR_ARG, "hydro needs the HLLC, LHLLC or HLLE solver");
   if (cfg->precision != ATHG_FP64 && cfg->precision != ATHG_MIXED)
     return fail(ATHG_ERR_ARG, "precision must be ATHG_FP64 or ATHG_MIXED");
   int ndev = 0;
@@ -519,6 +525,8 @@ int athg_set_blocks(athg_ctx* c, int nblocks, const athg_block* blocks) {
     CK(cudaMalloc(&c->r3, sizeof(double) * g.nf3 * nb));
     CK(cudaMalloc(&c->edge, tsz * 3 * g.ne * nb));
     if (c->mixed()) {
+      CK(cudaMalloc(&c->cce, sizeof(float) * 3 * g.ncell * nb));
+      CK(cudaMemsetAsync(c->cce, 0, sizeof(float) * 3 * g.ncell * nb, c->st));
       CK(cudaMalloc(&c->bf32[0], sizeof(float) * g.nf1 * nb));
       CK(cudaMalloc(&c->bf32[1], sizeof(float) * g.nf2 * nb));
       CK(cudaMalloc(&c->bf32[2], sizeof(float) * g.nf3 * nb));

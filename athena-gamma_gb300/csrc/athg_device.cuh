@@ -65,6 +65,7 @@ struct BlockGeo {
 struct Phys {
   double gamma, dfloor, pfloor;
   double gm1;  // gamma - 1
+  ff gm1f, pfloorf;  // the same as double-float pairs (mixed primitive recovery)
 };
 
 // Stage weights of the low-storage integrator (reference
@@ -466,6 +467,206 @@ __device__ __forceinline__ void rs_hlld(const T* wli, const T* wri, T bxi, T gam
     flxi[IDN] = fr.d + t0[0]; flxi[IVX] = fr.mx + t0[1]; flxi[IVY] = fr.my + t0[2];
     flxi[IVZ] = fr.mz + t0[3]; flxi[IEN] = fr.e + t0[4]; flxi[IBY] = fr.by + t0[5];
     flxi[IBZ] = fr.bz + t0[6];
+  }
+}
+
+// LHLLC, the fork's low-dissipation HLLC (hydro/rsolvers/hydro/lhllc.cpp:26-180): PVRS
+// wave speeds, the shock detector th = min(1, (cmax - min(dvn,0)) / (cmax - min(dvt,0)))^4
+// on the pressure jump of the contact speed and the low-Mach factor phi = chi (2 - chi) on
+// the contact pressure. dvn, dvt: Hydro::CalculateVelocityDifferences at the face.
+template <typename T>
+__device__ __forceinline__ void rs_lhllc(const T* wli, const T* wri, T gamma, T dvn,
+                     T dvt, T* flxi) {
+  T gm1 = gamma - T(1.0), igm1 = T(1.0) / gm1;
+  T fl[5], fr[5];
+  T cl = sqrt(gamma * wli[IPR] / wli[IDN]);
+  T cr = sqrt(gamma * wri[IPR] / wri[IDN]);
+  T vsql = sq(wli[IVX]) + sq(wli[IVY]) + sq(wli[IVZ]);
+  T vsqr = sq(wri[IVX]) + sq(wri[IVY]) + sq(wri[IVZ]);
+  T el = wli[IPR] * igm1 + T(0.5) * wli[IDN] * vsql;
+  T er = wri[IPR] * igm1 + T(0.5) * wri[IDN] * vsqr;
+  T rhoa = T(.5) * (wli[IDN] + wri[IDN]);
+  T ca = T(.5) * (cl + cr);
+  T pmid = T(.5) * (wli[IPR] + wri[IPR] + (wli[IVX] - wri[IVX]) * rhoa * ca);
+  T umid = T(.5) * (wli[IVX] + wri[IVX] + (wli[IPR] - wri[IPR]) / (rhoa * ca));
+  T rhol = wli[IDN] + (wli[IVX] - umid) * rhoa / ca;
+  T rhor = wri[IDN] + (umid - wri[IVX]) * rhoa / ca;
+  (void)rhol; (void)rhor;
+  T ql = (pmid <= wli[IPR]) ? T(1.0)
+              : sqrt(T(1.0) + (gamma + T(1)) / (T(2) * gamma) * (pmid / wli[IPR] - T(1.0)));
+  T qr = (pmid <= wri[IPR]) ? T(1.0)
+              : sqrt(T(1.0) + (gamma + T(1)) / (T(2) * gamma) * (pmid / wri[IPR] - T(1.0)));
+  T al = wli[IVX] - cl * ql;
+  T ar = wri[IVX] + cr * qr;
+  T bp = ar > T(0.0) ? ar : T(1.0e-20);
+  T bm = al < T(0.0) ? al : -T(1.0e-20);
+  T vxl = al - wli[IVX], vxr = ar - wri[IVX];
+  T ml = wli[IDN] * vxl, mr = wri[IDN] * vxr;
+  T cmax = mx(cl, cr);
+  T th1 = mn(T(1.0), (cmax - mn(dvn, T(0.0))) / (cmax - mn(dvt, T(0.0))));
+  T th = th1 * th1 * th1 * th1;
+  T am = (mr * wri[IVX] - ml * wli[IVX] - th * (wri[IPR] - wli[IPR])) / (mr - ml);
+  T chi = mn(T(1.0), sqrt(mx(vsql, vsqr)) / cmax);
+  T phi = chi * (T(2.0) - chi);
+  T cp = (mr * wli[IPR] - ml * wri[IPR] + phi * mr * ml * (wri[IVX] - wli[IVX])) / (mr - ml);
+  cp = cp > T(0.0) ? cp : T(0.0);
+  T uxl = wli[IVX] - bm, uxr = wri[IVX] - bp;
+  fl[IDN] = wli[IDN] * uxl; fr[IDN] = wri[IDN] * uxr;
+  fl[IVX] = wli[IDN] * wli[IVX] * uxl + wli[IPR]; fr[IVX] = wri[IDN] * wri[IVX] * uxr + wri[IPR];
+  fl[IVY] = wli[IDN] * wli[IVY] * uxl; fr[IVY] = wri[IDN] * wri[IVY] * uxr;
+  fl[IVZ] = wli[IDN] * wli[IVZ] * uxl; fr[IVZ] = wri[IDN] * wri[IVZ] * uxr;
+  fl[IEN] = el * uxl + wli[IPR] * wli[IVX]; fr[IEN] = er * uxr + wri[IPR] * wri[IVX];
+  T sl, sr, sm;
+  if (am >= T(0.0)) { sl = am / (am - bm); sr = T(0.0); sm = -bm / (am - bm); }
+  else { sl = T(0.0); sr = -am / (bp - am); sm = bp / (bp - am); }
+  flxi[IDN] = sl * fl[IDN] + sr * fr[IDN];
+  flxi[IVX] = sl * fl[IVX] + sr * fr[IVX] + sm * cp;
+  flxi[IVY] = sl * fl[IVY] + sr * fr[IVY];
+  flxi[IVZ] = sl * fl[IVZ] + sr * fr[IVZ];
+  flxi[IEN] = sl * fl[IEN] + sr * fr[IEN] + sm * cp * am;
+}
+
+// LHLLD, the fork's low-dissipation HLLD (hydro/rsolvers/mhd/lhlld.cpp:36-388): HLLD with
+// the shock detector on the total-pressure jump of S_M and phi in the star total pressure.
+template <typename T>
+__device__ __forceinline__ void rs_lhlld(const T* wli, const T* wri, T bxi, T gamma,
+                     T dvn, T dvt, T* flxi) {
+  T igm1 = T(1.0) / (gamma - T(1.0));
+  C1D<T> ul, ur, ulst, uldst, urdst, urst, fl, fr;
+  T spd[5];
+  T bxsq = bxi * bxi;
+  T pbl = T(0.5) * (bxsq + (sq(wli[IBY]) + sq(wli[IBZ])));
+  T pbr = T(0.5) * (bxsq + (sq(wri[IBY]) + sq(wri[IBZ])));
+  T kel = T(0.5) * wli[IDN] * (sq(wli[IVX]) + (sq(wli[IVY]) + sq(wli[IVZ])));
+  T ker = T(0.5) * wri[IDN] * (sq(wri[IVX]) + (sq(wri[IVY]) + sq(wri[IVZ])));
+  ul.d = wli[IDN]; ul.mx = wli[IVX] * ul.d; ul.my = wli[IVY] * ul.d; ul.mz = wli[IVZ] * ul.d;
+  ul.e = wli[IPR] * igm1 + kel + pbl; ul.by = wli[IBY]; ul.bz = wli[IBZ];
+  ur.d = wri[IDN]; ur.mx = wri[IVX] * ur.d; ur.my = wri[IVY] * ur.d; ur.mz = wri[IVZ] * ur.d;
+  ur.e = wri[IPR] * igm1 + ker + pbr; ur.by = wri[IBY]; ur.bz = wri[IBZ];
+  T cfl = fast_speed(wli[IDN], wli[IPR], wli[IBY], wli[IBZ], bxi, gamma);
+  T cfr = fast_speed(wri[IDN], wri[IPR], wri[IBY], wri[IBZ], bxi, gamma);
+  spd[0] = mn(wli[IVX] - cfl, wri[IVX] - cfr);
+  spd[4] = mx(wli[IVX] + cfl, wri[IVX] + cfr);
+  T cfmax = mx(cfl, cfr);
+  T ptl = wli[IPR] + pbl, ptr = wri[IPR] + pbr;
+  fl.d = ul.mx;
+  fl.mx = ul.mx * wli[IVX] + ptl - bxsq;
+  fl.my = ul.my * wli[IVX] - bxi * ul.by;
+  fl.mz = ul.mz * wli[IVX] - bxi * ul.bz;
+  fl.e = wli[IVX] * (ul.e + ptl - bxsq) - bxi * (wli[IVY] * ul.by + wli[IVZ] * ul.bz);
+  fl.by = ul.by * wli[IVX] - bxi * wli[IVY];
+  fl.bz = ul.bz * wli[IVX] - bxi * wli[IVZ];
+  fr.d = ur.mx;
+  fr.mx = ur.mx * wri[IVX] + ptr - bxsq;
+  fr.my = ur.my * wri[IVX] - bxi * ur.by;
+  fr.mz = ur.mz * wri[IVX] - bxi * ur.bz;
+  fr.e = wri[IVX] * (ur.e + ptr - bxsq) - bxi * (wri[IVY] * ur.by + wri[IVZ] * ur.bz);
+  fr.by = ur.by * wri[IVX] - bxi * wri[IVY];
+  fr.bz = ur.bz * wri[IVX] - bxi * wri[IVZ];
+  T sdl = spd[0] - wli[IVX], sdr = spd[4] - wri[IVX];
+  T sdld = sdl * ul.d, sdrd = sdr * ur.d;
+  T th1 = mn(T(1.0), (cfmax - mn(dvn, T(0.0))) / (cfmax - mn(dvt, T(0.0))));
+  T th = th1 * th1 * th1 * th1;
+  spd[2] = (sdr * ur.mx - sdl * ul.mx + th * (ptl - ptr)) / (sdrd - sdld);
+  T sdml = spd[0] - spd[2], sdmr = spd[4] - spd[2];
+  T sdml_inv = T(1.0) / sdml, sdmr_inv = T(1.0) / sdmr;
+  ulst.d = sdld * sdml_inv;
+  urst.d = sdrd * sdmr_inv;
+  T ulst_d_inv = T(1.0) / ulst.d, urst_d_inv = T(1.0) / urst.d;
+  T sqrtdl = sqrt(ulst.d), sqrtdr = sqrt(urst.d);
+  spd[1] = spd[2] - fabs(bxi) / sqrtdl;
+  spd[3] = spd[2] + fabs(bxi) / sqrtdr;
+  T clsq = ((pbl + kel) + sqrt(sq(pbl + kel) - T(2.0) * kel * bxsq)) / ul.d;
+  T crsq = ((pbr + ker) + sqrt(sq(pbr + ker) - T(2.0) * ker * bxsq)) / ur.d;
+  T chi = mn(T(1.0), sqrt(mx(clsq, crsq)) / cfmax);
+  T phi = chi * (T(2.0) - chi);
+  T ptst = (sdrd * ptl - sdld * ptr + phi * sdrd * sdld * (wri[IVX] - wli[IVX])) /
+                (sdrd - sdld);
+  ulst.mx = ulst.d * spd[2];
+  if (fabs(sdld * sdml - bxsq) < T(1.0e-8) * ptst) {
+    ulst.my = ulst.d * wli[IVY]; ulst.mz = ulst.d * wli[IVZ];
+    ulst.by = ul.by; ulst.bz = ul.bz;
+  } else {
+    T tmp = bxi * (sdl - sdml) / (sdld * sdml - bxsq);
+    ulst.my = ulst.d * (wli[IVY] - ul.by * tmp);
+    ulst.mz = ulst.d * (wli[IVZ] - ul.bz * tmp);
+    tmp = (sdld * sdl - bxsq) / (sdld * sdml - bxsq);
+    ulst.by = ul.by * tmp; ulst.bz = ul.bz * tmp;
+  }
+  T vbstl = (ulst.mx * bxi + (ulst.my * ulst.by + ulst.mz * ulst.bz)) * ulst_d_inv;
+  ulst.e = (sdl * ul.e - ptl * wli[IVX] + ptst * spd[2] +
+            bxi * (wli[IVX] * bxi + (wli[IVY] * ul.by + wli[IVZ] * ul.bz) - vbstl)) * sdml_inv;
+  urst.mx = urst.d * spd[2];
+  if (fabs(sdrd * sdmr - bxsq) < T(1.0e-8) * ptst) {
+    urst.my = urst.d * wri[IVY]; urst.mz = urst.d * wri[IVZ];
+    urst.by = ur.by; urst.bz = ur.bz;
+  } else {
+    T tmp = bxi * (sdr - sdmr) / (sdrd * sdmr - bxsq);
+    urst.my = urst.d * (wri[IVY] - ur.by * tmp);
+    urst.mz = urst.d * (wri[IVZ] - ur.bz * tmp);
+    tmp = (sdrd * sdr - bxsq) / (sdrd * sdmr - bxsq);
+    urst.by = ur.by * tmp; urst.bz = ur.bz * tmp;
+  }
+  T vbstr = (urst.mx * bxi + (urst.my * urst.by + urst.mz * urst.bz)) * urst_d_inv;
+  urst.e = (sdr * ur.e - ptr * wri[IVX] + ptst * spd[2] +
+            bxi * (wri[IVX] * bxi + (wri[IVY] * ur.by + wri[IVZ] * ur.bz) - vbstr)) * sdmr_inv;
+  if (T(0.5) * bxsq < T(1.0e-8) * ptst) {
+    uldst = ulst; urdst = urst;
+  } else {
+    T invsumd = T(1.0) / (sqrtdl + sqrtdr);
+    T bxsig = (bxi > T(0.0) ? T(1.0) : -T(1.0));
+    uldst.d = ulst.d; urdst.d = urst.d;
+    uldst.mx = ulst.mx; urdst.mx = urst.mx;
+    T tmp = invsumd * (sqrtdl * (ulst.my * ulst_d_inv) + sqrtdr * (urst.my * urst_d_inv) +
+                            bxsig * (urst.by - ulst.by));
+    uldst.my = uldst.d * tmp; urdst.my = urdst.d * tmp;
+    tmp = invsumd * (sqrtdl * (ulst.mz * ulst_d_inv) + sqrtdr * (urst.mz * urst_d_inv) +
+                     bxsig * (urst.bz - ulst.bz));
+    uldst.mz = uldst.d * tmp; urdst.mz = urdst.d * tmp;
+    tmp = invsumd * (sqrtdl * urst.by + sqrtdr * ulst.by +
+                     bxsig * sqrtdl * sqrtdr * ((urst.my * urst_d_inv) - (ulst.my * ulst_d_inv)));
+    uldst.by = urdst.by = tmp;
+    tmp = invsumd * (sqrtdl * urst.bz + sqrtdr * ulst.bz +
+                     bxsig * sqrtdl * sqrtdr * ((urst.mz * urst_d_inv) - (ulst.mz * ulst_d_inv)));
+    uldst.bz = urdst.bz = tmp;
+    tmp = spd[2] * bxi + (uldst.my * uldst.by + uldst.mz * uldst.bz) / uldst.d;
+    uldst.e = ulst.e - sqrtdl * bxsig * (vbstl - tmp);
+    urdst.e = urst.e + sqrtdr * bxsig * (vbstr - tmp);
+  }
+#define DIFFW(dst, a, b, sp) \
+  dst.d = sp * (a.d - b.d); dst.mx = sp * (a.mx - b.mx); dst.my = sp * (a.my - b.my); \
+  dst.mz = sp * (a.mz - b.mz); dst.e = sp * (a.e - b.e); dst.by = sp * (a.by - b.by); \
+  dst.bz = sp * (a.bz - b.bz);
+  C1D<T> t1, t0, t3, t4;
+  DIFFW(t1, uldst, ulst, spd[1]);
+  DIFFW(t0, ulst, ul, spd[0]);
+  DIFFW(t3, urdst, urst, spd[3]);
+  DIFFW(t4, urst, ur, spd[4]);
+#undef DIFFW
+  if (spd[0] >= T(0.0)) {
+    flxi[IDN] = fl.d; flxi[IVX] = fl.mx; flxi[IVY] = fl.my; flxi[IVZ] = fl.mz;
+    flxi[IEN] = fl.e; flxi[IBY] = fl.by; flxi[IBZ] = fl.bz;
+  } else if (spd[4] <= T(0.0)) {
+    flxi[IDN] = fr.d; flxi[IVX] = fr.mx; flxi[IVY] = fr.my; flxi[IVZ] = fr.mz;
+    flxi[IEN] = fr.e; flxi[IBY] = fr.by; flxi[IBZ] = fr.bz;
+  } else if (spd[1] >= T(0.0)) {
+    flxi[IDN] = fl.d + t0.d; flxi[IVX] = fl.mx + t0.mx; flxi[IVY] = fl.my + t0.my;
+    flxi[IVZ] = fl.mz + t0.mz; flxi[IEN] = fl.e + t0.e; flxi[IBY] = fl.by + t0.by;
+    flxi[IBZ] = fl.bz + t0.bz;
+  } else if (spd[2] >= T(0.0)) {
+    flxi[IDN] = fl.d + t0.d + t1.d; flxi[IVX] = fl.mx + t0.mx + t1.mx;
+    flxi[IVY] = fl.my + t0.my + t1.my; flxi[IVZ] = fl.mz + t0.mz + t1.mz;
+    flxi[IEN] = fl.e + t0.e + t1.e; flxi[IBY] = fl.by + t0.by + t1.by;
+    flxi[IBZ] = fl.bz + t0.bz + t1.bz;
+  } else if (spd[3] > T(0.0)) {
+    flxi[IDN] = fr.d + t4.d + t3.d; flxi[IVX] = fr.mx + t4.mx + t3.mx;
+    flxi[IVY] = fr.my + t4.my + t3.my; flxi[IVZ] = fr.mz + t4.mz + t3.mz;
+    flxi[IEN] = fr.e + t4.e + t3.e; flxi[IBY] = fr.by + t4.by + t3.by;
+    flxi[IBZ] = fr.bz + t4.bz + t3.bz;
+  } else {
+    flxi[IDN] = fr.d + t4.d; flxi[IVX] = fr.mx + t4.mx; flxi[IVY] = fr.my + t4.my;
+    flxi[IVZ] = fr.mz + t4.mz; flxi[IEN] = fr.e + t4.e; flxi[IBY] = fr.by + t4.by;
+    flxi[IBZ] = fr.bz + t4.bz;
   }
 }
 

@@ -61,11 +61,15 @@ static void flux_dir(const Geom& g, const StagePtrs<T>& p, bool mhd, int solver,
     if (mhd) {
       if (solver == HLLD)
         k_flux_march<T, DIR, ORDER, HLLD, true><<<grid, 128, 0, st>>>(g, p, pb, ph, fs, fe);
+      else if (solver == LHLLD)
+        k_flux_march<T, DIR, ORDER, LHLLD, true><<<grid, 128, 0, st>>>(g, p, pb, ph, fs, fe);
       else
         k_flux_march<T, DIR, ORDER, HLLE, true><<<grid, 128, 0, st>>>(g, p, pb, ph, fs, fe);
     } else {
       if (solver == HLLC)
         k_flux_march<T, DIR, ORDER, HLLC, false><<<grid, 128, 0, st>>>(g, p, pb, ph, fs, fe);
+      else if (solver == LHLLC)
+        k_flux_march<T, DIR, ORDER, LHLLC, false><<<grid, 128, 0, st>>>(g, p, pb, ph, fs, fe);
       else
         k_flux_march<T, DIR, ORDER, HLLE, false><<<grid, 128, 0, st>>>(g, p, pb, ph, fs, fe);
     }
@@ -74,9 +78,11 @@ static void flux_dir(const Geom& g, const StagePtrs<T>& p, bool mhd, int solver,
   dim3 grid = box_grid(b, g.nb, 128);
   if (mhd) {
     if (solver == HLLD) k_flux<T, DIR, ORDER, HLLD, true><<<grid, 128, 0, st>>>(g, p, b, ph);
+    else if (solver == LHLLD) k_flux<T, DIR, ORDER, LHLLD, true><<<grid, 128, 0, st>>>(g, p, b, ph);
     else k_flux<T, DIR, ORDER, HLLE, true><<<grid, 128, 0, st>>>(g, p, b, ph);
   } else {
     if (solver == HLLC) k_flux<T, DIR, ORDER, HLLC, false><<<grid, 128, 0, st>>>(g, p, b, ph);
+    else if (solver == LHLLC) k_flux<T, DIR, ORDER, LHLLC, false><<<grid, 128, 0, st>>>(g, p, b, ph);
     else k_flux<T, DIR, ORDER, HLLE, false><<<grid, 128, 0, st>>>(g, p, b, ph);
   }
   }

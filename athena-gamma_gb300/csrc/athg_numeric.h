@@ -7,6 +7,7 @@
 // (host and device), so the CPU tests check it bit for bit against the host's own casts.
 #pragma once
 #include <cstdint>
+#include <cmath>
 #include <cstring>
 
 #ifdef __CUDACC__
@@ -84,5 +85,98 @@ ATHG_HD void sum2diff(float a, float b, float c, float d, float& hi, float& lo) 
   two_sum(s1, s2, hi, e3);
   lo = (e1 + e2) + e3;
 }
+
+// ---- double-float (unevaluated FP32 pairs hi + lo) --------------------------------------
+// Used where an FP64-class result is needed from FP64 inputs without FP64 instructions:
+// |hi + lo - x| <= about 2^-46 |x|.
+struct ff {
+  float hi, lo;
+};
+
+// Split binary64 x into hi = x rounded to binary32 and lo ~ x - hi, on the integer pipe:
+// the 29 mantissa bits that rounding drops become a signed integer r, |r| <= 2^28, kept
+// to 22 bits and scaled by the exponent. |x| outside [2^-80, 2^120]: lo = 0.
+ATHG_HD ff split_ff(double x) {
+  const uint64_t b = bits_d(x);
+  const uint32_t hi32 = (uint32_t)(b >> 32);
+  const int e = (int)((hi32 >> 20) & 0x7ffu);
+  const uint64_t X = (b & 0x000fffffffffffffull) | 0x0010000000000000ull;  // 53-bit mantissa
+  const uint64_t H = (X + 0x0fffffffull + ((X >> 29) & 1ull)) >> 29;      // rounded to 24 bits
+  const int32_t r = (int32_t)(int64_t)(X - (H << 29));                     // |r| <= 2^28
+  ff o;
+  o.hi = d2f_int(x);
+  // (r >> 6) as a float through the 1.5 * 2^23 offset (exact for |r >> 6| <= 2^22), times
+  // 2^(e - 1075 + 6)
+  const float q = from_bits_f(0x4b400000u + (uint32_t)(r >> 6)) - 12582912.0f;
+  const int se = e - 1069 + 127;
+  const float scale = from_bits_f((uint32_t)(se > 0 && se < 255 ? se : 1) << 23);
+  float lo = (se > 0 && se < 255 && e >= 943 && e <= 1143) ? q * scale : 0.0f;
+  o.lo = (hi32 & 0x80000000u) ? -lo : lo;
+  return o;
+}
+
+// error-free product of two binary32 numbers (needs a fused multiply-add)
+ATHG_HD void two_prod(float a, float b, float& p, float& e) {
+  p = a * b;
+  e = std::fma(a, b, -p);
+}
+
+ATHG_HD ff ff_renorm(float s, float e) {
+  ff o;
+  two_sum(s, e, o.hi, o.lo);
+  return o;
+}
+
+ATHG_HD ff ff_add(ff a, ff b) {
+  float s, e;
+  two_sum(a.hi, b.hi, s, e);
+  e += a.lo + b.lo;
+  return ff_renorm(s, e);
+}
+
+ATHG_HD ff ff_sub(ff a, ff b) {
+  ff nb;
+  nb.hi = -b.hi;
+  nb.lo = -b.lo;
+  return ff_add(a, nb);
+}
+
+ATHG_HD ff ff_mul(ff a, ff b) {
+  float p, e;
+  two_prod(a.hi, b.hi, p, e);
+  e = std::fma(a.hi, b.lo, e);
+  e = std::fma(a.lo, b.hi, e);
+  return ff_renorm(p, e);
+}
+
+ATHG_HD ff ff_sqr(ff a) {
+  float p, e;
+  two_prod(a.hi, a.hi, p, e);
+  e = std::fma(2.0f * a.hi, a.lo, e);
+  return ff_renorm(p, e);
+}
+
+ATHG_HD ff ff_scale(ff a, float pow2) {  // exact for a power of two
+  ff o;
+  o.hi = a.hi * pow2;
+  o.lo = a.lo * pow2;
+  return o;
+}
+
+// 1 / a from an FP32 reciprocal and one double-float Newton step
+ATHG_HD ff ff_recip(ff a) {
+  const float r = 1.0f / a.hi;
+  // residual 1 - a r in double-float, then r + r (1 - a r)
+  float p, e;
+  two_prod(a.hi, r, p, e);
+  const float res = ((1.0f - p) - e) - a.lo * r;
+  return ff_renorm(r, r * res);
+}
+
+// value rounded to binary32
+ATHG_HD float ff_f(ff a) { return a.hi + a.lo; }
+
+// a > b for double-float values (normalised: |lo| <= ulp(hi) / 2)
+ATHG_HD bool ff_gt(ff a, ff b) { return a.hi > b.hi || (a.hi == b.hi && a.lo > b.lo); }
 
 }  // namespace athg

@@ -20,6 +20,8 @@ struct StagePtrs {
   T *flx[3];                 // per direction [nb][NF][faces]; NF = 5 (hydro) or 8 (MHD:
                              // 5 fluxes, ey, ez, CT weight)
   T *edge;                   // corner EMFs [nb][3][edges]
+  T *cce;                    // mixed path: cell-centred E = -v x B [nb][3][cells], written
+                             // by k_c2p for k_corner_emf (nullptr in the FP64 path)
   const BlockGeo *geo;       // [nb] cell widths (FP64)
   const T *coef;             // PLM interface coefficients [nb][3][2][ncmax]
   const T *dxT;              // [nb][3] cell widths in T
@@ -60,6 +62,40 @@ __device__ __forceinline__ T wave_var(const T* __restrict__ w, const T* __restri
   constexpr int by = DIR == 0 ? 1 : (DIR == 1 ? 2 : 0);
   constexpr int bz = DIR == 0 ? 2 : (DIR == 1 ? 0 : 1);
   return bcc[(n == IBY ? by : bz) * nc + c];
+}
+
+// Hydro::CalculateVelocityDifferences (hydro/calculate_velocity_differences.cpp:20-52,
+// 3-D) at face (k,j,i) of a DIR sweep: the normal velocity jump and the smallest
+// transverse velocity difference around the face (the LHLLC/LHLLD shock detector).
+template <typename T, int DIR>
+__device__ __forceinline__ void velocity_differences(const Geom& g, const T* __restrict__ w,
+                                                     int k, int j, int i, T& dvn, T& dvt) {
+  const int64_t nc = g.ncell;
+  const T* vx = w + IVX * nc;
+  const T* vy = w + IVY * nc;
+  const T* vz = w + IVZ * nc;
+  auto W = [&](const T* a, int kk, int jj, int ii) { return a[cidx(g, kk, jj, ii)]; };
+  T dvl, dvr, dwl, dwr;
+  if (DIR == 0) {
+    dvn = W(vx, k, j, i) - W(vx, k, j, i - 1);
+    dvl = mn(W(vy, k, j + 1, i - 1) - W(vy, k, j, i - 1), W(vy, k, j, i - 1) - W(vy, k, j - 1, i - 1));
+    dvr = mn(W(vy, k, j + 1, i) - W(vy, k, j, i), W(vy, k, j, i) - W(vy, k, j - 1, i));
+    dwl = mn(W(vz, k + 1, j, i - 1) - W(vz, k, j, i - 1), W(vz, k, j, i - 1) - W(vz, k - 1, j, i - 1));
+    dwr = mn(W(vz, k + 1, j, i) - W(vz, k, j, i), W(vz, k, j, i) - W(vz, k - 1, j, i));
+  } else if (DIR == 1) {
+    dvn = W(vy, k, j, i) - W(vy, k, j - 1, i);
+    dvl = mn(W(vz, k + 1, j - 1, i) - W(vz, k, j - 1, i), W(vz, k, j - 1, i) - W(vz, k - 1, j - 1, i));
+    dvr = mn(W(vz, k + 1, j, i) - W(vz, k, j, i), W(vz, k, j, i) - W(vz, k - 1, j, i));
+    dwl = mn(W(vx, k, j - 1, i + 1) - W(vx, k, j - 1, i), W(vx, k, j - 1, i) - W(vx, k, j - 1, i - 1));
+    dwr = mn(W(vx, k, j, i + 1) - W(vx, k, j, i), W(vx, k, j, i) - W(vx, k, j, i - 1));
+  } else {
+    dvn = W(vz, k, j, i) - W(vz, k - 1, j, i);
+    dvl = mn(W(vx, k - 1, j, i + 1) - W(vx, k - 1, j, i), W(vx, k - 1, j, i) - W(vx, k - 1, j, i - 1));
+    dvr = mn(W(vx, k, j, i + 1) - W(vx, k, j, i), W(vx, k, j, i) - W(vx, k, j, i - 1));
+    dwl = mn(W(vy, k - 1, j + 1, i) - W(vy, k - 1, j, i), W(vy, k - 1, j, i) - W(vy, k - 1, j - 1, i));
+    dwr = mn(W(vy, k, j + 1, i) - W(vy, k, j, i), W(vy, k, j, i) - W(vy, k, j - 1, i));
+  }
+  dvt = mn(mn(dvl, dvr), mn(dwl, dwr));
 }
 
 // Face-flux kernel: one thread per face. Reconstruction (donor cell or van Leer PLM,
@@ -141,14 +177,28 @@ k_flux(Geom g, StagePtrs<T> p, Box bx, Phys ph) {
     wli[IBY] = wl[IBY]; wli[IBZ] = wl[IBZ];
     wri[IBY] = wr[IBY]; wri[IBZ] = wr[IBZ];
     const T bxi = p.bf[DIR][(int64_t)b * nf + fi];
-    if (SOLVER == HLLD) rs_hlld<T>(wli, wri, bxi, gam, fx);
-    else rs_hlle_mhd<T>(wli, wri, bxi, gam, fx);
+    if (SOLVER == HLLD) {
+      rs_hlld<T>(wli, wri, bxi, gam, fx);
+    } else if (SOLVER == LHLLD) {
+      T dvn, dvt;
+      velocity_differences<T, DIR>(g, p.w + (int64_t)b * NHYD * g.ncell, k, j, i, dvn, dvt);
+      rs_lhlld<T>(wli, wri, bxi, gam, dvn, dvt, fx);
+    } else {
+      rs_hlle_mhd<T>(wli, wri, bxi, gam, fx);
+    }
     out[5 * nf + fi] = -fx[IBY];
     out[6 * nf + fi] = fx[IBZ];
     out[7 * nf + fi] = ct_weight<T>(fx[IDN], wli[IDN], wri[IDN], p.dxT[b * 3 + DIR], *p.dtT);
   } else {
-    if (SOLVER == HLLC) rs_hllc<T>(wli, wri, gam, fx);
-    else rs_hlle_hydro<T>(wli, wri, gam, fx);
+    if (SOLVER == HLLC) {
+      rs_hllc<T>(wli, wri, gam, fx);
+    } else if (SOLVER == LHLLC) {
+      T dvn, dvt;
+      velocity_differences<T, DIR>(g, p.w + (int64_t)b * NHYD * g.ncell, k, j, i, dvn, dvt);
+      rs_lhllc<T>(wli, wri, gam, dvn, dvt, fx);
+    } else {
+      rs_hlle_hydro<T>(wli, wri, gam, fx);
+    }
   }
   out[IDN * nf + fi] = fx[IDN];
   out[ivx * nf + fi] = fx[IVX];
@@ -161,7 +211,8 @@ k_flux(Geom g, StagePtrs<T> p, Box bx, Phys ph) {
 // flux (and for MHD the face EMFs and CT weight) like k_flux.
 template <typename T, int DIR, int SOLVER, bool MHD>
 __device__ __forceinline__ void face_solve(const Geom& g, const StagePtrs<T>& p, const Phys& ph,
-                                           int b, int64_t fi, const T* wl, const T* wr) {
+                                           int b, int64_t fi, const T* wl, const T* wr,
+                                           int k, int j, int i) {
   constexpr int NF = MHD ? 8 : 5;
   constexpr int ivx = IVX + DIR, ivy = IVX + (DIR + 1) % 3, ivz = IVX + (DIR + 2) % 3;
   T wli[7], wri[7], fx[7];
@@ -176,14 +227,28 @@ __device__ __forceinline__ void face_solve(const Geom& g, const StagePtrs<T>& p,
     wli[IBY] = wl[IBY]; wli[IBZ] = wl[IBZ];
     wri[IBY] = wr[IBY]; wri[IBZ] = wr[IBZ];
     const T bxi = p.bf[DIR][(int64_t)b * nf + fi];
-    if (SOLVER == HLLD) rs_hlld<T>(wli, wri, bxi, gam, fx);
-    else rs_hlle_mhd<T>(wli, wri, bxi, gam, fx);
+    if (SOLVER == HLLD) {
+      rs_hlld<T>(wli, wri, bxi, gam, fx);
+    } else if (SOLVER == LHLLD) {
+      T dvn, dvt;
+      velocity_differences<T, DIR>(g, p.w + (int64_t)b * NHYD * g.ncell, k, j, i, dvn, dvt);
+      rs_lhlld<T>(wli, wri, bxi, gam, dvn, dvt, fx);
+    } else {
+      rs_hlle_mhd<T>(wli, wri, bxi, gam, fx);
+    }
     out[5 * nf + fi] = -fx[IBY];
     out[6 * nf + fi] = fx[IBZ];
     out[7 * nf + fi] = ct_weight<T>(fx[IDN], wli[IDN], wri[IDN], p.dxT[b * 3 + DIR], *p.dtT);
   } else {
-    if (SOLVER == HLLC) rs_hllc<T>(wli, wri, gam, fx);
-    else rs_hlle_hydro<T>(wli, wri, gam, fx);
+    if (SOLVER == HLLC) {
+      rs_hllc<T>(wli, wri, gam, fx);
+    } else if (SOLVER == LHLLC) {
+      T dvn, dvt;
+      velocity_differences<T, DIR>(g, p.w + (int64_t)b * NHYD * g.ncell, k, j, i, dvn, dvt);
+      rs_lhllc<T>(wli, wri, gam, dvn, dvt, fx);
+    } else {
+      rs_hlle_hydro<T>(wli, wri, gam, fx);
+    }
   }
   out[IDN * nf + fi] = fx[IDN];
   out[ivx * nf + fi] = fx[IVX];
@@ -235,7 +300,8 @@ k_flux_march(Geom g, StagePtrs<T> p, Box bx, Phys ph, int fs, int fe) {
       int64_t cc = c + st;
 #pragma unroll
       for (int n = 0; n < NW; ++n) wr[n] = wave_var<T, DIR>(w, bcc, nc, n, cc);
-      face_solve<T, DIR, SOLVER, MHD>(g, p, ph, b, face_at(f), wlnext, wr);
+      face_solve<T, DIR, SOLVER, MHD>(g, p, ph, b, face_at(f), wlnext, wr, DIR == 1 ? a : f,
+                                      DIR == 1 ? f : a, i);
 #pragma unroll
       for (int n = 0; n < NW; ++n) wlnext[n] = wr[n];
       c = cc;
@@ -270,7 +336,8 @@ k_flux_march(Geom g, StagePtrs<T> p, Box bx, Phys ph, int fs, int fe) {
       }
       cm1[IDN] = (cm1[IDN] > df) ? cm1[IDN] : df; cm1[IPR] = (cm1[IPR] > pf) ? cm1[IPR] : pf;
       wr[IDN] = (wr[IDN] > df) ? wr[IDN] : df; wr[IPR] = (wr[IPR] > pf) ? wr[IPR] : pf;
-      face_solve<T, DIR, SOLVER, MHD>(g, p, ph, b, face_at(f), cm1, wr);
+      face_solve<T, DIR, SOLVER, MHD>(g, p, ph, b, face_at(f), cm1, wr, DIR == 1 ? a : f,
+                                      DIR == 1 ? f : a, i);
     }
     return;
   }
@@ -306,7 +373,8 @@ k_flux_march(Geom g, StagePtrs<T> p, Box bx, Phys ph, int fs, int fe) {
       cm1[n] = wlnext[n];                 // reuse the slot: left state of face f
       wlnext[n] = c0[n] + cpR * dwm;      // left state of face f+1
     }
-    face_solve<T, DIR, SOLVER, MHD>(g, p, ph, b, face_at(f), cm1, wr);
+    face_solve<T, DIR, SOLVER, MHD>(g, p, ph, b, face_at(f), cm1, wr, DIR == 1 ? a : f,
+                                    DIR == 1 ? f : a, i);
     c += st;
   }
 }
@@ -322,8 +390,10 @@ __global__ void __launch_bounds__(128) k_corner_emf(Geom g, StagePtrs<T> p, Box 
   const int64_t nc = g.ncell;
   const T* w = p.w + (int64_t)b * NHYD * nc;
   const T* bc = p.bcc + (int64_t)b * 3 * nc;
+  const T* ce = kMixed<T> ? p.cce + (int64_t)b * 3 * nc : nullptr;
   auto cce = [&](int n, int kk, int jj, int ii) -> T {
     int64_t c = cidx(g, kk, jj, ii);
+    if constexpr (kMixed<T>) return ce[n * nc + c];
     T vx = w[IVX * nc + c], vy = w[IVY * nc + c], vz = w[IVZ * nc + c];
     T bx1 = bc[c], by1 = bc[nc + c], bz1 = bc[2 * nc + c];
     if (n == 0) return vz * by1 - vy * bz1;
@@ -405,84 +475,113 @@ __global__ void __launch_bounds__(128) k_update(Geom g, StagePtrs<T> p, Box bx, 
     // the final U - (hi + lo) runs in FP64. The face fields take the same route with
     // edge-integrated EMFs (beta dt dx_e E), so each face's flux change is an exact sum
     // of shared edge values and div B stays at FP64 round-off.
+    // Every input is loaded before the first store (restrict-qualified, read-only path),
+    // so a thread keeps all its ~50 loads in flight at once.
     const MixedGeo mg = p.mg[b];
-    const float wf = __fmul_rn(sw.betaf, *p.dtT);
-    if (i <= g.ie && j <= g.je && k <= g.ke) {
-      const float cw1 = __fmul_rn(wf, mg.idx[0]), cw2 = __fmul_rn(wf, mg.idx[1]),
-                  cw3 = __fmul_rn(wf, mg.idx[2]);
-      const int64_t nc = g.ncell;
-      double* u = p.u + (int64_t)b * NHYD * nc;
-      double* u1 = p.u1 + (int64_t)b * NHYD * nc;
+    const float wf = __fmul_rn(sw.betaf, __ldg(p.dtT));
+    const bool cell = (i <= g.ie && j <= g.je && k <= g.ke);
+    const int64_t nc = g.ncell;
+    double* __restrict__ u = p.u + (int64_t)b * NHYD * nc;
+    double* __restrict__ u1 = p.u1 + (int64_t)b * NHYD * nc;
+    const int64_t c = cidx(g, k, j, i);
+    float fx[NHYD][6];
+    double uo[NHYD], ro[NHYD];
+    if (cell) {
       constexpr int NF = MHD ? 8 : 5;
-      const T* F1 = p.flx[0] + (int64_t)b * NF * g.nf1;
-      const T* F2 = p.flx[1] + (int64_t)b * NF * g.nf2;
-      const T* F3 = p.flx[2] + (int64_t)b * NF * g.nf3;
-      const int64_t c = cidx(g, k, j, i);
+      const T* __restrict__ F1 = p.flx[0] + (int64_t)b * NF * g.nf1;
+      const T* __restrict__ F2 = p.flx[1] + (int64_t)b * NF * g.nf2;
+      const T* __restrict__ F3 = p.flx[2] + (int64_t)b * NF * g.nf3;
       const int64_t q1 = f1idx(g, k, j, i), q2 = f2idx(g, k, j, i), q3 = f3idx(g, k, j, i);
       const int64_t s2 = g.nc1, s3 = (int64_t)g.nc1 * g.nc2;
 #pragma unroll
       for (int n = 0; n < NHYD; ++n) {
-        const double uo = u[n * nc + c];
-        double base;
-        if (sw.copy_reg) {  // first stage: register = u exactly
-          u1[n * nc + c] = uo;
-          base = sw.swap ? uo : sw.g1 * uo + sw.g2 * uo;
-        } else {
-          double r = sw.zero_reg ? 0.0 : u1[n * nc + c];
-          if (sw.has_delta) { r += sw.delta * uo; u1[n * nc + c] = r; }
-          base = sw.swap ? r : sw.g1 * uo + sw.g2 * r;
-        }
+        fx[n][0] = __ldg(F1 + n * g.nf1 + q1 + 1);
+        fx[n][1] = __ldg(F1 + n * g.nf1 + q1);
+        fx[n][2] = __ldg(F2 + n * g.nf2 + q2 + s2);
+        fx[n][3] = __ldg(F2 + n * g.nf2 + q2);
+        fx[n][4] = __ldg(F3 + n * g.nf3 + q3 + s3);
+        fx[n][5] = __ldg(F3 + n * g.nf3 + q3);
+        uo[n] = u[n * nc + c];
+        ro[n] = (sw.copy_reg || sw.zero_reg) ? 0.0 : u1[n * nc + c];
+      }
+    }
+    // face fields: base values and the four edge EMFs of each face
+    double bo[3] = {0.0, 0.0, 0.0}, rb[3] = {0.0, 0.0, 0.0};
+    float ed[3][4];
+    int64_t qf[3] = {0, 0, 0};
+    bool own[3] = {false, false, false};
+    if constexpr (MHD) {
+      const T* __restrict__ E1 = p.edge + (int64_t)b * 3 * g.ne;
+      const T* __restrict__ E2 = E1 + g.ne;
+      const T* __restrict__ E3 = E2 + g.ne;
+      const int64_t e = eidx(g, k, j, i);
+      const int64_t ej = (int64_t)g.nc1 + 1, ek = ((int64_t)g.nc1 + 1) * (g.nc2 + 1);
+      own[0] = (j <= g.je && k <= g.ke);
+      own[1] = (i <= g.ie && k <= g.ke);
+      own[2] = (i <= g.ie && j <= g.je);
+      qf[0] = (int64_t)b * g.nf1 + f1idx(g, k, j, i);
+      qf[1] = (int64_t)b * g.nf2 + f2idx(g, k, j, i);
+      qf[2] = (int64_t)b * g.nf3 + f3idx(g, k, j, i);
+      double* __restrict__ bb[3] = {p.b1, p.b2, p.b3};
+      double* __restrict__ rr[3] = {p.r1, p.r2, p.r3};
+      // dPhi1 = (eps3(j) - eps3(j+1)) + (eps2(k+1) - eps2(k))
+      // dPhi2 = (eps3(i+1) - eps3(i)) + (eps1(k) - eps1(k+1))
+      // dPhi3 = (eps2(i) - eps2(i+1)) + (eps1(j+1) - eps1(j))
+      const T* __restrict__ ea[3][2] = {{E3, E2}, {E3, E1}, {E2, E1}};
+      const int64_t eo[3][4] = {{e, e + ej, e + ek, e}, {e + 1, e, e, e + ek},
+                                {e, e + 1, e + ej, e}};
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        if (!own[d]) continue;
+        bo[d] = bb[d][qf[d]];
+        rb[d] = (sw.copy_reg || sw.zero_reg) ? 0.0 : rr[d][qf[d]];
+        ed[d][0] = __ldg(ea[d][0] + eo[d][0]);
+        ed[d][1] = __ldg(ea[d][0] + eo[d][1]);
+        ed[d][2] = __ldg(ea[d][1] + eo[d][2]);
+        ed[d][3] = __ldg(ea[d][1] + eo[d][3]);
+      }
+    }
+    auto base_of = [&](double vo, double& r) -> double {
+      if (sw.copy_reg) {  // first stage: register = state exactly
+        r = vo;
+        return sw.swap ? vo : sw.g1 * vo + sw.g2 * vo;
+      }
+      if (sw.has_delta) r += sw.delta * vo;
+      return sw.swap ? r : sw.g1 * vo + sw.g2 * r;
+    };
+    if (cell) {
+      const float cw1 = __fmul_rn(wf, mg.idx[0]), cw2 = __fmul_rn(wf, mg.idx[1]),
+                  cw3 = __fmul_rn(wf, mg.idx[2]);
+#pragma unroll
+      for (int n = 0; n < NHYD; ++n) {
+        double r = ro[n];
+        const double base = base_of(uo[n], r);
+        if (sw.copy_reg || sw.has_delta) u1[n * nc + c] = r;
         float hi, lo;
-        sum3diff(__fmul_rn(cw1, F1[n * g.nf1 + q1 + 1]), __fmul_rn(cw1, F1[n * g.nf1 + q1]),
-                 __fmul_rn(cw2, F2[n * g.nf2 + q2 + s2]), __fmul_rn(cw2, F2[n * g.nf2 + q2]),
-                 __fmul_rn(cw3, F3[n * g.nf3 + q3 + s3]), __fmul_rn(cw3, F3[n * g.nf3 + q3]),
-                 hi, lo);
+        sum3diff(__fmul_rn(cw1, fx[n][0]), __fmul_rn(cw1, fx[n][1]),
+                 __fmul_rn(cw2, fx[n][2]), __fmul_rn(cw2, fx[n][3]),
+                 __fmul_rn(cw3, fx[n][4]), __fmul_rn(cw3, fx[n][5]), hi, lo);
         u[n * nc + c] = (base - f2d_int(hi)) - f2d_int(lo);
       }
     }
     if constexpr (MHD) {
-      const T* E1 = p.edge + (int64_t)b * 3 * g.ne;
-      const T* E2 = E1 + g.ne;
-      const T* E3 = E2 + g.ne;
-      const float we1 = __fmul_rn(wf, mg.dx[0]), we2 = __fmul_rn(wf, mg.dx[1]),
-                  we3 = __fmul_rn(wf, mg.dx[2]);
-      const int64_t e = eidx(g, k, j, i);
-      const int64_t ej = (int64_t)g.nc1 + 1, ek = ((int64_t)g.nc1 + 1) * (g.nc2 + 1);
-      auto reg = [&](double* bb, double* rr, int64_t q) -> double {
-        const double bo = bb[q];
-        if (sw.copy_reg) {
-          rr[q] = bo;
-          return sw.swap ? bo : sw.g1 * bo + sw.g2 * bo;
-        }
-        double r = sw.zero_reg ? 0.0 : rr[q];
-        if (sw.has_delta) { r += sw.delta * bo; rr[q] = r; }
-        return sw.swap ? r : sw.g1 * bo + sw.g2 * r;
-      };
-      auto apply = [&](double v, float hi, float lo, double ia) {
-        v = fma(f2d_int(hi), ia, v);
-        return fma(f2d_int(lo), ia, v);
-      };
-      float hi, lo;
-      if (j <= g.je && k <= g.ke) {  // dPhi1 = -(eps3(j+1) - eps3(j)) + (eps2(k+1) - eps2(k))
-        int64_t q = (int64_t)b * g.nf1 + f1idx(g, k, j, i);
-        double v = reg(p.b1, p.r1, q);
-        sum2diff(__fmul_rn(we3, E3[e]), __fmul_rn(we3, E3[e + ej]),
-                 __fmul_rn(we2, E2[e + ek]), __fmul_rn(we2, E2[e]), hi, lo);
-        p.b1[q] = apply(v, hi, lo, mg.ia[0]);
-      }
-      if (i <= g.ie && k <= g.ke) {  // dPhi2 = (eps3(i+1) - eps3(i)) - (eps1(k+1) - eps1(k))
-        int64_t q = (int64_t)b * g.nf2 + f2idx(g, k, j, i);
-        double v = reg(p.b2, p.r2, q);
-        sum2diff(__fmul_rn(we3, E3[e + 1]), __fmul_rn(we3, E3[e]),
-                 __fmul_rn(we1, E1[e]), __fmul_rn(we1, E1[e + ek]), hi, lo);
-        p.b2[q] = apply(v, hi, lo, mg.ia[1]);
-      }
-      if (i <= g.ie && j <= g.je) {  // dPhi3 = -(eps2(i+1) - eps2(i)) + (eps1(j+1) - eps1(j))
-        int64_t q = (int64_t)b * g.nf3 + f3idx(g, k, j, i);
-        double v = reg(p.b3, p.r3, q);
-        sum2diff(__fmul_rn(we2, E2[e]), __fmul_rn(we2, E2[e + 1]),
-                 __fmul_rn(we1, E1[e + ej]), __fmul_rn(we1, E1[e]), hi, lo);
-        p.b3[q] = apply(v, hi, lo, mg.ia[2]);
+      const float we[3] = {__fmul_rn(wf, mg.dx[0]), __fmul_rn(wf, mg.dx[1]),
+                           __fmul_rn(wf, mg.dx[2])};
+      // the EMF component of each term: face 1 uses (e3, e2), face 2 (e3, e1), face 3 (e2, e1)
+      const int comp[3][2] = {{2, 1}, {2, 0}, {1, 0}};
+      double* __restrict__ bb[3] = {p.b1, p.b2, p.b3};
+      double* __restrict__ rr[3] = {p.r1, p.r2, p.r3};
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        if (!own[d]) continue;
+        double r = rb[d];
+        const double v = base_of(bo[d], r);
+        if (sw.copy_reg || sw.has_delta) rr[d][qf[d]] = r;
+        const float wa = we[comp[d][0]], wb = we[comp[d][1]];
+        float hi, lo;
+        sum2diff(__fmul_rn(wa, ed[d][0]), __fmul_rn(wa, ed[d][1]), __fmul_rn(wb, ed[d][2]),
+                 __fmul_rn(wb, ed[d][3]), hi, lo);
+        bb[d][qf[d]] = fma(f2d_int(lo), mg.ia[d], fma(f2d_int(hi), mg.ia[d], v));
       }
     }
   } else {
@@ -568,54 +667,74 @@ __global__ void __launch_bounds__(256) k_c2p(Geom g, StagePtrs<T> p, Box bx, Phy
   int i, j, k, b;
   if (!box_coords(bx, i, j, k, b)) return;
   if constexpr (kMixed<T>) {
-    // Mixed path: the internal energy is still formed in FP64 (it is the small difference
-    // of large terms); everything that is only stored in FP32 is formed in FP32, and the
-    // conversions run on the integer pipe. Density is floored in place, energy only where
-    // the pressure floor acts (the reference writes the same values).
+    // Mixed path. The FP64 state is split exactly (integer pipe) into double-float pairs
+    // and the internal energy E - m^2/2d - B^2/2 is formed in double-float arithmetic on
+    // the FP32 pipe (relative error ~1e-13 of E, the class of the FP64 formula), so no
+    // FP64 instruction runs outside the floor branches. Density is floored in place,
+    // energy only where the pressure floor acts (the values the reference writes).
     const int64_t nc = g.ncell;
     const int64_t c = cidx(g, k, j, i);
-    double* u = p.u + (int64_t)b * NHYD * nc;
-    float* w = p.w + (int64_t)b * NHYD * nc;
-    double ss = 0.0;  // (2 Bcc)^2
+    double* __restrict__ u = p.u + (int64_t)b * NHYD * nc;
+    float* __restrict__ w = p.w + (int64_t)b * NHYD * nc;
+    ff ss = {0.0f, 0.0f};  // (2 Bcc)^2
     if constexpr (MHD) {
-      const double* b1 = p.b1 + (int64_t)b * g.nf1;
-      const double* b2 = p.b2 + (int64_t)b * g.nf2;
-      const double* b3 = p.b3 + (int64_t)b * g.nf3;
+      const double* __restrict__ b1 = p.b1 + (int64_t)b * g.nf1;
+      const double* __restrict__ b2 = p.b2 + (int64_t)b * g.nf2;
+      const double* __restrict__ b3 = p.b3 + (int64_t)b * g.nf3;
       const int64_t q1 = f1idx(g, k, j, i), q2 = f2idx(g, k, j, i), q3 = f3idx(g, k, j, i);
-      const double f1 = b1[q1], f2 = b2[q2], f3 = b3[q3];
-      const double s1 = f1 + b1[q1 + 1], s2 = f2 + b2[q2 + g.nc1],
-                   s3 = f3 + b3[q3 + (int64_t)g.nc1 * g.nc2];
+      const ff f1 = split_ff(__ldg(b1 + q1)), f2 = split_ff(__ldg(b2 + q2)),
+               f3 = split_ff(__ldg(b3 + q3));
+      const ff s1 = ff_add(f1, split_ff(__ldg(b1 + q1 + 1)));
+      const ff s2 = ff_add(f2, split_ff(__ldg(b2 + q2 + g.nc1)));
+      const ff s3 = ff_add(f3, split_ff(__ldg(b3 + q3 + (int64_t)g.nc1 * g.nc2)));
       float* bcc = p.bcc + (int64_t)b * 3 * nc;
-      bcc[c] = 0.5f * d2f_int(s1);
-      bcc[nc + c] = 0.5f * d2f_int(s2);
-      bcc[2 * nc + c] = 0.5f * d2f_int(s3);
+      bcc[c] = 0.5f * ff_f(s1);
+      bcc[nc + c] = 0.5f * ff_f(s2);
+      bcc[2 * nc + c] = 0.5f * ff_f(s3);
       // FP32 copy of the lower faces of this cell for the flux kernels; every face index
       // the sweeps read (< nc along the normal) is the lower face of some cell
-      p.bfw[0][(int64_t)b * g.nf1 + q1] = d2f_int(f1);
-      p.bfw[1][(int64_t)b * g.nf2 + q2] = d2f_int(f2);
-      p.bfw[2][(int64_t)b * g.nf3 + q3] = d2f_int(f3);
-      ss = fma(s1, s1, fma(s2, s2, s3 * s3));
+      p.bfw[0][(int64_t)b * g.nf1 + q1] = f1.hi;
+      p.bfw[1][(int64_t)b * g.nf2 + q2] = f2.hi;
+      p.bfw[2][(int64_t)b * g.nf3 + q3] = f3.hi;
+      ss = ff_add(ff_add(ff_sqr(s1), ff_sqr(s2)), ff_sqr(s3));
     }
     double ud = u[c];
     const double m1 = u[nc + c], m2 = u[2 * nc + c], m3 = u[3 * nc + c], ue = u[4 * nc + c];
-    if (!(ud > ph.dfloor)) { ud = ph.dfloor; u[c] = ud; }
-    // FP32 reciprocal refined by one Newton step (relative error ~1e-14)
-    const float udf = d2f_int(ud);
-    const double r0 = f2d_int(1.0f / udf);
-    const double di = r0 * fma(-ud, r0, 2.0);
-    const double mm = fma(m1, m1, fma(m2, m2, m3 * m3));
-    const double x = MHD ? fma(mm, di, 0.25 * ss) : mm * di;  // 2 (e_k + p_B)
-    double wp = ph.gm1 * fma(-0.5, x, ue);
-    if (!(wp > ph.pfloor)) {
-      u[4 * nc + c] = (ph.pfloor / ph.gm1) + 0.5 * x;
-      wp = ph.pfloor;
+    // ud > dfloor on the bit patterns (dfloor > 0; negative, zero and NaN densities floor)
+    const uint64_t ub = bits_d(ud);
+    if (!((ub >> 63) == 0 && ub > bits_d(ph.dfloor) && ub <= 0x7ff0000000000000ull)) {
+      ud = ph.dfloor;
+      u[c] = ud;
     }
-    const float dif = d2f_int(di);
-    w[c] = udf;
-    w[nc + c] = d2f_int(m1) * dif;
-    w[2 * nc + c] = d2f_int(m2) * dif;
-    w[3 * nc + c] = d2f_int(m3) * dif;
-    w[4 * nc + c] = d2f_int(wp);
+    const ff dd = split_ff(ud), mx1 = split_ff(m1), mx2 = split_ff(m2), mx3 = split_ff(m3);
+    const ff di = ff_recip(dd);
+    const ff mm = ff_add(ff_add(ff_sqr(mx1), ff_sqr(mx2)), ff_sqr(mx3));
+    ff x = ff_mul(mm, di);  // 2 (e_k + p_B)
+    if constexpr (MHD) x = ff_add(x, ff_scale(ss, 0.25f));
+    const ff wp = ff_mul(ff_sub(split_ff(ue), ff_scale(x, 0.5f)), ph.gm1f);
+    float pf;
+    if (!ff_gt(wp, ph.pfloorf)) {
+      u[4 * nc + c] = (ph.pfloor / ph.gm1) + 0.5 * (f2d_int(x.hi) + f2d_int(x.lo));
+      pf = d2f_int(ph.pfloor);
+    } else {
+      pf = ff_f(wp);
+    }
+    const float dif = ff_f(di);
+    const float vx = mx1.hi * dif, vy = mx2.hi * dif, vz = mx3.hi * dif;
+    w[c] = dd.hi;
+    w[nc + c] = vx;
+    w[2 * nc + c] = vy;
+    w[3 * nc + c] = vz;
+    w[4 * nc + c] = pf;
+    if constexpr (MHD) {
+      // cell-centred EMF of field/calculate_corner_e.cpp:135-200 for the corner kernel
+      const float* bcc = p.bcc + (int64_t)b * 3 * nc;
+      const float bx = bcc[c], by = bcc[nc + c], bz = bcc[2 * nc + c];
+      float* ce = p.cce + (int64_t)b * 3 * nc;
+      ce[c] = vz * by - vy * bz;
+      ce[nc + c] = vx * bz - vz * bx;
+      ce[2 * nc + c] = vy * bx - vx * by;
+    }
     return;
   } else {
     const int64_t nc = g.ncell;

@@ -232,3 +232,52 @@ def orszag_tang(nx, domain=((-0.5, 0.5), (-0.5, 0.5), (-0.5, 0.5)), gamma=5.0 / 
     u[4] = (p0 / gm1 + 0.5 * (bc1 ** 2 + bc2 ** 2 + bc3 ** 2)
             + 0.5 * (u[1] ** 2 + u[2] ** 2 + u[3] ** 2) / u[0])
     return u, b1, b2, b3
+
+
+def turbulent_box(nx, seed=20261203, mach=5.0, beta=1.0, gamma=1.0001, kmin=1, kmax=4,
+                  expo=-4.0, jeans_number=2.0, domain=((0.0, 1.0),) * 3):
+    """Magnetised self-gravitating turbulent box (no reference problem generator: the
+    reference's turbulence driver needs FFTW). rho = 1, p = 1/gamma (c_s = 1), uniform
+    B along z with plasma beta = 2 p / B^2, and a seeded Gaussian random solenoidal
+    velocity: white noise filtered to a 3-D power spectrum |v_k|^2 ~ k^expo on the
+    integer shells kmin <= |k| <= kmax, projected divergence-free, mean removed and
+    scaled to rms Mach number `mach`. Returns (u, b1, b2, b3, four_pi_G, sha256 of the
+    velocity field), with G set for the Jeans number n_J = L / lambda_J,
+    lambda_J = c_s sqrt(pi / (G rho)):  G = pi n_J^2 c_s^2 / (rho L^2)."""
+    import hashlib
+    n1, n2, n3 = nx
+    rng = np.random.default_rng(seed)
+    k1 = np.fft.fftfreq(n1, 1.0 / n1)
+    k2 = np.fft.fftfreq(n2, 1.0 / n2)
+    k3 = np.fft.fftfreq(n3, 1.0 / n3)
+    K3, K2, K1 = np.meshgrid(k3, k2, k1, indexing="ij")
+    kk = np.sqrt(K1 ** 2 + K2 ** 2 + K3 ** 2)
+    shell = (kk >= kmin - 1e-9) & (kk <= kmax + 1e-9)
+    amp = np.zeros_like(kk)
+    amp[shell] = kk[shell] ** (0.5 * expo)
+    vk = []
+    for _ in range(3):
+        noise = rng.standard_normal((n3, n2, n1))
+        vk.append(np.fft.fftn(noise) * amp)
+    ksq = np.where(kk > 0, kk ** 2, 1.0)
+    div = (K1 * vk[0] + K2 * vk[1] + K3 * vk[2]) / ksq
+    vk = [vk[0] - K1 * div, vk[1] - K2 * div, vk[2] - K3 * div]
+    v = [np.real(np.fft.ifftn(a)) for a in vk]
+    v = [a - a.mean() for a in v]
+    rms = math.sqrt(float(np.mean(v[0] ** 2 + v[1] ** 2 + v[2] ** 2)))
+    cs = 1.0
+    v = [a * (mach * cs / rms) for a in v]
+    rho, p = 1.0, cs * cs / gamma
+    b0 = math.sqrt(2.0 * p / beta)
+    u = np.zeros((5, n3, n2, n1))
+    u[0] = rho
+    u[1], u[2], u[3] = rho * v[0], rho * v[1], rho * v[2]
+    ke = 0.5 * rho * (v[0] ** 2 + v[1] ** 2 + v[2] ** 2)
+    u[4] = p / (gamma - 1.0) + ke + 0.5 * b0 * b0
+    b1 = np.zeros((n3, n2, n1 + 1))
+    b2 = np.zeros((n3, n2 + 1, n1))
+    b3 = np.full((n3 + 1, n2, n1), b0)
+    L = domain[0][1] - domain[0][0]
+    G = math.pi * jeans_number ** 2 * cs * cs / (rho * L * L)
+    h = hashlib.sha256(np.ascontiguousarray(np.stack(v)).tobytes()).hexdigest()
+    return u, b1, b2, b3, 4.0 * math.pi * G, h

@@ -195,6 +195,72 @@ def run_mg(athg, torch, vcycles=5):
     return out
 
 
+def run_c5(args):
+    """Magnetised self-gravitating turbulent box (PLM + HLLD + VL2, gamma = 1.0001, beta = 1,
+    rms Mach 5, Jeans number 2) with a multigrid solve after every stage; prints its own
+    JSON line. Mixed path: K timed cycles; FP64 path: a shorter run for the L1 deviation."""
+    import torch
+    import athg
+    import pgens
+    n = args.c5_nx
+    nx = (n, n, n)
+    mb = (64, 64, 64) if n >= 64 else nx
+    u, b1, b2, b3, fpg, digest = pgens.turbulent_box(nx)
+    res = {}
+    states = {}
+    for prec, steps in (("mixed", args.steps), ("fp64", args.c5_fp64_steps)):
+        sim = athg.Sim(nx, mb, mhd=True, solver="hlld", precision=prec, cfl=0.3, tlim=1e30,
+                       gamma=1.0001)
+        mg = athg.Multigrid(n, domain=((0.0, 1.0),) * 3, bc="periodic", mode="FMG",
+                            threshold=-1.0, niteration=1, precision=prec)
+        sim.attach_gravity(mg, fpg)
+        sim.load_interior(u, b1, b2, b3)
+        sim.initialize()
+        sim.cycles(args.warmup)
+        sim.synchronize()
+        el = timed_cycles(sim, torch, steps)
+        res[prec] = {"el": el, "steps": steps, "zcps": n ** 3 * steps / el,
+                     "divb": sim.max_div_b()}
+        # the deviation is taken after the same number of cycles in both paths
+        if prec == "mixed":
+            sim.close()
+            sim = athg.Sim(nx, mb, mhd=True, solver="hlld", precision=prec, cfl=0.3,
+                           tlim=1e30, gamma=1.0001)
+            sim.attach_gravity(mg, fpg)
+            sim.load_interior(u, b1, b2, b3)
+            sim.initialize()
+            sim.cycles(args.c5_fp64_steps)
+        states[prec] = sim.interior()["u"][0]
+        ext = torch.cuda.ExternalStream(mg.stream())
+        sim.attach_gravity(None, 0.0)
+        s0, e0 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(ext):
+            mg.vcycles(2)
+            s0.record(ext)
+            mg.vcycles(5)
+            e0.record(ext)
+        e0.synchronize()
+        res[prec]["vcycle_ms"] = s0.elapsed_time(e0) / 5
+        sim.close()
+        mg.close()
+    l1 = float(np.mean(np.abs(states["mixed"] - states["fp64"])) / np.mean(np.abs(states["fp64"])))
+    m = res["mixed"]
+    line = {"metric": METRIC, "value": m["zcps"], "unit": METRIC, "n_gpus": 1,
+            "steps": m["steps"], "warmup": args.warmup, "ms_per_step": 1e3 * m["el"] / m["steps"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
+            "data": "synthetic (seeded solenoidal k^-4 velocity, sha256 %s)" % digest[:16],
+            "config": {"workload": "sg_turbulence_%d^3_mhd_plm_hlld_vl2_mg_each_stage" % n,
+                       "gamma": 1.0001, "mach": 5.0, "beta": 1.0, "jeans_number": 2.0,
+                       "four_pi_G": fpg, "mg": "FMG + 1 V(1,1) per stage"},
+            "fp64": {"value": res["fp64"]["zcps"], "steps": res["fp64"]["steps"],
+                     "ms_per_step": 1e3 * res["fp64"]["el"] / res["fp64"]["steps"]},
+            "mixed_over_fp64": m["zcps"] / res["fp64"]["zcps"],
+            "vcycle_ms": {"mixed": m["vcycle_ms"], "fp64": res["fp64"]["vcycle_ms"]},
+            "l1_rho_mixed_vs_fp64": {"cycles": args.c5_fp64_steps, "rel": l1},
+            "div_b_max": {"mixed": m["divb"], "fp64": res["fp64"]["divb"]}}
+    print(json.dumps(line), flush=True)
+
+
 def make_sim(athg, precision):
     return athg.Sim(NX, MB, mhd=True, solver="hlld", precision=precision, cfl=CFL, tlim=1e30,
                     domain=((-0.5, 0.5),) * 3)
@@ -262,12 +328,18 @@ def main():
     ap.add_argument("--nx", type=int, default=256, help="cells per side (profiling: 128)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-mg", action="store_true")
+    ap.add_argument("--c5", action="store_true",
+                    help="self-gravitating turbulent box instead of the headline workload")
+    ap.add_argument("--c5-nx", type=int, default=512)
+    ap.add_argument("--c5-fp64-steps", type=int, default=10)
     args = ap.parse_args()
     global NX, WORKLOAD
     NX = (args.nx,) * 3
     WORKLOAD = "orszag_tang_%d^3_mhd_plm_hlld_vl2" % args.nx
     if args.impl == "reference":
         return run_reference(args)
+    if args.c5:
+        return run_c5(args)
 
     import torch
     import athg

@@ -50,7 +50,9 @@ typedef struct {
   int nx1, nx2, nx3;  /* MeshBlock interior size (<meshblock> nx1..nx3); same for all blocks */
   int nghost;         /* NGHOST (2 for PLM, >= 3 for PPM) */
   int magnetic;       /* MAGNETIC_FIELDS_ENABLED */
-  int rsolver;        /* ATHG_HLLE / ATHG_HLLC (hydro) / ATHG_HLLD (MHD) */
+  int rsolver;        /* ATHG_HLLE; ATHG_HLLC / ATHG_LHLLC (hydro); ATHG_HLLD / ATHG_LHLLD (MHD).
+                         The L- solvers are the fork's low-dissipation variants with the
+                         velocity-difference shock detector */
   int xorder;         /* <time> xorder: 1 donor cell, 2 PLM, 3 PPM */
   int integrator;     /* ATHG_VL2 / ATHG_RK1 / ATHG_RK2 / ATHG_RK3 */
   int precision;      /* ATHG_FP64 or ATHG_MIXED */

@@ -61,7 +61,7 @@
 static inline double fmin_ref(double a, double b) { return (b < a) ? b : a; }
 static inline double fmax_ref(double a, double b) { return (a < b) ? b : a; }
 
-enum { ORC_HLLE = 0, ORC_HLLC = 1, ORC_HLLD = 2 };
+enum { ORC_HLLE = 0, ORC_HLLC = 1, ORC_HLLD = 2, ORC_LHLLC = 3, ORC_LHLLD = 4 };
 enum { ORC_VL2 = 0, ORC_RK1 = 1, ORC_RK2 = 2, ORC_RK3 = 3 };
 
 typedef struct {
@@ -631,6 +631,238 @@ static void rs_hlld(const double *wli, const double *wri, double bxi, double gam
   }
 }
 
+/* LHLLC, the fork's low-dissipation HLLC (hydro/rsolvers/hydro/lhllc.cpp:26-180): PVRS
+ * wave speeds, a shock detector th = min(1, (cmax - min(dvn,0)) / (cmax - min(dvt,0)))^4
+ * weighting the pressure jump in the contact speed, and a low-Mach factor phi on the
+ * contact pressure */
+static void rs_lhllc(const double *wli, const double *wri, double gamma, double dvn,
+                     double dvt, double *flxi) {
+  double gm1 = gamma - 1.0, igm1 = 1.0 / gm1;
+  double fl[5], fr[5];
+  double cl = sqrt(gamma * wli[IPR] / wli[IDN]);
+  double cr = sqrt(gamma * wri[IPR] / wri[IDN]);
+  double vsql = SQ(wli[IVX]) + SQ(wli[IVY]) + SQ(wli[IVZ]);
+  double vsqr = SQ(wri[IVX]) + SQ(wri[IVY]) + SQ(wri[IVZ]);
+  double el = wli[IPR] * igm1 + 0.5 * wli[IDN] * vsql;
+  double er = wri[IPR] * igm1 + 0.5 * wri[IDN] * vsqr;
+  double rhoa = .5 * (wli[IDN] + wri[IDN]);
+  double ca = .5 * (cl + cr);
+  double pmid = .5 * (wli[IPR] + wri[IPR] + (wli[IVX] - wri[IVX]) * rhoa * ca);
+  double umid = .5 * (wli[IVX] + wri[IVX] + (wli[IPR] - wri[IPR]) / (rhoa * ca));
+  double rhol = wli[IDN] + (wli[IVX] - umid) * rhoa / ca;
+  double rhor = wri[IDN] + (umid - wri[IVX]) * rhoa / ca;
+  (void)rhol; (void)rhor;
+  double ql = (pmid <= wli[IPR]) ? 1.0
+              : sqrt(1.0 + (gamma + 1) / (2 * gamma) * (pmid / wli[IPR] - 1.0));
+  double qr = (pmid <= wri[IPR]) ? 1.0
+              : sqrt(1.0 + (gamma + 1) / (2 * gamma) * (pmid / wri[IPR] - 1.0));
+  double al = wli[IVX] - cl * ql;
+  double ar = wri[IVX] + cr * qr;
+  double bp = ar > 0.0 ? ar : (TINYN);
+  double bm = al < 0.0 ? al : -(TINYN);
+  double vxl = al - wli[IVX], vxr = ar - wri[IVX];
+  double ml = wli[IDN] * vxl, mr = wri[IDN] * vxr;
+  double cmax = fmax_ref(cl, cr);
+  double th1 = fmin_ref(1.0, (cmax - fmin_ref(dvn, 0.0)) / (cmax - fmin_ref(dvt, 0.0)));
+  double th = th1 * th1 * th1 * th1;
+  double am = (mr * wri[IVX] - ml * wli[IVX] - th * (wri[IPR] - wli[IPR])) / (mr - ml);
+  double chi = fmin_ref(1.0, sqrt(fmax_ref(vsql, vsqr)) / cmax);
+  double phi = chi * (2.0 - chi);
+  double cp = (mr * wli[IPR] - ml * wri[IPR] + phi * mr * ml * (wri[IVX] - wli[IVX])) / (mr - ml);
+  cp = cp > 0.0 ? cp : 0.0;
+  double uxl = wli[IVX] - bm, uxr = wri[IVX] - bp;
+  fl[IDN] = wli[IDN] * uxl; fr[IDN] = wri[IDN] * uxr;
+  fl[IVX] = wli[IDN] * wli[IVX] * uxl + wli[IPR]; fr[IVX] = wri[IDN] * wri[IVX] * uxr + wri[IPR];
+  fl[IVY] = wli[IDN] * wli[IVY] * uxl; fr[IVY] = wri[IDN] * wri[IVY] * uxr;
+  fl[IVZ] = wli[IDN] * wli[IVZ] * uxl; fr[IVZ] = wri[IDN] * wri[IVZ] * uxr;
+  fl[IEN] = el * uxl + wli[IPR] * wli[IVX]; fr[IEN] = er * uxr + wri[IPR] * wri[IVX];
+  double sl, sr, sm;
+  if (am >= 0.0) { sl = am / (am - bm); sr = 0.0; sm = -bm / (am - bm); }
+  else { sl = 0.0; sr = -am / (bp - am); sm = bp / (bp - am); }
+  flxi[IDN] = sl * fl[IDN] + sr * fr[IDN];
+  flxi[IVX] = sl * fl[IVX] + sr * fr[IVX] + sm * cp;
+  flxi[IVY] = sl * fl[IVY] + sr * fr[IVY];
+  flxi[IVZ] = sl * fl[IVZ] + sr * fr[IVZ];
+  flxi[IEN] = sl * fl[IEN] + sr * fr[IEN] + sm * cp * am;
+}
+
+/* LHLLD, the fork's low-dissipation HLLD (hydro/rsolvers/mhd/lhlld.cpp:36-388): HLLD with
+ * the shock detector on the pressure jump of S_M and the low-Mach factor phi in the
+ * star-state total pressure */
+static void rs_lhlld(const double *wli, const double *wri, double bxi, double gamma,
+                     double dvn, double dvt, double *flxi) {
+  double igm1 = 1.0 / (gamma - 1.0);
+  cons1d ul, ur, ulst, uldst, urdst, urst, fl, fr;
+  double spd[5];
+  double bxsq = bxi * bxi;
+  double pbl = 0.5 * (bxsq + (SQ(wli[IBY]) + SQ(wli[IBZ])));
+  double pbr = 0.5 * (bxsq + (SQ(wri[IBY]) + SQ(wri[IBZ])));
+  double kel = 0.5 * wli[IDN] * (SQ(wli[IVX]) + (SQ(wli[IVY]) + SQ(wli[IVZ])));
+  double ker = 0.5 * wri[IDN] * (SQ(wri[IVX]) + (SQ(wri[IVY]) + SQ(wri[IVZ])));
+  ul.d = wli[IDN]; ul.mx = wli[IVX] * ul.d; ul.my = wli[IVY] * ul.d; ul.mz = wli[IVZ] * ul.d;
+  ul.e = wli[IPR] * igm1 + kel + pbl; ul.by = wli[IBY]; ul.bz = wli[IBZ];
+  ur.d = wri[IDN]; ur.mx = wri[IVX] * ur.d; ur.my = wri[IVY] * ur.d; ur.mz = wri[IVZ] * ur.d;
+  ur.e = wri[IPR] * igm1 + ker + pbr; ur.by = wri[IBY]; ur.bz = wri[IBZ];
+  double cfl = fast_speed(wli, bxi, gamma);
+  double cfr = fast_speed(wri, bxi, gamma);
+  spd[0] = fmin_ref(wli[IVX] - cfl, wri[IVX] - cfr);
+  spd[4] = fmax_ref(wli[IVX] + cfl, wri[IVX] + cfr);
+  double cfmax = fmax_ref(cfl, cfr);
+  double ptl = wli[IPR] + pbl, ptr = wri[IPR] + pbr;
+  fl.d = ul.mx;
+  fl.mx = ul.mx * wli[IVX] + ptl - bxsq;
+  fl.my = ul.my * wli[IVX] - bxi * ul.by;
+  fl.mz = ul.mz * wli[IVX] - bxi * ul.bz;
+  fl.e = wli[IVX] * (ul.e + ptl - bxsq) - bxi * (wli[IVY] * ul.by + wli[IVZ] * ul.bz);
+  fl.by = ul.by * wli[IVX] - bxi * wli[IVY];
+  fl.bz = ul.bz * wli[IVX] - bxi * wli[IVZ];
+  fr.d = ur.mx;
+  fr.mx = ur.mx * wri[IVX] + ptr - bxsq;
+  fr.my = ur.my * wri[IVX] - bxi * ur.by;
+  fr.mz = ur.mz * wri[IVX] - bxi * ur.bz;
+  fr.e = wri[IVX] * (ur.e + ptr - bxsq) - bxi * (wri[IVY] * ur.by + wri[IVZ] * ur.bz);
+  fr.by = ur.by * wri[IVX] - bxi * wri[IVY];
+  fr.bz = ur.bz * wri[IVX] - bxi * wri[IVZ];
+  double sdl = spd[0] - wli[IVX], sdr = spd[4] - wri[IVX];
+  double sdld = sdl * ul.d, sdrd = sdr * ur.d;
+  double th1 = fmin_ref(1.0, (cfmax - fmin_ref(dvn, 0.0)) / (cfmax - fmin_ref(dvt, 0.0)));
+  double th = th1 * th1 * th1 * th1;
+  spd[2] = (sdr * ur.mx - sdl * ul.mx + th * (ptl - ptr)) / (sdrd - sdld);
+  double sdml = spd[0] - spd[2], sdmr = spd[4] - spd[2];
+  double sdml_inv = 1.0 / sdml, sdmr_inv = 1.0 / sdmr;
+  ulst.d = sdld * sdml_inv;
+  urst.d = sdrd * sdmr_inv;
+  double ulst_d_inv = 1.0 / ulst.d, urst_d_inv = 1.0 / urst.d;
+  double sqrtdl = sqrt(ulst.d), sqrtdr = sqrt(urst.d);
+  spd[1] = spd[2] - fabs(bxi) / sqrtdl;
+  spd[3] = spd[2] + fabs(bxi) / sqrtdr;
+  double clsq = ((pbl + kel) + sqrt(SQ(pbl + kel) - 2.0 * kel * bxsq)) / ul.d;
+  double crsq = ((pbr + ker) + sqrt(SQ(pbr + ker) - 2.0 * ker * bxsq)) / ur.d;
+  double chi = fmin_ref(1.0, sqrt(fmax_ref(clsq, crsq)) / cfmax);
+  double phi = chi * (2.0 - chi);
+  double ptst = (sdrd * ptl - sdld * ptr + phi * sdrd * sdld * (wri[IVX] - wli[IVX])) /
+                (sdrd - sdld);
+  ulst.mx = ulst.d * spd[2];
+  if (fabs(sdld * sdml - bxsq) < (SMALLN) * ptst) {
+    ulst.my = ulst.d * wli[IVY]; ulst.mz = ulst.d * wli[IVZ];
+    ulst.by = ul.by; ulst.bz = ul.bz;
+  } else {
+    double tmp = bxi * (sdl - sdml) / (sdld * sdml - bxsq);
+    ulst.my = ulst.d * (wli[IVY] - ul.by * tmp);
+    ulst.mz = ulst.d * (wli[IVZ] - ul.bz * tmp);
+    tmp = (sdld * sdl - bxsq) / (sdld * sdml - bxsq);
+    ulst.by = ul.by * tmp; ulst.bz = ul.bz * tmp;
+  }
+  double vbstl = (ulst.mx * bxi + (ulst.my * ulst.by + ulst.mz * ulst.bz)) * ulst_d_inv;
+  ulst.e = (sdl * ul.e - ptl * wli[IVX] + ptst * spd[2] +
+            bxi * (wli[IVX] * bxi + (wli[IVY] * ul.by + wli[IVZ] * ul.bz) - vbstl)) * sdml_inv;
+  urst.mx = urst.d * spd[2];
+  if (fabs(sdrd * sdmr - bxsq) < (SMALLN) * ptst) {
+    urst.my = urst.d * wri[IVY]; urst.mz = urst.d * wri[IVZ];
+    urst.by = ur.by; urst.bz = ur.bz;
+  } else {
+    double tmp = bxi * (sdr - sdmr) / (sdrd * sdmr - bxsq);
+    urst.my = urst.d * (wri[IVY] - ur.by * tmp);
+    urst.mz = urst.d * (wri[IVZ] - ur.bz * tmp);
+    tmp = (sdrd * sdr - bxsq) / (sdrd * sdmr - bxsq);
+    urst.by = ur.by * tmp; urst.bz = ur.bz * tmp;
+  }
+  double vbstr = (urst.mx * bxi + (urst.my * urst.by + urst.mz * urst.bz)) * urst_d_inv;
+  urst.e = (sdr * ur.e - ptr * wri[IVX] + ptst * spd[2] +
+            bxi * (wri[IVX] * bxi + (wri[IVY] * ur.by + wri[IVZ] * ur.bz) - vbstr)) * sdmr_inv;
+  if (0.5 * bxsq < (SMALLN) * ptst) {
+    uldst = ulst; urdst = urst;
+  } else {
+    double invsumd = 1.0 / (sqrtdl + sqrtdr);
+    double bxsig = (bxi > 0.0 ? 1.0 : -1.0);
+    uldst.d = ulst.d; urdst.d = urst.d;
+    uldst.mx = ulst.mx; urdst.mx = urst.mx;
+    double tmp = invsumd * (sqrtdl * (ulst.my * ulst_d_inv) + sqrtdr * (urst.my * urst_d_inv) +
+                            bxsig * (urst.by - ulst.by));
+    uldst.my = uldst.d * tmp; urdst.my = urdst.d * tmp;
+    tmp = invsumd * (sqrtdl * (ulst.mz * ulst_d_inv) + sqrtdr * (urst.mz * urst_d_inv) +
+                     bxsig * (urst.bz - ulst.bz));
+    uldst.mz = uldst.d * tmp; urdst.mz = urdst.d * tmp;
+    tmp = invsumd * (sqrtdl * urst.by + sqrtdr * ulst.by +
+                     bxsig * sqrtdl * sqrtdr * ((urst.my * urst_d_inv) - (ulst.my * ulst_d_inv)));
+    uldst.by = urdst.by = tmp;
+    tmp = invsumd * (sqrtdl * urst.bz + sqrtdr * ulst.bz +
+                     bxsig * sqrtdl * sqrtdr * ((urst.mz * urst_d_inv) - (ulst.mz * ulst_d_inv)));
+    uldst.bz = urdst.bz = tmp;
+    tmp = spd[2] * bxi + (uldst.my * uldst.by + uldst.mz * uldst.bz) / uldst.d;
+    uldst.e = ulst.e - sqrtdl * bxsig * (vbstl - tmp);
+    urdst.e = urst.e + sqrtdr * bxsig * (vbstr - tmp);
+  }
+#define DIFFW(dst, a, b, sp) \
+  dst.d = sp * (a.d - b.d); dst.mx = sp * (a.mx - b.mx); dst.my = sp * (a.my - b.my); \
+  dst.mz = sp * (a.mz - b.mz); dst.e = sp * (a.e - b.e); dst.by = sp * (a.by - b.by); \
+  dst.bz = sp * (a.bz - b.bz);
+  cons1d t1, t0, t3, t4;
+  DIFFW(t1, uldst, ulst, spd[1]);
+  DIFFW(t0, ulst, ul, spd[0]);
+  DIFFW(t3, urdst, urst, spd[3]);
+  DIFFW(t4, urst, ur, spd[4]);
+#undef DIFFW
+  if (spd[0] >= 0.0) {
+    flxi[IDN] = fl.d; flxi[IVX] = fl.mx; flxi[IVY] = fl.my; flxi[IVZ] = fl.mz;
+    flxi[IEN] = fl.e; flxi[IBY] = fl.by; flxi[IBZ] = fl.bz;
+  } else if (spd[4] <= 0.0) {
+    flxi[IDN] = fr.d; flxi[IVX] = fr.mx; flxi[IVY] = fr.my; flxi[IVZ] = fr.mz;
+    flxi[IEN] = fr.e; flxi[IBY] = fr.by; flxi[IBZ] = fr.bz;
+  } else if (spd[1] >= 0.0) {
+    flxi[IDN] = fl.d + t0.d; flxi[IVX] = fl.mx + t0.mx; flxi[IVY] = fl.my + t0.my;
+    flxi[IVZ] = fl.mz + t0.mz; flxi[IEN] = fl.e + t0.e; flxi[IBY] = fl.by + t0.by;
+    flxi[IBZ] = fl.bz + t0.bz;
+  } else if (spd[2] >= 0.0) {
+    flxi[IDN] = fl.d + t0.d + t1.d; flxi[IVX] = fl.mx + t0.mx + t1.mx;
+    flxi[IVY] = fl.my + t0.my + t1.my; flxi[IVZ] = fl.mz + t0.mz + t1.mz;
+    flxi[IEN] = fl.e + t0.e + t1.e; flxi[IBY] = fl.by + t0.by + t1.by;
+    flxi[IBZ] = fl.bz + t0.bz + t1.bz;
+  } else if (spd[3] > 0.0) {
+    flxi[IDN] = fr.d + t4.d + t3.d; flxi[IVX] = fr.mx + t4.mx + t3.mx;
+    flxi[IVY] = fr.my + t4.my + t3.my; flxi[IVZ] = fr.mz + t4.mz + t3.mz;
+    flxi[IEN] = fr.e + t4.e + t3.e; flxi[IBY] = fr.by + t4.by + t3.by;
+    flxi[IBZ] = fr.bz + t4.bz + t3.bz;
+  } else {
+    flxi[IDN] = fr.d + t4.d; flxi[IVX] = fr.mx + t4.mx; flxi[IVY] = fr.my + t4.my;
+    flxi[IVZ] = fr.mz + t4.mz; flxi[IEN] = fr.e + t4.e; flxi[IBY] = fr.by + t4.by;
+    flxi[IBZ] = fr.bz + t4.bz;
+  }
+}
+
+/* Hydro::CalculateVelocityDifferences (hydro/calculate_velocity_differences.cpp:20-52,
+ * 3-D): normal velocity jump across the face and the smallest transverse velocity
+ * difference around it (the LHLLC/LHLLD shock detector) */
+static void velocity_differences(const orc_sim *s, int dir, int k, int j, int i, double *dvn,
+                                 double *dvt) {
+  const size_t nc = s->ncell;
+  const double *vx = s->w + (size_t)IVX * nc, *vy = s->w + (size_t)IVY * nc,
+               *vz = s->w + (size_t)IVZ * nc;
+#define W(a, kk, jj, ii) (a)[C3(s, kk, jj, ii)]
+  double dvl, dvr, dwl, dwr;
+  if (dir == 0) {
+    *dvn = W(vx, k, j, i) - W(vx, k, j, i - 1);
+    dvl = fmin_ref(W(vy, k, j + 1, i - 1) - W(vy, k, j, i - 1), W(vy, k, j, i - 1) - W(vy, k, j - 1, i - 1));
+    dvr = fmin_ref(W(vy, k, j + 1, i) - W(vy, k, j, i), W(vy, k, j, i) - W(vy, k, j - 1, i));
+    dwl = fmin_ref(W(vz, k + 1, j, i - 1) - W(vz, k, j, i - 1), W(vz, k, j, i - 1) - W(vz, k - 1, j, i - 1));
+    dwr = fmin_ref(W(vz, k + 1, j, i) - W(vz, k, j, i), W(vz, k, j, i) - W(vz, k - 1, j, i));
+  } else if (dir == 1) {
+    *dvn = W(vy, k, j, i) - W(vy, k, j - 1, i);
+    dvl = fmin_ref(W(vz, k + 1, j - 1, i) - W(vz, k, j - 1, i), W(vz, k, j - 1, i) - W(vz, k - 1, j - 1, i));
+    dvr = fmin_ref(W(vz, k + 1, j, i) - W(vz, k, j, i), W(vz, k, j, i) - W(vz, k - 1, j, i));
+    dwl = fmin_ref(W(vx, k, j - 1, i + 1) - W(vx, k, j - 1, i), W(vx, k, j - 1, i) - W(vx, k, j - 1, i - 1));
+    dwr = fmin_ref(W(vx, k, j, i + 1) - W(vx, k, j, i), W(vx, k, j, i) - W(vx, k, j, i - 1));
+  } else {
+    *dvn = W(vz, k, j, i) - W(vz, k - 1, j, i);
+    dvl = fmin_ref(W(vx, k - 1, j, i + 1) - W(vx, k - 1, j, i), W(vx, k - 1, j, i) - W(vx, k - 1, j, i - 1));
+    dvr = fmin_ref(W(vx, k, j, i + 1) - W(vx, k, j, i), W(vx, k, j, i) - W(vx, k, j, i - 1));
+    dwl = fmin_ref(W(vy, k - 1, j + 1, i) - W(vy, k - 1, j, i), W(vy, k - 1, j, i) - W(vy, k - 1, j - 1, i));
+    dwr = fmin_ref(W(vy, k, j + 1, i) - W(vy, k, j, i), W(vy, k, j, i) - W(vy, k, j - 1, i));
+  }
+#undef W
+  *dvt = fmin_ref(fmin_ref(dvl, dvr), fmin_ref(dwl, dwr));
+}
+
 /* ----------------------------------------------------------- reconstruction ---- */
 /* value of wave variable n of cell (k,j,i) for a sweep along dir; MHD transverse
  * components come from bcc in the cyclic order of reconstruct/plm.cpp:44-55,156-170,268-282 */
@@ -802,14 +1034,28 @@ static void sweep(orc_sim *s, int dir, int order) {
           wli[IBY] = wl[IBY]; wli[IBZ] = wl[IBZ];
           wri[IBY] = wr[IBY]; wri[IBZ] = wr[IBZ];
           double bx = bn[fi];
-          if (s->p.rsolver == ORC_HLLD) rs_hlld(wli, wri, bx, s->p.gamma, fx);
-          else rs_hlle_mhd(wli, wri, bx, s->p.gamma, fx);
+          if (s->p.rsolver == ORC_HLLD) {
+            rs_hlld(wli, wri, bx, s->p.gamma, fx);
+          } else if (s->p.rsolver == ORC_LHLLD) {
+            double dvn, dvt;
+            velocity_differences(s, dir, k, j, i, &dvn, &dvt);
+            rs_lhlld(wli, wri, bx, s->p.gamma, dvn, dvt, fx);
+          } else {
+            rs_hlle_mhd(wli, wri, bx, s->p.gamma, fx);
+          }
           ey[fi] = -fx[IBY];
           ez[fi] = fx[IBZ];
           wct[fi] = ct_weight(fx[IDN], wli[IDN], wri[IDN], dxw, s->dt);
         } else {
-          if (s->p.rsolver == ORC_HLLC) rs_hllc(wli, wri, s->p.gamma, fx);
-          else rs_hlle_hydro(wli, wri, s->p.gamma, fx);
+          if (s->p.rsolver == ORC_HLLC) {
+            rs_hllc(wli, wri, s->p.gamma, fx);
+          } else if (s->p.rsolver == ORC_LHLLC) {
+            double dvn, dvt;
+            velocity_differences(s, dir, k, j, i, &dvn, &dvt);
+            rs_lhllc(wli, wri, s->p.gamma, dvn, dvt, fx);
+          } else {
+            rs_hlle_hydro(wli, wri, s->p.gamma, fx);
+          }
         }
         flx[IDN * fn + fi] = fx[IDN];
         flx[ivx * fn + fi] = fx[IVX];

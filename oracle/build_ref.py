@@ -51,9 +51,10 @@ CONFIGS = {
     "state_hydro_hlle": ("harness:load_state.cpp", "hlle", False, 2, 0, False, None),
     "state_mhd_hlle": ("harness:load_state.cpp", "hlle", True, 2, 0, False, None),
     "state_hydro_hllc_ng4": ("harness:load_state.cpp", "hllc", False, 4, 0, False, None),
+    "state_hydro_lhllc": ("harness:load_state.cpp", "lhllc", False, 2, 0, False, None),
+    "state_mhd_lhlld": ("harness:load_state.cpp", "lhlld", True, 2, 0, False, None),
     # multigrid self-gravity
     "poisson_mg": ("poisson.cpp", "hllc", False, 2, 2, False, None),
-    "sphere_mg": ("harness:uniform_sphere.cpp", "hllc", False, 2, 2, False, None),
     "jeans_mg": ("jeans.cpp", "hllc", False, 2, 2, False, None),
     "sg_state_mhd_hlld": ("harness:load_state.cpp", "hlld", True, 2, 2, False, None),
     "sg_state_hydro": ("harness:load_state.cpp", "hllc", False, 2, 2, False, None),

@@ -40,6 +40,10 @@ CASES = {
     "hydro_hllc_ppm_rk3": ("state_hydro_hllc_ng4", False, "hllc", (16, 8, 8), (16, 8, 8), "rk3", 3, 3, 31, 0.8),
     "mhd_hlld_ppm_rk3": ("state_mhd_hlld_ng4", True, "hlld", (16, 8, 8), (16, 8, 8), "rk3", 3, 3, 32, 0.8),
     "mhd_hlld_ppm_vl2": ("state_mhd_hlld_ng4", True, "hlld", (16, 8, 8), (16, 8, 8), "vl2", 3, 3, 33, 0.4),
+    "hydro_lhllc_plm_vl2": ("state_hydro_lhllc", False, "lhllc", (16, 8, 8), (16, 8, 8), "vl2", 2, 3, 41, 0.4),
+    "hydro_lhllc_plm_rk3": ("state_hydro_lhllc", False, "lhllc", (16, 8, 8), (16, 8, 8), "rk3", 2, 3, 42, 0.8),
+    "mhd_lhlld_plm_vl2": ("state_mhd_lhlld", True, "lhlld", (16, 8, 8), (16, 8, 8), "vl2", 2, 3, 43, 0.4),
+    "mhd_lhlld_plm_rk2": ("state_mhd_lhlld", True, "lhlld", (16, 8, 8), (16, 8, 8), "rk2", 2, 3, 44, 0.8),
 }
 NGHOST = {"state_hydro_hllc_ng4": 4, "state_mhd_hlld_ng4": 4}
 

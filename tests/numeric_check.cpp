@@ -86,6 +86,47 @@ int main(int argc, char** argv) {
     double r2 = (double)(std::fabs((long double)hi + lo - ex2) / mag);
     if (r2 > worst2) worst2 = r2;
   }
+  // double-float split and the primitive-recovery pressure p = (g-1)(E - m^2/(2d) - B^2/2)
+  double worst_split = 0.0, worst_p = 0.0;
+  std::uniform_real_distribution<double> ud01(0.0, 1.0);
+  for (long t = 0; t < n / 4; ++t) {
+    double x = std::ldexp(0.5 + ud01(rng), ex(rng) % 60) * ((rng() & 1) ? 1 : -1);
+    ff sx = split_ff(x);
+    double es = std::fabs((double)((long double)sx.hi + sx.lo - x)) / std::fabs(x);
+    if (es > worst_split) worst_split = es;
+    CHECK(bits_f(sx.hi) == bits_f((float)x), "split hi %a", x);
+    // a cell: density, momenta, face fields (B = average of the two faces), energy with
+    // internal energy down to 1e-6 of the kinetic + magnetic energy
+    double d = std::ldexp(0.5 + ud01(rng), (int)(rng() % 20) - 10);
+    double m[3], f[6];
+    for (int q = 0; q < 3; ++q) m[q] = d * 3.0 * (ud01(rng) - 0.5);
+    for (int q = 0; q < 6; ++q) f[q] = 2.0 * (ud01(rng) - 0.5);
+    long double K = 0.5L * ((long double)m[0] * m[0] + (long double)m[1] * m[1] +
+                            (long double)m[2] * m[2]) / d;
+    long double M = 0.0L;
+    for (int q = 0; q < 3; ++q) {
+      long double bq = 0.5L * ((long double)f[2 * q] + f[2 * q + 1]);
+      M += 0.5L * bq * bq;
+    }
+    double eint = (double)((K + M) * std::pow(10.0L, -6.0L * ud01(rng)));
+    double E = (double)(K + M) + eint;
+    const double gm1 = 2.0 / 3.0;
+    long double pex = (long double)gm1 * ((long double)E - K - M);
+    ff dd = split_ff(d), mm = ff_sqr(split_ff(m[0]));
+    mm = ff_add(mm, ff_sqr(split_ff(m[1])));
+    mm = ff_add(mm, ff_sqr(split_ff(m[2])));
+    ff k2 = ff_mul(mm, ff_recip(dd));
+    ff ss = ff_sqr(ff_add(split_ff(f[0]), split_ff(f[1])));
+    ss = ff_add(ss, ff_sqr(ff_add(split_ff(f[2]), split_ff(f[3]))));
+    ss = ff_add(ss, ff_sqr(ff_add(split_ff(f[4]), split_ff(f[5]))));
+    ff xx = ff_add(k2, ff_scale(ss, 0.25f));
+    ff pp = ff_mul(ff_sub(split_ff(E), ff_scale(xx, 0.5f)), split_ff(gm1));
+    double ep = (double)(std::fabs((long double)pp.hi + pp.lo - pex) / (gm1 * (long double)E));
+    if (ep > worst_p) worst_p = ep;
+  }
+  CHECK(worst_split <= std::ldexp(1.0, -45), "split error %g", worst_split);
+  CHECK(worst_p <= std::ldexp(1.0, -42), "pressure error %g", worst_p);
+  std::printf("split=%.3g pressure(rel. to (g-1)E)=%.3g\n", worst_split, worst_p);
   CHECK(worst3 <= std::ldexp(1.0, -44), "sum3diff error %g", worst3);
   CHECK(worst2 <= std::ldexp(1.0, -45), "sum2diff error %g", worst2);
   std::printf("fails=%d worst3=%.3g worst2=%.3g\n", fails, worst3, worst2);

@@ -14,7 +14,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 ORACLE_DIR = os.path.join(ROOT, "oracle")
 LIB_PATH = os.path.join(ORACLE_DIR, "liboracle.so")
 
-SOLVERS = {"hlle": 0, "hllc": 1, "hlld": 2}
+SOLVERS = {"hlle": 0, "hllc": 1, "hlld": 2, "lhllc": 3, "lhlld": 4}
 INTEGRATORS = {"vl2": 0, "rk1": 1, "rk2": 2, "rk3": 3}
 FLOOR = float(np.sqrt(1024 * np.finfo(np.float32).tiny))  # eos/adiabatic_mhd.cpp:29-30
 

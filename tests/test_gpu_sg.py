@@ -56,3 +56,31 @@ def test_sg_mixed_close_to_reference(name):
         assert err < 5e-6, (k, err)
     err = np.abs(phi - a["phi_out"]).max() / np.abs(a["phi_out"]).max()
     assert err < 2e-7, err
+
+
+def test_turbulent_box_mixed_tracks_fp64():
+    """The self-gravitating turbulent box (rms Mach 5, beta 1, gamma 1.0001, Jeans number 2)
+    at 32^3: the mixed path stays within 1e-5 (L1 of rho) of the FP64 path over 5
+    cycles, with div B at round-off."""
+    import pgens
+    n = 32
+    u, b1, b2, b3, fpg, _ = pgens.turbulent_box((n, n, n))
+    rho = {}
+    for prec in ("fp64", "mixed"):
+        sim = athg.Sim((n, n, n), (16, 16, 16), True, "hlld", precision=prec, cfl=0.3,
+                       tlim=100.0, gamma=1.0001)
+        mg = athg.Multigrid(n, domain=((0.0, 1.0),) * 3, bc="periodic", mode="FMG",
+                            threshold=-1.0, niteration=1, precision=prec)
+        sim.attach_gravity(mg, fpg)
+        sim.load_interior(u, b1, b2, b3)
+        sim.initialize()
+        sim.cycles(5)
+        out = sim.interior()
+        assert np.all(np.isfinite(out["u"]))
+        assert sim.max_div_b() < 1e-12
+        rho[prec] = out["u"][0]
+        sim.attach_gravity(None, 0.0)
+        sim.close()
+        mg.close()
+    l1 = np.mean(np.abs(rho["mixed"] - rho["fp64"])) / np.mean(np.abs(rho["fp64"]))
+    assert l1 < 1e-5, l1
