@@ -2,6 +2,7 @@
 // CUDA-graph cycle. Declarations and reference interfaces: include/athena_gb300.h.
 #include <cmath>
 #include <type_traits>
+#include <utility>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -157,6 +158,13 @@ struct athg_ctx {
   std::vector<double> coords;  // host copies of x?f arrays owned by the context
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t gexec = nullptr;
+  // fused mixed VL2 path: the state alternates between (u, b) and (u1, r) every cycle,
+  // one captured cycle per direction; FP64 ghosts are refreshed only when read
+  bool fused_ok = true;        // cleared for good by the single-step entry points
+  bool ghosts_stale = false;
+  cudaGraph_t graph2 = nullptr;
+  cudaGraphExec_t gexec2 = nullptr;
+  const double* graph_src = nullptr;  // state buffer the first captured cycle reads
   int launches_per_cycle = 0;
   int counting = 0;
   // self-gravity (SELF_GRAVITY_ENABLED == 2): coupled multigrid solver, 4 pi G, the
@@ -215,7 +223,11 @@ void free_pool(athg_ctx* c) {
   c->bf32[0] = c->bf32[1] = c->bf32[2] = nullptr;
   if (c->gexec) cudaGraphExecDestroy(c->gexec);
   if (c->graph) cudaGraphDestroy(c->graph);
+  if (c->gexec2) cudaGraphExecDestroy(c->gexec2);
+  if (c->graph2) cudaGraphDestroy(c->graph2);
   c->gexec = nullptr; c->graph = nullptr;
+  c->gexec2 = nullptr; c->graph2 = nullptr;
+  c->ghosts_stale = false;
   if (c->phi) cudaFree(c->phi);
   if (c->boff) cudaFree(c->boff);
   c->phi = nullptr; c->boff = nullptr;
@@ -366,10 +378,91 @@ int launch_self_gravity(athg_ctx* c, int l) {
   return ATHG_OK;
 }
 
+bool fused(const athg_ctx* c) {
+  return c->fused_ok && c->mixed() && c->cfg.integrator == ATHG_VL2 && !c->grav;
+}
+
+// swap the two state buffers (after a fused cycle the new state is in (u1, r))
+void swap_state(athg_ctx* c) {
+  std::swap(c->u, c->u1);
+  std::swap(c->b1, c->r1);
+  std::swap(c->b2, c->r2);
+  std::swap(c->b3, c->r3);
+}
+
+int launch_update_c2p(athg_ctx* c, int l) {
+  StageW sw = stage_weights(c, l);
+  StateBufs sb;
+  sb.u_in = c->u; sb.u_out = c->u1;
+  sb.b_in[0] = c->b1; sb.b_in[1] = c->b2; sb.b_in[2] = c->b3;
+  sb.b_out[0] = c->r1; sb.b_out[1] = c->r2; sb.b_out[2] = c->r3;
+  Launcher<float>::update_c2p(c->g, ptrs<float>(c), c->cfg.magnetic != 0, sw, phys(c), sb, c->st);
+  c->counting += 1;
+  CKL();
+  return ATHG_OK;
+}
+
+int launch_ghosts_f32(athg_ctx* c) {
+  const Geom& g = c->g;
+  GhostPtrs32 gp;
+  const bool mhd = c->cfg.magnetic != 0;
+  gp.cell[0] = (float*)c->w; gp.ncomp[0] = NHYD;
+  gp.cell[1] = mhd ? (float*)c->bcc : nullptr; gp.ncomp[1] = 3;
+  gp.cell[2] = mhd ? c->cce : nullptr; gp.ncomp[2] = 3;
+  for (int d = 0; d < 3; ++d) gp.face[d] = mhd ? c->bf32[d] : nullptr;
+  gp.nbr = c->nbr;
+  dim3 grid((unsigned)(((g.nc1 + 1) * (g.nc2 + 1) + 255) / 256), (unsigned)(g.nc3 + 1),
+            (unsigned)c->nb);
+  if (mhd) k_ghost_f32<true><<<grid, 256, 0, c->st>>>(g, gp);
+  else k_ghost_f32<false><<<grid, 256, 0, c->st>>>(g, gp);
+  c->counting += 1;
+  CKL();
+  return ATHG_OK;
+}
+
+// FP64 ghost zones of the current state, when a fused cycle left them behind
+int refresh_ghosts(athg_ctx* c) {
+  if (!c->ghosts_stale) return ATHG_OK;
+  int rc = launch_ghosts(c);
+  if (rc) return rc;
+  c->ghosts_stale = false;
+  return ATHG_OK;
+}
+
+void drop_graphs(athg_ctx* c) {
+  if (c->gexec) cudaGraphExecDestroy(c->gexec);
+  if (c->graph) cudaGraphDestroy(c->graph);
+  if (c->gexec2) cudaGraphExecDestroy(c->gexec2);
+  if (c->graph2) cudaGraphDestroy(c->graph2);
+  c->gexec = nullptr; c->graph = nullptr; c->gexec2 = nullptr; c->graph2 = nullptr;
+  c->graph_src = nullptr;
+}
+
+// the single-step entry points work on the unfused path from here on
+int leave_fused(athg_ctx* c) {
+  int rc = refresh_ghosts(c);
+  if (rc) return rc;
+  if (c->fused_ok) {
+    c->fused_ok = false;
+    drop_graphs(c);
+  }
+  return ATHG_OK;
+}
+
 int do_stage(athg_ctx* c, int stage) {
   const int l = stage - 1;
   int order = (c->cfg.integrator == ATHG_VL2 && l == 0) ? 1 : c->cfg.xorder;
   int rc;
+  if (fused(c)) {
+    if ((rc = launch_fluxes(c, order))) return rc;
+    if ((rc = launch_corner(c))) return rc;
+    if ((rc = launch_update_c2p(c, l))) return rc;
+    if ((rc = launch_ghosts_f32(c))) return rc;
+    if (stage == c->integ.nstages)
+      if ((rc = launch_block_dt(c))) return rc;
+    c->ghosts_stale = true;
+    return ATHG_OK;
+  }
   if ((rc = launch_fluxes(c, order))) return rc;
   if ((rc = launch_corner(c))) return rc;
   if ((rc = launch_update(c, l))) return rc;
@@ -399,11 +492,12 @@ int need_pool(const athg_ctx* c) {
 
 // Captures one whole cycle on the context stream into a CUDA graph (once); the
 // graph reads dt/time from device memory, so the same graph serves every cycle.
-int build_graph(athg_ctx* c) {
-  if (c->gexec) return ATHG_OK;
+int capture_cycle(athg_ctx* c, cudaGraph_t* graph, cudaGraphExec_t* exec) {
   CK(cudaStreamBeginCapture(c->st, cudaStreamCaptureModeThreadLocal));
   c->counting = 0;
+  const bool stale = c->ghosts_stale;
   int rc = do_cycle(c);
+  c->ghosts_stale = stale;  // capturing runs nothing
   cudaGraph_t gr = nullptr;
   cudaError_t e = cudaStreamEndCapture(c->st, &gr);
   if (rc) {
@@ -412,9 +506,36 @@ int build_graph(athg_ctx* c) {
   }
   if (e != cudaSuccess)
     return fail(ATHG_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
-  c->graph = gr;
+  *graph = gr;
   c->launches_per_cycle = c->counting;
-  CK(cudaGraphInstantiate(&c->gexec, c->graph, 0));
+  CK(cudaGraphInstantiate(exec, gr, 0));
+  return ATHG_OK;
+}
+
+int build_graph(athg_ctx* c) {
+  if (c->gexec) return ATHG_OK;
+  int rc = capture_cycle(c, &c->graph, &c->gexec);
+  if (rc) return rc;
+  c->graph_src = c->u;
+  if (fused(c)) {  // the cycle that starts from the other buffer
+    swap_state(c);
+    rc = capture_cycle(c, &c->graph2, &c->gexec2);
+    swap_state(c);
+    if (rc) return rc;
+  }
+  return ATHG_OK;
+}
+
+// one whole cycle from the captured graphs; in the fused path the new state is then in
+// the other buffer
+int run_cycle_graph(athg_ctx* c) {
+  if (fused(c)) {
+    CK(cudaGraphLaunch(c->u == c->graph_src ? c->gexec : c->gexec2, c->st));
+    swap_state(c);
+    c->ghosts_stale = true;
+  } else {
+    CK(cudaGraphLaunch(c->gexec, c->st));
+  }
   return ATHG_OK;
 }
 
@@ -756,6 +877,8 @@ int athg_upload(athg_ctx* c, int block, int var, const double* host, size_t coun
 int athg_download(athg_ctx* c, int block, int var, double* host, size_t count) {
   int rc = need_pool(c);
   if (rc) return rc;
+  if (var == ATHG_VAR_CONS || var == ATHG_VAR_B1F || var == ATHG_VAR_B2F || var == ATHG_VAR_B3F)
+    if ((rc = refresh_ghosts(c))) return rc;
   size_t per;
   if ((rc = athg_var_size(c, var, &per))) return rc;
   void* d;
@@ -790,6 +913,7 @@ int athg_initialize(athg_ctx* c) {
   CK(cudaMemcpyAsync(c->scal, hs, sizeof(hs), cudaMemcpyHostToDevice, c->st));
   if (c->grav && (rc = gravity_solve(c))) return rc;  // mesh/mesh.cpp:1398-1402
   if ((rc = launch_ghosts(c))) return rc;
+  c->ghosts_stale = false;
   if ((rc = launch_c2p(c))) return rc;
   if ((rc = launch_block_dt(c))) return rc;
   if ((rc = launch_end(c, 0))) return rc;
@@ -807,7 +931,9 @@ int athg_stage(athg_ctx* c, int stage) {
 int athg_end_cycle(athg_ctx* c) {
   int rc = need_pool(c);
   if (rc) return rc;
-  return launch_end(c, 1);
+  if ((rc = launch_end(c, 1))) return rc;
+  if (fused(c)) swap_state(c);
+  return ATHG_OK;
 }
 
 int athg_cycles(athg_ctx* c, int n) {
@@ -821,7 +947,8 @@ int athg_cycles(athg_ctx* c, int n) {
     return ATHG_OK;
   }
   if ((rc = build_graph(c))) return rc;
-  for (int q = 0; q < n; ++q) CK(cudaGraphLaunch(c->gexec, c->st));
+  for (int q = 0; q < n; ++q)
+    if ((rc = run_cycle_graph(c))) return rc;
   return ATHG_OK;
 }
 
@@ -840,9 +967,8 @@ int athg_attach_gravity(athg_ctx* c, athg_mg* mg, double four_pi_G) {
   int rc = need_pool(c);
   if (rc) return rc;
   // drop any captured cycle: the stage sequence changes
-  if (c->gexec) cudaGraphExecDestroy(c->gexec);
-  if (c->graph) cudaGraphDestroy(c->graph);
-  c->gexec = nullptr; c->graph = nullptr;
+  drop_graphs(c);
+  if ((rc = refresh_ghosts(c))) return rc;
   if (c->grav) athg::mg_bind_stream(c->grav, nullptr);
   c->grav = nullptr;
   if (!mg) return ATHG_OK;
@@ -925,6 +1051,7 @@ int athg_stream(athg_ctx* c, void** stream) {
 int athg_calculate_fluxes(athg_ctx* c, int order) {
   int rc = need_pool(c);
   if (rc) return rc;
+  if ((rc = leave_fused(c))) return rc;
   if (order < 1 || order > 3) return fail(ATHG_ERR_ARG, "order must be 1, 2 or 3");
   if (order == 3 && c->g.ng < 3) return fail(ATHG_ERR_ARG, "PPM needs nghost >= 3");
   return launch_fluxes(c, order);
@@ -933,12 +1060,14 @@ int athg_calculate_fluxes(athg_ctx* c, int order) {
 int athg_compute_corner_e(athg_ctx* c) {
   int rc = need_pool(c);
   if (rc) return rc;
+  if ((rc = leave_fused(c))) return rc;
   return launch_corner(c);
 }
 
 int athg_integrate(athg_ctx* c, int stage) {
   int rc = need_pool(c);
   if (rc) return rc;
+  if ((rc = leave_fused(c))) return rc;
   if (stage < 1 || stage > c->integ.nstages) return fail(ATHG_ERR_ARG, "stage out of range");
   return launch_update(c, stage - 1);
 }
@@ -946,12 +1075,14 @@ int athg_integrate(athg_ctx* c, int stage) {
 int athg_exchange_ghosts(athg_ctx* c) {
   int rc = need_pool(c);
   if (rc) return rc;
+  if ((rc = leave_fused(c))) return rc;
   return launch_ghosts(c);
 }
 
 int athg_conserved_to_primitive(athg_ctx* c) {
   int rc = need_pool(c);
   if (rc) return rc;
+  if ((rc = leave_fused(c))) return rc;
   return launch_c2p(c);
 }
 

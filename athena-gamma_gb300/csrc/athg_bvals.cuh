@@ -42,9 +42,13 @@ __global__ void __launch_bounds__(256) k_ghost_same_level(Geom g, GhostPtrs p) {
       if (src >= 0) {
         int64_t d = cidx(g, k, j, i);
         int64_t s = cidx(g, k - o3 * g.nx3, j - o2 * g.nx2, i - o1 * g.nx1);
-        const double* us = p.u + (int64_t)src * p.nvar * g.ncell;
-        double* ud = p.u + (int64_t)b * p.nvar * g.ncell;
-        for (int n = 0; n < p.nvar; ++n) ud[n * g.ncell + d] = us[n * g.ncell + s];
+        const double* __restrict__ us = p.u + (int64_t)src * NHYD * g.ncell;
+        double* __restrict__ ud = p.u + (int64_t)b * NHYD * g.ncell;
+        double v[NHYD];
+#pragma unroll
+        for (int n = 0; n < NHYD; ++n) v[n] = __ldg(us + n * g.ncell + s);
+#pragma unroll
+        for (int n = 0; n < NHYD; ++n) ud[n * g.ncell + d] = v[n];
       }
     }
   }
@@ -75,6 +79,103 @@ __global__ void __launch_bounds__(256) k_ghost_same_level(Geom g, GhostPtrs p) {
         p.b3[(int64_t)b * g.nf3 + f3idx(g, k, j, i)] =
             p.b3[(int64_t)src * g.nf3 + f3idx(g, k - o3 * g.nx3, j - o2 * g.nx2, i - o1 * g.nx1)];
     }
+  }
+}
+
+// The same exchange for the mixed path's FP32 working arrays when the primitives of the
+// interior are recovered inside the update (k_update_c2p): up to three cell-variable groups
+// (W, bcc, cell-centred E) and the FP32 face-field copies, with the ownership rules above.
+struct GhostPtrs32 {
+  float* cell[3];  // [nb][ncomp[q]][cells]
+  int ncomp[3];
+  float* face[3];  // [nb][faces] per direction (nullptr: hydro)
+  const int* nbr;
+};
+
+// Every value is loaded before any is stored (the source is always a neighbour's interior,
+// never a ghost, so loads and stores never overlap), keeping all of a thread's loads in flight.
+template <bool MHD>
+__global__ void __launch_bounds__(256) k_ghost_f32(Geom g, GhostPtrs32 p) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int n1 = g.nc1 + 1, n2 = g.nc2 + 1;
+  if (t >= n1 * n2) return;
+  const int j = t / n1, i = t - j * n1, k = blockIdx.y, b = blockIdx.z;
+  const int* nb = p.nbr + (int64_t)b * 27;
+  const int64_t nc = g.ncell;
+  constexpr int NV = MHD ? 11 : 5;
+  float v[NV];
+  int64_t dst = -1;
+  if (i < g.nc1 && j < g.nc2 && k < g.nc3) {
+    int o1 = ghost_dir(i, g.is, g.ie), o2 = ghost_dir(j, g.js, g.je), o3 = ghost_dir(k, g.ks, g.ke);
+    if (o1 | o2 | o3) {
+      int src = nb[(o3 + 1) * 9 + (o2 + 1) * 3 + (o1 + 1)];
+      if (src >= 0) {
+        const int64_t s = cidx(g, k - o3 * g.nx3, j - o2 * g.nx2, i - o1 * g.nx1);
+        const float* __restrict__ w = p.cell[0] + (int64_t)src * 5 * nc;
+#pragma unroll
+        for (int n = 0; n < 5; ++n) v[n] = __ldg(w + n * nc + s);
+        if constexpr (MHD) {
+          const float* __restrict__ bc = p.cell[1] + (int64_t)src * 3 * nc;
+          const float* __restrict__ ce = p.cell[2] + (int64_t)src * 3 * nc;
+#pragma unroll
+          for (int n = 0; n < 3; ++n) {
+            v[5 + n] = __ldg(bc + n * nc + s);
+            v[8 + n] = __ldg(ce + n * nc + s);
+          }
+        }
+        dst = cidx(g, k, j, i);
+      }
+    }
+  }
+  float fv[3];
+  int64_t fd[3] = {-1, -1, -1};
+  if constexpr (MHD) {
+    if (i <= g.nc1 && j < g.nc2 && k < g.nc3) {
+      int o1 = ghost_dir(i, g.is, g.ie + 1), o2 = ghost_dir(j, g.js, g.je), o3 = ghost_dir(k, g.ks, g.ke);
+      int src = (o1 | o2 | o3) ? nb[(o3 + 1) * 9 + (o2 + 1) * 3 + (o1 + 1)] : -1;
+      if (src >= 0) {
+        fv[0] = __ldg(p.face[0] + (int64_t)src * g.nf1 +
+                      f1idx(g, k - o3 * g.nx3, j - o2 * g.nx2, i - o1 * g.nx1));
+        fd[0] = (int64_t)b * g.nf1 + f1idx(g, k, j, i);
+      }
+    }
+    if (i < g.nc1 && j <= g.nc2 && k < g.nc3) {
+      int o1 = ghost_dir(i, g.is, g.ie), o2 = ghost_dir(j, g.js, g.je + 1), o3 = ghost_dir(k, g.ks, g.ke);
+      int src = (o1 | o2 | o3) ? nb[(o3 + 1) * 9 + (o2 + 1) * 3 + (o1 + 1)] : -1;
+      if (src >= 0) {
+        fv[1] = __ldg(p.face[1] + (int64_t)src * g.nf2 +
+                      f2idx(g, k - o3 * g.nx3, j - o2 * g.nx2, i - o1 * g.nx1));
+        fd[1] = (int64_t)b * g.nf2 + f2idx(g, k, j, i);
+      }
+    }
+    if (i < g.nc1 && j < g.nc2 && k <= g.nc3) {
+      int o1 = ghost_dir(i, g.is, g.ie), o2 = ghost_dir(j, g.js, g.je), o3 = ghost_dir(k, g.ks, g.ke + 1);
+      int src = (o1 | o2 | o3) ? nb[(o3 + 1) * 9 + (o2 + 1) * 3 + (o1 + 1)] : -1;
+      if (src >= 0) {
+        fv[2] = __ldg(p.face[2] + (int64_t)src * g.nf3 +
+                      f3idx(g, k - o3 * g.nx3, j - o2 * g.nx2, i - o1 * g.nx1));
+        fd[2] = (int64_t)b * g.nf3 + f3idx(g, k, j, i);
+      }
+    }
+  }
+  if (dst >= 0) {
+    float* __restrict__ w = p.cell[0] + (int64_t)b * 5 * nc;
+#pragma unroll
+    for (int n = 0; n < 5; ++n) w[n * nc + dst] = v[n];
+    if constexpr (MHD) {
+      float* __restrict__ bc = p.cell[1] + (int64_t)b * 3 * nc;
+      float* __restrict__ ce = p.cell[2] + (int64_t)b * 3 * nc;
+#pragma unroll
+      for (int n = 0; n < 3; ++n) {
+        bc[n * nc + dst] = v[5 + n];
+        ce[n * nc + dst] = v[8 + n];
+      }
+    }
+  }
+  if constexpr (MHD) {
+#pragma unroll
+    for (int d = 0; d < 3; ++d)
+      if (fd[d] >= 0) p.face[d][fd[d]] = fv[d];
   }
 }
 

@@ -30,6 +30,10 @@ struct Launcher {
   // EquationOfState::ConservedToPrimitive over interior and ghost cells.
   static void c2p(const Geom& g, const StagePtrs<T>& p, bool mhd, const Phys& ph,
                   cudaStream_t st);
+  // Mixed VL2: update + interior primitive recovery from `sb.in` into `sb.out`
+  // (k_update_c2p; no-op for the FP64 path, which never takes this route).
+  static void update_c2p(const Geom& g, const StagePtrs<T>& p, bool mhd, const StageW& sw,
+                         const Phys& ph, const StateBufs& sb, cudaStream_t st);
   // HydroSourceTerms::SelfGravity over every block (phi: [nb][cells] potential).
   static void self_gravity(const Geom& g, const StagePtrs<T>& p, bool mhd, const StageW& sw,
                            const double* phi, cudaStream_t st);
@@ -119,6 +123,16 @@ void Launcher<T>::update(const Geom& g, const StagePtrs<T>& p, bool mhd, const S
               : make_box(g.is, g.ie, g.js, g.je, g.ks, g.ke);
   if (mhd) k_update<T, true><<<box_grid(b, g.nb, 128), 128, 0, st>>>(g, p, b, sw);
   else k_update<T, false><<<box_grid(b, g.nb, 128), 128, 0, st>>>(g, p, b, sw);
+}
+
+template <typename T>
+void Launcher<T>::update_c2p(const Geom& g, const StagePtrs<T>& p, bool mhd, const StageW& sw,
+                             const Phys& ph, const StateBufs& sb, cudaStream_t st) {
+  if constexpr (kMixed<T>) {
+    Box b = make_box(g.is, g.ie, g.js, g.je, g.ks, g.ke);
+    if (mhd) k_update_c2p<true><<<box_grid(b, g.nb, 128), 128, 0, st>>>(g, p, b, sw, ph, sb);
+    else k_update_c2p<false><<<box_grid(b, g.nb, 128), 128, 0, st>>>(g, p, b, sw, ph, sb);
+  }
 }
 
 template <typename T>

@@ -773,6 +773,166 @@ __global__ void __launch_bounds__(256) k_c2p(Geom g, StagePtrs<T> p, Box bx, Phy
   }
 }
 
+// ---------------------------------------------------------------------------------------
+// Mixed VL2 stage update with the primitive recovery of the interior fused in.
+// Both VL2 stages start from the state at the beginning of the cycle (stage 1: the
+// register is a copy of it; stage 2: the swap makes the register the base), so the state
+// is read from `in` and the new state written to `out`, and the two buffers trade places
+// after each cycle: no register copy, and no thread reads a value another thread writes.
+// Each thread updates its cell and the six faces around it (upper faces are recomputed by
+// the neighbouring thread, identically; a face is stored only by the cell it lies below,
+// or by the block's last cell along its axis), then recovers W, bcc, the FP32 face copies
+// and the cell-centred EMF from the values in registers. The arithmetic is that of
+// k_update and k_c2p in the mixed path.
+struct StateBufs {
+  const double* u_in;
+  const double* b_in[3];
+  double* u_out;
+  double* b_out[3];
+};
+
+template <bool MHD>
+__global__ void __launch_bounds__(128)
+k_update_c2p(Geom g, StagePtrs<float> p, Box bx, StageW sw, Phys ph, StateBufs sb) {
+  int i, j, k, b;
+  if (!box_coords(bx, i, j, k, b)) return;
+  const MixedGeo mg = p.mg[b];
+  const float wf = __fmul_rn(sw.betaf, __ldg(p.dtT));
+  const int64_t nc = g.ncell;
+  const int64_t c = cidx(g, k, j, i);
+  const double* __restrict__ uin = sb.u_in + (int64_t)b * NHYD * nc;
+  double* __restrict__ uout = sb.u_out + (int64_t)b * NHYD * nc;
+  constexpr int NF = MHD ? 8 : 5;
+  const float* __restrict__ F1 = p.flx[0] + (int64_t)b * NF * g.nf1;
+  const float* __restrict__ F2 = p.flx[1] + (int64_t)b * NF * g.nf2;
+  const float* __restrict__ F3 = p.flx[2] + (int64_t)b * NF * g.nf3;
+  const int64_t q1 = f1idx(g, k, j, i), q2 = f2idx(g, k, j, i), q3 = f3idx(g, k, j, i);
+  const int64_t s2 = g.nc1, s3 = (int64_t)g.nc1 * g.nc2;
+  float fx[NHYD][6];
+  double uo[NHYD];
+#pragma unroll
+  for (int n = 0; n < NHYD; ++n) {
+    fx[n][0] = __ldg(F1 + n * g.nf1 + q1 + 1);
+    fx[n][1] = __ldg(F1 + n * g.nf1 + q1);
+    fx[n][2] = __ldg(F2 + n * g.nf2 + q2 + s2);
+    fx[n][3] = __ldg(F2 + n * g.nf2 + q2);
+    fx[n][4] = __ldg(F3 + n * g.nf3 + q3 + s3);
+    fx[n][5] = __ldg(F3 + n * g.nf3 + q3);
+    uo[n] = __ldg(uin + n * nc + c);
+  }
+  // faces (lower, upper) per direction, base values and edge EMFs
+  double bl[3] = {0.0, 0.0, 0.0}, bu[3] = {0.0, 0.0, 0.0};
+  float E1[2][2], E2[2][2], E3[2][2];  // E1[dk][dj], E2[dk][di], E3[dj][di]
+  int64_t fl[3] = {0, 0, 0}, fu[3] = {0, 0, 0};
+  if constexpr (MHD) {
+    fl[0] = (int64_t)b * g.nf1 + q1;      fu[0] = fl[0] + 1;
+    fl[1] = (int64_t)b * g.nf2 + q2;      fu[1] = fl[1] + g.nc1;
+    fl[2] = (int64_t)b * g.nf3 + q3;      fu[2] = fl[2] + (int64_t)g.nc1 * g.nc2;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      bl[d] = __ldg(sb.b_in[d] + fl[d]);
+      bu[d] = __ldg(sb.b_in[d] + fu[d]);
+    }
+    const float* __restrict__ Ea = p.edge + (int64_t)b * 3 * g.ne;
+    const int64_t e = eidx(g, k, j, i);
+    const int64_t ej = (int64_t)g.nc1 + 1, ek = ((int64_t)g.nc1 + 1) * (g.nc2 + 1);
+#pragma unroll
+    for (int x = 0; x < 2; ++x)
+#pragma unroll
+      for (int y = 0; y < 2; ++y) {
+        E1[x][y] = __ldg(Ea + e + x * ek + y * ej);
+        E2[x][y] = __ldg(Ea + g.ne + e + x * ek + y);
+        E3[x][y] = __ldg(Ea + 2 * g.ne + e + x * ej + y);
+      }
+  }
+  // conserved update (base = the state at the start of the cycle)
+  const float cw1 = __fmul_rn(wf, mg.idx[0]), cw2 = __fmul_rn(wf, mg.idx[1]),
+              cw3 = __fmul_rn(wf, mg.idx[2]);
+  double un[NHYD];
+#pragma unroll
+  for (int n = 0; n < NHYD; ++n) {
+    float hi, lo;
+    sum3diff(__fmul_rn(cw1, fx[n][0]), __fmul_rn(cw1, fx[n][1]), __fmul_rn(cw2, fx[n][2]),
+             __fmul_rn(cw2, fx[n][3]), __fmul_rn(cw3, fx[n][4]), __fmul_rn(cw3, fx[n][5]), hi, lo);
+    un[n] = (uo[n] - f2d_int(hi)) - f2d_int(lo);
+  }
+  ff ss = {0.0f, 0.0f};
+  float* __restrict__ bcc = p.bcc + (int64_t)b * 3 * nc;
+  if constexpr (MHD) {
+    const float we1 = __fmul_rn(wf, mg.dx[0]), we2 = __fmul_rn(wf, mg.dx[1]),
+                we3 = __fmul_rn(wf, mg.dx[2]);
+    auto upd = [&](double base, float a, float b0, float c0, float d0, float wa, float wb,
+                   double ia) {
+      float hi, lo;
+      sum2diff(__fmul_rn(wa, a), __fmul_rn(wa, b0), __fmul_rn(wb, c0), __fmul_rn(wb, d0), hi, lo);
+      return fma(f2d_int(lo), ia, fma(f2d_int(hi), ia, base));
+    };
+    // dPhi1 = (eps3(j) - eps3(j+1)) + (eps2(k+1) - eps2(k)) at i and i+1
+    const double n1l = upd(bl[0], E3[0][0], E3[1][0], E2[1][0], E2[0][0], we3, we2, mg.ia[0]);
+    const double n1u = upd(bu[0], E3[0][1], E3[1][1], E2[1][1], E2[0][1], we3, we2, mg.ia[0]);
+    // dPhi2 = (eps3(i+1) - eps3(i)) + (eps1(k) - eps1(k+1)) at j and j+1
+    const double n2l = upd(bl[1], E3[0][1], E3[0][0], E1[0][0], E1[1][0], we3, we1, mg.ia[1]);
+    const double n2u = upd(bu[1], E3[1][1], E3[1][0], E1[0][1], E1[1][1], we3, we1, mg.ia[1]);
+    // dPhi3 = (eps2(i) - eps2(i+1)) + (eps1(j+1) - eps1(j)) at k and k+1
+    const double n3l = upd(bl[2], E2[0][0], E2[0][1], E1[0][1], E1[0][0], we2, we1, mg.ia[2]);
+    const double n3u = upd(bu[2], E2[1][0], E2[1][1], E1[1][1], E1[1][0], we2, we1, mg.ia[2]);
+    const ff f1 = split_ff(n1l), f2 = split_ff(n2l), f3 = split_ff(n3l);
+    sb.b_out[0][fl[0]] = n1l;
+    sb.b_out[1][fl[1]] = n2l;
+    sb.b_out[2][fl[2]] = n3l;
+    p.bfw[0][fl[0]] = f1.hi;
+    p.bfw[1][fl[1]] = f2.hi;
+    p.bfw[2][fl[2]] = f3.hi;
+    const ff u1f = split_ff(n1u), u2f = split_ff(n2u), u3f = split_ff(n3u);
+    if (i == g.ie) { sb.b_out[0][fu[0]] = n1u; p.bfw[0][fu[0]] = u1f.hi; }
+    if (j == g.je) { sb.b_out[1][fu[1]] = n2u; p.bfw[1][fu[1]] = u2f.hi; }
+    if (k == g.ke) { sb.b_out[2][fu[2]] = n3u; p.bfw[2][fu[2]] = u3f.hi; }
+    const ff s1 = ff_add(f1, u1f), s2f = ff_add(f2, u2f), s3f = ff_add(f3, u3f);
+    bcc[c] = 0.5f * ff_f(s1);
+    bcc[nc + c] = 0.5f * ff_f(s2f);
+    bcc[2 * nc + c] = 0.5f * ff_f(s3f);
+    ss = ff_add(ff_add(ff_sqr(s1), ff_sqr(s2f)), ff_sqr(s3f));
+  }
+  // primitive recovery (the mixed k_c2p)
+  float* __restrict__ w = p.w + (int64_t)b * NHYD * nc;
+  double ud = un[0];
+  const uint64_t ub = bits_d(ud);
+  if (!((ub >> 63) == 0 && ub > bits_d(ph.dfloor) && ub <= 0x7ff0000000000000ull)) ud = ph.dfloor;
+  const ff dd = split_ff(ud), mx1 = split_ff(un[1]), mx2 = split_ff(un[2]), mx3 = split_ff(un[3]);
+  const ff di = ff_recip(dd);
+  const ff mm = ff_add(ff_add(ff_sqr(mx1), ff_sqr(mx2)), ff_sqr(mx3));
+  ff x = ff_mul(mm, di);
+  if constexpr (MHD) x = ff_add(x, ff_scale(ss, 0.25f));
+  const ff wp = ff_mul(ff_sub(split_ff(un[4]), ff_scale(x, 0.5f)), ph.gm1f);
+  double ue = un[4];
+  float pf;
+  if (!ff_gt(wp, ph.pfloorf)) {
+    ue = (ph.pfloor / ph.gm1) + 0.5 * (f2d_int(x.hi) + f2d_int(x.lo));
+    pf = d2f_int(ph.pfloor);
+  } else {
+    pf = ff_f(wp);
+  }
+  uout[c] = ud;
+  uout[nc + c] = un[1];
+  uout[2 * nc + c] = un[2];
+  uout[3 * nc + c] = un[3];
+  uout[4 * nc + c] = ue;
+  const float dif = ff_f(di);
+  const float vx = mx1.hi * dif, vy = mx2.hi * dif, vz = mx3.hi * dif;
+  w[c] = dd.hi;
+  w[nc + c] = vx;
+  w[2 * nc + c] = vy;
+  w[3 * nc + c] = vz;
+  w[4 * nc + c] = pf;
+  if constexpr (MHD) {
+    const float bx = bcc[c], by = bcc[nc + c], bz = bcc[2 * nc + c];
+    float* __restrict__ ce = p.cce + (int64_t)b * 3 * nc;
+    ce[c] = vz * by - vy * bz;
+    ce[nc + c] = vx * bz - vz * bx;
+    ce[2 * nc + c] = vy * bx - vx * by;
+  }
+}
+
 // Self-gravity source (hydro/srcterms/self_gravity.cpp:35-125): momentum from the face
 // potentials, energy from the mass fluxes of this stage, applied after the flux
 // divergence with the stage weight beta dt. phi is the block pool's potential (one ghost

@@ -54,10 +54,11 @@ def test_fp64_bitexact_vs_reference(name):
         assert np.array_equal(out[k], ref), (k, float(np.abs(out[k] - ref).max()))
 
 
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
 @pytest.mark.parametrize("name", ["mhd_hlld_plm_vl2", "hydro_hllc_plm_rk3"])
-def test_stage_by_stage_equals_graph(name):
-    _, _, g1, t1 = _run_case(name, "fp64", use_graph=True)
-    _, _, g2, t2 = _run_case(name, "fp64", use_graph=False)
+def test_stage_by_stage_equals_graph(name, precision):
+    _, _, g1, t1 = _run_case(name, precision, use_graph=True)
+    _, _, g2, t2 = _run_case(name, precision, use_graph=False)
     assert t1 == t2
     for k in g1:
         assert np.array_equal(g1[k], g2[k])
@@ -162,3 +163,33 @@ def test_linear_wave_mixed_equal_l1(mhd, solver, tlim, cfl):
         out = sim.interior()
         res[prec] = lw.l1_errors(out["u"], out.get("b1"), out.get("b2"), out.get("b3"))[0]
     assert res["mixed"] <= 2.0 * res["fp64"], res
+
+
+@pytest.mark.parametrize("mhd", [True, False])
+def test_fused_mixed_stage_matches_unfused(mhd):
+    """The fused mixed VL2 stage (update + interior primitive recovery, FP32 ghost exchange,
+    alternating state buffers) against the separate-kernel mixed path on 8 blocks, over
+    five cycles run as captured graphs (odd count: the state ends in the other buffer)."""
+    nx, mb = (32, 32, 32), (16, 16, 16)
+    u, b1, b2, b3 = ol.smooth_random_state(nx, mhd, seed=17, amp=0.3)
+    out = {}
+    for mode in ("fused", "unfused"):
+        sim = athg.Sim(nx, mb, mhd=mhd, solver="hlld" if mhd else "hllc", precision="mixed",
+                       cfl=0.4, tlim=100.0)
+        sim.load_interior(u, b1, b2, b3)
+        sim.initialize()
+        if mode == "unfused":
+            # any single-step entry point leaves the fused path for good
+            athg.check(athg.lib().athg_exchange_ghosts(sim.h))
+        sim.cycles(5)
+        out[mode] = (sim.interior(), sim.download(athg.VAR_CONS), sim.get_time(),
+                     sim.max_div_b() if mhd else 0.0)
+        sim.close()
+    (fi, fu, ft, fd), (ui, uu, ut, ud) = out["fused"], out["unfused"]
+    assert ft == ut
+    for k in fi:
+        np.testing.assert_allclose(fi[k], ui[k], rtol=0, atol=1e-12 * np.abs(ui[k]).max())
+    # the ghost zones of the state (refreshed on download) match as well
+    np.testing.assert_allclose(fu, uu, rtol=0, atol=1e-12 * np.abs(uu).max())
+    if mhd:
+        assert fd < 1e-13
