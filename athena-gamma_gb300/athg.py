@@ -34,7 +34,8 @@ EXPORTS = [
     "athg_new_block_dt", "athg_max_div_b", "athg_sum_conserved", "athg_last_error",
     "athg_mg_create", "athg_mg_destroy", "athg_mg_load_source", "athg_mg_set_phi",
     "athg_mg_solve", "athg_mg_vcycles", "athg_mg_defect_norm", "athg_mg_get_phi",
-    "athg_mg_stream", "athg_mg_multipole", "athg_attach_gravity", "athg_block_cfl_dt_noalloc",
+    "athg_mg_stream", "athg_mg_multipole", "athg_attach_gravity", "athg_history",
+    "athg_block_cfl_dt_noalloc",
 ]
 MG_BC = {"periodic": 0, "zerograd": 1, "zerofixed": 2, "multipole": 3}
 
@@ -117,6 +118,7 @@ def lib():
         "athg_mg_stream": [vp, C.POINTER(vp)],
         "athg_mg_multipole": [vp, C.POINTER(d)],
         "athg_attach_gravity": [vp, vp, d],
+        "athg_history": [vp, C.POINTER(d), C.POINTER(i)],
         "athg_block_cfl_dt_noalloc": [C.POINTER(Config), vp, vp, vp, vp, vp, d, d, d, vp, vp],
     }
     for name, args in sig.items():
@@ -306,6 +308,13 @@ class Sim:
         v = C.c_double()
         check(lib().athg_new_block_dt(self.h, C.byref(v)))
         return v.value
+
+    def history(self):
+        """The 12 history sums of outputs/history.cpp, reduced on the device."""
+        a = np.zeros(12)
+        n = C.c_int()
+        check(lib().athg_history(self.h, _dptr(a), C.byref(n)))
+        return a[:n.value]
 
     def attach_gravity(self, mg, four_pi_G):
         """Self-gravity through a Multigrid on the same mesh (None detaches)."""

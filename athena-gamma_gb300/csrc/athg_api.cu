@@ -101,6 +101,67 @@ __global__ void k_sum_cons(Geom g, const double* u, const BlockGeo* geo, double*
   }
 }
 
+// HistoryOutput::WriteOutputFile sums (outputs/history.cpp:45-130): volume-weighted mass,
+// momenta, kinetic energy per direction, total energy, 1/2 rho phi (with self-gravity)
+// and magnetic energy per direction, over interior cells. One partial per thread block
+// (warp shuffles, then shared memory), summed on the host in a fixed order so the result
+// does not depend on scheduling.
+constexpr int kHist = 12;
+__global__ void __launch_bounds__(256)
+k_history(Geom g, const double* __restrict__ u, const double* __restrict__ b1,
+          const double* __restrict__ b2, const double* __restrict__ b3,
+          const double* __restrict__ phi, const BlockGeo* geo, int mhd, double* part) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  double s[kHist];
+#pragma unroll
+  for (int n = 0; n < kHist; ++n) s[n] = 0.0;
+  if (t < g.nx1 * g.nx2) {
+    const int jj = t / g.nx1, i = g.is + t - jj * g.nx1, j = g.js + jj;
+    const int k = g.ks + blockIdx.y, b = blockIdx.z;
+    const BlockGeo ge = geo[b];
+    const double vol = ge.dx[0] * ge.dx[1] * ge.dx[2];
+    const int64_t c = cidx(g, k, j, i);
+    const double* ub = u + (int64_t)b * NHYD * g.ncell;
+    const double d = ub[c], mx = ub[g.ncell + c], my = ub[2 * g.ncell + c],
+                 mz = ub[3 * g.ncell + c], e = ub[4 * g.ncell + c];
+    s[0] = vol * d;
+    s[1] = vol * mx;
+    s[2] = vol * my;
+    s[3] = vol * mz;
+    s[4] = vol * 0.5 * (mx * mx) / d;
+    s[5] = vol * 0.5 * (my * my) / d;
+    s[6] = vol * 0.5 * (mz * mz) / d;
+    s[7] = vol * e;
+    if (phi) s[8] = vol * 0.5 * d * phi[(int64_t)b * g.ncell + c];
+    if (mhd) {
+      const double c1 = 0.5 * b1[(int64_t)b * g.nf1 + f1idx(g, k, j, i)] +
+                        0.5 * b1[(int64_t)b * g.nf1 + f1idx(g, k, j, i + 1)];
+      const double c2 = 0.5 * b2[(int64_t)b * g.nf2 + f2idx(g, k, j, i)] +
+                        0.5 * b2[(int64_t)b * g.nf2 + f2idx(g, k, j + 1, i)];
+      const double c3 = 0.5 * b3[(int64_t)b * g.nf3 + f3idx(g, k, j, i)] +
+                        0.5 * b3[(int64_t)b * g.nf3 + f3idx(g, k + 1, j, i)];
+      s[9] = vol * 0.5 * c1 * c1;
+      s[10] = vol * 0.5 * c2 * c2;
+      s[11] = vol * 0.5 * c3 * c3;
+    }
+  }
+  __shared__ double sh[8][kHist];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int n = 0; n < kHist; ++n) {
+    double v = s[n];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == 0) sh[wid][n] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < kHist) {
+    double v = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) v += sh[w][threadIdx.x];
+    const int64_t blk = ((int64_t)blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
+    part[blk * kHist + threadIdx.x] = v;
+  }
+}
+
 // Stage weights of the low-storage integrators without orbital advection
 // (reference src/task_list/time_integrator.cpp:100-600).
 struct Integrator {
@@ -206,7 +267,8 @@ StagePtrs<T> ptrs(athg_ctx* c) {
 
 Phys phys(const athg_ctx* c) {
   return Phys{c->cfg.gamma, c->cfg.dfloor, c->cfg.pfloor, c->cfg.gamma - 1.0,
-              split_ff(c->cfg.gamma - 1.0), split_ff(c->cfg.pfloor)};
+              split_ff(c->cfg.gamma - 1.0), split_ff(c->cfg.pfloor), (float)c->cfg.gamma,
+              (float)c->cfg.dfloor, (float)c->cfg.pfloor};
 }
 
 void free_pool(athg_ctx* c) {
@@ -1130,6 +1192,32 @@ int athg_sum_conserved(athg_ctx* c, double* out5) {
   CKL();
   CK(cudaMemcpyAsync(out5, c->scal + 4, 5 * 8, cudaMemcpyDeviceToHost, c->st));
   CK(cudaStreamSynchronize(c->st));
+  return ATHG_OK;
+}
+
+int athg_history(athg_ctx* c, double* out, int* count) {
+  int rc = need_pool(c);
+  if (rc) return rc;
+  if (!out || !count) return fail(ATHG_ERR_ARG, "null argument");
+  if ((rc = refresh_ghosts(c))) return rc;
+  const Geom& g = c->g;
+  dim3 grid((unsigned)((g.nx1 * g.nx2 + 255) / 256), (unsigned)g.nx3, (unsigned)c->nb);
+  const size_t np = (size_t)grid.x * grid.y * grid.z;
+  double* part = nullptr;
+  CK(cudaMallocAsync(&part, np * kHist * sizeof(double), c->st));
+  k_history<<<grid, 256, 0, c->st>>>(g, c->u, c->b1, c->b2, c->b3, c->grav ? c->phi : nullptr,
+                                     c->geo, c->cfg.magnetic, part);
+  cudaError_t e = cudaGetLastError();
+  std::vector<double> h(np * kHist);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(h.data(), part, h.size() * sizeof(double), cudaMemcpyDeviceToHost, c->st);
+  cudaFreeAsync(part, c->st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
+  if (e != cudaSuccess) return fail(ATHG_ERR_CUDA, std::string("history: ") + cudaGetErrorString(e));
+  for (int n = 0; n < kHist; ++n) out[n] = 0.0;
+  for (size_t q = 0; q < np; ++q)
+    for (int n = 0; n < kHist; ++n) out[n] += h[q * kHist + n];
+  *count = kHist;
   return ATHG_OK;
 }
 

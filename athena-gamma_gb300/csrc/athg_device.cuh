@@ -66,7 +66,19 @@ struct Phys {
   double gamma, dfloor, pfloor;
   double gm1;  // gamma - 1
   ff gm1f, pfloorf;  // the same as double-float pairs (mixed primitive recovery)
+  float gammas, dfloors, pfloors;  // rounded to FP32 on the host (no FP64 pipe in FP32 kernels)
 };
+
+// gamma and the floors in the flux precision
+template <typename T> __device__ __forceinline__ T ph_gamma(const Phys& ph) {
+  if constexpr (sizeof(T) == 4) return ph.gammas; else return ph.gamma;
+}
+template <typename T> __device__ __forceinline__ T ph_dfloor(const Phys& ph) {
+  if constexpr (sizeof(T) == 4) return ph.dfloors; else return ph.dfloor;
+}
+template <typename T> __device__ __forceinline__ T ph_pfloor(const Phys& ph) {
+  if constexpr (sizeof(T) == 4) return ph.pfloors; else return ph.pfloor;
+}
 
 // Stage weights of the low-storage integrator (reference
 // src/task_list/time_integrator.cpp:100-600, applied as in :1563-1653).

@@ -3,6 +3,7 @@
 // kernels_f64.cu (built without FMA contraction, so the FP64 path reproduces the
 // reference's arithmetic bit for bit) and kernels_f32.cu.
 #pragma once
+#include <algorithm>
 #include "athg_stage.cuh"
 
 namespace athg {
@@ -61,7 +62,9 @@ static void flux_dir(const Geom& g, const StagePtrs<T>& p, bool mhd, int solver,
     // marching sweeps: pencils over (i, k) for DIR=1 and (i, j) for DIR=2
     Box pb = DIR == 1 ? make_box(il, iu, kl, ku, 0, 0) : make_box(il, iu, jl, ju, 0, 0);
     const int fs = DIR == 1 ? jl : kl, fe = DIR == 1 ? ju : ku;
-    dim3 grid((unsigned)((pb.ni * pb.nj + 127) / 128), 1, (unsigned)g.nb);
+    // pencils split into segments of ~16 faces
+    const unsigned nseg = (unsigned)std::max(1, (fe - fs + 1) / 16);
+    dim3 grid((unsigned)((pb.ni * pb.nj + 127) / 128), nseg, (unsigned)g.nb);
     if (mhd) {
       if (solver == HLLD)
         k_flux_march<T, DIR, ORDER, HLLD, true><<<grid, 128, 0, st>>>(g, p, pb, ph, fs, fe);

@@ -138,7 +138,7 @@ k_flux(Geom g, StagePtrs<T> p, Box bx, Phys ph) {
       wr[n] = qm;
     }
     // density and pressure floors on the PPM states (ppm.cpp:326-332)
-    const T df = (T)ph.dfloor, pf = (T)ph.pfloor;
+    const T df = ph_dfloor<T>(ph), pf = ph_pfloor<T>(ph);
     wl[IDN] = (wl[IDN] > df) ? wl[IDN] : df; wl[IPR] = (wl[IPR] > pf) ? wl[IPR] : pf;
     wr[IDN] = (wr[IDN] > df) ? wr[IDN] : df; wr[IPR] = (wr[IPR] > pf) ? wr[IPR] : pf;
   } else {
@@ -172,7 +172,7 @@ k_flux(Geom g, StagePtrs<T> p, Box bx, Phys ph) {
   const int64_t nf = fsize<DIR>(g);
   const int64_t fi = fidx<DIR>(g, k, j, i);
   T* __restrict__ out = p.flx[DIR] + (int64_t)b * NF * nf;
-  const T gam = (T)ph.gamma;
+  const T gam = ph_gamma<T>(ph);
   if constexpr (MHD) {
     wli[IBY] = wl[IBY]; wli[IBZ] = wl[IBZ];
     wri[IBY] = wr[IBY]; wri[IBZ] = wr[IBZ];
@@ -222,7 +222,7 @@ __device__ __forceinline__ void face_solve(const Geom& g, const StagePtrs<T>& p,
   wri[IPR] = wr[IPR];
   const int64_t nf = fsize<DIR>(g);
   T* __restrict__ out = p.flx[DIR] + (int64_t)b * NF * nf;
-  const T gam = (T)ph.gamma;
+  const T gam = ph_gamma<T>(ph);
   if constexpr (MHD) {
     wli[IBY] = wl[IBY]; wli[IBZ] = wl[IBZ];
     wri[IBY] = wr[IBY]; wri[IBZ] = wr[IBZ];
@@ -278,6 +278,16 @@ k_flux_march(Geom g, StagePtrs<T> p, Box bx, Phys ph, int fs, int fe) {
     b = blockIdx.z;
     (void)unused;
   }
+  // grid.y splits each pencil into segments (shorter dependency chains, more threads);
+  // every segment rebuilds its window from the cells before its first face
+  {
+    const int len = (fe - fs + (int)gridDim.y) / (int)gridDim.y;
+    const int s0 = fs + (int)blockIdx.y * len;
+    const int s1 = min(fe, s0 + len - 1);
+    if (s0 > s1) return;
+    fs = s0;
+    fe = s1;
+  }
   constexpr int NW = MHD ? 7 : 5;
   const int64_t nc = g.ncell;
   const T* __restrict__ w = p.w + (int64_t)b * NHYD * nc;
@@ -311,7 +321,7 @@ k_flux_march(Geom g, StagePtrs<T> p, Box bx, Phys ph, int fs, int fe) {
   if (ORDER == 3) {
     // PPM: window of five cells; cell f gives the right state of face f (qminus) and
     // the left state of face f+1 (qplus)
-    const T df = (T)ph.dfloor, pf = (T)ph.pfloor;
+    const T df = ph_dfloor<T>(ph), pf = ph_pfloor<T>(ph);
     T win[5][7];
     int64_t c = cell_at(fs - 1);
 #pragma unroll
@@ -792,7 +802,7 @@ struct StateBufs {
 };
 
 template <bool MHD>
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(128, 8)
 k_update_c2p(Geom g, StagePtrs<float> p, Box bx, StageW sw, Phys ph, StateBufs sb) {
   int i, j, k, b;
   if (!box_coords(bx, i, j, k, b)) return;
@@ -1008,7 +1018,7 @@ k_block_dt(Geom g, StagePtrs<T> p, Box bx, Phys ph, unsigned long long* dtmin) {
       const BlockGeo geo = p.geo[b];
       dx1 = geo.dx[0]; dx2 = geo.dx[1]; dx3 = geo.dx[2];
     }
-    const T gam = (T)ph.gamma;
+    const T gam = ph_gamma<T>(ph);
     T dt1, dt2, dt3;
     if constexpr (MHD) {
       const T* bcc = p.bcc + (int64_t)b * 3 * nc;

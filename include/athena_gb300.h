@@ -195,6 +195,13 @@ int athg_mg_stream(athg_mg* mg, void** stream);
 /* Multipole coefficients (25) and expansion origin (3), after a solve. */
 int athg_mg_multipole(athg_mg* mg, double* out28);
 
+/* HistoryOutput::WriteOutputFile sums (outputs/history.cpp:45-130), reduced on the
+ * device over all blocks' interior cells: out[0] mass, [1..3] momenta, [4..6] kinetic
+ * energy per direction, [7] total energy, [8] 1/2 rho phi (0 without self-gravity),
+ * [9..11] cell-centred magnetic energy per direction (0 for hydro). *count = 12.
+ * The reference's columns are these without the entries its build does not have. */
+int athg_history(athg_ctx* ctx, double* out, int* count);
+
 /* Self-gravity (SELF_GRAVITY_ENABLED == 2 with <problem> four_pi_G, Mesh::SetFourPiG).
  * Couples mg to the hydro context: the solve of MGGravityDriver::Solve
  * (gravity/mg_gravity.cpp:166) runs in athg_initialize (mesh/mesh.cpp:1398-1402) and

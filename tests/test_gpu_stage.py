@@ -193,3 +193,29 @@ def test_fused_mixed_stage_matches_unfused(mhd):
     np.testing.assert_allclose(fu, uu, rtol=0, atol=1e-12 * np.abs(uu).max())
     if mhd:
         assert fd < 1e-13
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_history_sums_match_host(precision):
+    """Device history reduction (outputs/history.cpp sums) against numpy on the downloaded
+    state, after a few cycles (the mixed VL2 path leaves the state in the other buffer)."""
+    nx, mb = (32, 32, 32), (16, 16, 16)
+    u, b1, b2, b3 = ol.smooth_random_state(nx, True, seed=23, amp=0.3)
+    sim = athg.Sim(nx, mb, mhd=True, solver="hlld", precision=precision, cfl=0.4, tlim=100.0)
+    sim.load_interior(u, b1, b2, b3)
+    sim.initialize()
+    sim.cycles(3)
+    h = sim.history()
+    st = sim.interior()
+    U = st["u"]
+    vol = (1.0 / 32) ** 3
+    c1 = 0.5 * (st["b1"][:, :, :-1] + st["b1"][:, :, 1:])
+    c2 = 0.5 * (st["b2"][:, :-1, :] + st["b2"][:, 1:, :])
+    c3 = 0.5 * (st["b3"][:-1, :, :] + st["b3"][1:, :, :])
+    ref = [U[0].sum(), U[1].sum(), U[2].sum(), U[3].sum(),
+           (0.5 * U[1] ** 2 / U[0]).sum(), (0.5 * U[2] ** 2 / U[0]).sum(),
+           (0.5 * U[3] ** 2 / U[0]).sum(), U[4].sum(), 0.0,
+           (0.5 * c1 ** 2).sum(), (0.5 * c2 ** 2).sum(), (0.5 * c3 ** 2).sum()]
+    ref = np.array(ref) * vol
+    np.testing.assert_allclose(h, ref, rtol=1e-12, atol=1e-14)
+    sim.close()
