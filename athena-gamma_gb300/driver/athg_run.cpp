@@ -1,0 +1,305 @@
+// athg_run.cpp -- a C++ host program above the C ABI, shaped like the reference's main
+// loop (src/main.cpp:430-495): read an athinput file (plus block/key=value overrides from
+// the command line, src/main.cpp:110-200 and inputs/parameter_input.cpp), build a uniform
+// periodic mesh of MeshBlocks, set the initial state from a built-in problem generator,
+// then cycle until tlim / nlim and write history sums (outputs/history.cpp) to
+// <problem_id>.hst. The physics options the reference fixes when it is configured
+// (magnetic fields, Riemann solver) are runtime keys of a <gb300> block here.
+//
+//   athg_run -i athinput.orszag_tang [mesh/nx1=128 time/nlim=10 ...]
+//
+// Problem generators: orszag_tang (src/pgen/orszag_tang.cpp:42-115) and blast
+// (src/pgen/blast.cpp:54-120, uniform sphere of high pressure, optional uniform field).
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <chrono>
+#include <fstream>
+#include <map>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "athena_gb300.h"
+
+namespace {
+
+using Params = std::map<std::string, std::string>;  // "block/key" -> value
+
+std::string trim(const std::string& s) {
+  size_t a = s.find_first_not_of(" \t\r\n"), b = s.find_last_not_of(" \t\r\n");
+  return a == std::string::npos ? std::string() : s.substr(a, b - a + 1);
+}
+
+// athinput: "<block>" lines, "key = value # comment" lines (inputs/parameter_input.cpp)
+bool read_athinput(const std::string& path, Params& p) {
+  std::ifstream f(path);
+  if (!f) return false;
+  std::string line, block;
+  while (std::getline(f, line)) {
+    size_t h = line.find('#');
+    if (h != std::string::npos) line = line.substr(0, h);
+    line = trim(line);
+    if (line.empty()) continue;
+    if (line[0] == '<') {
+      size_t e = line.find('>');
+      block = trim(line.substr(1, e - 1));
+      continue;
+    }
+    size_t eq = line.find('=');
+    if (eq == std::string::npos) continue;
+    p[block + "/" + trim(line.substr(0, eq))] = trim(line.substr(eq + 1));
+  }
+  return true;
+}
+
+std::string get(const Params& p, const std::string& k, const std::string& def) {
+  auto it = p.find(k);
+  return it == p.end() ? def : it->second;
+}
+double getd(const Params& p, const std::string& k, double def) {
+  auto it = p.find(k);
+  return it == p.end() ? def : std::atof(it->second.c_str());
+}
+int geti(const Params& p, const std::string& k, int def) {
+  auto it = p.find(k);
+  return it == p.end() ? def : std::atoi(it->second.c_str());
+}
+
+void check(int rc, const char* what) {
+  if (rc != ATHG_OK) {
+    std::fprintf(stderr, "### FATAL ERROR in %s: %s\n", what, athg_last_error());
+    std::exit(1);
+  }
+}
+
+// cell-centre / face positions of one axis of one block (uniform mesh)
+struct Axis {
+  std::vector<double> xf, xv;
+  double dx;
+};
+Axis axis_of(int nx, int ng, double lo, double hi, int64_t off, int64_t ntot) {
+  Axis a;
+  a.dx = (hi - lo) / (double)ntot;
+  a.xf.resize(nx + 2 * ng + 1);
+  for (int i = 0; i < nx + 2 * ng + 1; ++i) a.xf[i] = lo + (double)(off + i - ng) * a.dx;
+  a.xv.resize(nx + 2 * ng);
+  for (int i = 0; i < nx + 2 * ng; ++i) a.xv[i] = 0.5 * (a.xf[i] + a.xf[i + 1]);
+  return a;
+}
+
+}  // namespace
+
+int main(int argc, char** argv) {
+  Params p;
+  std::string input;
+  for (int a = 1; a < argc; ++a) {
+    if (!std::strcmp(argv[a], "-i") && a + 1 < argc) {
+      input = argv[++a];
+    } else if (std::strchr(argv[a], '=')) {
+      std::string s = argv[a];
+      size_t eq = s.find('=');
+      p["__cli__" + s.substr(0, eq)] = s.substr(eq + 1);
+    }
+  }
+  if (input.empty() || !read_athinput(input, p)) {
+    std::fprintf(stderr, "usage: athg_run -i athinput [block/key=value ...]\n");
+    return 1;
+  }
+  for (auto it = p.begin(); it != p.end();) {  // command-line overrides win
+    if (it->first.rfind("__cli__", 0) == 0) {
+      p[it->first.substr(7)] = it->second;
+      it = p.erase(it);
+    } else {
+      ++it;
+    }
+  }
+
+  const std::string pgen = get(p, "gb300/pgen", "orszag_tang");
+  const bool mhd = geti(p, "gb300/magnetic", 1) != 0;
+  const std::string rs = get(p, "gb300/rsolver", mhd ? "hlld" : "hllc");
+  const std::string integ = get(p, "time/integrator", "vl2");
+  athg_config c{};
+  athg_mesh m{};
+  m.nx1 = geti(p, "mesh/nx1", 64); m.nx2 = geti(p, "mesh/nx2", m.nx1); m.nx3 = geti(p, "mesh/nx3", m.nx1);
+  m.x1min = getd(p, "mesh/x1min", -0.5); m.x1max = getd(p, "mesh/x1max", 0.5);
+  m.x2min = getd(p, "mesh/x2min", -0.5); m.x2max = getd(p, "mesh/x2max", 0.5);
+  m.x3min = getd(p, "mesh/x3min", -0.5); m.x3max = getd(p, "mesh/x3max", 0.5);
+  m.periodic[0] = m.periodic[1] = m.periodic[2] = 1;
+  for (const char* bc : {"ix1_bc", "ox1_bc", "ix2_bc", "ox2_bc", "ix3_bc", "ox3_bc"})
+    if (get(p, std::string("mesh/") + bc, "periodic") != "periodic") {
+      std::fprintf(stderr, "### FATAL ERROR: only periodic mesh boundaries are supported\n");
+      return 1;
+    }
+  c.nx1 = geti(p, "meshblock/nx1", m.nx1);
+  c.nx2 = geti(p, "meshblock/nx2", m.nx2);
+  c.nx3 = geti(p, "meshblock/nx3", m.nx3);
+  c.xorder = geti(p, "time/xorder", 2);
+  c.nghost = geti(p, "gb300/nghost", c.xorder == 3 ? 3 : 2);
+  c.magnetic = mhd;
+  c.rsolver = rs == "hlle" ? ATHG_HLLE : rs == "hllc" ? ATHG_HLLC : rs == "hlld" ? ATHG_HLLD
+            : rs == "lhllc" ? ATHG_LHLLC : ATHG_LHLLD;
+  c.integrator = integ == "rk1" ? ATHG_RK1 : integ == "rk2" ? ATHG_RK2 : integ == "rk3" ? ATHG_RK3
+               : ATHG_VL2;
+  c.precision = get(p, "gb300/precision", "mixed") == "fp64" ? ATHG_FP64 : ATHG_MIXED;
+  c.gamma = getd(p, "hydro/gamma", 5.0 / 3.0);
+  const double fl = std::sqrt(1024.0 * 1.17549435e-38);  // eos/eos.cpp default floors
+  c.dfloor = getd(p, "hydro/dfloor", fl);
+  c.pfloor = getd(p, "hydro/pfloor", fl);
+  c.cfl_number = getd(p, "time/cfl_number", 0.3);
+  c.tlim = getd(p, "time/tlim", 1.0);
+  const int nlim = geti(p, "time/nlim", -1);
+
+  athg_ctx* ctx = nullptr;
+  check(athg_create(&c, &ctx), "athg_create");
+  check(athg_set_uniform_mesh(ctx, &m), "athg_set_uniform_mesh");
+  int nb = 0;
+  check(athg_num_blocks(ctx, &nb), "athg_num_blocks");
+  const int ng = c.nghost;
+  const int n1 = c.nx1 + 2 * ng, n2 = c.nx2 + 2 * ng, n3 = c.nx3 + 2 * ng;
+  const size_t nc = (size_t)n1 * n2 * n3;
+
+  // MeshBlock::ProblemGenerator for every block, then one upload per array
+  std::vector<double> U(5 * nc * nb, 0.0), B1, B2, B3;
+  if (mhd) {
+    B1.assign((size_t)n3 * n2 * (n1 + 1) * nb, 0.0);
+    B2.assign((size_t)n3 * (n2 + 1) * n1 * nb, 0.0);
+    B3.assign((size_t)(n3 + 1) * n2 * n1 * nb, 0.0);
+  }
+  const double gm1 = c.gamma - 1.0;
+  for (int b = 0; b < nb; ++b) {
+    int64_t loc[4];
+    check(athg_block_location(ctx, b, loc), "athg_block_location");
+    Axis ax = axis_of(c.nx1, ng, m.x1min, m.x1max, loc[0] * c.nx1, m.nx1);
+    Axis ay = axis_of(c.nx2, ng, m.x2min, m.x2max, loc[1] * c.nx2, m.nx2);
+    Axis az = axis_of(c.nx3, ng, m.x3min, m.x3max, loc[2] * c.nx3, m.nx3);
+    double* u = &U[5 * nc * b];
+    auto C = [&](int n, int k, int j, int i) -> double& {
+      return u[(size_t)n * nc + ((size_t)k * n2 + j) * n1 + i];
+    };
+    double* b1 = mhd ? &B1[(size_t)n3 * n2 * (n1 + 1) * b] : nullptr;
+    double* b2 = mhd ? &B2[(size_t)n3 * (n2 + 1) * n1 * b] : nullptr;
+    double* b3 = mhd ? &B3[(size_t)(n3 + 1) * n2 * n1 * b] : nullptr;
+    auto F1 = [&](int k, int j, int i) -> double& { return b1[((size_t)k * n2 + j) * (n1 + 1) + i]; };
+    auto F2 = [&](int k, int j, int i) -> double& { return b2[((size_t)k * (n2 + 1) + j) * n1 + i]; };
+    auto F3 = [&](int k, int j, int i) -> double& { return b3[((size_t)k * n2 + j) * n1 + i]; };
+    const int is = ng, ie = ng + c.nx1 - 1, js = ng, je = ng + c.nx2 - 1, ks = ng, ke = ng + c.nx3 - 1;
+    if (pgen == "orszag_tang") {
+      const double PI = 3.1415926535897932, TWO_PI = 6.2831853071795862;
+      const double B0 = 1.0 / std::sqrt(4.0 * PI), d0 = 25.0 / (36.0 * PI), v0 = 1.0,
+                   p0 = 5.0 / (12.0 * PI);
+      auto Az = [&](double x, double y) {
+        return B0 / (4.0 * PI) * (std::cos(4.0 * PI * x) - 2.0 * std::cos(TWO_PI * y));
+      };
+      for (int k = ks; k <= ke; ++k)
+        for (int j = js; j <= je; ++j)
+          for (int i = is; i <= ie; ++i) {
+            C(0, k, j, i) = d0;
+            C(1, k, j, i) = d0 * v0 * std::sin(TWO_PI * ay.xv[j]);
+            C(2, k, j, i) = -d0 * v0 * std::sin(TWO_PI * ax.xv[i]);
+            C(3, k, j, i) = 0.0;
+          }
+      if (mhd) {
+        for (int k = ks; k <= ke; ++k)
+          for (int j = js; j <= je; ++j)
+            for (int i = is; i <= ie + 1; ++i)
+              F1(k, j, i) = (Az(ax.xf[i], ay.xf[j + 1]) - Az(ax.xf[i], ay.xf[j])) / ay.dx;
+        for (int k = ks; k <= ke; ++k)
+          for (int j = js; j <= je + 1; ++j)
+            for (int i = is; i <= ie; ++i)
+              F2(k, j, i) = (Az(ax.xf[i], ay.xf[j]) - Az(ax.xf[i + 1], ay.xf[j])) / ax.dx;
+      }
+      for (int k = ks; k <= ke; ++k)
+        for (int j = js; j <= je; ++j)
+          for (int i = is; i <= ie; ++i) {
+            double pb = 0.0;
+            if (mhd) {
+              double c1 = 0.5 * (F1(k, j, i) + F1(k, j, i + 1));
+              double c2 = 0.5 * (F2(k, j, i) + F2(k, j + 1, i));
+              pb = 0.5 * (c1 * c1 + c2 * c2);
+            }
+            const double d = C(0, k, j, i);
+            C(4, k, j, i) = p0 / gm1 + pb +
+                            0.5 * (C(1, k, j, i) * C(1, k, j, i) + C(2, k, j, i) * C(2, k, j, i)) / d;
+          }
+    } else if (pgen == "blast") {
+      const double rad = getd(p, "problem/radius", 0.1), pa = getd(p, "problem/pamb", 0.1),
+                   prat = getd(p, "problem/prat", 100.0), da = getd(p, "problem/damb", 1.0),
+                   b0 = getd(p, "problem/b0", mhd ? 1.0 : 0.0),
+                   ang = getd(p, "problem/angle", 45.0) * 3.1415926535897932 / 180.0;
+      const double bx = b0 * std::cos(ang), by = b0 * std::sin(ang);
+      if (mhd) {
+        for (int k = ks; k <= ke; ++k) {
+          for (int j = js; j <= je; ++j)
+            for (int i = is; i <= ie + 1; ++i) F1(k, j, i) = bx;
+          for (int j = js; j <= je + 1; ++j)
+            for (int i = is; i <= ie; ++i) F2(k, j, i) = by;
+        }
+      }
+      for (int k = ks; k <= ke; ++k)
+        for (int j = js; j <= je; ++j)
+          for (int i = is; i <= ie; ++i) {
+            const double r = std::sqrt(ax.xv[i] * ax.xv[i] + ay.xv[j] * ay.xv[j] + az.xv[k] * az.xv[k]);
+            const double pr = r < rad ? pa * prat : pa;
+            C(0, k, j, i) = da;
+            C(1, k, j, i) = C(2, k, j, i) = C(3, k, j, i) = 0.0;
+            C(4, k, j, i) = pr / gm1 + (mhd ? 0.5 * (bx * bx + by * by) : 0.0);
+          }
+    } else {
+      std::fprintf(stderr, "### FATAL ERROR: unknown gb300/pgen %s\n", pgen.c_str());
+      return 1;
+    }
+  }
+  check(athg_upload(ctx, -1, ATHG_VAR_CONS, U.data(), U.size()), "upload U");
+  if (mhd) {
+    check(athg_upload(ctx, -1, ATHG_VAR_B1F, B1.data(), B1.size()), "upload B1");
+    check(athg_upload(ctx, -1, ATHG_VAR_B2F, B2.data(), B2.size()), "upload B2");
+    check(athg_upload(ctx, -1, ATHG_VAR_B3F, B3.data(), B3.size()), "upload B3");
+  }
+  check(athg_initialize(ctx), "athg_initialize");
+
+  // history output (<output1> file_type = hst, dt)
+  const std::string base = get(p, "job/problem_id", pgen);
+  const double hst_dt = getd(p, "output1/dt", -1.0);
+  std::FILE* hst = std::fopen((base + ".hst").c_str(), "w");
+  std::fprintf(hst, "# Athena++ history data (athg_run)\n"
+                    "# [1]=time [2]=dt [3]=mass [4]=1-mom [5]=2-mom [6]=3-mom [7]=1-KE [8]=2-KE "
+                    "[9]=3-KE [10]=tot-E [11]=grav-E [12]=1-ME [13]=2-ME [14]=3-ME\n");
+  auto write_hst = [&]() {
+    double h[12], t, dt;
+    int n;
+    int64_t nc_;
+    check(athg_history(ctx, h, &n), "athg_history");
+    check(athg_get_time(ctx, &t, &dt, &nc_), "athg_get_time");
+    std::fprintf(hst, "%.14e %.14e", t, dt);
+    for (int q = 0; q < n; ++q) std::fprintf(hst, " %.14e", h[q]);
+    std::fprintf(hst, "\n");
+  };
+  write_hst();
+  double t, dt, next_hst = hst_dt;
+  int64_t ncycle = 0;
+  check(athg_get_time(ctx, &t, &dt, &ncycle), "athg_get_time");
+  const auto t0 = std::chrono::steady_clock::now();
+  int64_t cycles = 0;
+  while (t < c.tlim && (nlim < 0 || cycles < nlim)) {
+    check(athg_cycles(ctx, 1), "athg_cycles");
+    ++cycles;
+    check(athg_get_time(ctx, &t, &dt, &ncycle), "athg_get_time");
+    if (hst_dt > 0.0 && t >= next_hst) {
+      write_hst();
+      next_hst += hst_dt;
+    }
+  }
+  check(athg_synchronize(ctx), "athg_synchronize");
+  const double el = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  write_hst();
+  std::fclose(hst);
+  const double zones = (double)m.nx1 * m.nx2 * m.nx3;
+  // main.cpp:580-600 summary
+  std::printf("cycle=%lld time=%.10e dt=%.10e\n", (long long)ncycle, t, dt);
+  std::printf("zone-cycles = %.0f\nwall time = %.6f s\nzone-cycles/wsecond = %.6e\n",
+              zones * cycles, el, zones * cycles / el);
+  athg_destroy(ctx);
+  return 0;
+}
