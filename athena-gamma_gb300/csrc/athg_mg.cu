@@ -22,6 +22,7 @@
 
 #include "athena_gb300.h"
 #include "athg_internal.h"
+#include "athg_numeric.h"
 
 namespace athg {
 // the error channel of athg_last_error() (defined in athg_api.cu)
@@ -275,25 +276,33 @@ __global__ void k_bc_face(T* a, int n, int dir, FaceBC f, MpCoef mp) {
   const int nt = n + 2;
   int gi = side ? n + 1 : 0, si = side ? n : 1;
   long long g, s;
-  double px, py, pz;
   if (dir == 0) {
     g = ix(nt, a2, a1, gi); s = ix(nt, a2, a1, si);
-    px = xface(side ? n + 1 : 1, n, f.lo[0], f.hi[0]);
-    py = xcen(a1, n, f.lo[1], f.hi[1]); pz = xcen(a2, n, f.lo[2], f.hi[2]);
   } else if (dir == 1) {
     g = ix(nt, a2, gi, a1); s = ix(nt, a2, si, a1);
-    px = xcen(a1, n, f.lo[0], f.hi[0]);
-    py = xface(side ? n + 1 : 1, n, f.lo[1], f.hi[1]); pz = xcen(a2, n, f.lo[2], f.hi[2]);
   } else {
     g = ix(nt, gi, a2, a1); s = ix(nt, si, a2, a1);
-    px = xcen(a1, n, f.lo[0], f.hi[0]); py = xcen(a2, n, f.lo[1], f.hi[1]);
-    pz = xface(side ? n + 1 : 1, n, f.lo[2], f.hi[2]);
   }
   const int bc = f.type[side];
-  if (bc == ATHG_MG_ZEROGRAD) a[g] = a[s];
-  else if (bc == ATHG_MG_ZEROFIXED || (bc == ATHG_MG_MULTIPOLE && f.homogeneous)) a[g] = -a[s];
-  else if (bc == ATHG_MG_MULTIPOLE)
+  if (bc == ATHG_MG_ZEROGRAD) {
+    a[g] = a[s];
+  } else if (bc == ATHG_MG_ZEROFIXED || (bc == ATHG_MG_MULTIPOLE && f.homogeneous)) {
+    a[g] = -a[s];
+  } else if (bc == ATHG_MG_MULTIPOLE) {
+    // face-centre position (only here: the coordinates cost FP64 divisions)
+    double px, py, pz;
+    if (dir == 0) {
+      px = xface(side ? n + 1 : 1, n, f.lo[0], f.hi[0]);
+      py = xcen(a1, n, f.lo[1], f.hi[1]); pz = xcen(a2, n, f.lo[2], f.hi[2]);
+    } else if (dir == 1) {
+      px = xcen(a1, n, f.lo[0], f.hi[0]);
+      py = xface(side ? n + 1 : 1, n, f.lo[1], f.hi[1]); pz = xcen(a2, n, f.lo[2], f.hi[2]);
+    } else {
+      px = xcen(a1, n, f.lo[0], f.hi[0]); py = xcen(a2, n, f.lo[1], f.hi[1]);
+      pz = xface(side ? n + 1 : 1, n, f.lo[2], f.hi[2]);
+    }
     a[g] = (T)(2.0 * mp_phi(mp, px - mp.o[0], py - mp.o[1], pz - mp.o[2]) - (double)a[s]);
+  }
 }
 
 // ---- reductions (FP64 accumulation) ----
@@ -366,22 +375,23 @@ __global__ void k_defect_to32(const double* u, const double* src, int n, double 
   int j = (int)(r % n) + 1, k = (int)(r / n) + 1;
   const int nt = n + 2;
   const long long q = ix(nt, k, j, i), sk = (long long)nt * nt, sj = nt;
-  double d = (6.0 * u[q] - u[q + sk] - u[q + sj] - u[q + 1] - u[q - sk] - u[q - sj] - u[q - 1]) *
-                 idx2 + src[q];
-  r32[q] = (float)d;
+  // mixed path only: FP64 is 1/64 of the FP32 rate here, so the defect is formed with
+  // fused operations (7 FP64 instructions) and converted on the integer pipe
+  const double s = ((u[q + sk] + u[q - sk]) + (u[q + sj] + u[q - sj])) + (u[q + 1] + u[q - 1]);
+  r32[q] = athg::d2f_int(fma(fma(6.0, u[q], -s), idx2, src[q]));
 }
 
 __global__ void k_add_correction(double* u, const float* e, long long cnt) {
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t < cnt) u[t] += (double)e[t];
+  if (t < cnt) u[t] += athg::f2d_int(e[t]);
 }
 __global__ void k_widen(const float* a, double* b, long long cnt) {
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t < cnt) b[t] = (double)a[t];
+  if (t < cnt) b[t] = athg::f2d_int(a[t]);
 }
 __global__ void k_narrow(const double* a, float* b, long long cnt) {
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t < cnt) b[t] = (float)a[t];
+  if (t < cnt) b[t] = athg::d2f_int(a[t]);
 }
 
 // multipole moments (and the centre of mass) of the finest source, FP64
@@ -511,6 +521,12 @@ struct athg_mg {
   int coffset32 = 0;
   int iterations = 0;
   double last_norm = 0.0;
+  // one captured cycle per colour-offset parity (the kernels take colour ^ offset); the
+  // multipole coefficients are kernel arguments, so a new expansion invalidates them
+  cudaGraph_t cyc_graph[2] = {nullptr, nullptr};
+  cudaGraphExec_t cyc_exec[2] = {nullptr, nullptr};
+  int cyc_mp[2] = {-1, -1};
+  int mp_version = 0;
 };
 
 namespace {
@@ -734,6 +750,7 @@ int multipole_setup(athg_mg* m) {
   for (int q = 0; q < 25; ++q) m->mp.c[q] = q < nc ? mm[q] * sc[q] : 0.0;
   for (int d = 0; d < 3; ++d) m->mp.o[d] = origin[d];
   m->mp.order = c.mporder;
+  ++m->mp_version;
   return ATHG_OK;
 }
 
@@ -760,6 +777,42 @@ int one_cycle(athg_mg* m) {
   const int top = m->lmax;
   if (m->cfg.precision == ATHG_MIXED) return refine_once(m);
   return vcycle(m, m->h64, top, m->fas, false, m->subtract, m->coffset);
+}
+
+// one_cycle from a captured CUDA graph: the ~20-200 small launches of a V-cycle become one
+// graph launch. Not used while the stream is itself being captured (the self-gravity
+// solve inside a captured hydro cycle).
+int cycle(athg_mg* m) {
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  MCK(cudaStreamIsCapturing(m->st, &cs));
+  if (cs != cudaStreamCaptureStatusNone) return one_cycle(m);
+  const bool mixed = m->cfg.precision == ATHG_MIXED;
+  int& coff = mixed ? m->coffset32 : m->coffset;
+  const int par = coff & 1;
+  if (!m->cyc_exec[par] || m->cyc_mp[par] != m->mp_version) {
+    if (m->cyc_exec[par]) cudaGraphExecDestroy(m->cyc_exec[par]);
+    if (m->cyc_graph[par]) cudaGraphDestroy(m->cyc_graph[par]);
+    m->cyc_exec[par] = nullptr;
+    m->cyc_graph[par] = nullptr;
+    const int c32 = m->coffset32, c64 = m->coffset;
+    MCK(cudaStreamBeginCapture(m->st, cudaStreamCaptureModeThreadLocal));
+    int rc = one_cycle(m);
+    cudaGraph_t gr = nullptr;
+    cudaError_t e = cudaStreamEndCapture(m->st, &gr);
+    m->coffset32 = c32;
+    m->coffset = c64;
+    if (rc) {
+      if (gr) cudaGraphDestroy(gr);
+      return rc;
+    }
+    if (e != cudaSuccess) return mgfail(ATHG_ERR_CUDA, "multigrid cycle capture failed");
+    m->cyc_graph[par] = gr;
+    MCK(cudaGraphInstantiate(&m->cyc_exec[par], gr, 0));
+    m->cyc_mp[par] = m->mp_version;
+  }
+  MCK(cudaGraphLaunch(m->cyc_exec[par], m->st));
+  coff ^= 1;  // what the captured cycle did to the host-side colour offset
+  return ATHG_OK;
 }
 
 }  // namespace
@@ -832,6 +885,10 @@ int athg_mg_destroy(athg_mg* m) {
   free_hier(m->h32);
   if (m->red) cudaFree(m->red);
   if (m->mpo_d) cudaFree(m->mpo_d);
+  for (int q = 0; q < 2; ++q) {
+    if (m->cyc_exec[q]) cudaGraphExecDestroy(m->cyc_exec[q]);
+    if (m->cyc_graph[q]) cudaGraphDestroy(m->cyc_graph[q]);
+  }
   if (m->own_st) cudaStreamDestroy(m->own_st);
   delete m;
   return ATHG_OK;
@@ -928,7 +985,7 @@ int mg_solve(athg_mg* m, bool want_norm, int* iterations, double* defect_norm) {
     RC(defect_norm64(m, &def));
     int nit = 0;
     while (def > m->cfg.threshold) {
-      RC(one_cycle(m));
+      RC(cycle(m));
       m->iterations++;
       double old = def;
       RC(defect_norm64(m, &def));
@@ -938,7 +995,7 @@ int mg_solve(athg_mg* m, bool want_norm, int* iterations, double* defect_norm) {
     }
   } else {
     for (int q = 0; q < m->cfg.niteration; ++q) {
-      RC(one_cycle(m));
+      RC(cycle(m));
       m->iterations++;
     }
     if (want_norm) RC(defect_norm64(m, &def));
@@ -963,7 +1020,7 @@ int athg_mg_solve(athg_mg* m, int* iterations, double* defect_norm) {
 
 int athg_mg_vcycles(athg_mg* m, int n) {
   if (!m) return mgfail(ATHG_ERR_ARG, "null argument");
-  for (int q = 0; q < n; ++q) RC(one_cycle(m));
+  for (int q = 0; q < n; ++q) RC(cycle(m));
   return ATHG_OK;
 }
 
