@@ -301,8 +301,7 @@ void free_pool(athg_ctx* c) {
 int launch_ghosts(athg_ctx* c) {
   GhostPtrs gp{c->u, c->b1, c->b2, c->b3, c->nbr, NHYD, c->cfg.magnetic};
   const Geom& g = c->g;
-  dim3 grid((unsigned)(((g.nc1 + 1) * (g.nc2 + 1) + 255) / 256), (unsigned)(g.nc3 + 1),
-            (unsigned)c->nb);
+  dim3 grid((unsigned)((ghost_shell_size(g) + 255) / 256), (unsigned)c->nb);
   k_ghost_same_level<<<grid, 256, 0, c->st>>>(g, gp);
   c->counting += 1;
   CKL();
@@ -452,13 +451,15 @@ void swap_state(athg_ctx* c) {
   std::swap(c->b3, c->r3);
 }
 
-int launch_update_c2p(athg_ctx* c, int l) {
+// dt_too: the last stage also reduces the CFL time step (k_block_dt folded in)
+int launch_update_c2p(athg_ctx* c, int l, bool dt_too) {
   StageW sw = stage_weights(c, l);
   StateBufs sb;
   sb.u_in = c->u; sb.u_out = c->u1;
   sb.b_in[0] = c->b1; sb.b_in[1] = c->b2; sb.b_in[2] = c->b3;
   sb.b_out[0] = c->r1; sb.b_out[1] = c->r2; sb.b_out[2] = c->r3;
-  Launcher<float>::update_c2p(c->g, ptrs<float>(c), c->cfg.magnetic != 0, sw, phys(c), sb, c->st);
+  Launcher<float>::update_c2p(c->g, ptrs<float>(c), c->cfg.magnetic != 0, sw, phys(c), sb,
+                              dt_too ? (unsigned long long*)(c->scal + 3) : nullptr, c->st);
   c->counting += 1;
   CKL();
   return ATHG_OK;
@@ -473,8 +474,7 @@ int launch_ghosts_f32(athg_ctx* c) {
   gp.cell[2] = mhd ? c->cce : nullptr; gp.ncomp[2] = 3;
   for (int d = 0; d < 3; ++d) gp.face[d] = mhd ? c->bf32[d] : nullptr;
   gp.nbr = c->nbr;
-  dim3 grid((unsigned)(((g.nc1 + 1) * (g.nc2 + 1) + 255) / 256), (unsigned)(g.nc3 + 1),
-            (unsigned)c->nb);
+  dim3 grid((unsigned)((ghost_shell_size(g) + 255) / 256), (unsigned)c->nb);
   if (mhd) k_ghost_f32<true><<<grid, 256, 0, c->st>>>(g, gp);
   else k_ghost_f32<false><<<grid, 256, 0, c->st>>>(g, gp);
   c->counting += 1;
@@ -518,10 +518,8 @@ int do_stage(athg_ctx* c, int stage) {
   if (fused(c)) {
     if ((rc = launch_fluxes(c, order))) return rc;
     if ((rc = launch_corner(c))) return rc;
-    if ((rc = launch_update_c2p(c, l))) return rc;
+    if ((rc = launch_update_c2p(c, l, stage == c->integ.nstages))) return rc;
     if ((rc = launch_ghosts_f32(c))) return rc;
-    if (stage == c->integ.nstages)
-      if ((rc = launch_block_dt(c))) return rc;
     c->ghosts_stale = true;
     return ATHG_OK;
   }

@@ -26,13 +26,50 @@ __device__ __forceinline__ int ghost_dir(int i, int s, int e) {
   return i < s ? -1 : (i > e ? 1 : 0);
 }
 
+// The positions (k,j,i) of [0,nc3]x[0,nc2]x[0,nc1] (the edge-sized box, so the last face
+// of each axis is included) that hold any ghost value, as three disjoint regions: A, the
+// k-ghost planes; B, the j-ghost rows of the interior planes; C, the i-ghost columns of the
+// interior rows. One thread per position of the ghost shell instead of the whole box.
+__host__ __device__ inline int64_t ghost_shell_size(const Geom& g) {
+  const int64_t gk = g.nc3 + 1 - g.nx3, gj = g.nc2 + 1 - g.nx2, gi = g.nc1 + 1 - g.nx1;
+  return gk * (g.nc2 + 1) * (g.nc1 + 1) + (int64_t)g.nx3 * gj * (g.nc1 + 1) +
+         (int64_t)g.nx3 * g.nx2 * gi;
+}
+__device__ __forceinline__ void ghost_shell_pos(const Geom& g, int64_t t, int& k, int& j, int& i) {
+  const int gk = g.nc3 + 1 - g.nx3, gj = g.nc2 + 1 - g.nx2, gi = g.nc1 + 1 - g.nx1;
+  const int64_t na = (int64_t)gk * (g.nc2 + 1) * (g.nc1 + 1);
+  const int64_t nbb = (int64_t)g.nx3 * gj * (g.nc1 + 1);
+  if (t < na) {
+    i = (int)(t % (g.nc1 + 1));
+    const int64_t r = t / (g.nc1 + 1);
+    j = (int)(r % (g.nc2 + 1));
+    const int q = (int)(r / (g.nc2 + 1));
+    k = q < g.ks ? q : q + g.nx3;  // 0..ks-1, then ke+1..nc3
+  } else if (t < na + nbb) {
+    const int64_t u = t - na;
+    i = (int)(u % (g.nc1 + 1));
+    const int64_t r = u / (g.nc1 + 1);
+    const int q = (int)(r % gj);
+    j = q < g.js ? q : q + g.nx2;
+    k = g.ks + (int)(r / gj);
+  } else {
+    const int64_t u = t - na - nbb;
+    const int q = (int)(u % gi);
+    i = q < g.is ? q : q + g.nx1;
+    const int64_t r = u / gi;
+    j = g.js + (int)(r % g.nx2);
+    k = g.ks + (int)(r / g.nx2);
+  }
+}
+
 // One thread per (k,j,i) of the largest (edge-sized) box of every block; each thread
 // handles the cell and the three faces that share this index, when they are ghosts.
 __global__ void __launch_bounds__(256) k_ghost_same_level(Geom g, GhostPtrs p) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  const int n1 = g.nc1 + 1, n2 = g.nc2 + 1;
-  if (t >= n1 * n2) return;
-  const int j = t / n1, i = t - j * n1, k = blockIdx.y, b = blockIdx.z;
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= ghost_shell_size(g)) return;
+  int k, j, i;
+  ghost_shell_pos(g, t, k, j, i);
+  const int b = blockIdx.y;
   const int* nb = p.nbr + (int64_t)b * 27;
   // cell-centred variables
   if (i < g.nc1 && j < g.nc2 && k < g.nc3) {
@@ -96,10 +133,11 @@ struct GhostPtrs32 {
 // never a ghost, so loads and stores never overlap), keeping all of a thread's loads in flight.
 template <bool MHD>
 __global__ void __launch_bounds__(256) k_ghost_f32(Geom g, GhostPtrs32 p) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  const int n1 = g.nc1 + 1, n2 = g.nc2 + 1;
-  if (t >= n1 * n2) return;
-  const int j = t / n1, i = t - j * n1, k = blockIdx.y, b = blockIdx.z;
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= ghost_shell_size(g)) return;
+  int k, j, i;
+  ghost_shell_pos(g, t, k, j, i);
+  const int b = blockIdx.y;
   const int* nb = p.nbr + (int64_t)b * 27;
   const int64_t nc = g.ncell;
   constexpr int NV = MHD ? 11 : 5;

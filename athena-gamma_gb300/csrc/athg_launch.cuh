@@ -34,7 +34,8 @@ struct Launcher {
   // Mixed VL2: update + interior primitive recovery from `sb.in` into `sb.out`
   // (k_update_c2p; no-op for the FP64 path, which never takes this route).
   static void update_c2p(const Geom& g, const StagePtrs<T>& p, bool mhd, const StageW& sw,
-                         const Phys& ph, const StateBufs& sb, cudaStream_t st);
+                         const Phys& ph, const StateBufs& sb, unsigned long long* dtmin,
+                         cudaStream_t st);
   // HydroSourceTerms::SelfGravity over every block (phi: [nb][cells] potential).
   static void self_gravity(const Geom& g, const StagePtrs<T>& p, bool mhd, const StageW& sw,
                            const double* phi, cudaStream_t st);
@@ -130,11 +131,18 @@ void Launcher<T>::update(const Geom& g, const StagePtrs<T>& p, bool mhd, const S
 
 template <typename T>
 void Launcher<T>::update_c2p(const Geom& g, const StagePtrs<T>& p, bool mhd, const StageW& sw,
-                             const Phys& ph, const StateBufs& sb, cudaStream_t st) {
+                             const Phys& ph, const StateBufs& sb, unsigned long long* dtmin,
+                             cudaStream_t st) {
   if constexpr (kMixed<T>) {
     Box b = make_box(g.is, g.ie, g.js, g.je, g.ks, g.ke);
-    if (mhd) k_update_c2p<true><<<box_grid(b, g.nb, 128), 128, 0, st>>>(g, p, b, sw, ph, sb);
-    else k_update_c2p<false><<<box_grid(b, g.nb, 128), 128, 0, st>>>(g, p, b, sw, ph, sb);
+    const dim3 gr = box_grid(b, g.nb, 128);
+    if (mhd) {
+      if (dtmin) k_update_c2p<true, true><<<gr, 128, 0, st>>>(g, p, b, sw, ph, sb, dtmin);
+      else k_update_c2p<true, false><<<gr, 128, 0, st>>>(g, p, b, sw, ph, sb, dtmin);
+    } else {
+      if (dtmin) k_update_c2p<false, true><<<gr, 128, 0, st>>>(g, p, b, sw, ph, sb, dtmin);
+      else k_update_c2p<false, false><<<gr, 128, 0, st>>>(g, p, b, sw, ph, sb, dtmin);
+    }
   }
 }
 

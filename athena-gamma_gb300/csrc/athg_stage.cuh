@@ -801,11 +801,12 @@ struct StateBufs {
   double* b_out[3];
 };
 
-template <bool MHD>
-__global__ void __launch_bounds__(128, 8)
-k_update_c2p(Geom g, StagePtrs<float> p, Box bx, StageW sw, Phys ph, StateBufs sb) {
-  int i, j, k, b;
-  if (!box_coords(bx, i, j, k, b)) return;
+// One cell of k_update_c2p; returns the cell's CFL time step (new_blockdt.cpp:58-158,
+// as k_block_dt computes it) when DT, so the last stage folds the time-step kernel in.
+template <bool MHD, bool DT>
+__device__ __forceinline__ float update_c2p_cell(const Geom& g, const StagePtrs<float>& p,
+                                                 int i, int j, int k, int b, const StageW& sw,
+                                                 const Phys& ph, const StateBufs& sb) {
   const MixedGeo mg = p.mg[b];
   const float wf = __fmul_rn(sw.betaf, __ldg(p.dtT));
   const int64_t nc = g.ncell;
@@ -868,6 +869,7 @@ k_update_c2p(Geom g, StagePtrs<float> p, Box bx, StageW sw, Phys ph, StateBufs s
   }
   ff ss = {0.0f, 0.0f};
   float* __restrict__ bcc = p.bcc + (int64_t)b * 3 * nc;
+  float fl32[3] = {0.0f, 0.0f, 0.0f};  // FP32 copies of the lower faces
   if constexpr (MHD) {
     const float we1 = __fmul_rn(wf, mg.dx[0]), we2 = __fmul_rn(wf, mg.dx[1]),
                 we3 = __fmul_rn(wf, mg.dx[2]);
@@ -893,6 +895,7 @@ k_update_c2p(Geom g, StagePtrs<float> p, Box bx, StageW sw, Phys ph, StateBufs s
     p.bfw[0][fl[0]] = f1.hi;
     p.bfw[1][fl[1]] = f2.hi;
     p.bfw[2][fl[2]] = f3.hi;
+    fl32[0] = f1.hi; fl32[1] = f2.hi; fl32[2] = f3.hi;
     const ff u1f = split_ff(n1u), u2f = split_ff(n2u), u3f = split_ff(n3u);
     if (i == g.ie) { sb.b_out[0][fu[0]] = n1u; p.bfw[0][fu[0]] = u1f.hi; }
     if (j == g.je) { sb.b_out[1][fu[1]] = n2u; p.bfw[1][fu[1]] = u2f.hi; }
@@ -934,12 +937,58 @@ k_update_c2p(Geom g, StagePtrs<float> p, Box bx, StageW sw, Phys ph, StateBufs s
   w[2 * nc + c] = vy;
   w[3 * nc + c] = vz;
   w[4 * nc + c] = pf;
+  float bx = 0.0f, by = 0.0f, bz = 0.0f;
   if constexpr (MHD) {
-    const float bx = bcc[c], by = bcc[nc + c], bz = bcc[2 * nc + c];
+    bx = bcc[c]; by = bcc[nc + c]; bz = bcc[2 * nc + c];
     float* __restrict__ ce = p.cce + (int64_t)b * 3 * nc;
     ce[c] = vz * by - vy * bz;
     ce[nc + c] = vx * bz - vz * bx;
     ce[2 * nc + c] = vy * bx - vx * by;
+  }
+  if constexpr (DT) {
+    const float dx1 = p.dxT[b * 3], dx2 = p.dxT[b * 3 + 1], dx3 = p.dxT[b * 3 + 2];
+    const float gam = ph.gammas, d = dd.hi;
+    float dt1, dt2, dt3;
+    if constexpr (MHD) {
+      float cf = fast_speed<float>(d, pf, by, bz, bx + fabsf(fl32[0] - bx), gam);
+      dt1 = dx1 / (fabsf(vx) + cf);
+      cf = fast_speed<float>(d, pf, bz, bx, by + fabsf(fl32[1] - by), gam);
+      dt2 = dx2 / (fabsf(vy) + cf);
+      cf = fast_speed<float>(d, pf, bx, by, bz + fabsf(fl32[2] - bz), gam);
+      dt3 = dx3 / (fabsf(vz) + cf);
+    } else {
+      const float cs = sqrtf(gam * pf / d);
+      dt1 = dx1 / (fabsf(vx) + cs);
+      dt2 = dx2 / (fabsf(vy) + cs);
+      dt3 = dx3 / (fabsf(vz) + cs);
+    }
+    return mn(mn(mn(3.402823466e38f, dt1), dt2), dt3);
+  }
+  return 3.402823466e38f;
+}
+
+template <bool MHD, bool DT>
+__global__ void __launch_bounds__(128, 8)
+k_update_c2p(Geom g, StagePtrs<float> p, Box bx, StageW sw, Phys ph, StateBufs sb,
+             unsigned long long* dtmin) {
+  int i, j, k, b;
+  const bool active = box_coords(bx, i, j, k, b);
+  float mindt = 3.402823466e38f;
+  if (active) mindt = update_c2p_cell<MHD, DT>(g, p, i, j, k, b, sw, ph, sb);
+  if constexpr (DT) {  // block minimum, then one 64-bit atomicMin (as k_block_dt)
+    for (int o = 16; o > 0; o >>= 1) mindt = mn(mindt, __shfl_xor_sync(0xffffffffu, mindt, o));
+    __shared__ float red[32];
+    const int tid = threadIdx.x;
+    if ((tid & 31) == 0) red[tid >> 5] = mindt;
+    __syncthreads();
+    if (tid < 32) {
+      float v = (tid < (int)((blockDim.x + 31) / 32)) ? red[tid] : 3.402823466e38f;
+      for (int o = 16; o > 0; o >>= 1) v = mn(v, __shfl_xor_sync(0xffffffffu, v, o));
+      if (tid == 0) {
+        const double vd = (v == 3.402823466e38f) ? 1.79769313486231570815e308 : f2d_int(v);
+        atomicMin(dtmin, (unsigned long long)__double_as_longlong(vd));
+      }
+    }
   }
 }
 

@@ -210,6 +210,25 @@ def run_mg(athg, torch, vcycles=5):
     return out
 
 
+def run_mg_profile(prec, bc, n):
+    import torch
+    import athg
+    n = int(n)
+    x = (np.arange(n) + 0.5) / n - 0.5
+    r2 = x[None, None, :] ** 2 + x[None, :, None] ** 2 + x[:, None, None] ** 2
+    rho = np.where(r2 < 0.0625, 1.0, 1.0e-6)
+    mg = athg.Multigrid(n, bc=bc, mporder=4, mode="FMG", threshold=-1.0, niteration=2,
+                        precision=prec)
+    mg.load_source(rho, 4.0 * np.pi)
+    mg.solve()
+    torch.cuda.synchronize()
+    torch.cuda.profiler.start()
+    mg.vcycles(1)
+    torch.cuda.synchronize()
+    torch.cuda.profiler.stop()
+    mg.close()
+
+
 def run_c5(args):
     """Magnetised self-gravitating turbulent box (PLM + HLLD + VL2, gamma = 1.0001, beta = 1,
     rms Mach 5, Jeans number 2) with a multigrid solve after every stage; prints its own
@@ -349,6 +368,9 @@ def main():
     ap.add_argument("--nx", type=int, default=256, help="cells per side (profiling: 128)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-mg", action="store_true")
+    ap.add_argument("--mg-profile", nargs=3, metavar=("PREC", "BC", "N"), default=None,
+                    help="profiling run: solve the uniform sphere once, then one V-cycle "
+                         "between cudaProfilerStart/Stop (for ncu --profile-from-start off)")
     ap.add_argument("--c5", action="store_true",
                     help="self-gravitating turbulent box instead of the headline workload")
     ap.add_argument("--c5-nx", type=int, default=512)
@@ -361,6 +383,8 @@ def main():
         return run_reference(args)
     if args.c5:
         return run_c5(args)
+    if args.mg_profile:
+        return run_mg_profile(*args.mg_profile)
 
     import torch
     import athg
