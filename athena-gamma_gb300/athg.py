@@ -35,6 +35,7 @@ EXPORTS = [
     "athg_mg_create", "athg_mg_destroy", "athg_mg_load_source", "athg_mg_set_phi",
     "athg_mg_solve", "athg_mg_vcycles", "athg_mg_defect_norm", "athg_mg_get_phi",
     "athg_mg_stream", "athg_mg_multipole", "athg_attach_gravity", "athg_history",
+    "athg_get_tuning", "athg_set_tuning",
     "athg_block_cfl_dt_noalloc",
 ]
 MG_BC = {"periodic": 0, "zerograd": 1, "zerofixed": 2, "multipole": 3}
@@ -119,6 +120,8 @@ def lib():
         "athg_mg_multipole": [vp, C.POINTER(d)],
         "athg_attach_gravity": [vp, vp, d],
         "athg_history": [vp, C.POINTER(d), C.POINTER(i)],
+        "athg_get_tuning": [vp, C.POINTER(i)],
+        "athg_set_tuning": [vp, C.POINTER(i)],
         "athg_block_cfl_dt_noalloc": [C.POINTER(Config), vp, vp, vp, vp, vp, d, d, d, vp, vp],
     }
     for name, args in sig.items():
@@ -308,6 +311,16 @@ class Sim:
         v = C.c_double()
         check(lib().athg_new_block_dt(self.h, C.byref(v)))
         return v.value
+
+    def tuning(self):
+        """(x1 threads per block, marching threads per block, faces per segment)."""
+        a = (C.c_int * 3)()
+        check(lib().athg_get_tuning(self.h, a))
+        return tuple(a)
+
+    def set_tuning(self, x1_tpb, march_tpb, seg):
+        a = (C.c_int * 3)(x1_tpb, march_tpb, seg)
+        check(lib().athg_set_tuning(self.h, a))
 
     def history(self):
         """The 12 history sums of outputs/history.cpp, reduced on the device."""

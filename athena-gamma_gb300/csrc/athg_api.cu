@@ -1,5 +1,6 @@
 // athg_api.cu -- the C ABI: context, device block pool, stage sequencing and the
 // CUDA-graph cycle. Declarations and reference interfaces: include/athena_gb300.h.
+#include <algorithm>
 #include <cmath>
 #include <type_traits>
 #include <utility>
@@ -226,6 +227,8 @@ struct athg_ctx {
   cudaGraph_t graph2 = nullptr;
   cudaGraphExec_t gexec2 = nullptr;
   const double* graph_src = nullptr;  // state buffer the first captured cycle reads
+  FluxTune tune;        // launch shape of the flux sweeps
+  bool tuned = false;   // autotuned (or set by the caller)
   int launches_per_cycle = 0;
   int counting = 0;
   // self-gravity (SELF_GRAVITY_ENABLED == 2): coupled multigrid solver, 4 pi G, the
@@ -311,9 +314,11 @@ int launch_ghosts(athg_ctx* c) {
 int launch_fluxes(athg_ctx* c, int order) {
   bool mhd = c->cfg.magnetic != 0;
   if (c->mixed())
-    Launcher<float>::fluxes(c->g, ptrs<float>(c), mhd, c->cfg.rsolver, order, phys(c), c->st);
+    Launcher<float>::fluxes(c->g, ptrs<float>(c), mhd, c->cfg.rsolver, order, phys(c), c->tune,
+                            c->st);
   else
-    Launcher<double>::fluxes(c->g, ptrs<double>(c), mhd, c->cfg.rsolver, order, phys(c), c->st);
+    Launcher<double>::fluxes(c->g, ptrs<double>(c), mhd, c->cfg.rsolver, order, phys(c),
+                             c->tune, c->st);
   c->counting += 3;
   CKL();
   return ATHG_OK;
@@ -572,8 +577,59 @@ int capture_cycle(athg_ctx* c, cudaGraph_t* graph, cudaGraphExec_t* exec) {
   return ATHG_OK;
 }
 
+// Autotuner of the flux sweeps' launch shape (threads per block of the x1 and marching
+// sweeps, faces per marching segment): every candidate runs the three sweeps of one stage
+// on the context's own state (they only write the flux arrays) three times, timed with
+// CUDA events on the context's stream; the fastest median wins. Mixed path only (the FP64
+// path is the reference-order check, not the fast path); runs once, before the first
+// captured cycle.
+int autotune(athg_ctx* c) {
+  if (c->tuned || !c->mixed()) return ATHG_OK;
+  c->tuned = true;
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  CK(cudaStreamIsCapturing(c->st, &cs));
+  if (cs != cudaStreamCaptureStatusNone) return ATHG_OK;
+  const int tpbs[2] = {64, 128}, segs[4] = {8, 16, 32, 0};
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  const bool mhd = c->cfg.magnetic != 0;
+  const int saved = c->counting;
+  FluxTune best = c->tune;
+  float best_ms = 1e30f;
+  int rc = ATHG_OK;
+  for (int a = 0; a < 2 && !rc; ++a)
+    for (int m = 0; m < 2 && !rc; ++m)
+      for (int q = 0; q < 4 && !rc; ++q) {
+        FluxTune t;
+        t.x1_tpb = tpbs[a]; t.march_tpb = tpbs[m]; t.seg = segs[q];
+        float ms[3];
+        for (int r = 0; r < 3; ++r) {
+          cudaEventRecord(e0, c->st);
+          Launcher<float>::fluxes(c->g, ptrs<float>(c), mhd, c->cfg.rsolver, c->cfg.xorder,
+                                  phys(c), t, c->st);
+          cudaEventRecord(e1, c->st);
+          if (cudaEventSynchronize(e1) != cudaSuccess || cudaGetLastError() != cudaSuccess) {
+            rc = fail(ATHG_ERR_CUDA, "autotune launch failed");
+            break;
+          }
+          cudaEventElapsedTime(&ms[r], e0, e1);
+        }
+        if (rc) break;
+        std::sort(ms, ms + 3);
+        if (ms[1] < best_ms) { best_ms = ms[1]; best = t; }
+      }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  c->counting = saved;
+  if (!rc) c->tune = best;
+  return rc;
+}
+
 int build_graph(athg_ctx* c) {
   if (c->gexec) return ATHG_OK;
+  int trc = autotune(c);
+  if (trc) return trc;
   int rc = capture_cycle(c, &c->graph, &c->gexec);
   if (rc) return rc;
   c->graph_src = c->u;
@@ -1190,6 +1246,26 @@ int athg_sum_conserved(athg_ctx* c, double* out5) {
   CKL();
   CK(cudaMemcpyAsync(out5, c->scal + 4, 5 * 8, cudaMemcpyDeviceToHost, c->st));
   CK(cudaStreamSynchronize(c->st));
+  return ATHG_OK;
+}
+
+int athg_get_tuning(athg_ctx* c, int* out3) {
+  int rc = need_pool(c);
+  if (rc) return rc;
+  if (!out3) return fail(ATHG_ERR_ARG, "null argument");
+  out3[0] = c->tune.x1_tpb; out3[1] = c->tune.march_tpb; out3[2] = c->tune.seg;
+  return ATHG_OK;
+}
+
+int athg_set_tuning(athg_ctx* c, const int* in3) {
+  int rc = need_pool(c);
+  if (rc) return rc;
+  if (!in3) return fail(ATHG_ERR_ARG, "null argument");
+  if ((in3[0] != 64 && in3[0] != 128) || (in3[1] != 64 && in3[1] != 128) || in3[2] < 0)
+    return fail(ATHG_ERR_ARG, "threads per block must be 64 or 128, segment length >= 0");
+  drop_graphs(c);  // captured cycles hold the old launch shape
+  c->tune.x1_tpb = in3[0]; c->tune.march_tpb = in3[1]; c->tune.seg = in3[2];
+  c->tuned = true;
   return ATHG_OK;
 }
 

@@ -18,11 +18,20 @@ inline dim3 box_grid(const Box& b, int nblocks, int tpb) {
   return dim3((unsigned)((b.ni * b.nj + tpb - 1) / tpb), (unsigned)b.nk, (unsigned)nblocks);
 }
 
+// Launch shape of the flux sweeps, picked per context by the autotuner in athg_api.cu:
+// threads per block of the x1 sweep and of the marching sweeps, and the faces per segment of
+// a marching pencil (0: whole pencil).
+struct FluxTune {
+  int x1_tpb = 128;
+  int march_tpb = 128;
+  int seg = 16;
+};
+
 template <typename T>
 struct Launcher {
   // Hydro::CalculateFluxes over every block: three directional sweeps.
   static void fluxes(const Geom& g, const StagePtrs<T>& p, bool mhd, int solver, int order,
-                     const Phys& ph, cudaStream_t st);
+                     const Phys& ph, const FluxTune& tune, cudaStream_t st);
   // Field::ComputeCornerE over every block.
   static void corner_emf(const Geom& g, const StagePtrs<T>& p, cudaStream_t st);
   // IntegrateHydro + IntegrateField (register average, flux divergence, CT).
@@ -47,7 +56,7 @@ struct Launcher {
 #ifdef ATHG_LAUNCH_IMPL
 template <typename T, int DIR, int ORDER>
 static void flux_dir(const Geom& g, const StagePtrs<T>& p, bool mhd, int solver,
-                     const Phys& ph, cudaStream_t st) {
+                     const Phys& ph, const FluxTune& tune, cudaStream_t st) {
   int il = g.is, iu = g.ie, jl = g.js, ju = g.je, kl = g.ks, ku = g.ke;
   if (DIR == 0) {
     iu = g.ie + 1;
@@ -63,54 +72,56 @@ static void flux_dir(const Geom& g, const StagePtrs<T>& p, bool mhd, int solver,
     // marching sweeps: pencils over (i, k) for DIR=1 and (i, j) for DIR=2
     Box pb = DIR == 1 ? make_box(il, iu, kl, ku, 0, 0) : make_box(il, iu, jl, ju, 0, 0);
     const int fs = DIR == 1 ? jl : kl, fe = DIR == 1 ? ju : ku;
-    // pencils split into segments of ~16 faces
-    const unsigned nseg = (unsigned)std::max(1, (fe - fs + 1) / 16);
-    dim3 grid((unsigned)((pb.ni * pb.nj + 127) / 128), nseg, (unsigned)g.nb);
+    // pencils split into segments of ~tune.seg faces
+    const unsigned nseg = tune.seg > 0 ? (unsigned)std::max(1, (fe - fs + 1) / tune.seg) : 1u;
+    const int tpb = tune.march_tpb;
+    dim3 grid((unsigned)((pb.ni * pb.nj + tpb - 1) / tpb), nseg, (unsigned)g.nb);
     if (mhd) {
       if (solver == HLLD)
-        k_flux_march<T, DIR, ORDER, HLLD, true><<<grid, 128, 0, st>>>(g, p, pb, ph, fs, fe);
+        k_flux_march<T, DIR, ORDER, HLLD, true><<<grid, tpb, 0, st>>>(g, p, pb, ph, fs, fe);
       else if (solver == LHLLD)
-        k_flux_march<T, DIR, ORDER, LHLLD, true><<<grid, 128, 0, st>>>(g, p, pb, ph, fs, fe);
+        k_flux_march<T, DIR, ORDER, LHLLD, true><<<grid, tpb, 0, st>>>(g, p, pb, ph, fs, fe);
       else
-        k_flux_march<T, DIR, ORDER, HLLE, true><<<grid, 128, 0, st>>>(g, p, pb, ph, fs, fe);
+        k_flux_march<T, DIR, ORDER, HLLE, true><<<grid, tpb, 0, st>>>(g, p, pb, ph, fs, fe);
     } else {
       if (solver == HLLC)
-        k_flux_march<T, DIR, ORDER, HLLC, false><<<grid, 128, 0, st>>>(g, p, pb, ph, fs, fe);
+        k_flux_march<T, DIR, ORDER, HLLC, false><<<grid, tpb, 0, st>>>(g, p, pb, ph, fs, fe);
       else if (solver == LHLLC)
-        k_flux_march<T, DIR, ORDER, LHLLC, false><<<grid, 128, 0, st>>>(g, p, pb, ph, fs, fe);
+        k_flux_march<T, DIR, ORDER, LHLLC, false><<<grid, tpb, 0, st>>>(g, p, pb, ph, fs, fe);
       else
-        k_flux_march<T, DIR, ORDER, HLLE, false><<<grid, 128, 0, st>>>(g, p, pb, ph, fs, fe);
+        k_flux_march<T, DIR, ORDER, HLLE, false><<<grid, tpb, 0, st>>>(g, p, pb, ph, fs, fe);
     }
   } else {
   Box b = make_box(il, iu, jl, ju, kl, ku);
-  dim3 grid = box_grid(b, g.nb, 128);
+  const int tpb = tune.x1_tpb;
+  dim3 grid = box_grid(b, g.nb, tpb);
   if (mhd) {
-    if (solver == HLLD) k_flux<T, DIR, ORDER, HLLD, true><<<grid, 128, 0, st>>>(g, p, b, ph);
-    else if (solver == LHLLD) k_flux<T, DIR, ORDER, LHLLD, true><<<grid, 128, 0, st>>>(g, p, b, ph);
-    else k_flux<T, DIR, ORDER, HLLE, true><<<grid, 128, 0, st>>>(g, p, b, ph);
+    if (solver == HLLD) k_flux<T, DIR, ORDER, HLLD, true><<<grid, tpb, 0, st>>>(g, p, b, ph);
+    else if (solver == LHLLD) k_flux<T, DIR, ORDER, LHLLD, true><<<grid, tpb, 0, st>>>(g, p, b, ph);
+    else k_flux<T, DIR, ORDER, HLLE, true><<<grid, tpb, 0, st>>>(g, p, b, ph);
   } else {
-    if (solver == HLLC) k_flux<T, DIR, ORDER, HLLC, false><<<grid, 128, 0, st>>>(g, p, b, ph);
-    else if (solver == LHLLC) k_flux<T, DIR, ORDER, LHLLC, false><<<grid, 128, 0, st>>>(g, p, b, ph);
-    else k_flux<T, DIR, ORDER, HLLE, false><<<grid, 128, 0, st>>>(g, p, b, ph);
+    if (solver == HLLC) k_flux<T, DIR, ORDER, HLLC, false><<<grid, tpb, 0, st>>>(g, p, b, ph);
+    else if (solver == LHLLC) k_flux<T, DIR, ORDER, LHLLC, false><<<grid, tpb, 0, st>>>(g, p, b, ph);
+    else k_flux<T, DIR, ORDER, HLLE, false><<<grid, tpb, 0, st>>>(g, p, b, ph);
   }
   }
 }
 
 template <typename T>
 void Launcher<T>::fluxes(const Geom& g, const StagePtrs<T>& p, bool mhd, int solver,
-                         int order, const Phys& ph, cudaStream_t st) {
+                         int order, const Phys& ph, const FluxTune& tune, cudaStream_t st) {
   if (order == 1) {
-    flux_dir<T, 0, 1>(g, p, mhd, solver, ph, st);
-    flux_dir<T, 1, 1>(g, p, mhd, solver, ph, st);
-    flux_dir<T, 2, 1>(g, p, mhd, solver, ph, st);
+    flux_dir<T, 0, 1>(g, p, mhd, solver, ph, tune, st);
+    flux_dir<T, 1, 1>(g, p, mhd, solver, ph, tune, st);
+    flux_dir<T, 2, 1>(g, p, mhd, solver, ph, tune, st);
   } else if (order == 3) {
-    flux_dir<T, 0, 3>(g, p, mhd, solver, ph, st);
-    flux_dir<T, 1, 3>(g, p, mhd, solver, ph, st);
-    flux_dir<T, 2, 3>(g, p, mhd, solver, ph, st);
+    flux_dir<T, 0, 3>(g, p, mhd, solver, ph, tune, st);
+    flux_dir<T, 1, 3>(g, p, mhd, solver, ph, tune, st);
+    flux_dir<T, 2, 3>(g, p, mhd, solver, ph, tune, st);
   } else {
-    flux_dir<T, 0, 2>(g, p, mhd, solver, ph, st);
-    flux_dir<T, 1, 2>(g, p, mhd, solver, ph, st);
-    flux_dir<T, 2, 2>(g, p, mhd, solver, ph, st);
+    flux_dir<T, 0, 2>(g, p, mhd, solver, ph, tune, st);
+    flux_dir<T, 1, 2>(g, p, mhd, solver, ph, tune, st);
+    flux_dir<T, 2, 2>(g, p, mhd, solver, ph, tune, st);
   }
 }
 

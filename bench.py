@@ -418,6 +418,7 @@ def main():
         el = max_over_ranks(torch, el, world, "cuda")
         res[prec] = {"el": el, "steps": steps, "zcps": replica_throughput(zones, steps, world, el),
                      "launches": sim.launches_per_cycle(), "clocks": clk,
+                     "tuning": sim.tuning(),
                      "t": sim.get_time(), "divb": sim.max_div_b()}
         sim.close()
         del sim
@@ -474,6 +475,8 @@ def main():
         "config": {"workload": WORKLOAD, "cells": list(NX), "meshblock": list(MB),
                    "blocks": int(np.prod([a // b for a, b in zip(NX, MB)])),
                    "precision": "mixed: FP32 reconstruction+Riemann, FP64 U/B/CT",
+                   "flux_launch_shape": dict(zip(("x1_tpb", "march_tpb", "march_segment"),
+                                                 m["tuning"])),
                    "l2": "working set (~2.9 GB) far larger than L2; no flush needed",
                    "parallelism": "replicas" if world > 1 else "1 GPU"},
         "fp64": {"value": res["fp64"]["zcps"], "ms_per_step": 1e3 * res["fp64"]["el"] / res["fp64"]["steps"],

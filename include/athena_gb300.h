@@ -195,6 +195,14 @@ int athg_mg_stream(athg_mg* mg, void** stream);
 /* Multipole coefficients (25) and expansion origin (3), after a solve. */
 int athg_mg_multipole(athg_mg* mg, double* out28);
 
+/* Launch shape of the flux sweeps: out3/in3 = {threads per block of the x1 sweep (64 or
+ * 128), of the marching x2/x3 sweeps (64 or 128), faces per marching segment (0: whole
+ * pencil)}. No counterpart in the reference. The mixed path autotunes it before its first
+ * captured cycle (every candidate timed on the context's own state); setting it disables
+ * the autotuner. Results do not depend on it. */
+int athg_get_tuning(athg_ctx* ctx, int* out3);
+int athg_set_tuning(athg_ctx* ctx, const int* in3);
+
 /* HistoryOutput::WriteOutputFile sums (outputs/history.cpp:45-130), reduced on the
  * device over all blocks' interior cells: out[0] mass, [1..3] momenta, [4..6] kinetic
  * energy per direction, [7] total energy, [8] 1/2 rho phi (0 without self-gravity),

@@ -219,3 +219,30 @@ def test_history_sums_match_host(precision):
     ref = np.array(ref) * vol
     np.testing.assert_allclose(h, ref, rtol=1e-12, atol=1e-14)
     sim.close()
+
+
+def test_flux_launch_shape_does_not_change_results():
+    """The autotuned launch shape of the flux sweeps (threads per block, marching segment
+    length) changes scheduling only: two extreme shapes give bitwise identical states."""
+    nx, mb = (32, 32, 32), (16, 16, 16)
+    u, b1, b2, b3 = ol.smooth_random_state(nx, True, seed=29, amp=0.3)
+    out = []
+    for shape in ((64, 64, 4), (128, 128, 0)):
+        sim = athg.Sim(nx, mb, mhd=True, solver="hlld", precision="mixed", cfl=0.4, tlim=100.0)
+        sim.load_interior(u, b1, b2, b3)
+        sim.initialize()
+        sim.set_tuning(*shape)
+        sim.cycles(3)
+        assert sim.tuning() == shape
+        out.append(sim.interior())
+        sim.close()
+    for k in out[0]:
+        assert np.array_equal(out[0][k], out[1][k]), k
+    # the autotuner picks one of its candidates
+    sim = athg.Sim(nx, mb, mhd=True, solver="hlld", precision="mixed", cfl=0.4, tlim=100.0)
+    sim.load_interior(u, b1, b2, b3)
+    sim.initialize()
+    sim.cycles(1)
+    x1, mt, seg = sim.tuning()
+    assert x1 in (64, 128) and mt in (64, 128) and seg in (8, 16, 32, 0)
+    sim.close()
