@@ -97,21 +97,32 @@ struct ff {
 // the 29 mantissa bits that rounding drops become a signed integer r, |r| <= 2^28, kept
 // to 22 bits and scaled by the exponent. |x| outside [2^-80, 2^120]: lo = 0.
 ATHG_HD ff split_ff(double x) {
+  // the rounding of d2f_int, and its remainder, on the 32-bit halves
   const uint64_t b = bits_d(x);
-  const uint32_t hi32 = (uint32_t)(b >> 32);
-  const int e = (int)((hi32 >> 20) & 0x7ffu);
-  const uint64_t X = (b & 0x000fffffffffffffull) | 0x0010000000000000ull;  // 53-bit mantissa
-  const uint64_t H = (X + 0x0fffffffull + ((X >> 29) & 1ull)) >> 29;      // rounded to 24 bits
-  const int32_t r = (int32_t)(int64_t)(X - (H << 29));                     // |r| <= 2^28
+  const uint32_t hi32 = (uint32_t)(b >> 32), lo32 = (uint32_t)b;
+  const uint32_t s = hi32 & 0x80000000u;
+  const uint32_t ed = (hi32 >> 20) & 0x7ffu;
+  const uint32_t m23 = ((hi32 & 0x000fffffu) << 3) | (lo32 >> 29);
+  const uint32_t rb = lo32 & 0x1fffffffu;
+  const uint32_t up = (rb > 0x10000000u || (rb == 0x10000000u && (m23 & 1u))) ? 1u : 0u;
+  const int fe = (int)ed - 896;
+  uint32_t m;
+  if (ed == 0x7ffu) m = (m23 | (hi32 & 0x000fffffu) | lo32) ? 0x7fc00000u : 0x7f800000u;
+  else if (fe >= 255) m = 0x7f800000u;
+  else if (fe <= 0) m = (fe == 0 && m23 == 0x7fffffu && up) ? 0x00800000u : 0u;
+  else m = (((uint32_t)fe << 23) | m23) + up;
   ff o;
-  o.hi = d2f_int(x);
+  o.hi = from_bits_f(s | m);
+  // remainder x - hi in units of 2^(e-1075): the dropped bits, less 2^29 when rounded up
+  const int32_t r = (int32_t)rb - (int32_t)(up << 29);  // |r| <= 2^28
   // (r >> 6) as a float through the 1.5 * 2^23 offset (exact for |r >> 6| <= 2^22), times
-  // 2^(e - 1075 + 6)
+  // 2^(e - 1075 + 6); |x| outside [2^-80, 2^120]: lo = 0
   const float q = from_bits_f(0x4b400000u + (uint32_t)(r >> 6)) - 12582912.0f;
-  const int se = e - 1069 + 127;
-  const float scale = from_bits_f((uint32_t)(se > 0 && se < 255 ? se : 1) << 23);
-  float lo = (se > 0 && se < 255 && e >= 943 && e <= 1143) ? q * scale : 0.0f;
-  o.lo = (hi32 & 0x80000000u) ? -lo : lo;
+  const int se = (int)ed - 1069 + 127;
+  const bool ok = se > 0 && se < 255 && ed >= 943u && ed <= 1143u;
+  const float scale = from_bits_f((uint32_t)(ok ? se : 1) << 23);
+  const float lo = ok ? q * scale : 0.0f;
+  o.lo = s ? -lo : lo;
   return o;
 }
 
