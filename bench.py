@@ -229,6 +229,31 @@ def run_mg_profile(prec, bc, n):
     mg.close()
 
 
+def run_c5_profile(n):
+    import torch
+    import athg
+    import pgens
+    nx = (n, n, n)
+    mb = (64, 64, 64) if n >= 64 else nx
+    u, b1, b2, b3, fpg, _ = pgens.turbulent_box(nx)
+    sim = athg.Sim(nx, mb, mhd=True, solver="hlld", precision="mixed", cfl=0.3, tlim=1e30,
+                   gamma=1.0001)
+    mg = athg.Multigrid(n, domain=((0.0, 1.0),) * 3, bc="periodic", mode="FMG",
+                        threshold=-1.0, niteration=1, precision="mixed")
+    sim.attach_gravity(mg, fpg)
+    sim.load_interior(u, b1, b2, b3)
+    sim.initialize()
+    sim.cycles(2)
+    sim.synchronize()
+    torch.cuda.profiler.start()
+    sim.cycles(1)
+    sim.synchronize()
+    torch.cuda.profiler.stop()
+    sim.attach_gravity(None, 0.0)
+    sim.close()
+    mg.close()
+
+
 def run_c5(args):
     """Magnetised self-gravitating turbulent box (PLM + HLLD + VL2, gamma = 1.0001, beta = 1,
     rms Mach 5, Jeans number 2) with a multigrid solve after every stage; prints its own
@@ -371,6 +396,9 @@ def main():
     ap.add_argument("--mg-profile", nargs=3, metavar=("PREC", "BC", "N"), default=None,
                     help="profiling run: solve the uniform sphere once, then one V-cycle "
                          "between cudaProfilerStart/Stop (for ncu --profile-from-start off)")
+    ap.add_argument("--c5-profile", type=int, default=0, metavar="N",
+                    help="profiling run: the turbulent box at N^3 (mixed), two cycles, then "
+                         "one cycle between cudaProfilerStart/Stop")
     ap.add_argument("--c5", action="store_true",
                     help="self-gravitating turbulent box instead of the headline workload")
     ap.add_argument("--c5-nx", type=int, default=512)
@@ -385,6 +413,8 @@ def main():
         return run_c5(args)
     if args.mg_profile:
         return run_mg_profile(*args.mg_profile)
+    if args.c5_profile:
+        return run_c5_profile(args.c5_profile)
 
     import torch
     import athg

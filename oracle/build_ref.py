@@ -53,6 +53,10 @@ CONFIGS = {
     "state_hydro_hllc_ng4": ("harness:load_state.cpp", "hllc", False, 4, 0, False, None),
     "state_hydro_lhllc": ("harness:load_state.cpp", "lhllc", False, 2, 0, False, None),
     "state_mhd_lhlld": ("harness:load_state.cpp", "lhlld", True, 2, 0, False, None),
+    # multi-level (SMR) meshes from per-block states
+    "smr_mhd_hlld": ("harness:load_blocks.cpp", "hlld", True, 2, 0, False, None),
+    "smr_mhd_hlld_ng4": ("harness:load_blocks.cpp", "hlld", True, 4, 0, False, None),
+    "smr_hydro_hllc": ("harness:load_blocks.cpp", "hllc", False, 2, 0, False, None),
     # multigrid self-gravity
     "poisson_mg": ("poisson.cpp", "hllc", False, 2, 2, False, None),
     "jeans_mg": ("jeans.cpp", "hllc", False, 2, 2, False, None),
