@@ -215,3 +215,37 @@ def run_reference_smr(exe, workdir, root_nx, mb, domain, regions, blocks, states
     if r.returncode != 0 or "FATAL" in r.stdout:
         raise RuntimeError("reference run failed:\n" + r.stdout[-2000:] + r.stderr[-2000:])
     return read_blocks_out(os.path.join(workdir, "state_out.bin"), mb, ng, mhd, ghosts)
+
+
+def write_check_in(path, blocks, states, mesh_nx, mb, ng, domain, mhd, gamma, dfloor, pfloor):
+    """Input of tests/smr_check.cpp (see its header)."""
+    with open(path, "wb") as f:
+        f.write(struct.pack("<9i", mb[0], mb[1], mb[2], ng, mesh_nx[0], mesh_nx[1], mesh_nx[2],
+                            1 if mhd else 0, len(blocks)))
+        f.write(struct.pack("<9d", domain[0][0], domain[0][1], domain[1][0], domain[1][1],
+                            domain[2][0], domain[2][1], gamma, dfloor, pfloor))
+        for blk in blocks:
+            f.write(struct.pack("<4q", *blk))
+            u, b1, b2, b3 = states[blk]
+            f.write(np.ascontiguousarray(u, dtype="<f8").tobytes())
+            if mhd:
+                for a in (b1, b2, b3):
+                    f.write(np.ascontiguousarray(a, dtype="<f8").tobytes())
+
+
+def read_check_out(path, blocks, mb, ng, mhd):
+    n1, n2, n3 = (m + 2 * ng for m in mb)
+    res = {}
+    with open(path, "rb") as f:
+        for blk in blocks:
+            def take(shape):
+                cnt = int(np.prod(shape))
+                return np.frombuffer(f.read(8 * cnt), dtype="<f8").reshape(shape).copy()
+            d = {"u": take((NHYD, n3, n2, n1)), "w": take((NHYD, n3, n2, n1))}
+            if mhd:
+                d["b1"] = take((n3, n2, n1 + 1))
+                d["b2"] = take((n3, n2 + 1, n1))
+                d["b3"] = take((n3 + 1, n2, n1))
+            res[blk] = d
+        sizes = struct.unpack("<8q", f.read(64))
+    return res, sizes
