@@ -36,7 +36,8 @@ EXPORTS = [
     "athg_mg_solve", "athg_mg_vcycles", "athg_mg_defect_norm", "athg_mg_get_phi",
     "athg_mg_stream", "athg_mg_multipole", "athg_attach_gravity", "athg_history",
     "athg_get_tuning", "athg_set_tuning",
-    "athg_block_cfl_dt_noalloc",
+    "athg_block_cfl_dt_noalloc", "athg_set_refined_mesh", "athg_set_multilevel_blocks",
+    "athg_smr_stats",
 ]
 MG_BC = {"periodic": 0, "zerograd": 1, "zerofixed": 2, "multipole": 3}
 
@@ -63,6 +64,12 @@ class Mesh(C.Structure):
                 ("x1min", C.c_double), ("x1max", C.c_double), ("x2min", C.c_double),
                 ("x2max", C.c_double), ("x3min", C.c_double), ("x3max", C.c_double),
                 ("periodic", C.c_int * 3)]
+
+
+class Region(C.Structure):
+    _fields_ = [("x1min", C.c_double), ("x1max", C.c_double), ("x2min", C.c_double),
+                ("x2max", C.c_double), ("x3min", C.c_double), ("x3max", C.c_double),
+                ("level", C.c_int)]
 
 
 class AthgError(RuntimeError):
@@ -123,6 +130,9 @@ def lib():
         "athg_get_tuning": [vp, C.POINTER(i)],
         "athg_set_tuning": [vp, C.POINTER(i)],
         "athg_block_cfl_dt_noalloc": [C.POINTER(Config), vp, vp, vp, vp, vp, d, d, d, vp, vp],
+        "athg_set_refined_mesh": [vp, C.POINTER(Mesh), i, C.POINTER(Region)],
+        "athg_set_multilevel_blocks": [vp, C.POINTER(Mesh), i, C.POINTER(C.c_int64)],
+        "athg_smr_stats": [vp, C.POINTER(C.c_int64)],
     }
     for name, args in sig.items():
         f = getattr(L, name)
@@ -143,12 +153,14 @@ def _dptr(a):
 
 
 class Sim:
-    """A uniform periodic mesh of MeshBlocks on the GPU."""
+    """A periodic mesh of MeshBlocks on the GPU: uniform, or refined by `regions`
+    ([(x1min, x1max, x2min, x2max, x3min, x3max, level)]) or given as an explicit leaf list
+    `leaves` ([(level, lx1, lx2, lx3)])."""
 
     def __init__(self, mesh_nx, block_nx, mhd, solver, precision="fp64", xorder=2,
                  integrator="vl2", gamma=5.0 / 3.0, cfl=0.4, tlim=1.0, ng=2,
                  domain=((0.0, 1.0), (0.0, 1.0), (0.0, 1.0)), dfloor=FLOOR, pfloor=FLOOR,
-                 periodic=(1, 1, 1)):
+                 periodic=(1, 1, 1), regions=None, leaves=None):
         L = lib()
         c = Config()
         c.nx1, c.nx2, c.nx3 = block_nx
@@ -170,16 +182,30 @@ class Sim:
         (m.x1min, m.x1max), (m.x2min, m.x2max), (m.x3min, m.x3max) = domain
         for q in range(3):
             m.periodic[q] = int(periodic[q])
-        check(L.athg_set_uniform_mesh(h, C.byref(m)))
+        if regions is not None:
+            rs = (Region * max(1, len(regions)))()
+            for q, r in enumerate(regions):
+                rs[q].x1min, rs[q].x1max, rs[q].x2min, rs[q].x2max, rs[q].x3min, rs[q].x3max = r[:6]
+                rs[q].level = int(r[6]) if len(r) > 6 else 1
+            check(L.athg_set_refined_mesh(h, C.byref(m), len(regions), rs))
+        elif leaves is not None:
+            a = np.ascontiguousarray(np.asarray(leaves, dtype=np.int64).reshape(-1, 4))
+            check(L.athg_set_multilevel_blocks(h, C.byref(m), a.shape[0],
+                                               a.ctypes.data_as(C.POINTER(C.c_int64))))
+        else:
+            check(L.athg_set_uniform_mesh(h, C.byref(m)))
         self.mesh_nx, self.block_nx, self.ng, self.mhd = tuple(mesh_nx), tuple(block_nx), ng, mhd
         nb = C.c_int()
         check(L.athg_num_blocks(h, C.byref(nb)))
         self.nb = nb.value
         self.locs = []
+        self.leaves = []  # (level, lx1, lx2, lx3) of every block
         loc = (C.c_int64 * 4)()
         for b in range(self.nb):
             check(L.athg_block_location(h, b, loc))
             self.locs.append((loc[0], loc[1], loc[2]))
+            self.leaves.append((int(loc[3]), int(loc[0]), int(loc[1]), int(loc[2])))
+        self.multilevel = regions is not None or leaves is not None
         self.nc = tuple(n + 2 * ng for n in block_nx)
 
     def close(self):
@@ -231,6 +257,53 @@ class Sim:
                     b3[o3:o3 + nx3 + 1, o2:o2 + nx2, o1:o1 + nx1]
             for v, arr in zip((VAR_B1F, VAR_B2F, VAR_B3F), B):
                 self.upload(v, arr)
+
+    def load_blocks(self, states):
+        """Interior state per block: states[(level, lx1, lx2, lx3)] = (u, b1, b2, b3) in the
+        interior layout (ghosts zero, filled by initialize())."""
+        g = self.ng
+        nx1, nx2, nx3 = self.block_nx
+        U = np.zeros((self.nb,) + self._shape(VAR_CONS))
+        B = [np.zeros((self.nb,) + self._shape(v)) for v in (VAR_B1F, VAR_B2F, VAR_B3F)]
+        for b, key in enumerate(self.leaves):
+            u, b1, b2, b3 = states[key]
+            U[b, :, g:g + nx3, g:g + nx2, g:g + nx1] = u
+            if self.mhd:
+                B[0][b, g:g + nx3, g:g + nx2, g:g + nx1 + 1] = b1
+                B[1][b, g:g + nx3, g:g + nx2 + 1, g:g + nx1] = b2
+                B[2][b, g:g + nx3 + 1, g:g + nx2, g:g + nx1] = b3
+        self.upload(VAR_CONS, U)
+        if self.mhd:
+            for v, arr in zip((VAR_B1F, VAR_B2F, VAR_B3F), B):
+                self.upload(v, arr)
+
+    def blocks(self, ghosts=True):
+        """dict (level, lx1, lx2, lx3) -> {u, w, b1, b2, b3} (whole arrays with ghosts, or
+        the interior)."""
+        g = self.ng
+        nx1, nx2, nx3 = self.block_nx
+        arrs = {"u": self.download(VAR_CONS), "w": self.download(VAR_PRIM)}
+        if self.mhd:
+            arrs.update(b1=self.download(VAR_B1F), b2=self.download(VAR_B2F),
+                        b3=self.download(VAR_B3F))
+        out = {}
+        for b, key in enumerate(self.leaves):
+            d = {}
+            for k, a in arrs.items():
+                x = a[b]
+                if not ghosts:
+                    e1 = 1 if k == "b1" else 0
+                    e2 = 1 if k == "b2" else 0
+                    e3 = 1 if k == "b3" else 0
+                    x = x[..., g:g + nx3 + e3, g:g + nx2 + e2, g:g + nx1 + e1]
+                d[k] = x
+            out[key] = d
+        return out
+
+    def smr_stats(self):
+        out = (C.c_int64 * 8)()
+        check(lib().athg_smr_stats(self.h, out))
+        return tuple(out)
 
     def interior(self, prim=False):
         """Gather global interior arrays (u, and b1/b2/b3 for MHD)."""

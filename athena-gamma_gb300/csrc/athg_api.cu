@@ -2,6 +2,8 @@
 // CUDA-graph cycle. Declarations and reference interfaces: include/athena_gb300.h.
 #include <algorithm>
 #include <cmath>
+#include <set>
+#include <tuple>
 #include <type_traits>
 #include <utility>
 #include <cstdio>
@@ -237,6 +239,8 @@ struct athg_ctx {
   double four_pi_G = 0.0;
   double* phi = nullptr;
   int* boff = nullptr;
+  // multi-level mesh (static refinement): work lists, coarse buffers (FP64 path only)
+  athg::SmrDevice* smr = nullptr;
   bool mixed() const { return cfg.precision == ATHG_MIXED; }
 };
 
@@ -298,10 +302,29 @@ void free_pool(athg_ctx* c) {
   c->phi = nullptr; c->boff = nullptr;
   if (c->grav) athg::mg_bind_stream(c->grav, nullptr);
   c->grav = nullptr;
+  athg::smr_destroy(c->smr);
+  c->smr = nullptr;
   c->nb = 0;
 }
 
+// the block pool as the SMR work lists see it
+SmrPool smr_pool_of(athg_ctx* c) {
+  SmrPool P = athg::smr_pool(c->smr);
+  P.u = c->u; P.w = (double*)c->w;
+  P.b1 = c->b1; P.b2 = c->b2; P.b3 = c->b3; P.bcc = (double*)c->bcc;
+  for (int d = 0; d < 3; ++d) P.flx[d] = (double*)c->flx[d];
+  P.nflx = c->cfg.magnetic ? 8 : 5;
+  P.edge = (double*)c->edge;
+  P.gamma = c->cfg.gamma; P.dfloor = c->cfg.dfloor; P.pfloor = c->cfg.pfloor;
+  return P;
+}
+
 int launch_ghosts(athg_ctx* c) {
+  if (c->smr) {  // ghost fill across refinement levels and prolongation
+    c->counting += athg::smr_fill(c->smr, smr_pool_of(c), c->st);
+    CKL();
+    return ATHG_OK;
+  }
   GhostPtrs gp{c->u, c->b1, c->b2, c->b3, c->nbr, NHYD, c->cfg.magnetic};
   const Geom& g = c->g;
   dim3 grid((unsigned)((ghost_shell_size(g) + 255) / 256), (unsigned)c->nb);
@@ -320,6 +343,8 @@ int launch_fluxes(athg_ctx* c, int order) {
     Launcher<double>::fluxes(c->g, ptrs<double>(c), mhd, c->cfg.rsolver, order, phys(c),
                              c->tune, c->st);
   c->counting += 3;
+  // SendFluxCorrection / ReceiveFluxCorrection (time_integrator.cpp: SEND_HYDFLX, RECV_HYDFLX)
+  if (c->smr) c->counting += athg::smr_correct_flux(c->smr, smr_pool_of(c), c->st);
   CKL();
   return ATHG_OK;
 }
@@ -329,6 +354,8 @@ int launch_corner(athg_ctx* c) {
   if (c->mixed()) Launcher<float>::corner_emf(c->g, ptrs<float>(c), c->st);
   else Launcher<double>::corner_emf(c->g, ptrs<double>(c), c->st);
   c->counting += 1;
+  // EMF correction at block boundaries (time_integrator.cpp: SEND_FLDFLX, RECV_FLDFLX)
+  if (c->smr) c->counting += athg::smr_correct_emf(c->smr, smr_pool_of(c), c->st);
   CKL();
   return ATHG_OK;
 }
@@ -665,6 +692,151 @@ double gen_x(double rx, double xmin, double xmax) {
   return 0.5 * (xmin + xmax) + (rx * xmax - rx * xmin);
 }
 
+// ---- multi-level meshes ----------------------------------------------------------------
+using LocKey = std::tuple<int, int64_t, int64_t, int64_t>;
+
+// Leaves of a root grid refined by <refinementN> regions (Mesh::Mesh, mesh/mesh.cpp:334-462:
+// logical range of each region at its level widened to whole parents, AddMeshBlock), then
+// refined further until neighbouring leaves differ by at most one level (the balance
+// MeshBlockTree::Refine keeps, mesh/meshblock_tree.cpp)
+int refined_leaves(const int nmx[3], const int nrb[3], const double lo[3], const double hi[3],
+                   int nreg, const athg_region* reg, std::vector<SmrLoc>* out) {
+  std::set<LocKey> leaves;
+  for (int k = 0; k < nrb[2]; ++k)
+    for (int j = 0; j < nrb[1]; ++j)
+      for (int i = 0; i < nrb[0]; ++i) leaves.insert(LocKey(0, i, j, k));
+  auto refine = [&](const LocKey& key) {
+    leaves.erase(key);
+    const int l = std::get<0>(key);
+    for (int c8 = 0; c8 < 8; ++c8)
+      leaves.insert(LocKey(l + 1, 2 * std::get<1>(key) + (c8 & 1),
+                           2 * std::get<2>(key) + ((c8 >> 1) & 1), 2 * std::get<3>(key) + (c8 >> 2)));
+  };
+  auto add_block = [&](int L, const int64_t x[3]) {
+    for (int lv = 0; lv < L; ++lv) {
+      const int sh = L - lv;
+      LocKey a(lv, x[0] >> sh, x[1] >> sh, x[2] >> sh);
+      if (leaves.count(a)) refine(a);
+    }
+  };
+  for (int r = 0; r < nreg; ++r) {
+    const int L = reg[r].level;
+    if (L < 1 || L > 10) return fail(ATHG_ERR_ARG, "refinement level must be in 1..10");
+    const double rlo[3] = {reg[r].x1min, reg[r].x2min, reg[r].x3min};
+    const double rhi[3] = {reg[r].x1max, reg[r].x2max, reg[r].x3max};
+    int64_t a[3], b[3];
+    for (int d = 0; d < 3; ++d) {
+      if (rlo[d] > rhi[d] || rlo[d] < lo[d] || rhi[d] > hi[d])
+        return fail(ATHG_ERR_ARG, "invalid refinement region");
+      const int64_t lmax = (int64_t)nrb[d] << L;
+      int64_t x = 0;
+      for (; x < lmax; ++x)
+        if (gen_x(gen_rx(x + 1, lmax), lo[d], hi[d]) > rlo[d]) break;
+      int64_t y = x;
+      for (; y < lmax; ++y)
+        if (gen_x(gen_rx(y + 1, lmax), lo[d], hi[d]) >= rhi[d]) break;
+      if (x % 2 == 1) x--;
+      if (y % 2 == 0) y++;
+      a[d] = x; b[d] = y;
+    }
+    for (int64_t k = a[2]; k < b[2]; k += 2)
+      for (int64_t j = a[1]; j < b[1]; j += 2)
+        for (int64_t i = a[0]; i < b[0]; i += 2) {
+          const int64_t x[3] = {i, j, k};
+          add_block(L, x);
+        }
+  }
+  // 2:1 balance
+  for (bool changed = true; changed;) {
+    changed = false;
+    for (const LocKey& key : leaves) {
+      const int L = std::get<0>(key);
+      if (L < 2) continue;
+      const int64_t x[3] = {std::get<1>(key), std::get<2>(key), std::get<3>(key)};
+      for (int o = 0; o < 27 && !changed; ++o) {
+        if (o == 13) continue;
+        const int off[3] = {o % 3 - 1, (o / 3) % 3 - 1, o / 9 - 1};
+        int64_t y[3];
+        for (int d = 0; d < 3; ++d) {
+          const int64_t n = (int64_t)nrb[d] << L;
+          y[d] = ((x[d] + off[d]) % n + n) % n;
+        }
+        for (int lv = L - 2; lv >= 0; --lv) {
+          const int sh = L - lv;
+          LocKey an(lv, y[0] >> sh, y[1] >> sh, y[2] >> sh);
+          if (leaves.count(an)) { refine(an); changed = true; break; }
+        }
+      }
+      if (changed) break;
+    }
+  }
+  out->clear();
+  for (const LocKey& key : leaves) {
+    SmrLoc l;
+    l.level = std::get<0>(key);
+    l.lx[0] = std::get<1>(key); l.lx[1] = std::get<2>(key); l.lx[2] = std::get<3>(key);
+    out->push_back(l);
+  }
+  // level, then lx3, lx2, lx1
+  std::sort(out->begin(), out->end(), [](const SmrLoc& p, const SmrLoc& q) {
+    return std::make_tuple(p.level, p.lx[2], p.lx[1], p.lx[0]) <
+           std::make_tuple(q.level, q.lx[2], q.lx[1], q.lx[0]);
+  });
+  (void)nmx;
+  return ATHG_OK;
+}
+
+// Allocates the pool for the leaves `loc` of a periodic mesh and plans its level
+// boundaries; coordinates follow the reference's uniform generator per level
+int set_multilevel(athg_ctx* c, const athg_mesh* m, const std::vector<SmrLoc>& loc) {
+  if (c->mixed())
+    return fail(ATHG_ERR_ARG, "multi-level meshes run on the FP64 path (precision ATHG_FP64)");
+  for (int d = 0; d < 3; ++d)
+    if (!m->periodic[d]) return fail(ATHG_ERR_ARG, "multi-level meshes: periodic boundaries only");
+  const Geom& g = c->g;
+  const int nmx[3] = {m->nx1, m->nx2, m->nx3};
+  const int nbx[3] = {g.nx1, g.nx2, g.nx3};
+  const double lo[3] = {m->x1min, m->x2min, m->x3min}, hi[3] = {m->x1max, m->x2max, m->x3max};
+  int nrb[3];
+  for (int d = 0; d < 3; ++d) {
+    if (nmx[d] % nbx[d] != 0)
+      return fail(ATHG_ERR_ARG, "mesh size must be a multiple of the MeshBlock size");
+    nrb[d] = nmx[d] / nbx[d];
+  }
+  const int nb = (int)loc.size();
+  const int ncs[3] = {g.nc1, g.nc2, g.nc3};
+  const int ncmax = std::max(g.nc1, std::max(g.nc2, g.nc3));
+  const int nccmax = std::max(nbx[0], std::max(nbx[1], nbx[2])) / 2 + 2 * g.ng;
+  c->coords.assign((size_t)nb * (ncs[0] + ncs[1] + ncs[2] + 3), 0.0);
+  std::vector<double> dxv((size_t)nb * 3), xvf((size_t)nb * 3 * ncmax, 0.0),
+      xvc((size_t)nb * 3 * nccmax, 0.0);
+  std::vector<athg_block> bl(nb);
+  size_t off = 0;
+  for (int b = 0; b < nb; ++b) {
+    athg_block& B = bl[b];
+    B.lx1 = loc[b].lx[0]; B.lx2 = loc[b].lx[1]; B.lx3 = loc[b].lx[2];
+    B.level = loc[b].level;
+    double* xfs[3];
+    for (int d = 0; d < 3; ++d) {
+      xfs[d] = &c->coords[off];
+      off += ncs[d] + 1;
+      smr_axis_coords(nmx[d], nrb[d], lo[d], hi[d], loc[b].level, loc[b].lx[d], nbx[d], g.ng,
+                      &dxv[3 * b + d], &xvf[((size_t)b * 3 + d) * ncmax],
+                      &xvc[((size_t)b * 3 + d) * nccmax], xfs[d]);
+    }
+    B.x1f = xfs[0]; B.x2f = xfs[1]; B.x3f = xfs[2];
+    B.dx1 = dxv[3 * b]; B.dx2 = dxv[3 * b + 1]; B.dx3 = dxv[3 * b + 2];
+    for (int n = 0; n < 27; ++n) B.neighbor[n] = -1;  // level boundaries use the SMR lists
+  }
+  int rc = athg_set_blocks(c, nb, bl.data());
+  if (rc) return rc;
+  SmrDims d = smr_dims(g.nx1, g.nx2, g.nx3, g.ng);
+  std::string err;
+  rc = athg::smr_create(&c->smr, d, nrb, loc, dxv, xvf, xvc, c->cfg.magnetic != 0, c->st, &err);
+  if (rc) return fail(rc == -1 ? ATHG_ERR_ARG : ATHG_ERR_CUDA, err);
+  return ATHG_OK;
+}
+
 }  // namespace
 
 // =================================================================== C ABI ==========
@@ -922,6 +1094,48 @@ int athg_set_uniform_mesh(athg_ctx* c, const athg_mesh* m) {
   return athg_set_blocks(c, nblocks, bl.data());
 }
 
+int athg_set_refined_mesh(athg_ctx* c, const athg_mesh* m, int nregions,
+                          const athg_region* regions) {
+  if (!c || !m || nregions < 0 || (nregions > 0 && !regions))
+    return fail(ATHG_ERR_ARG, "null argument");
+  const Geom& g = c->g;
+  const int nmx[3] = {m->nx1, m->nx2, m->nx3};
+  const int nbx[3] = {g.nx1, g.nx2, g.nx3};
+  const double lo[3] = {m->x1min, m->x2min, m->x3min}, hi[3] = {m->x1max, m->x2max, m->x3max};
+  int nrb[3];
+  for (int d = 0; d < 3; ++d) {
+    if (nbx[d] <= 0 || nmx[d] % nbx[d] != 0)
+      return fail(ATHG_ERR_ARG, "mesh size must be a multiple of the MeshBlock size");
+    nrb[d] = nmx[d] / nbx[d];
+  }
+  std::vector<SmrLoc> loc;
+  int rc = refined_leaves(nmx, nrb, lo, hi, nregions, regions, &loc);
+  if (rc) return rc;
+  return set_multilevel(c, m, loc);
+}
+
+int athg_set_multilevel_blocks(athg_ctx* c, const athg_mesh* m, int nblocks,
+                               const int64_t* locs) {
+  if (!c || !m || nblocks <= 0 || !locs) return fail(ATHG_ERR_ARG, "null argument");
+  std::vector<SmrLoc> loc(nblocks);
+  for (int b = 0; b < nblocks; ++b) {
+    loc[b].level = (int)locs[4 * b];
+    for (int d = 0; d < 3; ++d) loc[b].lx[d] = locs[4 * b + 1 + d];
+    if (loc[b].level < 0 || loc[b].level > 10) return fail(ATHG_ERR_ARG, "block level out of range");
+  }
+  return set_multilevel(c, m, loc);
+}
+
+int athg_smr_stats(athg_ctx* c, int64_t* out8) {
+  if (!c || !out8) return fail(ATHG_ERR_ARG, "null argument");
+  for (int i = 0; i < 8; ++i) out8[i] = 0;
+  if (!c->smr) return ATHG_OK;
+  const athg::SmrDevice* s = c->smr;
+  out8[0] = s->nxfer; out8[1] = s->npre; out8[2] = s->nflux; out8[3] = s->nemf;
+  out8[4] = s->nc2p; out8[5] = s->npcc; out8[6] = s->npint; out8[7] = s->npfine;
+  return ATHG_OK;
+}
+
 int athg_num_blocks(const athg_ctx* c, int* nblocks) {
   if (!c || !nblocks) return fail(ATHG_ERR_ARG, "null argument");
   *nblocks = c->nb;
@@ -1088,6 +1302,7 @@ int athg_attach_gravity(athg_ctx* c, athg_mg* mg, double four_pi_G) {
   if (c->grav) athg::mg_bind_stream(c->grav, nullptr);
   c->grav = nullptr;
   if (!mg) return ATHG_OK;
+  if (c->smr) return fail(ATHG_ERR_ARG, "self-gravity on a multi-level mesh is not supported");
   double *um, *src;
   int n;
   if ((rc = athg::mg_finest(mg, &um, &src, &n))) return rc;

@@ -82,6 +82,12 @@ typedef struct {
   int periodic[3];                           /* 1 if ix/ox bc are periodic on this axis */
 } athg_mesh;
 
+/* A static-refinement region (<refinementN> x1min..x3max, level >= 1). */
+typedef struct {
+  double x1min, x1max, x2min, x2max, x3min, x3max;
+  int level;
+} athg_region;
+
 /* ---- context and pool ---------------------------------------------------------- */
 int athg_create(const athg_config* cfg, athg_ctx** out);
 int athg_destroy(athg_ctx* ctx);
@@ -92,6 +98,23 @@ int athg_set_blocks(athg_ctx* ctx, int nblocks, const athg_block* blocks);
  * mesh/mesh.cpp:1668, Coordinates ctor) and calls athg_set_blocks. Blocks are ordered
  * with lx1 fastest, then lx2, then lx3. */
 int athg_set_uniform_mesh(athg_ctx* ctx, const athg_mesh* mesh);
+/* Static mesh refinement (<mesh> refinement = static): the root grid of `mesh`, refined
+ * where `regions` say, with the leaves and their 2:1 balance of Mesh::Mesh
+ * (mesh/mesh.cpp:334-462, mesh/meshblock_tree.cpp) and the level-boundary work of
+ * bvals/bvals_refine.cpp, bvals/cc/flux_correction_cc.cpp and bvals/fc/flux_correction_fc.cpp
+ * done on the device (ghost fill through coarse buffers, prolongation, flux and EMF
+ * correction). FP64 precision and periodic boundaries only. Blocks are ordered by level,
+ * then lx3, lx2, lx1 (athg_block_location gives each one). */
+int athg_set_refined_mesh(athg_ctx* ctx, const athg_mesh* mesh, int nregions,
+                          const athg_region* regions);
+/* The same for an explicit list of leaves, as the reference's MeshBlockTree holds them:
+ * locs[4*b .. 4*b+3] = level (relative to the root grid), lx1, lx2, lx3 of block b. */
+int athg_set_multilevel_blocks(athg_ctx* ctx, const athg_mesh* mesh, int nblocks,
+                               const int64_t* locs);
+/* Sizes of the multi-level work lists (all 0 on a single-level mesh): out[0..7] = ghost-fill
+ * elements, same-level restrictions, flux corrections, EMF corrections, coarse cells
+ * converted to primitives, prolongated cells, internal-field cells, fine cells rebuilt. */
+int athg_smr_stats(athg_ctx* ctx, int64_t* out8);
 int athg_num_blocks(const athg_ctx* ctx, int* nblocks);
 /* logical location of block b: out[0..3] = lx1, lx2, lx3, level */
 int athg_block_location(const athg_ctx* ctx, int block, int64_t* out);
