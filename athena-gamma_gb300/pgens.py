@@ -281,3 +281,50 @@ def turbulent_box(nx, seed=20261203, mach=5.0, beta=1.0, gamma=1.0001, kmin=1, k
     G = math.pi * jeans_number ** 2 * cs * cs / (rho * L * L)
     h = hashlib.sha256(np.ascontiguousarray(np.stack(v)).tobytes()).hexdigest()
     return u, b1, b2, b3, 4.0 * math.pi * G, h
+
+
+def block_axis(level, lx, mesh_nx, nrb, nx, lo, hi):
+    """Cell centres of block (level, lx) along one axis of a multi-level mesh: the uniform
+    generator at the level's resolution with the block edges of Mesh::SetBlockSizeAndBoundaries
+    (mesh/mesh.cpp:1675-1690, coordinates/coordinates.cpp:127-145, cartesian.cpp:29)."""
+    nroot = mesh_nx << level
+    nrbl = nrb << level
+
+    def gx(index, nrange):
+        rx = _gen_rx(index, nrange)
+        return 0.5 * (lo + hi) + (rx * hi - rx * lo)
+
+    xf = np.array([gx(t + lx * nx, nroot) for t in range(nx + 1)])
+    xf[0] = lo if lx == 0 else gx(lx, nrbl)
+    xf[-1] = hi if lx == nrbl - 1 else gx(lx + 1, nrbl)
+    return 0.5 * (xf[1:] + xf[:-1])
+
+
+def blast_blocks(leaves, mesh_nx, block_nx, domain=((-1.0, 1.0),) * 3, gamma=5.0 / 3.0,
+                 radius=0.1, pamb=0.1, prat=100.0, damb=1.0, drat=1.0, b0=1.0, angle=45.0,
+                 mhd=True):
+    """Spherical (M)HD blast wave, src/pgen/blast.cpp:54-211 (Cartesian, no ramp), per block
+    of a multi-level mesh: dict (level, lx1, lx2, lx3) -> (u, b1, b2, b3) interiors."""
+    nrb = [mesh_nx[d] // block_nx[d] for d in range(3)]
+    ang = (math.pi / 180.0) * angle
+    gm1 = gamma - 1.0
+    out = {}
+    n1, n2, n3 = block_nx
+    for leaf in leaves:
+        level = leaf[0]
+        xv = [block_axis(level, leaf[1 + d], mesh_nx[d], nrb[d], block_nx[d], *domain[d])
+              for d in range(3)]
+        Z, Y, X = np.meshgrid(xv[2], xv[1], xv[0], indexing="ij")
+        rad = np.sqrt((X - 0.0) ** 2 + (Y - 0.0) ** 2 + (Z - 0.0) ** 2)
+        inside = rad < radius
+        u = np.zeros((5, n3, n2, n1))
+        u[0] = np.where(inside, drat * damb, damb)
+        u[4] = np.where(inside, prat * pamb, pamb) / gm1
+        b1 = b2 = b3 = None
+        if mhd:
+            b1 = np.full((n3, n2, n1 + 1), b0 * math.cos(ang))
+            b2 = np.full((n3, n2 + 1, n1), b0 * math.sin(ang))
+            b3 = np.zeros((n3 + 1, n2, n1))
+            u[4] += 0.5 * b0 * b0
+        out[tuple(leaf)] = (u, b1, b2, b3)
+    return out

@@ -229,6 +229,60 @@ def run_mg_profile(prec, bc, n):
     mg.close()
 
 
+# MHD blast with static refinement (the reference's athinput.blast with <refinement1>):
+# root 128^3 on [-1,1]^3, the central half refined one level, 16^3 blocks (960 of them),
+# PPM + HLLD + RK3, NGHOST 4, FP64 (the precision of the reference). The reference's own
+# CPU throughput on this configuration, measured with its binary on one core, is
+# 2.10e5 zone-cycles/s.
+C3_REF_CPU_ZCPS = 2.10e5
+
+
+def c3_setup(athg, pgens, root=128, mb=16):
+    sim = athg.Sim((root,) * 3, (mb,) * 3, True, "hlld", precision="fp64", xorder=3,
+                   integrator="rk3", gamma=5.0 / 3.0, cfl=0.3, tlim=1e30, ng=4,
+                   domain=((-1.0, 1.0),) * 3, regions=[(-0.5, 0.5, -0.5, 0.5, -0.5, 0.5, 1)])
+    sim.load_blocks(pgens.blast_blocks(sim.leaves, (root,) * 3, (mb,) * 3))
+    sim.initialize()
+    return sim
+
+
+def run_c3(athg, torch, steps, warmup):
+    import pgens
+    sim = c3_setup(athg, pgens)
+    cells = sim.nb * 16 ** 3
+    sim.cycles(warmup)
+    sim.synchronize()
+    el = timed_cycles(sim, torch, steps)
+    zcps = cells * steps / el
+    res = {"workload": "mhd_blast_smr_128^3_root_central_half_level1_16^3_blocks_ppm_hlld_rk3",
+           "precision": "fp64", "blocks": sim.nb,
+           "fine_blocks": sum(1 for l in sim.leaves if l[0] == 1), "cells": cells,
+           "steps": steps, "ms_per_cycle": 1e3 * el / steps, "zone_cycles_per_s": zcps,
+           "launches_per_cycle": sim.launches_per_cycle(),
+           "smr_lists": dict(zip(("ghost_fill", "same_level_restrict", "flux_corr", "emf_corr",
+                                  "coarse_c2p", "prolong_cells", "internal_field",
+                                  "fine_rebuild"), sim.smr_stats())),
+           "div_b_max": sim.max_div_b(),
+           "reference_cpu_zone_cycles_per_s_1core": C3_REF_CPU_ZCPS,
+           "speedup_vs_reference_1core": zcps / C3_REF_CPU_ZCPS}
+    sim.close()
+    return res
+
+
+def run_c3_profile():
+    import torch
+    import athg
+    import pgens
+    sim = c3_setup(athg, pgens)
+    sim.cycles(2)
+    sim.synchronize()
+    torch.cuda.profiler.start()
+    sim.cycles(1)
+    sim.synchronize()
+    torch.cuda.profiler.stop()
+    sim.close()
+
+
 def run_c5_profile(n):
     import torch
     import athg
@@ -399,6 +453,12 @@ def main():
     ap.add_argument("--c5-profile", type=int, default=0, metavar="N",
                     help="profiling run: the turbulent box at N^3 (mixed), two cycles, then "
                          "one cycle between cudaProfilerStart/Stop")
+    ap.add_argument("--no-c3", action="store_true",
+                    help="skip the MHD blast with static refinement")
+    ap.add_argument("--c3-steps", type=int, default=5)
+    ap.add_argument("--c3-profile", action="store_true",
+                    help="profiling run: the refined MHD blast, two cycles, then one cycle "
+                         "between cudaProfilerStart/Stop")
     ap.add_argument("--c5", action="store_true",
                     help="self-gravitating turbulent box instead of the headline workload")
     ap.add_argument("--c5-nx", type=int, default=512)
@@ -415,6 +475,8 @@ def main():
         return run_mg_profile(*args.mg_profile)
     if args.c5_profile:
         return run_c5_profile(args.c5_profile)
+    if args.c3_profile:
+        return run_c3_profile()
 
     import torch
     import athg
@@ -476,6 +538,11 @@ def main():
     if not args.no_mg:
         mgres = run_mg(athg, torch)
 
+    # ---------------- MHD blast with static mesh refinement ----------------
+    c3res = None
+    if not args.no_c3:
+        c3res = run_c3(athg, torch, args.c3_steps, max(args.warmup, 3))
+
     # ---------------- CPU baseline (oracle port) ----------------
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -524,6 +591,7 @@ def main():
         "gpu_launches": m["launches"] * m["steps"],
         "clocks": m["clocks"],
         "mg": mgres,
+        "smr_blast": c3res,
     }
     if rank == 0:
         print(json.dumps(line), flush=True)
