@@ -37,7 +37,7 @@ EXPORTS = [
     "athg_mg_stream", "athg_mg_multipole", "athg_attach_gravity", "athg_history",
     "athg_get_tuning", "athg_set_tuning",
     "athg_block_cfl_dt_noalloc", "athg_set_refined_mesh", "athg_set_multilevel_blocks",
-    "athg_smr_stats",
+    "athg_smr_stats", "athg_resume",
 ]
 MG_BC = {"periodic": 0, "zerograd": 1, "zerofixed": 2, "multipole": 3}
 
@@ -133,6 +133,7 @@ def lib():
         "athg_set_refined_mesh": [vp, C.POINTER(Mesh), i, C.POINTER(Region)],
         "athg_set_multilevel_blocks": [vp, C.POINTER(Mesh), i, C.POINTER(C.c_int64)],
         "athg_smr_stats": [vp, C.POINTER(C.c_int64)],
+        "athg_resume": [vp],
     }
     for name, args in sig.items():
         f = getattr(L, name)

@@ -1251,6 +1251,24 @@ int athg_initialize(athg_ctx* c) {
   return ATHG_OK;
 }
 
+int athg_resume(athg_ctx* c) {
+  int rc = need_pool(c);
+  if (rc) return rc;
+  // Mesh::Initialize on a restart (res_flag = 1): time, dt and ncycle stay as read from
+  // the restart file (athg_set_time); ghosts, W(U), then NewTimeStep from the stored dt
+  unsigned long long big;
+  std::memcpy(&big, &kDblMax, 8);
+  CK(cudaMemcpyAsync(c->scal + 3, &big, 8, cudaMemcpyHostToDevice, c->st));
+  if (c->grav && (rc = gravity_solve(c))) return rc;
+  if ((rc = launch_ghosts(c))) return rc;
+  c->ghosts_stale = false;
+  if ((rc = launch_c2p(c))) return rc;
+  if ((rc = launch_block_dt(c))) return rc;
+  if ((rc = launch_end(c, 0))) return rc;
+  CK(cudaStreamSynchronize(c->st));
+  return ATHG_OK;
+}
+
 int athg_stage(athg_ctx* c, int stage) {
   int rc = need_pool(c);
   if (rc) return rc;

@@ -7,6 +7,11 @@
 // (magnetic fields, Riemann solver) are runtime keys of a <gb300> block here.
 //
 //   athg_run -i athinput.orszag_tang [mesh/nx1=128 time/nlim=10 ...]
+//   athg_run -r OrszagTang.00001.rst [time/nlim=10 ...]     restart (also from the reference)
+//
+// Outputs (<outputN> blocks, outputs/outputs.cpp:786-803 timing): file_type = hst (history
+// sums), vtk (variable = prim | cons, outputs/vtk.cpp) and rst (restart files readable by
+// the reference, outputs/restart.cpp; a final <problem_id>.final.rst at the end).
 //
 // Problem generators: orszag_tang (src/pgen/orszag_tang.cpp:42-115) and blast
 // (src/pgen/blast.cpp:54-120, uniform sphere of high pressure, optional uniform field).
@@ -22,6 +27,7 @@
 #include <vector>
 
 #include "athena_gb300.h"
+#include "athg_io.h"
 
 namespace {
 
@@ -32,10 +38,9 @@ std::string trim(const std::string& s) {
   return a == std::string::npos ? std::string() : s.substr(a, b - a + 1);
 }
 
-// athinput: "<block>" lines, "key = value # comment" lines (inputs/parameter_input.cpp)
-bool read_athinput(const std::string& path, Params& p) {
-  std::ifstream f(path);
-  if (!f) return false;
+// athinput: "<block>" lines, "key = value # comment" lines (inputs/parameter_input.cpp);
+// a restart file's parameter dump ends at "<par_end>"
+void parse_athinput(std::istream& f, Params& p) {
   std::string line, block;
   while (std::getline(f, line)) {
     size_t h = line.find('#');
@@ -51,7 +56,34 @@ bool read_athinput(const std::string& path, Params& p) {
     if (eq == std::string::npos) continue;
     p[block + "/" + trim(line.substr(0, eq))] = trim(line.substr(eq + 1));
   }
+}
+
+bool read_athinput(const std::string& path, Params& p) {
+  std::ifstream f(path);
+  if (!f) return false;
+  parse_athinput(f, p);
   return true;
+}
+
+// ParameterInput::ParameterDump (parameter_input.cpp:834-859): blocks, "name = value"
+// lines, closed by "<par_end>"
+std::string dump_params(const Params& p) {
+  std::ostringstream os;
+  os << "#------------------------- PAR_DUMP -------------------------\n";
+  std::string cur;
+  for (const auto& kv : p) {
+    const size_t sl = kv.first.find('/');
+    const std::string block = kv.first.substr(0, sl), key = kv.first.substr(sl + 1);
+    if (block == "par_end") continue;
+    if (block != cur) {
+      os << "<" << block << ">\n";
+      cur = block;
+    }
+    os << key << " = " << kv.second << "\n";
+  }
+  os << "#------------------------- PAR_DUMP -------------------------\n";
+  os << "<par_end>\n";
+  return os.str();
 }
 
 std::string get(const Params& p, const std::string& k, const std::string& def) {
@@ -93,18 +125,28 @@ Axis axis_of(int nx, int ng, double lo, double hi, int64_t off, int64_t ntot) {
 
 int main(int argc, char** argv) {
   Params p;
-  std::string input;
+  std::string input, restart;
   for (int a = 1; a < argc; ++a) {
     if (!std::strcmp(argv[a], "-i") && a + 1 < argc) {
       input = argv[++a];
+    } else if (!std::strcmp(argv[a], "-r") && a + 1 < argc) {
+      restart = argv[++a];
     } else if (std::strchr(argv[a], '=')) {
       std::string s = argv[a];
       size_t eq = s.find('=');
       p["__cli__" + s.substr(0, eq)] = s.substr(eq + 1);
     }
   }
-  if (input.empty() || !read_athinput(input, p)) {
-    std::fprintf(stderr, "usage: athg_run -i athinput [block/key=value ...]\n");
+  if (!restart.empty()) {
+    std::string text, err;
+    if (!athg_io::read_restart_params(restart, &text, &err)) {
+      std::fprintf(stderr, "### FATAL ERROR reading %s: %s\n", restart.c_str(), err.c_str());
+      return 1;
+    }
+    std::istringstream is(text);
+    parse_athinput(is, p);
+  } else if (input.empty() || !read_athinput(input, p)) {
+    std::fprintf(stderr, "usage: athg_run -i athinput | -r file.rst [block/key=value ...]\n");
     return 1;
   }
   for (auto it = p.begin(); it != p.end();) {  // command-line overrides win
@@ -153,153 +195,313 @@ int main(int argc, char** argv) {
 
   athg_ctx* ctx = nullptr;
   check(athg_create(&c, &ctx), "athg_create");
-  check(athg_set_uniform_mesh(ctx, &m), "athg_set_uniform_mesh");
-  int nb = 0;
-  check(athg_num_blocks(ctx, &nb), "athg_num_blocks");
-  const int ng = c.nghost;
-  const int n1 = c.nx1 + 2 * ng, n2 = c.nx2 + 2 * ng, n3 = c.nx3 + 2 * ng;
-  const size_t nc = (size_t)n1 * n2 * n3;
-
-  // MeshBlock::ProblemGenerator for every block, then one upload per array
-  std::vector<double> U(5 * nc * nb, 0.0), B1, B2, B3;
-  if (mhd) {
-    B1.assign((size_t)n3 * n2 * (n1 + 1) * nb, 0.0);
-    B2.assign((size_t)n3 * (n2 + 1) * n1 * nb, 0.0);
-    B3.assign((size_t)(n3 + 1) * n2 * n1 * nb, 0.0);
-  }
-  const double gm1 = c.gamma - 1.0;
-  for (int b = 0; b < nb; ++b) {
-    int64_t loc[4];
-    check(athg_block_location(ctx, b, loc), "athg_block_location");
-    Axis ax = axis_of(c.nx1, ng, m.x1min, m.x1max, loc[0] * c.nx1, m.nx1);
-    Axis ay = axis_of(c.nx2, ng, m.x2min, m.x2max, loc[1] * c.nx2, m.nx2);
-    Axis az = axis_of(c.nx3, ng, m.x3min, m.x3max, loc[2] * c.nx3, m.nx3);
-    double* u = &U[5 * nc * b];
-    auto C = [&](int n, int k, int j, int i) -> double& {
-      return u[(size_t)n * nc + ((size_t)k * n2 + j) * n1 + i];
-    };
-    double* b1 = mhd ? &B1[(size_t)n3 * n2 * (n1 + 1) * b] : nullptr;
-    double* b2 = mhd ? &B2[(size_t)n3 * (n2 + 1) * n1 * b] : nullptr;
-    double* b3 = mhd ? &B3[(size_t)(n3 + 1) * n2 * n1 * b] : nullptr;
-    auto F1 = [&](int k, int j, int i) -> double& { return b1[((size_t)k * n2 + j) * (n1 + 1) + i]; };
-    auto F2 = [&](int k, int j, int i) -> double& { return b2[((size_t)k * (n2 + 1) + j) * n1 + i]; };
-    auto F3 = [&](int k, int j, int i) -> double& { return b3[((size_t)k * n2 + j) * n1 + i]; };
-    const int is = ng, ie = ng + c.nx1 - 1, js = ng, je = ng + c.nx2 - 1, ks = ng, ke = ng + c.nx3 - 1;
-    if (pgen == "orszag_tang") {
-      const double PI = 3.1415926535897932, TWO_PI = 6.2831853071795862;
-      const double B0 = 1.0 / std::sqrt(4.0 * PI), d0 = 25.0 / (36.0 * PI), v0 = 1.0,
-                   p0 = 5.0 / (12.0 * PI);
-      auto Az = [&](double x, double y) {
-        return B0 / (4.0 * PI) * (std::cos(4.0 * PI * x) - 2.0 * std::cos(TWO_PI * y));
-      };
-      for (int k = ks; k <= ke; ++k)
-        for (int j = js; j <= je; ++j)
-          for (int i = is; i <= ie; ++i) {
-            C(0, k, j, i) = d0;
-            C(1, k, j, i) = d0 * v0 * std::sin(TWO_PI * ay.xv[j]);
-            C(2, k, j, i) = -d0 * v0 * std::sin(TWO_PI * ax.xv[i]);
-            C(3, k, j, i) = 0.0;
-          }
-      if (mhd) {
-        for (int k = ks; k <= ke; ++k)
-          for (int j = js; j <= je; ++j)
-            for (int i = is; i <= ie + 1; ++i)
-              F1(k, j, i) = (Az(ax.xf[i], ay.xf[j + 1]) - Az(ax.xf[i], ay.xf[j])) / ay.dx;
-        for (int k = ks; k <= ke; ++k)
-          for (int j = js; j <= je + 1; ++j)
-            for (int i = is; i <= ie; ++i)
-              F2(k, j, i) = (Az(ax.xf[i], ay.xf[j]) - Az(ax.xf[i + 1], ay.xf[j])) / ax.dx;
-      }
-      for (int k = ks; k <= ke; ++k)
-        for (int j = js; j <= je; ++j)
-          for (int i = is; i <= ie; ++i) {
-            double pb = 0.0;
-            if (mhd) {
-              double c1 = 0.5 * (F1(k, j, i) + F1(k, j, i + 1));
-              double c2 = 0.5 * (F2(k, j, i) + F2(k, j + 1, i));
-              pb = 0.5 * (c1 * c1 + c2 * c2);
-            }
-            const double d = C(0, k, j, i);
-            C(4, k, j, i) = p0 / gm1 + pb +
-                            0.5 * (C(1, k, j, i) * C(1, k, j, i) + C(2, k, j, i) * C(2, k, j, i)) / d;
-          }
-    } else if (pgen == "blast") {
-      const double rad = getd(p, "problem/radius", 0.1), pa = getd(p, "problem/pamb", 0.1),
-                   prat = getd(p, "problem/prat", 100.0), da = getd(p, "problem/damb", 1.0),
-                   b0 = getd(p, "problem/b0", mhd ? 1.0 : 0.0),
-                   ang = getd(p, "problem/angle", 45.0) * 3.1415926535897932 / 180.0;
-      const double bx = b0 * std::cos(ang), by = b0 * std::sin(ang);
-      if (mhd) {
-        for (int k = ks; k <= ke; ++k) {
-          for (int j = js; j <= je; ++j)
-            for (int i = is; i <= ie + 1; ++i) F1(k, j, i) = bx;
-          for (int j = js; j <= je + 1; ++j)
-            for (int i = is; i <= ie; ++i) F2(k, j, i) = by;
-        }
-      }
-      for (int k = ks; k <= ke; ++k)
-        for (int j = js; j <= je; ++j)
-          for (int i = is; i <= ie; ++i) {
-            const double r = std::sqrt(ax.xv[i] * ax.xv[i] + ay.xv[j] * ay.xv[j] + az.xv[k] * az.xv[k]);
-            const double pr = r < rad ? pa * prat : pa;
-            C(0, k, j, i) = da;
-            C(1, k, j, i) = C(2, k, j, i) = C(3, k, j, i) = 0.0;
-            C(4, k, j, i) = pr / gm1 + (mhd ? 0.5 * (bx * bx + by * by) : 0.0);
-          }
-    } else {
-      std::fprintf(stderr, "### FATAL ERROR: unknown gb300/pgen %s\n", pgen.c_str());
+  // the mesh as the restart/VTK writers describe it
+  athg_io::State st;
+  st.mesh_nx[0] = m.nx1; st.mesh_nx[1] = m.nx2; st.mesh_nx[2] = m.nx3;
+  st.xmin[0] = m.x1min; st.xmin[1] = m.x2min; st.xmin[2] = m.x3min;
+  st.xmax[0] = m.x1max; st.xmax[1] = m.x2max; st.xmax[2] = m.x3max;
+  st.block_nx[0] = c.nx1; st.block_nx[1] = c.nx2; st.block_nx[2] = c.nx3;
+  st.ng = c.nghost;
+  st.mhd = mhd;
+  if (!restart.empty()) {
+    // Mesh::Mesh(pin, restartfile) + Mesh::Initialize(res_flag = 1)
+    std::string text, err;
+    if (!athg_io::read_restart(restart, &text, &st, &err)) {
+      std::fprintf(stderr, "### FATAL ERROR reading %s: %s\n", restart.c_str(), err.c_str());
       return 1;
     }
-  }
-  check(athg_upload(ctx, -1, ATHG_VAR_CONS, U.data(), U.size()), "upload U");
-  if (mhd) {
-    check(athg_upload(ctx, -1, ATHG_VAR_B1F, B1.data(), B1.size()), "upload B1");
-    check(athg_upload(ctx, -1, ATHG_VAR_B2F, B2.data(), B2.size()), "upload B2");
-    check(athg_upload(ctx, -1, ATHG_VAR_B3F, B3.data(), B3.size()), "upload B3");
-  }
-  check(athg_initialize(ctx), "athg_initialize");
+    const int nf = (int)st.blocks.size();
+    bool multi = false;
+    std::vector<int64_t> locs(4 * nf);
+    for (int q = 0; q < nf; ++q) {
+      multi = multi || st.blocks[q].level != 0;
+      locs[4 * q] = st.blocks[q].level;
+      for (int d = 0; d < 3; ++d) locs[4 * q + 1 + d] = st.blocks[q].lx[d];
+    }
+    if (multi) check(athg_set_multilevel_blocks(ctx, &m, nf, locs.data()), "athg_set_multilevel_blocks");
+    else check(athg_set_uniform_mesh(ctx, &m), "athg_set_uniform_mesh");
+    int nlib = 0;
+    check(athg_num_blocks(ctx, &nlib), "athg_num_blocks");
+    if (nlib != nf) {
+      std::fprintf(stderr, "### FATAL ERROR: restart file has %d blocks, the mesh %d\n", nf, nlib);
+      return 1;
+    }
+    std::map<std::vector<int64_t>, int> lib_of;
+    for (int b = 0; b < nlib; ++b) {
+      int64_t loc[4];
+      check(athg_block_location(ctx, b, loc), "athg_block_location");
+      lib_of[{loc[3], loc[0], loc[1], loc[2]}] = b;
+    }
+    const size_t nu = 5 * st.cell_count();
+    const size_t nfc[3] = {st.face_count(0), st.face_count(1), st.face_count(2)};
+    for (int q = 0; q < nf; ++q) {
+      auto it = lib_of.find({st.blocks[q].level, st.blocks[q].lx[0], st.blocks[q].lx[1], st.blocks[q].lx[2]});
+      if (it == lib_of.end()) {
+        std::fprintf(stderr, "### FATAL ERROR: restart block not in the mesh\n");
+        return 1;
+      }
+      const int b = it->second;
+      check(athg_upload(ctx, b, ATHG_VAR_CONS, &st.u[q * nu], nu), "upload U");
+      if (mhd) {
+        check(athg_upload(ctx, b, ATHG_VAR_B1F, &st.b1[q * nfc[0]], nfc[0]), "upload B1");
+        check(athg_upload(ctx, b, ATHG_VAR_B2F, &st.b2[q * nfc[1]], nfc[1]), "upload B2");
+        check(athg_upload(ctx, b, ATHG_VAR_B3F, &st.b3[q * nfc[2]], nfc[2]), "upload B3");
+      }
+    }
+    check(athg_set_time(ctx, st.time, st.dt, st.ncycle), "athg_set_time");
+    check(athg_resume(ctx), "athg_resume");
+  } else {
+    check(athg_set_uniform_mesh(ctx, &m), "athg_set_uniform_mesh");
+    int nb = 0;
+    check(athg_num_blocks(ctx, &nb), "athg_num_blocks");
+    const int ng = c.nghost;
+    const int n1 = c.nx1 + 2 * ng, n2 = c.nx2 + 2 * ng, n3 = c.nx3 + 2 * ng;
+    const size_t nc = (size_t)n1 * n2 * n3;
 
-  // history output (<output1> file_type = hst, dt)
+    // MeshBlock::ProblemGenerator for every block, then one upload per array
+    std::vector<double> U(5 * nc * nb, 0.0), B1, B2, B3;
+    if (mhd) {
+      B1.assign((size_t)n3 * n2 * (n1 + 1) * nb, 0.0);
+      B2.assign((size_t)n3 * (n2 + 1) * n1 * nb, 0.0);
+      B3.assign((size_t)(n3 + 1) * n2 * n1 * nb, 0.0);
+    }
+    const double gm1 = c.gamma - 1.0;
+    for (int b = 0; b < nb; ++b) {
+      int64_t loc[4];
+      check(athg_block_location(ctx, b, loc), "athg_block_location");
+      Axis ax = axis_of(c.nx1, ng, m.x1min, m.x1max, loc[0] * c.nx1, m.nx1);
+      Axis ay = axis_of(c.nx2, ng, m.x2min, m.x2max, loc[1] * c.nx2, m.nx2);
+      Axis az = axis_of(c.nx3, ng, m.x3min, m.x3max, loc[2] * c.nx3, m.nx3);
+      double* u = &U[5 * nc * b];
+      auto C = [&](int n, int k, int j, int i) -> double& {
+        return u[(size_t)n * nc + ((size_t)k * n2 + j) * n1 + i];
+      };
+      double* b1 = mhd ? &B1[(size_t)n3 * n2 * (n1 + 1) * b] : nullptr;
+      double* b2 = mhd ? &B2[(size_t)n3 * (n2 + 1) * n1 * b] : nullptr;
+      double* b3 = mhd ? &B3[(size_t)(n3 + 1) * n2 * n1 * b] : nullptr;
+      auto F1 = [&](int k, int j, int i) -> double& { return b1[((size_t)k * n2 + j) * (n1 + 1) + i]; };
+      auto F2 = [&](int k, int j, int i) -> double& { return b2[((size_t)k * (n2 + 1) + j) * n1 + i]; };
+      (void)b3;
+      const int is = ng, ie = ng + c.nx1 - 1, js = ng, je = ng + c.nx2 - 1, ks = ng, ke = ng + c.nx3 - 1;
+      if (pgen == "orszag_tang") {
+        const double PI = 3.1415926535897932, TWO_PI = 6.2831853071795862;
+        const double B0 = 1.0 / std::sqrt(4.0 * PI), d0 = 25.0 / (36.0 * PI), v0 = 1.0,
+                     p0 = 5.0 / (12.0 * PI);
+        auto Az = [&](double x, double y) {
+          return B0 / (4.0 * PI) * (std::cos(4.0 * PI * x) - 2.0 * std::cos(TWO_PI * y));
+        };
+        for (int k = ks; k <= ke; ++k)
+          for (int j = js; j <= je; ++j)
+            for (int i = is; i <= ie; ++i) {
+              C(0, k, j, i) = d0;
+              C(1, k, j, i) = d0 * v0 * std::sin(TWO_PI * ay.xv[j]);
+              C(2, k, j, i) = -d0 * v0 * std::sin(TWO_PI * ax.xv[i]);
+              C(3, k, j, i) = 0.0;
+            }
+        if (mhd) {
+          for (int k = ks; k <= ke; ++k)
+            for (int j = js; j <= je; ++j)
+              for (int i = is; i <= ie + 1; ++i)
+                F1(k, j, i) = (Az(ax.xf[i], ay.xf[j + 1]) - Az(ax.xf[i], ay.xf[j])) / ay.dx;
+          for (int k = ks; k <= ke; ++k)
+            for (int j = js; j <= je + 1; ++j)
+              for (int i = is; i <= ie; ++i)
+                F2(k, j, i) = (Az(ax.xf[i], ay.xf[j]) - Az(ax.xf[i + 1], ay.xf[j])) / ax.dx;
+        }
+        for (int k = ks; k <= ke; ++k)
+          for (int j = js; j <= je; ++j)
+            for (int i = is; i <= ie; ++i) {
+              double pb = 0.0;
+              if (mhd) {
+                double c1 = 0.5 * (F1(k, j, i) + F1(k, j, i + 1));
+                double c2 = 0.5 * (F2(k, j, i) + F2(k, j + 1, i));
+                pb = 0.5 * (c1 * c1 + c2 * c2);
+              }
+              const double d = C(0, k, j, i);
+              C(4, k, j, i) = p0 / gm1 + pb +
+                              0.5 * (C(1, k, j, i) * C(1, k, j, i) + C(2, k, j, i) * C(2, k, j, i)) / d;
+            }
+      } else if (pgen == "blast") {
+        const double rad = getd(p, "problem/radius", 0.1), pa = getd(p, "problem/pamb", 0.1),
+                     prat = getd(p, "problem/prat", 100.0), da = getd(p, "problem/damb", 1.0),
+                     b0 = getd(p, "problem/b0", mhd ? 1.0 : 0.0),
+                     ang = getd(p, "problem/angle", 45.0) * 3.1415926535897932 / 180.0;
+        const double bx = b0 * std::cos(ang), by = b0 * std::sin(ang);
+        if (mhd) {
+          for (int k = ks; k <= ke; ++k) {
+            for (int j = js; j <= je; ++j)
+              for (int i = is; i <= ie + 1; ++i) F1(k, j, i) = bx;
+            for (int j = js; j <= je + 1; ++j)
+              for (int i = is; i <= ie; ++i) F2(k, j, i) = by;
+          }
+        }
+        for (int k = ks; k <= ke; ++k)
+          for (int j = js; j <= je; ++j)
+            for (int i = is; i <= ie; ++i) {
+              const double r = std::sqrt(ax.xv[i] * ax.xv[i] + ay.xv[j] * ay.xv[j] + az.xv[k] * az.xv[k]);
+              const double pr = r < rad ? pa * prat : pa;
+              C(0, k, j, i) = da;
+              C(1, k, j, i) = C(2, k, j, i) = C(3, k, j, i) = 0.0;
+              C(4, k, j, i) = pr / gm1 + (mhd ? 0.5 * (bx * bx + by * by) : 0.0);
+            }
+      } else {
+        std::fprintf(stderr, "### FATAL ERROR: unknown gb300/pgen %s\n", pgen.c_str());
+        return 1;
+      }
+    }
+    check(athg_upload(ctx, -1, ATHG_VAR_CONS, U.data(), U.size()), "upload U");
+    if (mhd) {
+      check(athg_upload(ctx, -1, ATHG_VAR_B1F, B1.data(), B1.size()), "upload B1");
+      check(athg_upload(ctx, -1, ATHG_VAR_B2F, B2.data(), B2.size()), "upload B2");
+      check(athg_upload(ctx, -1, ATHG_VAR_B3F, B3.data(), B3.size()), "upload B3");
+    }
+    check(athg_initialize(ctx), "athg_initialize");
+  }
+
+  // outputs: <outputN> file_type = hst | vtk | rst (Outputs::MakeOutputs timing)
   const std::string base = get(p, "job/problem_id", pgen);
-  const double hst_dt = getd(p, "output1/dt", -1.0);
-  std::FILE* hst = std::fopen((base + ".hst").c_str(), "w");
-  std::fprintf(hst, "# Athena++ history data (athg_run)\n"
-                    "# [1]=time [2]=dt [3]=mass [4]=1-mom [5]=2-mom [6]=3-mom [7]=1-KE [8]=2-KE "
-                    "[9]=3-KE [10]=tot-E [11]=grav-E [12]=1-ME [13]=2-ME [14]=3-ME\n");
-  auto write_hst = [&]() {
-    double h[12], t, dt;
-    int n;
-    int64_t nc_;
-    check(athg_history(ctx, h, &n), "athg_history");
-    check(athg_get_time(ctx, &t, &dt, &nc_), "athg_get_time");
-    std::fprintf(hst, "%.14e %.14e", t, dt);
-    for (int q = 0; q < n; ++q) std::fprintf(hst, " %.14e", h[q]);
-    std::fprintf(hst, "\n");
+  struct Out {
+    int id;
+    std::string type, var;
+    double dt, next;
+    int number;
   };
-  write_hst();
-  double t, dt, next_hst = hst_dt;
+  double t = 0.0, dt = 0.0;
   int64_t ncycle = 0;
   check(athg_get_time(ctx, &t, &dt, &ncycle), "athg_get_time");
+  const double start_time = t;
+  std::vector<Out> outs;
+  for (int id = 1; id < 100; ++id) {
+    const std::string blk = "output" + std::to_string(id) + "/";
+    if (!p.count(blk + "file_type")) continue;
+    Out o;
+    o.id = id;
+    o.type = get(p, blk + "file_type", "hst");
+    o.var = get(p, blk + "variable", "prim");
+    o.dt = getd(p, blk + "dt", -1.0);
+    o.next = getd(p, blk + "next_time", start_time);
+    o.number = geti(p, blk + "file_number", 0);
+    outs.push_back(o);
+  }
+  std::FILE* hst = nullptr;
+  bool hst_header = false;
+  int nb_all = 0;
+  check(athg_num_blocks(ctx, &nb_all), "athg_num_blocks");
+  // every block's location and arrays, in the library's order
+  auto download_state = [&](bool prim) {
+    st.blocks.resize(nb_all);
+    for (int b = 0; b < nb_all; ++b) {
+      int64_t loc[4];
+      check(athg_block_location(ctx, b, loc), "athg_block_location");
+      st.blocks[b].level = (int)loc[3];
+      for (int d = 0; d < 3; ++d) st.blocks[b].lx[d] = loc[d];
+    }
+    st.u.resize(5 * st.cell_count() * nb_all);
+    check(athg_download(ctx, -1, ATHG_VAR_CONS, st.u.data(), st.u.size()), "download U");
+    if (mhd) {
+      st.b1.resize(st.face_count(0) * nb_all);
+      st.b2.resize(st.face_count(1) * nb_all);
+      st.b3.resize(st.face_count(2) * nb_all);
+      check(athg_download(ctx, -1, ATHG_VAR_B1F, st.b1.data(), st.b1.size()), "download B1");
+      check(athg_download(ctx, -1, ATHG_VAR_B2F, st.b2.data(), st.b2.size()), "download B2");
+      check(athg_download(ctx, -1, ATHG_VAR_B3F, st.b3.data(), st.b3.size()), "download B3");
+    }
+    double tt, dd;
+    int64_t nn;
+    check(athg_get_time(ctx, &tt, &dd, &nn), "athg_get_time");
+    st.time = tt; st.dt = dd; st.ncycle = (int)nn;
+    std::vector<double> w, bcc;
+    if (prim) {
+      w.resize(5 * st.cell_count() * nb_all);
+      check(athg_download(ctx, -1, ATHG_VAR_PRIM, w.data(), w.size()), "download W");
+      if (mhd) {
+        bcc.resize(3 * st.cell_count() * nb_all);
+        check(athg_download(ctx, -1, ATHG_VAR_BCC, bcc.data(), bcc.size()), "download Bcc");
+      }
+    }
+    return std::make_pair(w, bcc);
+  };
+  auto write_output = [&](Out& o, bool final) {
+    const std::string blk = "output" + std::to_string(o.id) + "/";
+    std::string err;
+    if (o.type == "hst") {  // HistoryOutput::WriteOutputFile (outputs/history.cpp)
+      if (!hst) hst = std::fopen((base + ".hst").c_str(), restart.empty() ? "w" : "a");
+      if (!hst_header && restart.empty()) {
+        std::fprintf(hst, "# Athena++ history data (athg_run)\n"
+                          "# [1]=time [2]=dt [3]=mass [4]=1-mom [5]=2-mom [6]=3-mom [7]=1-KE "
+                          "[8]=2-KE [9]=3-KE [10]=tot-E [11]=grav-E [12]=1-ME [13]=2-ME [14]=3-ME\n");
+      }
+      hst_header = true;
+      double h[12], tt, dd;
+      int n;
+      int64_t nn;
+      check(athg_history(ctx, h, &n), "athg_history");
+      check(athg_get_time(ctx, &tt, &dd, &nn), "athg_get_time");
+      std::fprintf(hst, "%.14e %.14e", tt, dd);
+      for (int q = 0; q < n; ++q) std::fprintf(hst, " %.14e", h[q]);
+      std::fprintf(hst, "\n");
+      std::fflush(hst);
+      o.next += o.dt;
+    } else if (o.type == "vtk") {  // VTKOutput::WriteOutputFile
+      auto wb = download_state(true);
+      if (!athg_io::write_vtk(base, "out" + std::to_string(o.id), o.number, o.var, st, wb.first,
+                              wb.second, &err)) {
+        std::fprintf(stderr, "### FATAL ERROR in vtk output: %s\n", err.c_str());
+        std::exit(1);
+      }
+      o.number++;
+      o.next += o.dt;
+    } else if (o.type == "rst") {  // RestartOutput::WriteOutputFile
+      char num[16];
+      std::snprintf(num, sizeof(num), "%05d", o.number);
+      const std::string fname = base + "." + (final ? std::string("final") : std::string(num)) + ".rst";
+      if (!final) {
+        o.number++;
+        o.next += o.dt;
+      }
+      p[blk + "file_number"] = std::to_string(o.number);
+      char nt[64];
+      std::snprintf(nt, sizeof(nt), "%.17g", o.next);
+      p[blk + "next_time"] = nt;
+      download_state(false);
+      if (!athg_io::write_restart(fname, dump_params(p), st, &err)) {
+        std::fprintf(stderr, "### FATAL ERROR in restart output: %s\n", err.c_str());
+        std::exit(1);
+      }
+      return;
+    }
+    p[blk + "file_number"] = std::to_string(o.number);
+    char nt[64];
+    std::snprintf(nt, sizeof(nt), "%.17g", o.next);
+    p[blk + "next_time"] = nt;
+  };
+  auto make_outputs = [&](bool final) {
+    double tt, dd;
+    int64_t nn;
+    check(athg_get_time(ctx, &tt, &dd, &nn), "athg_get_time");
+    for (Out& o : outs)
+      if (tt == start_time || (o.dt > 0.0 && tt >= o.next) || tt >= c.tlim ||
+          (final && (o.type == "rst" || o.type == "hst")))  // history: a closing row
+        write_output(o, final);
+  };
+  make_outputs(false);
   const auto t0 = std::chrono::steady_clock::now();
   int64_t cycles = 0;
-  while (t < c.tlim && (nlim < 0 || cycles < nlim)) {
+  while (t < c.tlim && (nlim < 0 || ncycle < nlim)) {
     check(athg_cycles(ctx, 1), "athg_cycles");
     ++cycles;
     check(athg_get_time(ctx, &t, &dt, &ncycle), "athg_get_time");
-    if (hst_dt > 0.0 && t >= next_hst) {
-      write_hst();
-      next_hst += hst_dt;
-    }
+    make_outputs(false);
   }
   check(athg_synchronize(ctx), "athg_synchronize");
   const double el = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
-  write_hst();
-  std::fclose(hst);
-  const double zones = (double)m.nx1 * m.nx2 * m.nx3;
+  make_outputs(true);
+  if (hst) std::fclose(hst);
+  const double zones = (double)nb_all * c.nx1 * c.nx2 * c.nx3;
   // main.cpp:580-600 summary
   std::printf("cycle=%lld time=%.10e dt=%.10e\n", (long long)ncycle, t, dt);
   std::printf("zone-cycles = %.0f\nwall time = %.6f s\nzone-cycles/wsecond = %.6e\n",
-              zones * cycles, el, zones * cycles / el);
+              zones * cycles, el, cycles > 0 ? zones * cycles / el : 0.0);
   athg_destroy(ctx);
   return 0;
 }

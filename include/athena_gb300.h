@@ -129,6 +129,10 @@ int athg_download(athg_ctx* ctx, int block, int var, double* host, size_t count)
 /* Tail of Mesh::Initialize (mesh/mesh.cpp:1405-1649): ghost exchange, W(U) over interior
  * and ghosts, first NewBlockTimeStep and Mesh::NewTimeStep. */
 int athg_initialize(athg_ctx* ctx);
+/* Mesh::Initialize after a restart (res_flag = 1, mesh/mesh.cpp:1367-1656): the same, but
+ * time, dt and ncycle keep the values set by athg_set_time (read from the restart file),
+ * and the first Mesh::NewTimeStep starts from that dt. */
+int athg_resume(athg_ctx* ctx);
 /* One stage (1-based) of TimeIntegratorTaskList::DoTaskListOneStage
  * (task_list/task_list.cpp:66) over every block: CalculateHydroFlux (donor cell on the
  * first VL2 stage), CalculateEMF, IntegrateHydro, IntegrateField, ghost exchange,
