@@ -251,7 +251,23 @@ int main(int argc, char** argv) {
     check(athg_set_time(ctx, st.time, st.dt, st.ncycle), "athg_set_time");
     check(athg_resume(ctx), "athg_resume");
   } else {
-    check(athg_set_uniform_mesh(ctx, &m), "athg_set_uniform_mesh");
+    // <refinementN> blocks (static refinement, mesh/mesh.cpp:334-462)
+    std::vector<athg_region> regions;
+    for (int id = 1; id < 100; ++id) {
+      const std::string blk = "refinement" + std::to_string(id) + "/";
+      if (!p.count(blk + "level")) continue;
+      athg_region r{};
+      r.x1min = getd(p, blk + "x1min", m.x1min); r.x1max = getd(p, blk + "x1max", m.x1max);
+      r.x2min = getd(p, blk + "x2min", m.x2min); r.x2max = getd(p, blk + "x2max", m.x2max);
+      r.x3min = getd(p, blk + "x3min", m.x3min); r.x3max = getd(p, blk + "x3max", m.x3max);
+      r.level = geti(p, blk + "level", 1);
+      regions.push_back(r);
+    }
+    if (!regions.empty())
+      check(athg_set_refined_mesh(ctx, &m, (int)regions.size(), regions.data()),
+            "athg_set_refined_mesh");
+    else
+      check(athg_set_uniform_mesh(ctx, &m), "athg_set_uniform_mesh");
     int nb = 0;
     check(athg_num_blocks(ctx, &nb), "athg_num_blocks");
     const int ng = c.nghost;
@@ -269,9 +285,11 @@ int main(int argc, char** argv) {
     for (int b = 0; b < nb; ++b) {
       int64_t loc[4];
       check(athg_block_location(ctx, b, loc), "athg_block_location");
-      Axis ax = axis_of(c.nx1, ng, m.x1min, m.x1max, loc[0] * c.nx1, m.nx1);
-      Axis ay = axis_of(c.nx2, ng, m.x2min, m.x2max, loc[1] * c.nx2, m.nx2);
-      Axis az = axis_of(c.nx3, ng, m.x3min, m.x3max, loc[2] * c.nx3, m.nx3);
+      // cells of the block's level (loc[3]) across the whole domain
+      const int64_t lv = loc[3];
+      Axis ax = axis_of(c.nx1, ng, m.x1min, m.x1max, loc[0] * c.nx1, (int64_t)m.nx1 << lv);
+      Axis ay = axis_of(c.nx2, ng, m.x2min, m.x2max, loc[1] * c.nx2, (int64_t)m.nx2 << lv);
+      Axis az = axis_of(c.nx3, ng, m.x3min, m.x3max, loc[2] * c.nx3, (int64_t)m.nx3 << lv);
       double* u = &U[5 * nc * b];
       auto C = [&](int n, int k, int j, int i) -> double& {
         return u[(size_t)n * nc + ((size_t)k * n2 + j) * n1 + i];

@@ -136,3 +136,40 @@ def test_driver_vtk_output(tmp_path):
     np.testing.assert_allclose(rho, 25.0 / (36.0 * np.pi), rtol=1e-6)
     for tag in (b"SCALARS press float", b"VECTORS vel float", b"VECTORS Bcc float"):
         assert tag in data
+
+
+def test_driver_refined_blast_restart_is_seamless(tmp_path):
+    """Blast with a refined central region from athinput.blast_smr (reduced to a 32^3 root
+    grid of 8^3 blocks): mass and energy are conserved across the level boundaries, and a
+    run restarted from its own restart file after 2 cycles ends, after 4, bit for bit where
+    the uninterrupted run ends (multi-level restart through athg_set_multilevel_blocks)."""
+    import __graft_entry__ as g
+    import rst_lib
+    exe = g.build_driver()
+    inp = os.path.join(PKG, "inputs", "athinput.blast_smr")
+    small = ["mesh/nx1=32", "mesh/nx2=32", "mesh/nx3=32", "meshblock/nx1=8", "meshblock/nx2=8",
+             "meshblock/nx3=8", "output1/dt=-1", "output2/file_type=rst", "output2/dt=100.0"]
+    runs = {}
+    for name, extra in (("full", ["time/nlim=4"]), ("half", ["time/nlim=2"])):
+        wd = tmp_path / name
+        wd.mkdir()
+        r = subprocess.run([exe, "-i", inp] + small + extra, cwd=wd, capture_output=True,
+                           text=True, timeout=600)
+        assert r.returncode == 0, r.stdout + r.stderr
+        runs[name] = wd
+    rows = np.loadtxt(os.path.join(runs["full"], "Blast.hst"))
+    np.testing.assert_allclose(rows[-1][2], rows[0][2], rtol=1e-13)   # mass
+    np.testing.assert_allclose(rows[-1][9], rows[0][9], rtol=1e-13)   # total energy
+    wd = tmp_path / "resumed"
+    wd.mkdir()
+    r = subprocess.run([exe, "-r", os.path.join(runs["half"], "Blast.final.rst"), "time/nlim=4"],
+                       cwd=wd, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr
+    a = rst_lib.read_rst(os.path.join(runs["full"], "Blast.final.rst"), (8, 8, 8), 4, True)
+    b = rst_lib.read_rst(os.path.join(wd, "Blast.final.rst"), (8, 8, 8), 4, True)
+    assert a["ncycle"] == b["ncycle"] == 4 and a["time"] == b["time"]
+    assert a["blocks"] == b["blocks"] and len(a["blocks"]) == 120
+    assert sum(1 for bl in a["blocks"] if bl[0] == 1) == 64
+    for x, y in zip(a["arrays"], b["arrays"]):
+        for k in x:
+            np.testing.assert_array_equal(x[k], y[k])
