@@ -37,7 +37,7 @@ EXPORTS = [
     "athg_mg_stream", "athg_mg_multipole", "athg_attach_gravity", "athg_history",
     "athg_get_tuning", "athg_set_tuning",
     "athg_block_cfl_dt_noalloc", "athg_set_refined_mesh", "athg_set_multilevel_blocks",
-    "athg_smr_stats", "athg_resume",
+    "athg_smr_stats", "athg_resume", "athg_cycle_timing",
 ]
 MG_BC = {"periodic": 0, "zerograd": 1, "zerofixed": 2, "multipole": 3}
 
@@ -134,6 +134,7 @@ def lib():
         "athg_set_multilevel_blocks": [vp, C.POINTER(Mesh), i, C.POINTER(C.c_int64)],
         "athg_smr_stats": [vp, C.POINTER(C.c_int64)],
         "athg_resume": [vp],
+        "athg_cycle_timing": [vp, i, C.POINTER(d), C.POINTER(i), C.c_char_p, sz],
     }
     for name, args in sig.items():
         f = getattr(L, name)
@@ -300,6 +301,15 @@ class Sim:
                 d[k] = x
             out[key] = d
         return out
+
+    def cycle_timing(self):
+        """One cycle launch group by launch group: [(name, ms)] in launch order."""
+        ms = (C.c_double * 64)()
+        n = C.c_int()
+        buf = C.create_string_buffer(8192)
+        check(lib().athg_cycle_timing(self.h, 64, ms, C.byref(n), buf, 8192))
+        names = buf.value.decode().split("\n")
+        return [(names[q], ms[q]) for q in range(n.value)]
 
     def smr_stats(self):
         out = (C.c_int64 * 8)()

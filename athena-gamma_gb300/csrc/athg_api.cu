@@ -241,6 +241,8 @@ struct athg_ctx {
   int* boff = nullptr;
   // multi-level mesh (static refinement): work lists, coarse buffers (FP64 path only)
   athg::SmrDevice* smr = nullptr;
+  // athg_cycle_timing: events recorded between launch groups, with their names
+  std::vector<std::pair<std::string, cudaEvent_t>>* tev = nullptr;
   bool mixed() const { return cfg.precision == ATHG_MIXED; }
 };
 
@@ -543,28 +545,50 @@ int leave_fused(athg_ctx* c) {
   return ATHG_OK;
 }
 
+// an event after the launch group `what` of stage `stage` (athg_cycle_timing only)
+void mark(athg_ctx* c, int stage, const char* what) {
+  if (!c->tev) return;
+  cudaEvent_t e;
+  if (cudaEventCreate(&e) != cudaSuccess) return;
+  cudaEventRecord(e, c->st);
+  c->tev->push_back(std::make_pair("stage " + std::to_string(stage) + ": " + what, e));
+}
+
 int do_stage(athg_ctx* c, int stage) {
   const int l = stage - 1;
   int order = (c->cfg.integrator == ATHG_VL2 && l == 0) ? 1 : c->cfg.xorder;
   int rc;
   if (fused(c)) {
     if ((rc = launch_fluxes(c, order))) return rc;
+    mark(c, stage, "flux sweeps");
     if ((rc = launch_corner(c))) return rc;
+    mark(c, stage, "corner EMF");
     if ((rc = launch_update_c2p(c, l, stage == c->integ.nstages))) return rc;
+    mark(c, stage, "update + primitives (k_update_c2p)");
     if ((rc = launch_ghosts_f32(c))) return rc;
+    mark(c, stage, "ghost exchange");
     c->ghosts_stale = true;
     return ATHG_OK;
   }
   if ((rc = launch_fluxes(c, order))) return rc;
+  mark(c, stage, "flux sweeps");
   if ((rc = launch_corner(c))) return rc;
+  mark(c, stage, "corner EMF");
   if ((rc = launch_update(c, l))) return rc;
+  mark(c, stage, "update (k_update)");
   // AddSourceTerms (time_integrator.cpp:1655-1676); every stage here is a main stage
   if (c->grav && (rc = launch_self_gravity(c, l))) return rc;
+  if (c->grav) mark(c, stage, "self-gravity source");
   if ((rc = launch_ghosts(c))) return rc;
+  mark(c, stage, "ghost exchange");
   if ((rc = launch_c2p(c))) return rc;
+  mark(c, stage, "primitives (k_c2p)");
   if (c->grav && (rc = gravity_solve(c))) return rc;  // main.cpp:461-466
-  if (stage == c->integ.nstages)
+  if (c->grav) mark(c, stage, "gravity solve");
+  if (stage == c->integ.nstages) {
     if ((rc = launch_block_dt(c))) return rc;
+    mark(c, stage, "time step");
+  }
   return ATHG_OK;
 }
 
@@ -573,7 +597,9 @@ int do_cycle(athg_ctx* c) {
     int rc = do_stage(c, s);
     if (rc) return rc;
   }
-  return launch_end(c, 1);
+  int rc = launch_end(c, 1);
+  mark(c, c->integ.nstages, "end of cycle");
+  return rc;
 }
 
 int need_pool(const athg_ctx* c) {
@@ -1297,6 +1323,44 @@ int athg_cycles(athg_ctx* c, int n) {
   if ((rc = build_graph(c))) return rc;
   for (int q = 0; q < n; ++q)
     if ((rc = run_cycle_graph(c))) return rc;
+  return ATHG_OK;
+}
+
+int athg_cycle_timing(athg_ctx* c, int max, double* ms, int* n, char* names,
+                      size_t names_size) {
+  int rc = need_pool(c);
+  if (rc) return rc;
+  if (!ms || !n || max <= 0) return fail(ATHG_ERR_ARG, "null argument");
+  if ((rc = autotune(c))) return rc;
+  std::vector<std::pair<std::string, cudaEvent_t>> ev;
+  c->tev = &ev;
+  mark(c, 0, "start");
+  rc = do_cycle(c);
+  c->tev = nullptr;
+  if (!rc && fused(c)) {  // as run_cycle_graph: the new state is in the other buffer
+    swap_state(c);
+    c->ghosts_stale = true;
+  }
+  cudaError_t e = ev.empty() ? cudaSuccess : cudaEventSynchronize(ev.back().second);
+  std::string all;
+  int k = 0;
+  for (size_t q = 1; q < ev.size() && e == cudaSuccess; ++q) {
+    float t = 0.0f;
+    e = cudaEventElapsedTime(&t, ev[q - 1].second, ev[q].second);
+    if (k < max) {
+      ms[k++] = t;
+      all += ev[q].first + "\n";
+    }
+  }
+  for (auto& x : ev) cudaEventDestroy(x.second);
+  if (rc) return rc;
+  if (e != cudaSuccess) return fail(ATHG_ERR_CUDA, std::string("timing: ") + cudaGetErrorString(e));
+  *n = k;
+  if (names && names_size > 0) {
+    const size_t m = std::min(all.size(), names_size - 1);
+    std::memcpy(names, all.data(), m);
+    names[m] = 0;
+  }
   return ATHG_OK;
 }
 

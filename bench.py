@@ -29,6 +29,11 @@ NX = (256, 256, 256)
 MB = (64, 64, 64)
 CFL = 0.4
 BYTES_PER_ZC = 384  # VL2 MHD: 2 stages x (read 2 + write 1) x (40 B U + 24 B face B)
+# algorithmic bytes of one launch of the fused update + primitive recovery (k_update_c2p),
+# per cell: FP64 U in and out (80 B), the cell's three FP64 lower faces in and out (48 B),
+# FP32 hydro fluxes of its three lower faces (60 B), its three FP32 edge EMFs (12 B), FP32
+# W, bcc, cell-centred EMF and face copies out (56 B)
+BYTES_UPDATE_C2P = 256
 METRIC = "zone-cycles/s"
 WORKLOAD = "orszag_tang_256^3_mhd_plm_hlld_vl2"
 
@@ -508,7 +513,13 @@ def main():
         else:
             el = timed_cycles(sim, torch, steps)
         el = max_over_ranks(torch, el, world, "cuda")
+        timing = None
+        if prec == "mixed":
+            # one cycle launch group by launch group (CUDA events on the context stream),
+            # three times: the dominant kernel's launch time for the roofline
+            timing = [sim.cycle_timing() for _ in range(3)]
         res[prec] = {"el": el, "steps": steps, "zcps": replica_throughput(zones, steps, world, el),
+                     "timing": timing,
                      "launches": sim.launches_per_cycle(), "clocks": clk,
                      "tuning": sim.tuning(),
                      "t": sim.get_time(), "divb": sim.max_div_b()}
@@ -555,6 +566,24 @@ def main():
     m = res["mixed"]
     sec_per_cycle = m["el"] / m["steps"]
     achieved = BYTES_PER_ZC * zones / sec_per_cycle / 1e9
+    # the dominant kernel, k_update_c2p: median over the three timed cycles of its mean
+    # launch time (two launches per cycle)
+    upd = []
+    groups = {}
+    for rep in m["timing"]:
+        ts = [t for name, t in rep if "k_update_c2p" in name]
+        upd.append(sum(ts) / len(ts))
+        for name, t in rep:
+            groups.setdefault(name, []).append(t)
+    t_upd = float(np.median(upd)) / 1e3
+    k_achieved = BYTES_UPDATE_C2P * zones / t_upd / 1e9
+    k_traffic = None
+    kpath = os.path.join(ROOT, "profiles", "update_c2p_fused_ncu_192.md")
+    if os.path.exists(kpath):
+        with open(kpath) as f:
+            for ln in f:
+                if ln.startswith("dram_bytes_per_cell:"):
+                    k_traffic = float(ln.split(":")[1]) * zones
     # DRAM bytes of one cycle from the ncu summary (bytes per zone-cycle measured at 128^3,
     # scaled by the cells of this run)
     traffic = None
@@ -581,11 +610,22 @@ def main():
         "mixed_over_fp64": m["zcps"] / res["fp64"]["zcps"],
         "l1_rho_mixed_vs_fp64": {"cycles": n_cmp, "abs": l1_dev, "rel": l1_rel},
         "div_b_max": {"mixed": m["divb"], "fp64": res["fp64"]["divb"]},
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": traffic,
-                     "note": "one launch = one captured VL2 cycle (graph); algorithmic bytes "
-                             "384 B/zone-cycle; peak %s; traffic = ncu DRAM bytes per cycle "
-                             "(128^3 capture scaled to the cells)" % peak_kind},
+        "roofline": {"bound": "hbm", "kernel": "k_update_c2p (fused VL2 update + primitive "
+                               "recovery, 44% of the cycle)",
+                     "achieved": k_achieved, "peak": peak, "unit": "GB/s",
+                     "frac": k_achieved / peak, "traffic": k_traffic,
+                     "launch_ms": 1e3 * t_upd,
+                     "note": "algorithmic bytes %d B/cell x %d cells per launch; launch time "
+                             "from CUDA events between launch groups on the context stream "
+                             "(athg_cycle_timing, median of 3 cycles); peak %s copy bandwidth; "
+                             "traffic = ncu DRAM bytes per launch (192^3 capture scaled to the "
+                             "cells)" % (BYTES_UPDATE_C2P, zones, peak_kind)},
+        "cycle_roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                           "frac": achieved / peak, "traffic": traffic,
+                           "note": "one launch = one captured VL2 cycle (graph); algorithmic "
+                                   "bytes 384 B/zone-cycle; traffic = ncu DRAM bytes per cycle "
+                                   "(128^3 capture scaled to the cells)"},
+        "cycle_breakdown_ms": {k: float(np.median(v)) for k, v in groups.items()},
         "cpu_baseline": cpu,
         "e2e": e2e,
         "gpu_launches": m["launches"] * m["steps"],

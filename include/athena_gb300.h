@@ -149,6 +149,12 @@ int athg_set_time(athg_ctx* ctx, double time, double dt, int64_t ncycle);
 int athg_synchronize(athg_ctx* ctx);
 /* The context's CUDA stream (a cudaStream_t), for callers that time or order work. */
 int athg_stream(athg_ctx* ctx, void** stream);
+/* One whole cycle run launch group by launch group (not from the captured graph), with
+ * CUDA events on the context's stream between groups: device time of each group in ms,
+ * in launch order (ms[0..*n-1], at most max), and the groups' names, '\n'-separated, in
+ * `names` (names_size bytes, may be NULL). The cycle is a real one: the state advances. */
+int athg_cycle_timing(athg_ctx* ctx, int max, double* ms, int* n, char* names,
+                      size_t names_size);
 /* Kernel launches of one whole cycle (what athg_cycles replays per cycle). */
 int athg_launches_per_cycle(athg_ctx* ctx, int* n);
 
