@@ -37,7 +37,8 @@ EXPORTS = [
     "athg_mg_stream", "athg_mg_multipole", "athg_attach_gravity", "athg_history",
     "athg_get_tuning", "athg_set_tuning",
     "athg_block_cfl_dt_noalloc", "athg_set_refined_mesh", "athg_set_multilevel_blocks",
-    "athg_smr_stats", "athg_resume", "athg_cycle_timing",
+    "athg_smr_stats", "athg_resume", "athg_cycle_timing", "athg_amr_enable",
+    "athg_amr_regrid",
 ]
 MG_BC = {"periodic": 0, "zerograd": 1, "zerofixed": 2, "multipole": 3}
 
@@ -70,6 +71,11 @@ class Region(C.Structure):
     _fields_ = [("x1min", C.c_double), ("x1max", C.c_double), ("x2min", C.c_double),
                 ("x2max", C.c_double), ("x3min", C.c_double), ("x3max", C.c_double),
                 ("level", C.c_int)]
+
+
+class AmrConfig(C.Structure):
+    _fields_ = [("threshold", C.c_double), ("deref_fraction", C.c_double),
+                ("max_level", C.c_int), ("derefine_count", C.c_int)]
 
 
 class AthgError(RuntimeError):
@@ -135,6 +141,8 @@ def lib():
         "athg_smr_stats": [vp, C.POINTER(C.c_int64)],
         "athg_resume": [vp],
         "athg_cycle_timing": [vp, i, C.POINTER(d), C.POINTER(i), C.c_char_p, sz],
+        "athg_amr_enable": [vp, C.POINTER(AmrConfig)],
+        "athg_amr_regrid": [vp, C.POINTER(i)],
     }
     for name, args in sig.items():
         f = getattr(L, name)
@@ -197,18 +205,39 @@ class Sim:
         else:
             check(L.athg_set_uniform_mesh(h, C.byref(m)))
         self.mesh_nx, self.block_nx, self.ng, self.mhd = tuple(mesh_nx), tuple(block_nx), ng, mhd
+        self._list_blocks()
+        self.multilevel = regions is not None or leaves is not None
+        self.nc = tuple(n + 2 * ng for n in block_nx)
+
+    def _list_blocks(self):
+        L = lib()
         nb = C.c_int()
-        check(L.athg_num_blocks(h, C.byref(nb)))
+        check(L.athg_num_blocks(self.h, C.byref(nb)))
         self.nb = nb.value
         self.locs = []
         self.leaves = []  # (level, lx1, lx2, lx3) of every block
         loc = (C.c_int64 * 4)()
         for b in range(self.nb):
-            check(L.athg_block_location(h, b, loc))
+            check(L.athg_block_location(self.h, b, loc))
             self.locs.append((loc[0], loc[1], loc[2]))
             self.leaves.append((int(loc[3]), int(loc[0]), int(loc[1]), int(loc[2])))
-        self.multilevel = regions is not None or leaves is not None
-        self.nc = tuple(n + 2 * ng for n in block_nx)
+
+    def amr_enable(self, threshold, max_level, derefine_count=10, deref_fraction=0.25):
+        """Adaptive refinement with the blast criterion (athg_amr_enable); the block list
+        (nb, leaves) is refreshed after every call that may regrid."""
+        a = AmrConfig()
+        a.threshold, a.deref_fraction = threshold, deref_fraction
+        a.max_level, a.derefine_count = max_level, derefine_count
+        check(lib().athg_amr_enable(self.h, C.byref(a)))
+        self.multilevel = True
+        self._list_blocks()
+
+    def amr_regrid(self):
+        """One refinement check and regrid; returns whether the mesh changed."""
+        ch = C.c_int()
+        check(lib().athg_amr_regrid(self.h, C.byref(ch)))
+        self._list_blocks()
+        return bool(ch.value)
 
     def close(self):
         if getattr(self, "h", None):
@@ -352,6 +381,8 @@ class Sim:
 
     def cycles(self, n):
         check(lib().athg_cycles(self.h, n))
+        if self.multilevel:
+            self._list_blocks()
 
     def synchronize(self):
         check(lib().athg_synchronize(self.h))

@@ -14,6 +14,7 @@
 #include "athena_gb300.h"
 #include "athg_bvals.cuh"
 #include "athg_launch.cuh"
+#include "athg_amr.h"
 #include "athg_internal.h"
 
 using namespace athg;
@@ -241,6 +242,13 @@ struct athg_ctx {
   int* boff = nullptr;
   // multi-level mesh (static refinement): work lists, coarse buffers (FP64 path only)
   athg::SmrDevice* smr = nullptr;
+  // adaptive refinement (FP64, periodic): criterion and counters; the root mesh of the
+  // last athg_set_*mesh call; per-block criterion values on the device
+  bool amr = false;
+  athg_amr_config amrc{};
+  std::vector<int> amr_deref;
+  athg_mesh mesh{};
+  unsigned long long* amr_bits = nullptr;
   // athg_cycle_timing: events recorded between launch groups, with their names
   std::vector<std::pair<std::string, cudaEvent_t>>* tev = nullptr;
   bool mixed() const { return cfg.precision == ATHG_MIXED; }
@@ -306,6 +314,8 @@ void free_pool(athg_ctx* c) {
   c->grav = nullptr;
   athg::smr_destroy(c->smr);
   c->smr = nullptr;
+  if (c->amr_bits) cudaFree(c->amr_bits);
+  c->amr_bits = nullptr;
   c->nb = 0;
 }
 
@@ -812,6 +822,33 @@ int refined_leaves(const int nmx[3], const int nrb[3], const double lo[3], const
   return ATHG_OK;
 }
 
+// Cell widths, cell centres (fine and coarse buffer) and face positions of the leaves
+// `loc`, as the reference's Coordinates computes them for its levels
+void leaf_coords(const athg_ctx* c, const athg_mesh* m, const std::vector<SmrLoc>& loc,
+                 std::vector<double>* dxv, std::vector<double>* xvf, std::vector<double>* xvc,
+                 std::vector<double>* faces, int* ncmax, int* nccmax) {
+  const Geom& g = c->g;
+  const int nmx[3] = {m->nx1, m->nx2, m->nx3};
+  const int nbx[3] = {g.nx1, g.nx2, g.nx3};
+  const double lo[3] = {m->x1min, m->x2min, m->x3min}, hi[3] = {m->x1max, m->x2max, m->x3max};
+  const int ncs[3] = {g.nc1, g.nc2, g.nc3};
+  *ncmax = std::max(g.nc1, std::max(g.nc2, g.nc3));
+  *nccmax = std::max(nbx[0], std::max(nbx[1], nbx[2])) / 2 + 2 * g.ng;
+  const size_t nb = loc.size();
+  dxv->assign(nb * 3, 0.0);
+  xvf->assign(nb * 3 * *ncmax, 0.0);
+  xvc->assign(nb * 3 * *nccmax, 0.0);
+  faces->assign(nb * (ncs[0] + ncs[1] + ncs[2] + 3), 0.0);
+  size_t off = 0;
+  for (size_t b = 0; b < nb; ++b)
+    for (int d = 0; d < 3; ++d) {
+      smr_axis_coords(nmx[d], nmx[d] / nbx[d], lo[d], hi[d], loc[b].level, loc[b].lx[d], nbx[d],
+                      g.ng, &(*dxv)[3 * b + d], &(*xvf)[(b * 3 + d) * *ncmax],
+                      &(*xvc)[(b * 3 + d) * *nccmax], &(*faces)[off]);
+      off += ncs[d] + 1;
+    }
+}
+
 // Allocates the pool for the leaves `loc` of a periodic mesh and plans its level
 // boundaries; coordinates follow the reference's uniform generator per level
 int set_multilevel(athg_ctx* c, const athg_mesh* m, const std::vector<SmrLoc>& loc) {
@@ -822,20 +859,19 @@ int set_multilevel(athg_ctx* c, const athg_mesh* m, const std::vector<SmrLoc>& l
   const Geom& g = c->g;
   const int nmx[3] = {m->nx1, m->nx2, m->nx3};
   const int nbx[3] = {g.nx1, g.nx2, g.nx3};
-  const double lo[3] = {m->x1min, m->x2min, m->x3min}, hi[3] = {m->x1max, m->x2max, m->x3max};
   int nrb[3];
   for (int d = 0; d < 3; ++d) {
     if (nmx[d] % nbx[d] != 0)
       return fail(ATHG_ERR_ARG, "mesh size must be a multiple of the MeshBlock size");
     nrb[d] = nmx[d] / nbx[d];
   }
+  const athg_mesh mcopy = *m;  // m may point at c->mesh
   const int nb = (int)loc.size();
   const int ncs[3] = {g.nc1, g.nc2, g.nc3};
-  const int ncmax = std::max(g.nc1, std::max(g.nc2, g.nc3));
-  const int nccmax = std::max(nbx[0], std::max(nbx[1], nbx[2])) / 2 + 2 * g.ng;
-  c->coords.assign((size_t)nb * (ncs[0] + ncs[1] + ncs[2] + 3), 0.0);
-  std::vector<double> dxv((size_t)nb * 3), xvf((size_t)nb * 3 * ncmax, 0.0),
-      xvc((size_t)nb * 3 * nccmax, 0.0);
+  std::vector<double> dxv, xvf, xvc, faces;
+  int ncmax, nccmax;
+  leaf_coords(c, &mcopy, loc, &dxv, &xvf, &xvc, &faces, &ncmax, &nccmax);
+  c->coords = faces;
   std::vector<athg_block> bl(nb);
   size_t off = 0;
   for (int b = 0; b < nb; ++b) {
@@ -846,9 +882,6 @@ int set_multilevel(athg_ctx* c, const athg_mesh* m, const std::vector<SmrLoc>& l
     for (int d = 0; d < 3; ++d) {
       xfs[d] = &c->coords[off];
       off += ncs[d] + 1;
-      smr_axis_coords(nmx[d], nrb[d], lo[d], hi[d], loc[b].level, loc[b].lx[d], nbx[d], g.ng,
-                      &dxv[3 * b + d], &xvf[((size_t)b * 3 + d) * ncmax],
-                      &xvc[((size_t)b * 3 + d) * nccmax], xfs[d]);
     }
     B.x1f = xfs[0]; B.x2f = xfs[1]; B.x3f = xfs[2];
     B.dx1 = dxv[3 * b]; B.dx2 = dxv[3 * b + 1]; B.dx3 = dxv[3 * b + 2];
@@ -856,10 +889,123 @@ int set_multilevel(athg_ctx* c, const athg_mesh* m, const std::vector<SmrLoc>& l
   }
   int rc = athg_set_blocks(c, nb, bl.data());
   if (rc) return rc;
+  c->mesh = mcopy;
   SmrDims d = smr_dims(g.nx1, g.nx2, g.nx3, g.ng);
   std::string err;
   rc = athg::smr_create(&c->smr, d, nrb, loc, dxv, xvf, xvc, c->cfg.magnetic != 0, c->st, &err);
   if (rc) return fail(rc == -1 ? ATHG_ERR_ARG : ATHG_ERR_CUDA, err);
+  CK(cudaMalloc(&c->amr_bits, sizeof(unsigned long long) * nb));
+  if ((int)c->amr_deref.size() != nb) c->amr_deref.assign(nb, 0);
+  return ATHG_OK;
+}
+
+std::vector<SmrLoc> current_leaves(const athg_ctx* c) {
+  std::vector<SmrLoc> l(c->nb);
+  for (int b = 0; b < c->nb; ++b) {
+    l[b].level = c->blocks[b].level;
+    l[b].lx[0] = c->blocks[b].lx1; l[b].lx[1] = c->blocks[b].lx2; l[b].lx[2] = c->blocks[b].lx3;
+  }
+  return l;
+}
+
+template <typename V>
+cudaError_t dl(V* host, const double* dev, size_t n, cudaStream_t st) {
+  host->resize(n);
+  return cudaMemcpyAsync(host->data(), dev, n * sizeof(double), cudaMemcpyDeviceToHost, st);
+}
+cudaError_t ul(double* dev, const std::vector<double>& host, cudaStream_t st) {
+  return cudaMemcpyAsync(dev, host.data(), host.size() * sizeof(double), cudaMemcpyHostToDevice, st);
+}
+
+// Mesh::LoadBalancingAndAdaptiveMeshRefinement on one GPU: the criterion on the current
+// state, CheckRefinementCondition, UpdateMeshBlockTree and, when the tree changed, the
+// new pool (kept blocks, prolongated and restricted ones), its level-boundary plan and
+// Initialize(2): ghosts, W(U) and one NewTimeStep from dt_prev. in_cycle adds the main
+// loop's NewTimeStep (main.cpp:476-477).
+int amr_regrid(athg_ctx* c, bool in_cycle, double dt_prev, int* changed) {
+  *changed = 0;
+  if (!c->amr || !c->smr) return fail(ATHG_ERR_STATE, "adaptive refinement is not enabled");
+  const Geom& g = c->g;
+  const int nb = c->nb;
+  const SmrDims d = smr_dims(g.nx1, g.nx2, g.nx3, g.ng);
+  athg::amr_criterion(d, nb, (const double*)c->w, c->amr_bits, c->st);
+  CKL();
+  std::vector<unsigned long long> bits(nb);
+  CK(cudaMemcpyAsync(bits.data(), c->amr_bits, sizeof(unsigned long long) * nb,
+                     cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  const std::vector<SmrLoc> leaves = current_leaves(c);
+  const int nrb[3] = {c->mesh.nx1 / g.nx1, c->mesh.nx2 / g.nx2, c->mesh.nx3 / g.nx3};
+  std::vector<int> lv;
+  std::string err;
+  if (!smr_neighbor_levels(nrb, leaves, &lv, &err)) return fail(ATHG_ERR_STATE, err);
+  std::vector<int> flags(nb);
+  for (int b = 0; b < nb; ++b) {
+    double maxeps;
+    std::memcpy(&maxeps, &bits[b], 8);
+    flags[b] = amr_flag(maxeps, c->amrc.threshold, c->amrc.deref_fraction, leaves[b].level,
+                        c->amrc.max_level, &lv[27 * b], c->amrc.derefine_count, &c->amr_deref[b]);
+  }
+  std::vector<SmrLoc> nl;
+  if (!amr_update_tree(nrb, leaves, flags, &nl)) return ATHG_OK;
+  // the old pool on the host
+  const bool mhd = c->cfg.magnetic != 0;
+  AmrArrays old;
+  const int64_t nbl = nb;
+  CK(dl(&old.u, c->u, (size_t)(NHYD * g.ncell * nbl), c->st));
+  CK(dl(&old.cu, c->smr->cu, (size_t)(5 * d.ccell * nbl), c->st));
+  if (mhd) {
+    CK(dl(&old.b1, c->b1, (size_t)(g.nf1 * nbl), c->st));
+    CK(dl(&old.b2, c->b2, (size_t)(g.nf2 * nbl), c->st));
+    CK(dl(&old.b3, c->b3, (size_t)(g.nf3 * nbl), c->st));
+    CK(dl(&old.cb1, c->smr->cb1, (size_t)(d.cf1 * nbl), c->st));
+    CK(dl(&old.cb2, c->smr->cb2, (size_t)(d.cf2 * nbl), c->st));
+    CK(dl(&old.cb3, c->smr->cb3, (size_t)(d.cf3 * nbl), c->st));
+  }
+  double hs[3];
+  CK(cudaMemcpyAsync(hs, c->scal, sizeof(hs), cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  long long ncyc;
+  std::memcpy(&ncyc, &hs[2], 8);
+  std::vector<double> old_dx(3 * nbl);
+  for (int b = 0; b < nb; ++b) {
+    old_dx[3 * b] = c->blocks[b].dx1; old_dx[3 * b + 1] = c->blocks[b].dx2;
+    old_dx[3 * b + 2] = c->blocks[b].dx3;
+  }
+  std::vector<double> dxv, xvf, xvc, faces;
+  int ncmax, nccmax;
+  leaf_coords(c, &c->mesh, nl, &dxv, &xvf, &xvc, &faces, &ncmax, &nccmax);
+  AmrArrays nw;
+  std::vector<int> nderef;
+  amr_fill(d, mhd, leaves, old, old_dx, c->amr_deref, nl, dxv, xvf, xvc, ncmax, nccmax, &nw,
+           &nderef);
+  int rc = set_multilevel(c, &c->mesh, nl);
+  if (rc) return rc;
+  c->amr_deref = nderef;
+  CK(ul(c->u, nw.u, c->st));
+  CK(ul(c->smr->cu, nw.cu, c->st));
+  if (mhd) {
+    CK(ul(c->b1, nw.b1, c->st)); CK(ul(c->b2, nw.b2, c->st)); CK(ul(c->b3, nw.b3, c->st));
+    CK(ul(c->smr->cb1, nw.cb1, c->st)); CK(ul(c->smr->cb2, nw.cb2, c->st));
+    CK(ul(c->smr->cb3, nw.cb3, c->st));
+  }
+  // Initialize(2): time and ncycle stay, dt restarts from the cycle's dt
+  double ts[3] = {hs[0], dt_prev, 0.0};
+  std::memcpy(&ts[2], &ncyc, 8);
+  CK(cudaMemcpyAsync(c->scal, ts, sizeof(ts), cudaMemcpyHostToDevice, c->st));
+  unsigned long long big;
+  std::memcpy(&big, &kDblMax, 8);
+  CK(cudaMemcpyAsync(c->scal + 3, &big, 8, cudaMemcpyHostToDevice, c->st));
+  if ((rc = launch_ghosts(c))) return rc;
+  if ((rc = launch_c2p(c))) return rc;
+  if ((rc = launch_block_dt(c))) return rc;
+  if ((rc = launch_end(c, 0))) return rc;
+  if (in_cycle) {
+    if ((rc = launch_block_dt(c))) return rc;
+    if ((rc = launch_end(c, 0))) return rc;
+  }
+  CK(cudaStreamSynchronize(c->st));  // the host arrays above go out of scope
+  *changed = 1;
   return ATHG_OK;
 }
 
@@ -1117,7 +1263,10 @@ int athg_set_uniform_mesh(athg_ctx* c, const athg_mesh* m) {
                   ok ? (n[2] * nrb[1] + n[1]) * nrb[0] + n[0] : -1;
             }
       }
-  return athg_set_blocks(c, nblocks, bl.data());
+  const athg_mesh mcopy = *m;
+  int rc = athg_set_blocks(c, nblocks, bl.data());
+  if (!rc) c->mesh = mcopy;
+  return rc;
 }
 
 int athg_set_refined_mesh(athg_ctx* c, const athg_mesh* m, int nregions,
@@ -1150,6 +1299,49 @@ int athg_set_multilevel_blocks(athg_ctx* c, const athg_mesh* m, int nblocks,
     if (loc[b].level < 0 || loc[b].level > 10) return fail(ATHG_ERR_ARG, "block level out of range");
   }
   return set_multilevel(c, m, loc);
+}
+
+int athg_amr_enable(athg_ctx* c, const athg_amr_config* cfg) {
+  int rc = need_pool(c);
+  if (rc) return rc;
+  if (!cfg) return fail(ATHG_ERR_ARG, "null argument");
+  if (c->mixed())
+    return fail(ATHG_ERR_ARG, "adaptive refinement runs on the FP64 path (precision ATHG_FP64)");
+  if (cfg->max_level < 0 || cfg->max_level > 10 || cfg->derefine_count < 1 ||
+      !(cfg->threshold > 0.0))
+    return fail(ATHG_ERR_ARG, "invalid adaptive refinement parameters");
+  if (!c->smr) {  // a uniform mesh becomes a one-level multi-level mesh, state kept
+    const Geom& g = c->g;
+    const bool mhd = c->cfg.magnetic != 0;
+    const int64_t nb = c->nb;
+    std::vector<double> u, b1, b2, b3;
+    CK(dl(&u, c->u, (size_t)(NHYD * g.ncell * nb), c->st));
+    if (mhd) {
+      CK(dl(&b1, c->b1, (size_t)(g.nf1 * nb), c->st));
+      CK(dl(&b2, c->b2, (size_t)(g.nf2 * nb), c->st));
+      CK(dl(&b3, c->b3, (size_t)(g.nf3 * nb), c->st));
+    }
+    CK(cudaStreamSynchronize(c->st));
+    const athg_mesh m = c->mesh;
+    if ((rc = set_multilevel(c, &m, current_leaves(c)))) return rc;
+    CK(ul(c->u, u, c->st));
+    if (mhd) { CK(ul(c->b1, b1, c->st)); CK(ul(c->b2, b2, c->st)); CK(ul(c->b3, b3, c->st)); }
+    CK(cudaStreamSynchronize(c->st));
+  }
+  c->amr = true;
+  c->amrc = *cfg;
+  c->amr_deref.assign(c->nb, 0);
+  return ATHG_OK;
+}
+
+int athg_amr_regrid(athg_ctx* c, int* changed) {
+  int rc = need_pool(c);
+  if (rc) return rc;
+  if (!changed) return fail(ATHG_ERR_ARG, "null argument");
+  double dt;
+  CK(cudaMemcpyAsync(&dt, c->scal + 1, 8, cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  return amr_regrid(c, false, dt, changed);
 }
 
 int athg_smr_stats(athg_ctx* c, int64_t* out8) {
@@ -1318,6 +1510,18 @@ int athg_cycles(athg_ctx* c, int n) {
     // the solve iterates to a threshold or sets up multipole moments on the host
     for (int q = 0; q < n; ++q)
       if ((rc = do_cycle(c))) return rc;
+    return ATHG_OK;
+  }
+  if (c->amr) {  // the refinement check after every cycle (main.cpp:470-477)
+    for (int q = 0; q < n; ++q) {
+      double dt;
+      CK(cudaMemcpyAsync(&dt, c->scal + 1, 8, cudaMemcpyDeviceToHost, c->st));
+      CK(cudaStreamSynchronize(c->st));
+      if ((rc = build_graph(c))) return rc;
+      if ((rc = run_cycle_graph(c))) return rc;
+      int changed;
+      if ((rc = amr_regrid(c, true, dt, &changed))) return rc;
+    }
     return ATHG_OK;
   }
   if ((rc = build_graph(c))) return rc;

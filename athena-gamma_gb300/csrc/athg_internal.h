@@ -70,5 +70,9 @@ int smr_fill(const SmrDevice* s, const SmrPool& P, cudaStream_t st);
 int smr_correct_flux(const SmrDevice* s, const SmrPool& P, cudaStream_t st);
 // EMF correction of every block-boundary edge; returns the kernels launched
 int smr_correct_emf(const SmrDevice* s, const SmrPool& P, cudaStream_t st);
+// Blast refinement criterion (max |grad p| / p per block) of FP64 primitives w into
+// maxbits[nb] (bit patterns of non-negative doubles); returns the kernels launched
+int amr_criterion(const SmrDims& d, int nb, const double* w, unsigned long long* maxbits,
+                  cudaStream_t st);
 
 }  // namespace athg

@@ -68,7 +68,43 @@ cudaError_t zeros(double** p, int64_t n, cudaStream_t st) {
   return cudaMemsetAsync(*p, 0, sizeof(double) * n, st);
 }
 
+// Refinement criterion of the reference's blast (pgen/blast.cpp:413-442): the largest
+// |grad p| / p over the interior and one ring of ghost cells of each block, reduced to one
+// value per block (non-negative doubles order like their bit patterns)
+__global__ void k_amr_pgrad(SmrDims d, const double* __restrict__ w,
+                            unsigned long long* __restrict__ maxbits) {
+  const int b = blockIdx.y;
+  const int n1 = d.nx1 + 2, n2 = d.nx2 + 2, n3 = d.nx3 + 2;
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  double eps = 0.0;
+  if (t < (int64_t)n1 * n2 * n3) {
+    const int i = d.is - 1 + (int)(t % n1), j = d.js - 1 + (int)((t / n1) % n2),
+              k = d.ks - 1 + (int)(t / ((int64_t)n1 * n2));
+    const double* p = w + ((int64_t)b * 5 + 4) * d.ncell;
+    const int64_t c = d.c(k, j, i), sj = d.nc1, sk = (int64_t)d.nc1 * d.nc2;
+    const double gx = 0.5 * (p[c + 1] - p[c - 1]), gy = 0.5 * (p[c + sj] - p[c - sj]),
+                 gz = 0.5 * (p[c + sk] - p[c - sk]);
+    eps = sqrt(gx * gx + gy * gy + gz * gz) / p[c];
+    if (!(eps > 0.0)) eps = 0.0;  // std::max(maxeps, eps) never picks NaN or negatives
+  }
+  unsigned long long v = (unsigned long long)__double_as_longlong(eps);
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long x = __shfl_xor_sync(0xffffffffu, v, o);
+    v = x > v ? x : v;
+  }
+  if ((threadIdx.x & 31) == 0 && v) atomicMax(maxbits + b, v);
+}
+
 }  // namespace
+
+int amr_criterion(const SmrDims& d, int nb, const double* w, unsigned long long* maxbits,
+                  cudaStream_t st) {
+  cudaMemsetAsync(maxbits, 0, sizeof(unsigned long long) * nb, st);
+  const int64_t n = (int64_t)(d.nx1 + 2) * (d.nx2 + 2) * (d.nx3 + 2);
+  dim3 grid((unsigned)((n + kThreads - 1) / kThreads), (unsigned)nb);
+  k_amr_pgrad<<<grid, kThreads, 0, st>>>(d, w, maxbits);
+  return 1;
+}
 
 void smr_destroy(SmrDevice* s) {
   if (!s) return;

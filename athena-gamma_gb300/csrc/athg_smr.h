@@ -141,6 +141,11 @@ struct SmrLoc {
 bool smr_plan(const SmrDims& d, const int nrb[3], const std::vector<SmrLoc>& loc,
               const double* dx, bool mhd, SmrPlan* plan, std::string* err);
 
+// Levels of every block's 26 neighbours (BoundaryBase::nblevel; -1 where none), 27 per
+// block, index (ox3+1)*9 + (ox2+1)*3 + (ox1+1), the centre being the block's own level.
+bool smr_neighbor_levels(const int nrb[3], const std::vector<SmrLoc>& loc, std::vector<int>* lv,
+                         std::string* err);
+
 // Cell widths and cell centres of one block along one axis, fine (nx + 2 ng entries) and
 // of its coarse buffer (nx/2 + 2 ng entries), as the reference's Coordinates constructor
 // computes them for a uniform mesh (coordinates/coordinates.cpp:88-145, coarse_flag

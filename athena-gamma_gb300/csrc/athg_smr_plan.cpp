@@ -822,6 +822,29 @@ void smr_axis_coords(int mesh_nx, int nrb, double xmin, double xmax, int level, 
   *dx = (bmax - bmin) / nx;
 }
 
+bool smr_neighbor_levels(const int nrb[3], const std::vector<SmrLoc>& loc, std::vector<int>* lv,
+                         std::string* err) {
+  Tree t;
+  for (int a = 0; a < 3; ++a) t.nrb[a] = nrb[a];
+  for (size_t b = 0; b < loc.size(); ++b) {
+    const SmrLoc& l = loc[b];
+    t.leaf[Key(l.level, l.lx[0], l.lx[1], l.lx[2])] = (int)b;
+    for (int q = l.level - 1; q >= 0; --q) {
+      const int sh = l.level - q;
+      t.inner.insert(Key(q, l.lx[0] >> sh, l.lx[1] >> sh, l.lx[2] >> sh));
+    }
+  }
+  lv->assign(27 * loc.size(), -1);
+  BlockNb B;
+  for (size_t b = 0; b < loc.size(); ++b) {
+    if (!search_neighbors(t, loc, (int)b, &B, err)) return false;
+    for (int k = 0; k < 3; ++k)
+      for (int j = 0; j < 3; ++j)
+        for (int i = 0; i < 3; ++i) (*lv)[27 * b + (k * 3 + j) * 3 + i] = B.nblevel[k][j][i];
+  }
+  return true;
+}
+
 bool smr_plan(const SmrDims& d, const int nrb[3], const std::vector<SmrLoc>& loc,
               const double* dx, bool mhd, SmrPlan* plan, std::string* err) {
   if (d.nx1 % 2 || d.nx2 % 2 || d.nx3 % 2 || d.ng % 2) {

@@ -106,18 +106,32 @@ void check(int rc, const char* what) {
   }
 }
 
-// cell-centre / face positions of one axis of one block (uniform mesh)
+// cell-centre / face positions of one axis of one block
 struct Axis {
   std::vector<double> xf, xv;
   double dx;
 };
-Axis axis_of(int nx, int ng, double lo, double hi, int64_t off, int64_t ntot) {
+// The uniform mesh generator (mesh/mesh.hpp:389-470): position of face `index` of `nrange`
+double gen_x(int64_t index, int64_t nrange, double lo, double hi) {
+  const int64_t noffset = index - nrange / 2, noffset_ceil = index - (nrange + 1) / 2;
+  const double rx = static_cast<double>(noffset + noffset_ceil) / (2.0 * nrange);
+  return 0.5 * (lo + hi) + (rx * hi - rx * lo);
+}
+// Faces of block lx at `level` (root-relative), ghosts included, with the block edges of
+// Mesh::SetBlockSizeAndBoundaries (mesh/mesh.cpp:1675-1690) and the face loop of
+// Coordinates::Coordinates (coordinates/coordinates.cpp:127-145, cartesian.cpp:29)
+Axis axis_of(int nx, int ng, double lo, double hi, int mesh_nx, int level, int64_t lx) {
   Axis a;
-  a.dx = (hi - lo) / (double)ntot;
+  const int64_t nroot = (int64_t)mesh_nx << level, nrbl = (int64_t)(mesh_nx / nx) << level;
+  const double bmin = (lx == 0) ? lo : gen_x(lx, nrbl, lo, hi);
+  const double bmax = (lx == nrbl - 1) ? hi : gen_x(lx + 1, nrbl, lo, hi);
+  a.dx = (bmax - bmin) / nx;
   a.xf.resize(nx + 2 * ng + 1);
-  for (int i = 0; i < nx + 2 * ng + 1; ++i) a.xf[i] = lo + (double)(off + i - ng) * a.dx;
+  for (int i = 0; i < nx + 2 * ng + 1; ++i) a.xf[i] = gen_x((i - ng) + lx * nx, nroot, lo, hi);
+  a.xf[ng] = bmin;
+  a.xf[ng + nx] = bmax;
   a.xv.resize(nx + 2 * ng);
-  for (int i = 0; i < nx + 2 * ng; ++i) a.xv[i] = 0.5 * (a.xf[i] + a.xf[i + 1]);
+  for (int i = 0; i < nx + 2 * ng; ++i) a.xv[i] = 0.5 * (a.xf[i + 1] + a.xf[i]);
   return a;
 }
 
@@ -203,6 +217,14 @@ int main(int argc, char** argv) {
   st.block_nx[0] = c.nx1; st.block_nx[1] = c.nx2; st.block_nx[2] = c.nx3;
   st.ng = c.nghost;
   st.mhd = mhd;
+  // <mesh> refinement = adaptive: the blast's criterion (<problem> thr), numlevel,
+  // derefine_count (mesh/mesh_refinement.cpp:39-120, pgen/blast.cpp:38-44)
+  const bool adaptive = get(p, "mesh/refinement", "none") == "adaptive";
+  athg_amr_config amr_cfg{};
+  amr_cfg.threshold = getd(p, "problem/thr", 0.0);
+  amr_cfg.deref_fraction = 0.25;
+  amr_cfg.max_level = geti(p, "mesh/numlevel", 1) - 1;
+  amr_cfg.derefine_count = geti(p, "mesh/derefine_count", 10);
   if (!restart.empty()) {
     // Mesh::Mesh(pin, restartfile) + Mesh::Initialize(res_flag = 1)
     std::string text, err;
@@ -220,6 +242,7 @@ int main(int argc, char** argv) {
     }
     if (multi) check(athg_set_multilevel_blocks(ctx, &m, nf, locs.data()), "athg_set_multilevel_blocks");
     else check(athg_set_uniform_mesh(ctx, &m), "athg_set_uniform_mesh");
+    if (adaptive) check(athg_amr_enable(ctx, &amr_cfg), "athg_amr_enable");
     int nlib = 0;
     check(athg_num_blocks(ctx, &nlib), "athg_num_blocks");
     if (nlib != nf) {
@@ -268,112 +291,161 @@ int main(int argc, char** argv) {
             "athg_set_refined_mesh");
     else
       check(athg_set_uniform_mesh(ctx, &m), "athg_set_uniform_mesh");
-    int nb = 0;
-    check(athg_num_blocks(ctx, &nb), "athg_num_blocks");
-    const int ng = c.nghost;
-    const int n1 = c.nx1 + 2 * ng, n2 = c.nx2 + 2 * ng, n3 = c.nx3 + 2 * ng;
-    const size_t nc = (size_t)n1 * n2 * n3;
-
+    if (adaptive) check(athg_amr_enable(ctx, &amr_cfg), "athg_amr_enable");
     // MeshBlock::ProblemGenerator for every block, then one upload per array
-    std::vector<double> U(5 * nc * nb, 0.0), B1, B2, B3;
-    if (mhd) {
-      B1.assign((size_t)n3 * n2 * (n1 + 1) * nb, 0.0);
-      B2.assign((size_t)n3 * (n2 + 1) * n1 * nb, 0.0);
-      B3.assign((size_t)(n3 + 1) * n2 * n1 * nb, 0.0);
-    }
-    const double gm1 = c.gamma - 1.0;
-    for (int b = 0; b < nb; ++b) {
-      int64_t loc[4];
-      check(athg_block_location(ctx, b, loc), "athg_block_location");
-      // cells of the block's level (loc[3]) across the whole domain
-      const int64_t lv = loc[3];
-      Axis ax = axis_of(c.nx1, ng, m.x1min, m.x1max, loc[0] * c.nx1, (int64_t)m.nx1 << lv);
-      Axis ay = axis_of(c.nx2, ng, m.x2min, m.x2max, loc[1] * c.nx2, (int64_t)m.nx2 << lv);
-      Axis az = axis_of(c.nx3, ng, m.x3min, m.x3max, loc[2] * c.nx3, (int64_t)m.nx3 << lv);
-      double* u = &U[5 * nc * b];
-      auto C = [&](int n, int k, int j, int i) -> double& {
-        return u[(size_t)n * nc + ((size_t)k * n2 + j) * n1 + i];
-      };
-      double* b1 = mhd ? &B1[(size_t)n3 * n2 * (n1 + 1) * b] : nullptr;
-      double* b2 = mhd ? &B2[(size_t)n3 * (n2 + 1) * n1 * b] : nullptr;
-      double* b3 = mhd ? &B3[(size_t)(n3 + 1) * n2 * n1 * b] : nullptr;
-      auto F1 = [&](int k, int j, int i) -> double& { return b1[((size_t)k * n2 + j) * (n1 + 1) + i]; };
-      auto F2 = [&](int k, int j, int i) -> double& { return b2[((size_t)k * (n2 + 1) + j) * n1 + i]; };
-      (void)b3;
-      const int is = ng, ie = ng + c.nx1 - 1, js = ng, je = ng + c.nx2 - 1, ks = ng, ke = ng + c.nx3 - 1;
-      if (pgen == "orszag_tang") {
-        const double PI = 3.1415926535897932, TWO_PI = 6.2831853071795862;
-        const double B0 = 1.0 / std::sqrt(4.0 * PI), d0 = 25.0 / (36.0 * PI), v0 = 1.0,
-                     p0 = 5.0 / (12.0 * PI);
-        auto Az = [&](double x, double y) {
-          return B0 / (4.0 * PI) * (std::cos(4.0 * PI * x) - 2.0 * std::cos(TWO_PI * y));
+    auto generate = [&]() -> int {
+      int nb = 0;
+      check(athg_num_blocks(ctx, &nb), "athg_num_blocks");
+      const int ng = c.nghost;
+      const int n1 = c.nx1 + 2 * ng, n2 = c.nx2 + 2 * ng, n3 = c.nx3 + 2 * ng;
+      const size_t nc = (size_t)n1 * n2 * n3;
+
+      // MeshBlock::ProblemGenerator for every block, then one upload per array
+      std::vector<double> U(5 * nc * nb, 0.0), B1, B2, B3;
+      if (mhd) {
+        B1.assign((size_t)n3 * n2 * (n1 + 1) * nb, 0.0);
+        B2.assign((size_t)n3 * (n2 + 1) * n1 * nb, 0.0);
+        B3.assign((size_t)(n3 + 1) * n2 * n1 * nb, 0.0);
+      }
+      const double gm1 = c.gamma - 1.0;
+      for (int b = 0; b < nb; ++b) {
+        int64_t loc[4];
+        check(athg_block_location(ctx, b, loc), "athg_block_location");
+        // cells of the block's level (loc[3]) across the whole domain
+        const int64_t lv = loc[3];
+        Axis ax = axis_of(c.nx1, ng, m.x1min, m.x1max, m.nx1, (int)lv, loc[0]);
+        Axis ay = axis_of(c.nx2, ng, m.x2min, m.x2max, m.nx2, (int)lv, loc[1]);
+        Axis az = axis_of(c.nx3, ng, m.x3min, m.x3max, m.nx3, (int)lv, loc[2]);
+        double* u = &U[5 * nc * b];
+        auto C = [&](int n, int k, int j, int i) -> double& {
+          return u[(size_t)n * nc + ((size_t)k * n2 + j) * n1 + i];
         };
-        for (int k = ks; k <= ke; ++k)
-          for (int j = js; j <= je; ++j)
-            for (int i = is; i <= ie; ++i) {
-              C(0, k, j, i) = d0;
-              C(1, k, j, i) = d0 * v0 * std::sin(TWO_PI * ay.xv[j]);
-              C(2, k, j, i) = -d0 * v0 * std::sin(TWO_PI * ax.xv[i]);
-              C(3, k, j, i) = 0.0;
-            }
-        if (mhd) {
+        double* b1 = mhd ? &B1[(size_t)n3 * n2 * (n1 + 1) * b] : nullptr;
+        double* b2 = mhd ? &B2[(size_t)n3 * (n2 + 1) * n1 * b] : nullptr;
+        double* b3 = mhd ? &B3[(size_t)(n3 + 1) * n2 * n1 * b] : nullptr;
+        auto F1 = [&](int k, int j, int i) -> double& { return b1[((size_t)k * n2 + j) * (n1 + 1) + i]; };
+        auto F2 = [&](int k, int j, int i) -> double& { return b2[((size_t)k * (n2 + 1) + j) * n1 + i]; };
+        (void)b3;
+        const int is = ng, ie = ng + c.nx1 - 1, js = ng, je = ng + c.nx2 - 1, ks = ng, ke = ng + c.nx3 - 1;
+        if (pgen == "orszag_tang") {
+          const double PI = 3.1415926535897932, TWO_PI = 6.2831853071795862;
+          const double B0 = 1.0 / std::sqrt(4.0 * PI), d0 = 25.0 / (36.0 * PI), v0 = 1.0,
+                       p0 = 5.0 / (12.0 * PI);
+          auto Az = [&](double x, double y) {
+            return B0 / (4.0 * PI) * (std::cos(4.0 * PI * x) - 2.0 * std::cos(TWO_PI * y));
+          };
           for (int k = ks; k <= ke; ++k)
             for (int j = js; j <= je; ++j)
-              for (int i = is; i <= ie + 1; ++i)
-                F1(k, j, i) = (Az(ax.xf[i], ay.xf[j + 1]) - Az(ax.xf[i], ay.xf[j])) / ay.dx;
-          for (int k = ks; k <= ke; ++k)
-            for (int j = js; j <= je + 1; ++j)
-              for (int i = is; i <= ie; ++i)
-                F2(k, j, i) = (Az(ax.xf[i], ay.xf[j]) - Az(ax.xf[i + 1], ay.xf[j])) / ax.dx;
-        }
-        for (int k = ks; k <= ke; ++k)
-          for (int j = js; j <= je; ++j)
-            for (int i = is; i <= ie; ++i) {
-              double pb = 0.0;
-              if (mhd) {
-                double c1 = 0.5 * (F1(k, j, i) + F1(k, j, i + 1));
-                double c2 = 0.5 * (F2(k, j, i) + F2(k, j + 1, i));
-                pb = 0.5 * (c1 * c1 + c2 * c2);
+              for (int i = is; i <= ie; ++i) {
+                C(0, k, j, i) = d0;
+                C(1, k, j, i) = d0 * v0 * std::sin(TWO_PI * ay.xv[j]);
+                C(2, k, j, i) = -d0 * v0 * std::sin(TWO_PI * ax.xv[i]);
+                C(3, k, j, i) = 0.0;
               }
-              const double d = C(0, k, j, i);
-              C(4, k, j, i) = p0 / gm1 + pb +
-                              0.5 * (C(1, k, j, i) * C(1, k, j, i) + C(2, k, j, i) * C(2, k, j, i)) / d;
-            }
-      } else if (pgen == "blast") {
-        const double rad = getd(p, "problem/radius", 0.1), pa = getd(p, "problem/pamb", 0.1),
-                     prat = getd(p, "problem/prat", 100.0), da = getd(p, "problem/damb", 1.0),
-                     b0 = getd(p, "problem/b0", mhd ? 1.0 : 0.0),
-                     ang = getd(p, "problem/angle", 45.0) * 3.1415926535897932 / 180.0;
-        const double bx = b0 * std::cos(ang), by = b0 * std::sin(ang);
-        if (mhd) {
-          for (int k = ks; k <= ke; ++k) {
-            for (int j = js; j <= je; ++j)
-              for (int i = is; i <= ie + 1; ++i) F1(k, j, i) = bx;
-            for (int j = js; j <= je + 1; ++j)
-              for (int i = is; i <= ie; ++i) F2(k, j, i) = by;
+          if (mhd) {
+            for (int k = ks; k <= ke; ++k)
+              for (int j = js; j <= je; ++j)
+                for (int i = is; i <= ie + 1; ++i)
+                  F1(k, j, i) = (Az(ax.xf[i], ay.xf[j + 1]) - Az(ax.xf[i], ay.xf[j])) / ay.dx;
+            for (int k = ks; k <= ke; ++k)
+              for (int j = js; j <= je + 1; ++j)
+                for (int i = is; i <= ie; ++i)
+                  F2(k, j, i) = (Az(ax.xf[i], ay.xf[j]) - Az(ax.xf[i + 1], ay.xf[j])) / ax.dx;
           }
-        }
-        for (int k = ks; k <= ke; ++k)
-          for (int j = js; j <= je; ++j)
-            for (int i = is; i <= ie; ++i) {
-              const double r = std::sqrt(ax.xv[i] * ax.xv[i] + ay.xv[j] * ay.xv[j] + az.xv[k] * az.xv[k]);
-              const double pr = r < rad ? pa * prat : pa;
-              C(0, k, j, i) = da;
-              C(1, k, j, i) = C(2, k, j, i) = C(3, k, j, i) = 0.0;
-              C(4, k, j, i) = pr / gm1 + (mhd ? 0.5 * (bx * bx + by * by) : 0.0);
+          for (int k = ks; k <= ke; ++k)
+            for (int j = js; j <= je; ++j)
+              for (int i = is; i <= ie; ++i) {
+                double pb = 0.0;
+                if (mhd) {
+                  double c1 = 0.5 * (F1(k, j, i) + F1(k, j, i + 1));
+                  double c2 = 0.5 * (F2(k, j, i) + F2(k, j + 1, i));
+                  pb = 0.5 * (c1 * c1 + c2 * c2);
+                }
+                const double d = C(0, k, j, i);
+                C(4, k, j, i) = p0 / gm1 + pb +
+                                0.5 * (C(1, k, j, i) * C(1, k, j, i) + C(2, k, j, i) * C(2, k, j, i)) / d;
+              }
+        } else if (pgen == "blast") {  // pgen/blast.cpp:54-211, Cartesian
+          const double PI = 3.1415926535897932;
+          const double rout = getd(p, "problem/radius", 0.1);
+          const double rin = rout - getd(p, "problem/ramp", 0.0);
+          const double pa = getd(p, "problem/pamb", 1.0), da = getd(p, "problem/damb", 1.0);
+          const double prat = getd(p, "problem/prat", 100.0), drat = getd(p, "problem/drat", 1.0);
+          const double b0 = mhd ? getd(p, "problem/b0", 1.0) : 0.0;
+          const double angle = (PI / 180.0) * getd(p, "problem/angle", 45.0);
+          const double x0 = getd(p, "problem/x1_0", 0.0), y0 = getd(p, "problem/x2_0", 0.0),
+                       z0 = getd(p, "problem/x3_0", 0.0);
+          for (int k = ks; k <= ke; ++k)
+            for (int j = js; j <= je; ++j)
+              for (int i = is; i <= ie; ++i) {
+                const double x = ax.xv[i] - x0, y = ay.xv[j] - y0, z = az.xv[k] - z0;
+                const double rad = std::sqrt(x * x + y * y + z * z);
+                double den = da, pres = pa;
+                if (rad < rout) {
+                  if (rad < rin) {
+                    den = drat * da;
+                    pres = prat * pa;
+                  } else {  // smooth ramp between rin and rout
+                    const double f = (rad - rin) / (rout - rin);
+                    den = std::exp((1.0 - f) * std::log(drat * da) + f * std::log(da));
+                    pres = std::exp((1.0 - f) * std::log(prat * pa) + f * std::log(pa));
+                  }
+                }
+                C(0, k, j, i) = den;
+                C(1, k, j, i) = C(2, k, j, i) = C(3, k, j, i) = 0.0;
+                C(4, k, j, i) = pres / gm1;
+              }
+          if (mhd) {
+            const double bx = b0 * std::cos(angle), by = b0 * std::sin(angle);
+            for (int k = ks; k <= ke; ++k) {
+              for (int j = js; j <= je; ++j)
+                for (int i = is; i <= ie + 1; ++i) F1(k, j, i) = bx;
+              for (int j = js; j <= je + 1; ++j)
+                for (int i = is; i <= ie; ++i) F2(k, j, i) = by;
             }
-      } else {
-        std::fprintf(stderr, "### FATAL ERROR: unknown gb300/pgen %s\n", pgen.c_str());
-        return 1;
+            for (int k = ks; k <= ke; ++k)
+              for (int j = js; j <= je; ++j)
+                for (int i = is; i <= ie; ++i) C(4, k, j, i) += 0.5 * b0 * b0;
+          }
+        } else {
+          std::fprintf(stderr, "### FATAL ERROR: unknown gb300/pgen %s\n", pgen.c_str());
+          return 1;
+        }
+      }
+      check(athg_upload(ctx, -1, ATHG_VAR_CONS, U.data(), U.size()), "upload U");
+      if (mhd) {
+        check(athg_upload(ctx, -1, ATHG_VAR_B1F, B1.data(), B1.size()), "upload B1");
+        check(athg_upload(ctx, -1, ATHG_VAR_B2F, B2.data(), B2.size()), "upload B2");
+        check(athg_upload(ctx, -1, ATHG_VAR_B3F, B3.data(), B3.size()), "upload B3");
+      }
+
+      return 0;
+    };
+    // Mesh::Initialize(0) (mesh/mesh.cpp:1367-1656): with adaptive refinement the problem
+    // generator runs again on every refined mesh until the criterion leaves it unchanged
+    if (generate()) return 1;
+    check(athg_initialize(ctx), "athg_initialize");
+    if (adaptive) {
+      for (int pass = 0;; ++pass) {
+        double tt, dd, dd_prev = 1.79769313486231570815e308;
+        int64_t nn;
+        if (pass > 0) {
+          check(athg_get_time(ctx, &tt, &dd_prev, &nn), "athg_get_time");
+          if (generate()) return 1;
+          check(athg_resume(ctx), "athg_resume");
+        }
+        check(athg_get_time(ctx, &tt, &dd, &nn), "athg_get_time");
+        // the check runs before the pass's NewTimeStep in the reference
+        check(athg_set_time(ctx, tt, dd_prev, nn), "athg_set_time");
+        int changed = 0;
+        check(athg_amr_regrid(ctx, &changed), "athg_amr_regrid");
+        if (!changed) {
+          check(athg_set_time(ctx, tt, dd, nn), "athg_set_time");
+          break;
+        }
       }
     }
-    check(athg_upload(ctx, -1, ATHG_VAR_CONS, U.data(), U.size()), "upload U");
-    if (mhd) {
-      check(athg_upload(ctx, -1, ATHG_VAR_B1F, B1.data(), B1.size()), "upload B1");
-      check(athg_upload(ctx, -1, ATHG_VAR_B2F, B2.data(), B2.size()), "upload B2");
-      check(athg_upload(ctx, -1, ATHG_VAR_B3F, B3.data(), B3.size()), "upload B3");
-    }
-    check(athg_initialize(ctx), "athg_initialize");
+
   }
 
   // outputs: <outputN> file_type = hst | vtk | rst (Outputs::MakeOutputs timing)
@@ -404,9 +476,10 @@ int main(int argc, char** argv) {
   std::FILE* hst = nullptr;
   bool hst_header = false;
   int nb_all = 0;
-  check(athg_num_blocks(ctx, &nb_all), "athg_num_blocks");
-  // every block's location and arrays, in the library's order
+  // every block's location and arrays, in the library's order (adaptive refinement
+  // changes the list from cycle to cycle)
   auto download_state = [&](bool prim) {
+    check(athg_num_blocks(ctx, &nb_all), "athg_num_blocks");
     st.blocks.resize(nb_all);
     for (int b = 0; b < nb_all; ++b) {
       int64_t loc[4];
@@ -505,7 +578,10 @@ int main(int argc, char** argv) {
   make_outputs(false);
   const auto t0 = std::chrono::steady_clock::now();
   int64_t cycles = 0;
+  double zone_cycles = 0.0;
   while (t < c.tlim && (nlim < 0 || ncycle < nlim)) {
+    check(athg_num_blocks(ctx, &nb_all), "athg_num_blocks");
+    zone_cycles += (double)nb_all * c.nx1 * c.nx2 * c.nx3;
     check(athg_cycles(ctx, 1), "athg_cycles");
     ++cycles;
     check(athg_get_time(ctx, &t, &dt, &ncycle), "athg_get_time");
@@ -515,11 +591,12 @@ int main(int argc, char** argv) {
   const double el = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
   make_outputs(true);
   if (hst) std::fclose(hst);
-  const double zones = (double)nb_all * c.nx1 * c.nx2 * c.nx3;
+  check(athg_num_blocks(ctx, &nb_all), "athg_num_blocks");
   // main.cpp:580-600 summary
   std::printf("cycle=%lld time=%.10e dt=%.10e\n", (long long)ncycle, t, dt);
+  std::printf("Number of MeshBlocks = %d\n", nb_all);
   std::printf("zone-cycles = %.0f\nwall time = %.6f s\nzone-cycles/wsecond = %.6e\n",
-              zones * cycles, el, cycles > 0 ? zones * cycles / el : 0.0);
+              zone_cycles, el, cycles > 0 ? zone_cycles / el : 0.0);
   athg_destroy(ctx);
   return 0;
 }

@@ -111,6 +111,27 @@ int athg_set_refined_mesh(athg_ctx* ctx, const athg_mesh* mesh, int nregions,
  * locs[4*b .. 4*b+3] = level (relative to the root grid), lx1, lx2, lx3 of block b. */
 int athg_set_multilevel_blocks(athg_ctx* ctx, const athg_mesh* mesh, int nblocks,
                                const int64_t* locs);
+/* Adaptive refinement (<mesh> refinement = adaptive) with the blast's criterion
+ * (pgen/blast.cpp:413-442): a block is flagged for refinement where max |grad p| / p over
+ * its cells exceeds `threshold`, for derefinement below deref_fraction * threshold;
+ * MeshRefinement::CheckRefinementCondition (derefinement counters, no derefinement next to
+ * finer blocks), Mesh::UpdateMeshBlockTree / MeshBlockTree::Refine / Derefine and the data
+ * of new blocks (FillSameRankCoarseToFineAMR / FineToCoarseAMR) follow the reference. */
+typedef struct {
+  double threshold;       /* <problem> thr */
+  double deref_fraction;  /* 0.25 in the reference's blast */
+  int max_level;          /* levels above the root: <mesh> numlevel - 1 */
+  int derefine_count;     /* <mesh> derefine_count (the reference's default is 10) */
+} athg_amr_config;
+/* Turns adaptive refinement on (FP64, periodic); a uniform mesh keeps its state. From
+ * then on athg_cycles checks the criterion after every cycle and regrids (the main loop's
+ * LoadBalancingAndAdaptiveMeshRefinement + NewTimeStep); blocks may change order and
+ * number (athg_num_blocks, athg_block_location). */
+int athg_amr_enable(athg_ctx* ctx, const athg_amr_config* cfg);
+/* One refinement check and regrid on the current state, with Mesh::Initialize(2) after a
+ * change (the initial refinement loop of Mesh::Initialize): *changed = 1 if the mesh
+ * changed. */
+int athg_amr_regrid(athg_ctx* ctx, int* changed);
 /* Sizes of the multi-level work lists (all 0 on a single-level mesh): out[0..7] = ghost-fill
  * elements, same-level restrictions, flux corrections, EMF corrections, coarse cells
  * converted to primitives, prolongated cells, internal-field cells, fine cells rebuilt. */

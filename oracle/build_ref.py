@@ -44,6 +44,8 @@ CONFIGS = {
     "ot_mhd_hlld_omp": ("orszag_tang.cpp", "hlld", True, 2, 0, True, None),
     "blast_mhd_hlld": ("blast.cpp", "hlld", True, 4, 0, False, None),
     "blast_hydro_hllc": ("blast.cpp", "hllc", False, 4, 0, False, None),
+    "blast_mhd_hlld_ng2": ("blast.cpp", "hlld", True, 2, 0, False, None),
+    "blast_hydro_hllc_ng2": ("blast.cpp", "hllc", False, 2, 0, False, None),
     # harness: loads a raw state file written by the tests (own pgen)
     "state_mhd_hlld": ("harness:load_state.cpp", "hlld", True, 2, 0, False, None),
     "state_mhd_hlld_ng4": ("harness:load_state.cpp", "hlld", True, 4, 0, False, None),
