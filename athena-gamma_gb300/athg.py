@@ -38,7 +38,7 @@ EXPORTS = [
     "athg_get_tuning", "athg_set_tuning",
     "athg_block_cfl_dt_noalloc", "athg_set_refined_mesh", "athg_set_multilevel_blocks",
     "athg_smr_stats", "athg_resume", "athg_cycle_timing", "athg_amr_enable",
-    "athg_amr_regrid",
+    "athg_amr_regrid", "athg_turb_attach", "athg_turb_drive", "athg_attach_fft_gravity",
 ]
 MG_BC = {"periodic": 0, "zerograd": 1, "zerofixed": 2, "multipole": 3}
 
@@ -76,6 +76,12 @@ class Region(C.Structure):
 class AmrConfig(C.Structure):
     _fields_ = [("threshold", C.c_double), ("deref_fraction", C.c_double),
                 ("max_level", C.c_int), ("derefine_count", C.c_int)]
+
+
+class TurbConfig(C.Structure):
+    _fields_ = [("turb_flag", C.c_int), ("rseed", C.c_int64), ("nlow", C.c_int),
+                ("nhigh", C.c_int), ("dtdrive", C.c_double), ("tcorr", C.c_double),
+                ("f_shear", C.c_double), ("expo", C.c_double), ("dedt", C.c_double)]
 
 
 class AthgError(RuntimeError):
@@ -143,6 +149,9 @@ def lib():
         "athg_cycle_timing": [vp, i, C.POINTER(d), C.POINTER(i), C.c_char_p, sz],
         "athg_amr_enable": [vp, C.POINTER(AmrConfig)],
         "athg_amr_regrid": [vp, C.POINTER(i)],
+        "athg_turb_attach": [vp, C.POINTER(Mesh), C.POINTER(TurbConfig)],
+        "athg_turb_drive": [vp],
+        "athg_attach_fft_gravity": [vp, C.POINTER(Mesh), d],
     }
     for name, args in sig.items():
         f = getattr(L, name)
@@ -205,6 +214,7 @@ class Sim:
         else:
             check(L.athg_set_uniform_mesh(h, C.byref(m)))
         self.mesh_nx, self.block_nx, self.ng, self.mhd = tuple(mesh_nx), tuple(block_nx), ng, mhd
+        self._mesh = m
         self._list_blocks()
         self.multilevel = regions is not None or leaves is not None
         self.nc = tuple(n + 2 * ng for n in block_nx)
@@ -392,6 +402,9 @@ class Sim:
         check(lib().athg_get_time(self.h, C.byref(t), C.byref(dt), C.byref(n)))
         return t.value, dt.value, n.value
 
+    def set_time(self, time, dt, ncycle):
+        check(lib().athg_set_time(self.h, time, dt, ncycle))
+
     def run(self, tlim, nlim=-1, chunk=1):
         """Whole cycles until time >= tlim (main.cpp:430 loop condition)."""
         n = 0
@@ -448,6 +461,27 @@ class Sim:
         """Self-gravity through a Multigrid on the same mesh (None detaches)."""
         check(lib().athg_attach_gravity(self.h, mg.h if mg is not None else None, four_pi_G))
         self._grav = mg  # the solver must outlive the coupling
+
+    def attach_fft_gravity(self, four_pi_G):
+        """FFT self-gravity over the whole periodic mesh (0 detaches)."""
+        check(lib().athg_attach_fft_gravity(self.h, C.byref(self._mesh), four_pi_G))
+        self._grav = None
+
+    def attach_turbulence(self, turb_flag, dedt, rseed=1, nlow=0, nhigh=None, dtdrive=0.0,
+                          tcorr=0.0, f_shear=-1.0, expo=2.0):
+        """The reference's turbulence driver (<problem> turb_flag, <turbulence> block);
+        nhigh defaults to mesh nx1 / 2 as there; turb_flag 0 detaches."""
+        if not turb_flag:
+            check(lib().athg_turb_attach(self.h, C.byref(self._mesh), None))
+            return
+        t = TurbConfig()
+        t.turb_flag, t.rseed, t.nlow = turb_flag, rseed, nlow
+        t.nhigh = self.mesh_nx[0] // 2 if nhigh is None else nhigh
+        t.dtdrive, t.tcorr, t.f_shear, t.expo, t.dedt = dtdrive, tcorr, f_shear, expo, dedt
+        check(lib().athg_turb_attach(self.h, C.byref(self._mesh), C.byref(t)))
+
+    def turb_drive(self):
+        check(lib().athg_turb_drive(self.h))
 
     def phi(self):
         """Global potential with one ghost layer around the mesh: (N3+2, N2+2, N1+2)."""

@@ -15,6 +15,7 @@
 #include "athg_bvals.cuh"
 #include "athg_launch.cuh"
 #include "athg_amr.h"
+#include "athg_fft.h"
 #include "athg_internal.h"
 
 using namespace athg;
@@ -240,6 +241,10 @@ struct athg_ctx {
   double four_pi_G = 0.0;
   double* phi = nullptr;
   int* boff = nullptr;
+  // FFT self-gravity (SELF_GRAVITY_ENABLED == 1) in place of the multigrid, and the
+  // turbulence driver; both transform the whole mesh (blocks placed by boff)
+  athg::FftGravity* fgrav = nullptr;
+  athg::Turb* turb = nullptr;
   // multi-level mesh (static refinement): work lists, coarse buffers (FP64 path only)
   athg::SmrDevice* smr = nullptr;
   // adaptive refinement (FP64, periodic): criterion and counters; the root mesh of the
@@ -312,6 +317,10 @@ void free_pool(athg_ctx* c) {
   c->phi = nullptr; c->boff = nullptr;
   if (c->grav) athg::mg_bind_stream(c->grav, nullptr);
   c->grav = nullptr;
+  athg::fftgrav_destroy(c->fgrav);
+  c->fgrav = nullptr;
+  athg::turb_destroy(c->turb);
+  c->turb = nullptr;
   athg::smr_destroy(c->smr);
   c->smr = nullptr;
   if (c->amr_bits) cudaFree(c->amr_bits);
@@ -454,8 +463,69 @@ __global__ void k_scatter_phi(Geom g, double* __restrict__ phi, const int* __res
       um[((int64_t)K * nt + J) * nt + I];
 }
 
+bool has_gravity(const athg_ctx* c) { return c->grav || c->fgrav; }
+
+// whether a cycle can be captured as a CUDA graph: no host synchronisation (multigrid
+// iterating to a threshold or with multipole boundaries) and no cuFFT call inside
+bool captured(const athg_ctx* c) {
+  return !(c->grav && !athg::mg_solve_capturable(c->grav)) && !c->fgrav;
+}
+
+// TurbulenceDriver::Driving at the context's current time and dt
+int turb_drive(athg_ctx* c) {
+  double hs[2];
+  CK(cudaMemcpyAsync(hs, c->scal, sizeof(hs), cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  std::string err;
+  if (athg::turb_drive(c->turb, c->g, c->nb, c->u, c->boff, hs[0], hs[1], c->st, &err))
+    return fail(ATHG_ERR_CUDA, err);
+  c->counting += 6;
+  return ATHG_OK;
+}
+
+// Offsets of every block in a mesh-wide array of n1 x n2 x n3 cells (one uniform level
+// tiling it) into c->boff; the phi array of the gravity coupling is allocated with it.
+int tile_blocks(athg_ctx* c, int n1, int n2, int n3) {
+  const Geom& g = c->g;
+  if (c->smr) return fail(ATHG_ERR_ARG, "a mesh-wide solver on a multi-level mesh is not supported");
+  if (n1 % g.nx1 || n2 % g.nx2 || n3 % g.nx3)
+    return fail(ATHG_ERR_ARG, "mesh size is not a multiple of the block size");
+  const int64_t nbx = n1 / g.nx1, nby = n2 / g.nx2, nbz = n3 / g.nx3;
+  if (nbx * nby * nbz != c->nb) return fail(ATHG_ERR_ARG, "blocks do not tile the mesh");
+  std::vector<int> hb(3 * c->nb);
+  std::vector<char> seen((size_t)nbx * nby * nbz, 0);
+  for (int b = 0; b < c->nb; ++b) {
+    const athg_block& B = c->blocks[b];
+    if (B.level != c->blocks[0].level)
+      return fail(ATHG_ERR_ARG, "a mesh-wide solver needs blocks of one refinement level");
+    if (B.lx1 < 0 || B.lx1 >= nbx || B.lx2 < 0 || B.lx2 >= nby || B.lx3 < 0 || B.lx3 >= nbz)
+      return fail(ATHG_ERR_ARG, "block location outside the mesh");
+    char& f = seen[((size_t)B.lx3 * nby + B.lx2) * nbx + B.lx1];
+    if (f) return fail(ATHG_ERR_ARG, "two blocks at one location");
+    f = 1;
+    hb[3 * b] = (int)(B.lx1 * g.nx1);
+    hb[3 * b + 1] = (int)(B.lx2 * g.nx2);
+    hb[3 * b + 2] = (int)(B.lx3 * g.nx3);
+  }
+  if (!c->boff) CK(cudaMalloc(&c->boff, sizeof(int) * 3 * c->nb));
+  if (!c->phi) {
+    CK(cudaMalloc(&c->phi, sizeof(double) * g.ncell * c->nb));
+    CK(cudaMemsetAsync(c->phi, 0, sizeof(double) * g.ncell * c->nb, c->st));
+  }
+  CK(cudaMemcpyAsync(c->boff, hb.data(), sizeof(int) * hb.size(), cudaMemcpyHostToDevice, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  return ATHG_OK;
+}
+
 // MGGravityDriver::Solve (gravity/mg_gravity.cpp:166-211) on the context's stream
 int gravity_solve(athg_ctx* c) {
+  if (c->fgrav) {  // FFTGravityDriver::Solve (gravity/fft_gravity.cpp:58-100)
+    std::string err;
+    if (athg::fftgrav_solve(c->fgrav, c->g, c->nb, c->u, c->boff, c->phi, c->st, &err))
+      return fail(ATHG_ERR_CUDA, err);
+    c->counting += 4;
+    return ATHG_OK;
+  }
   double *um, *src;
   int n;
   int rc = athg::mg_finest(c->grav, &um, &src, &n);
@@ -484,7 +554,7 @@ int launch_self_gravity(athg_ctx* c, int l) {
 }
 
 bool fused(const athg_ctx* c) {
-  return c->fused_ok && c->mixed() && c->cfg.integrator == ATHG_VL2 && !c->grav;
+  return c->fused_ok && c->mixed() && c->cfg.integrator == ATHG_VL2 && !has_gravity(c);
 }
 
 // swap the two state buffers (after a fused cycle the new state is in (u1, r))
@@ -587,14 +657,14 @@ int do_stage(athg_ctx* c, int stage) {
   if ((rc = launch_update(c, l))) return rc;
   mark(c, stage, "update (k_update)");
   // AddSourceTerms (time_integrator.cpp:1655-1676); every stage here is a main stage
-  if (c->grav && (rc = launch_self_gravity(c, l))) return rc;
-  if (c->grav) mark(c, stage, "self-gravity source");
+  if (has_gravity(c) && (rc = launch_self_gravity(c, l))) return rc;
+  if (has_gravity(c)) mark(c, stage, "self-gravity source");
   if ((rc = launch_ghosts(c))) return rc;
   mark(c, stage, "ghost exchange");
   if ((rc = launch_c2p(c))) return rc;
   mark(c, stage, "primitives (k_c2p)");
-  if (c->grav && (rc = gravity_solve(c))) return rc;  // main.cpp:461-466
-  if (c->grav) mark(c, stage, "gravity solve");
+  if (has_gravity(c) && (rc = gravity_solve(c))) return rc;  // main.cpp:461-466
+  if (has_gravity(c)) mark(c, stage, "gravity solve");
   if (stage == c->integ.nstages) {
     if ((rc = launch_block_dt(c))) return rc;
     mark(c, stage, "time step");
@@ -1459,7 +1529,9 @@ int athg_initialize(athg_ctx* c) {
   std::memcpy(&big, &kDblMax, 8);
   std::memcpy(&hs[3], &big, 8);
   CK(cudaMemcpyAsync(c->scal, hs, sizeof(hs), cudaMemcpyHostToDevice, c->st));
-  if (c->grav && (rc = gravity_solve(c))) return rc;  // mesh/mesh.cpp:1398-1402
+  // the first perturbation of decaying or impulsive turbulence (mesh/mesh.cpp:1383-1384)
+  if (c->turb && athg::turb_flag(c->turb) <= 2 && (rc = turb_drive(c))) return rc;
+  if (has_gravity(c) && (rc = gravity_solve(c))) return rc;  // mesh/mesh.cpp:1398-1402
   if ((rc = launch_ghosts(c))) return rc;
   c->ghosts_stale = false;
   if ((rc = launch_c2p(c))) return rc;
@@ -1477,7 +1549,7 @@ int athg_resume(athg_ctx* c) {
   unsigned long long big;
   std::memcpy(&big, &kDblMax, 8);
   CK(cudaMemcpyAsync(c->scal + 3, &big, 8, cudaMemcpyHostToDevice, c->st));
-  if (c->grav && (rc = gravity_solve(c))) return rc;
+  if (has_gravity(c) && (rc = gravity_solve(c))) return rc;
   if ((rc = launch_ghosts(c))) return rc;
   c->ghosts_stale = false;
   if ((rc = launch_c2p(c))) return rc;
@@ -1506,8 +1578,22 @@ int athg_cycles(athg_ctx* c, int n) {
   int rc = need_pool(c);
   if (rc) return rc;
   if (n <= 0) return ATHG_OK;
-  if (c->grav && !athg::mg_solve_capturable(c->grav)) {
-    // the solve iterates to a threshold or sets up multipole moments on the host
+  if (c->turb && athg::turb_flag(c->turb) > 1) {
+    // driven turbulence: Driving before every cycle (main.cpp:457), random numbers on the host
+    for (int q = 0; q < n; ++q) {
+      if ((rc = turb_drive(c))) return rc;
+      if (!captured(c)) {
+        if ((rc = do_cycle(c))) return rc;
+      } else {
+        if ((rc = build_graph(c))) return rc;
+        if ((rc = run_cycle_graph(c))) return rc;
+      }
+    }
+    return ATHG_OK;
+  }
+  if (!captured(c)) {
+    // the solve iterates to a threshold or sets up multipole moments on the host, or
+    // runs cuFFT
     for (int q = 0; q < n; ++q)
       if ((rc = do_cycle(c))) return rc;
     return ATHG_OK;
@@ -1572,8 +1658,8 @@ int athg_launches_per_cycle(athg_ctx* c, int* n) {
   int rc = need_pool(c);
   if (rc) return rc;
   if (!n) return fail(ATHG_ERR_ARG, "null argument");
-  if (c->grav && !athg::mg_solve_capturable(c->grav))
-    return fail(ATHG_ERR_STATE, "cycles with this multigrid mode are not captured as a graph");
+  if (!captured(c))
+    return fail(ATHG_ERR_STATE, "cycles with this gravity solver are not captured as a graph");
   if ((rc = build_graph(c))) return rc;
   *n = c->launches_per_cycle;
   return ATHG_OK;
@@ -1587,42 +1673,67 @@ int athg_attach_gravity(athg_ctx* c, athg_mg* mg, double four_pi_G) {
   if ((rc = refresh_ghosts(c))) return rc;
   if (c->grav) athg::mg_bind_stream(c->grav, nullptr);
   c->grav = nullptr;
+  athg::fftgrav_destroy(c->fgrav);
+  c->fgrav = nullptr;
   if (!mg) return ATHG_OK;
   if (c->smr) return fail(ATHG_ERR_ARG, "self-gravity on a multi-level mesh is not supported");
   double *um, *src;
   int n;
   if ((rc = athg::mg_finest(mg, &um, &src, &n))) return rc;
   // one uniform level tiling the solver's n^3 root grid
-  const Geom& g = c->g;
-  std::vector<int> hb(3 * c->nb);
-  std::vector<char> seen((size_t)(n / g.nx1 + 1) * (n / g.nx2 + 1) * (n / g.nx3 + 1), 0);
-  if (n % g.nx1 || n % g.nx2 || n % g.nx3)
-    return fail(ATHG_ERR_ARG, "multigrid size is not a multiple of the block size");
-  const int64_t nbx = n / g.nx1, nby = n / g.nx2, nbz = n / g.nx3;
-  if (nbx * nby * nbz != c->nb)
-    return fail(ATHG_ERR_ARG, "blocks do not tile the multigrid root grid");
-  for (int b = 0; b < c->nb; ++b) {
-    const athg_block& B = c->blocks[b];
-    if (B.level != c->blocks[0].level)
-      return fail(ATHG_ERR_ARG, "self-gravity needs blocks of one refinement level");
-    if (B.lx1 < 0 || B.lx1 >= nbx || B.lx2 < 0 || B.lx2 >= nby || B.lx3 < 0 || B.lx3 >= nbz)
-      return fail(ATHG_ERR_ARG, "block location outside the multigrid root grid");
-    char& f = seen[((size_t)B.lx3 * nby + B.lx2) * nbx + B.lx1];
-    if (f) return fail(ATHG_ERR_ARG, "two blocks at one location");
-    f = 1;
-    hb[3 * b] = (int)(B.lx1 * g.nx1);
-    hb[3 * b + 1] = (int)(B.lx2 * g.nx2);
-    hb[3 * b + 2] = (int)(B.lx3 * g.nx3);
-  }
-  if (!c->boff) CK(cudaMalloc(&c->boff, sizeof(int) * 3 * c->nb));
-  if (!c->phi) CK(cudaMalloc(&c->phi, sizeof(double) * g.ncell * c->nb));
-  CK(cudaMemsetAsync(c->phi, 0, sizeof(double) * g.ncell * c->nb, c->st));
-  CK(cudaMemcpyAsync(c->boff, hb.data(), sizeof(int) * hb.size(), cudaMemcpyHostToDevice, c->st));
-  CK(cudaStreamSynchronize(c->st));
+  if ((rc = tile_blocks(c, n, n, n))) return rc;
+  CK(cudaMemsetAsync(c->phi, 0, sizeof(double) * c->g.ncell * c->nb, c->st));
   if ((rc = athg::mg_bind_stream(mg, c->st))) return rc;
   c->grav = mg;
   c->four_pi_G = four_pi_G;
   return ATHG_OK;
+}
+
+int athg_attach_fft_gravity(athg_ctx* c, const athg_mesh* mesh, double four_pi_G) {
+  int rc = need_pool(c);
+  if (rc) return rc;
+  drop_graphs(c);
+  if ((rc = refresh_ghosts(c))) return rc;
+  if (c->grav) athg::mg_bind_stream(c->grav, nullptr);
+  c->grav = nullptr;
+  athg::fftgrav_destroy(c->fgrav);
+  c->fgrav = nullptr;
+  if (four_pi_G == 0.0) return ATHG_OK;
+  if (!mesh) return fail(ATHG_ERR_ARG, "null argument");
+  if ((rc = tile_blocks(c, mesh->nx1, mesh->nx2, mesh->nx3))) return rc;
+  CK(cudaMemsetAsync(c->phi, 0, sizeof(double) * c->g.ncell * c->nb, c->st));
+  athg::FftMesh fm{{mesh->nx1, mesh->nx2, mesh->nx3},
+                   {mesh->x1max - mesh->x1min, mesh->x2max - mesh->x2min, mesh->x3max - mesh->x3min}};
+  std::string err;
+  if (athg::fftgrav_create(fm, four_pi_G, &c->fgrav, &err)) return fail(ATHG_ERR_CUDA, err);
+  c->four_pi_G = four_pi_G;
+  return ATHG_OK;
+}
+
+int athg_turb_attach(athg_ctx* c, const athg_mesh* mesh, const athg_turb_config* cfg) {
+  int rc = need_pool(c);
+  if (rc) return rc;
+  athg::turb_destroy(c->turb);
+  c->turb = nullptr;
+  if (!cfg) return ATHG_OK;
+  if (!mesh) return fail(ATHG_ERR_ARG, "null argument");
+  if ((rc = tile_blocks(c, mesh->nx1, mesh->nx2, mesh->nx3))) return rc;
+  double t0;
+  CK(cudaMemcpyAsync(&t0, c->scal, 8, cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  athg::FftMesh fm{{mesh->nx1, mesh->nx2, mesh->nx3},
+                   {mesh->x1max - mesh->x1min, mesh->x2max - mesh->x2min, mesh->x3max - mesh->x3min}};
+  std::string err;
+  if ((rc = athg::turb_create(fm, *cfg, t0, &c->turb, &err)))
+    return fail(rc > 0 ? ATHG_ERR_ARG : ATHG_ERR_CUDA, err);
+  return ATHG_OK;
+}
+
+int athg_turb_drive(athg_ctx* c) {
+  int rc = need_pool(c);
+  if (rc) return rc;
+  if (!c->turb) return fail(ATHG_ERR_STATE, "no turbulence driver attached");
+  return turb_drive(c);
 }
 
 int athg_get_time(athg_ctx* c, double* time, double* dt, int64_t* ncycle) {
@@ -1780,7 +1891,7 @@ int athg_history(athg_ctx* c, double* out, int* count) {
   const size_t np = (size_t)grid.x * grid.y * grid.z;
   double* part = nullptr;
   CK(cudaMallocAsync(&part, np * kHist * sizeof(double), c->st));
-  k_history<<<grid, 256, 0, c->st>>>(g, c->u, c->b1, c->b2, c->b3, c->grav ? c->phi : nullptr,
+  k_history<<<grid, 256, 0, c->st>>>(g, c->u, c->b1, c->b2, c->b3, has_gravity(c) ? c->phi : nullptr,
                                      c->geo, c->cfg.magnetic, part);
   cudaError_t e = cudaGetLastError();
   std::vector<double> h(np * kHist);

@@ -225,6 +225,27 @@ int main(int argc, char** argv) {
   amr_cfg.deref_fraction = 0.25;
   amr_cfg.max_level = geti(p, "mesh/numlevel", 1) - 1;
   amr_cfg.derefine_count = geti(p, "mesh/derefine_count", 10);
+  // <problem> turb_flag with the <turbulence> block (fft/turbulence.cpp:42-63) and FFT
+  // self-gravity (<gb300> gravity = fft, <problem> four_pi_G; pgen/turb.cpp:36-43)
+  const int turb_flag = geti(p, "problem/turb_flag", 0);
+  auto attach_fft_parts = [&]() {
+    if (turb_flag != 0) {
+      athg_turb_config tc{};
+      tc.turb_flag = turb_flag;
+      tc.rseed = geti(p, "turbulence/rseed", -1);
+      tc.nlow = geti(p, "turbulence/nlow", 0);
+      tc.nhigh = geti(p, "turbulence/nhigh", m.nx1 / 2);
+      tc.dtdrive = getd(p, "turbulence/dtdrive", 0.0);
+      tc.tcorr = getd(p, "turbulence/tcorr", 0.0);
+      tc.f_shear = getd(p, "turbulence/f_shear", -1.0);
+      tc.expo = getd(p, "turbulence/expo", 2.0);
+      tc.dedt = getd(p, "turbulence/dedt", 0.0);
+      check(athg_turb_attach(ctx, &m, &tc), "athg_turb_attach");
+    }
+    if (get(p, "gb300/gravity", "none") == "fft")
+      check(athg_attach_fft_gravity(ctx, &m, getd(p, "problem/four_pi_G", 0.0)),
+            "athg_attach_fft_gravity");
+  };
   if (!restart.empty()) {
     // Mesh::Mesh(pin, restartfile) + Mesh::Initialize(res_flag = 1)
     std::string text, err;
@@ -272,6 +293,7 @@ int main(int argc, char** argv) {
       }
     }
     check(athg_set_time(ctx, st.time, st.dt, st.ncycle), "athg_set_time");
+    attach_fft_parts();  // the driver starts at the restart time (tdrive = time)
     check(athg_resume(ctx), "athg_resume");
   } else {
     // <refinementN> blocks (static refinement, mesh/mesh.cpp:334-462)
@@ -292,6 +314,7 @@ int main(int argc, char** argv) {
     else
       check(athg_set_uniform_mesh(ctx, &m), "athg_set_uniform_mesh");
     if (adaptive) check(athg_amr_enable(ctx, &amr_cfg), "athg_amr_enable");
+    attach_fft_parts();
     // MeshBlock::ProblemGenerator for every block, then one upload per array
     auto generate = [&]() -> int {
       int nb = 0;
@@ -299,8 +322,6 @@ int main(int argc, char** argv) {
       const int ng = c.nghost;
       const int n1 = c.nx1 + 2 * ng, n2 = c.nx2 + 2 * ng, n3 = c.nx3 + 2 * ng;
       const size_t nc = (size_t)n1 * n2 * n3;
-
-      // MeshBlock::ProblemGenerator for every block, then one upload per array
       std::vector<double> U(5 * nc * nb, 0.0), B1, B2, B3;
       if (mhd) {
         B1.assign((size_t)n3 * n2 * (n1 + 1) * nb, 0.0);
@@ -407,6 +428,14 @@ int main(int argc, char** argv) {
               for (int j = js; j <= je; ++j)
                 for (int i = is; i <= ie; ++i) C(4, k, j, i) += 0.5 * b0 * b0;
           }
+        } else if (pgen == "turb") {  // pgen/turb.cpp:58-78: uniform gas at rest
+          for (int k = ks; k <= ke; ++k)
+            for (int j = js; j <= je; ++j)
+              for (int i = is; i <= ie; ++i) {
+                C(0, k, j, i) = 1.0;
+                C(1, k, j, i) = C(2, k, j, i) = C(3, k, j, i) = 0.0;
+                C(4, k, j, i) = 1.0;
+              }
         } else {
           std::fprintf(stderr, "### FATAL ERROR: unknown gb300/pgen %s\n", pgen.c_str());
           return 1;
@@ -454,7 +483,7 @@ int main(int argc, char** argv) {
     int id;
     std::string type, var;
     double dt, next;
-    int number;
+    int number, dcycle;
   };
   double t = 0.0, dt = 0.0;
   int64_t ncycle = 0;
@@ -469,6 +498,7 @@ int main(int argc, char** argv) {
     o.type = get(p, blk + "file_type", "hst");
     o.var = get(p, blk + "variable", "prim");
     o.dt = getd(p, blk + "dt", -1.0);
+    o.dcycle = geti(p, blk + "dcycle", 0);
     o.next = getd(p, blk + "next_time", start_time);
     o.number = geti(p, blk + "file_number", 0);
     outs.push_back(o);
@@ -571,11 +601,11 @@ int main(int argc, char** argv) {
     int64_t nn;
     check(athg_get_time(ctx, &tt, &dd, &nn), "athg_get_time");
     for (Out& o : outs)
-      if (tt == start_time || (o.dt > 0.0 && tt >= o.next) || tt >= c.tlim ||
-          (final && (o.type == "rst" || o.type == "hst")))  // history: a closing row
+      if (tt == start_time || (o.dt > 0.0 && tt >= o.next) ||
+          (o.dcycle > 0 && nn % o.dcycle == 0) || tt >= c.tlim || (final && o.type == "rst"))
         write_output(o, final);
   };
-  make_outputs(false);
+  if (restart.empty()) make_outputs(false);  // main.cpp:397
   const auto t0 = std::chrono::steady_clock::now();
   int64_t cycles = 0;
   double zone_cycles = 0.0;
@@ -585,7 +615,7 @@ int main(int argc, char** argv) {
     check(athg_cycles(ctx, 1), "athg_cycles");
     ++cycles;
     check(athg_get_time(ctx, &t, &dt, &ncycle), "athg_get_time");
-    make_outputs(false);
+    if (t < c.tlim) make_outputs(false);  // the final output happens after the loop
   }
   check(athg_synchronize(ctx), "athg_synchronize");
   const double el = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();

@@ -132,6 +132,34 @@ int athg_amr_enable(athg_ctx* ctx, const athg_amr_config* cfg);
  * change (the initial refinement loop of Mesh::Initialize): *changed = 1 if the mesh
  * changed. */
 int athg_amr_regrid(athg_ctx* ctx, int* changed);
+/* ---- FFT over the whole uniform periodic mesh (cuFFT) ------------------------------ */
+/* Turbulence driving (fft/turbulence.cpp, <problem> turb_flag and the <turbulence> block):
+ * a power-law spectrum with Gaussian amplitudes and uniform phases from std::mt19937_64
+ * (the same sequence as the reference for a given rseed >= 0), optional projection onto
+ * compressive/shear parts, Ornstein-Uhlenbeck smoothing in time, transformed to a velocity
+ * perturbation that is mean-free in momentum and scaled to inject dedt (per unit time for
+ * driven turbulence) into the kinetic energy. */
+typedef struct {
+  int turb_flag;   /* 1 decaying (once at athg_initialize), 2 impulsive every dtdrive,
+                      3 continuous (every cycle) */
+  int64_t rseed;   /* <turbulence> rseed; < 0 seeds from std::random_device */
+  int nlow, nhigh; /* <turbulence> nlow (0), nhigh (mesh nx1 / 2): kept shells */
+  double dtdrive;  /* <turbulence> dtdrive (turb_flag 2) */
+  double tcorr;    /* <turbulence> tcorr: OU correlation time (turb_flag > 1) */
+  double f_shear;  /* <turbulence> f_shear: shear fraction; < 0 no projection */
+  double expo;     /* <turbulence> expo (2) */
+  double dedt;     /* <turbulence> dedt */
+} athg_turb_config;
+/* Attaches the driver (uniform single-level mesh whose blocks tile `mesh`; FP64 state).
+ * athg_initialize then drives once for turb_flag 1 and 2 (mesh/mesh.cpp:1383-1384) and
+ * athg_cycles drives before every cycle for turb_flag > 1 (main.cpp:457). cfg NULL detaches. */
+int athg_turb_attach(athg_ctx* ctx, const athg_mesh* mesh, const athg_turb_config* cfg);
+/* One TurbulenceDriver::Driving at the current time and dt. */
+int athg_turb_drive(athg_ctx* ctx);
+/* FFT self-gravity (SELF_GRAVITY_ENABLED == 1, gravity/fft_gravity.cpp): Poisson's equation
+ * with the 7-point Laplacian's eigenvalues, periodic, solved after every stage and in
+ * athg_initialize like the multigrid coupling (replaces it); four_pi_G = 0 detaches. */
+int athg_attach_fft_gravity(athg_ctx* ctx, const athg_mesh* mesh, double four_pi_G);
 /* Sizes of the multi-level work lists (all 0 on a single-level mesh): out[0..7] = ghost-fill
  * elements, same-level restrictions, flux corrections, EMF corrections, coarse cells
  * converted to primitives, prolongated cells, internal-field cells, fine cells rebuilt. */

@@ -3,9 +3,10 @@
 ghost cells), two levels, run by the unmodified reference (tests/golden/make_amr_golden.py)
 and by the C++ host athg_run.
 
-Each fixture holds the block list of every restart dump (one per 0.01 of time), and of the
+Each fixture holds the block list of every restart dump (one per 0.01 of time), of the
 final dump its time, dt and cycle and the interior of every block (all of U and of the face
-fields; or, for `full=False`, per-block sums and sums of squares of each array)."""
+fields; or, for `full=False`, per-block sums and sums of squares of each array), and the
+history sums of the same run every 0.002 of time."""
 import os
 
 import numpy as np
@@ -88,6 +89,23 @@ def athinput(name, host=False):
     if host:
         s += GB300.format(magnetic=int(mhd), rsolver=rsolver, ng=ng)
     return s
+
+
+def athinput_history(name, host=False):
+    """The same run writing history sums every 0.002 (full precision) instead of dumps."""
+    s = athinput(name, host).replace("file_type = rst\ndt = 0.01",
+                                     "file_type = hst\ndt = 0.002\ndata_format = %.16e")
+    assert "file_type = hst" in s
+    return s
+
+
+def history_columns(mhd):
+    """Columns of the reference's history file without self-gravity (outputs/history.cpp):
+    time, dt, mass, 3 momenta, 3 kinetic energies, total energy, then 3 magnetic energies
+    with MHD. The C++ host always writes the gravitational energy after the total energy."""
+    ref = list(range(10)) + ([10, 11, 12] if mhd else [])
+    host = list(range(10)) + ([11, 12, 13] if mhd else [])
+    return ref, host
 
 
 def keys(mhd):

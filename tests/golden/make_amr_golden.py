@@ -54,6 +54,13 @@ def make(name):
     out["final_ncycle"] = np.int64(fin["ncycle"])
     for k, v in amr_golden.summarize(fin, ng, mhd, full, bnx).items():
         out[k] = v
+    # the same run with history sums every 0.002 at full precision
+    with open(os.path.join(wd, "athinput.hst"), "w") as f:
+        f.write(amr_golden.athinput_history(name))
+    r = subprocess.run([exe, "-i", "athinput.hst"], cwd=wd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(r.stdout[-2000:] + r.stderr[-2000:])
+    out["hst"] = np.loadtxt(os.path.join(wd, "Blast.hst"))
     np.savez_compressed(amr_golden.path(name), **out)
     shutil.rmtree(wd)  # the dumps hold every block with ghosts: hundreds of MB
     print(name, "dumps", len(dumps), "final blocks", len(fin["blocks"]),

@@ -1,5 +1,5 @@
-"""ctypes binding to the CPU oracle (oracle/athena_oracle.c) and helpers to run the
-reference solver on a seeded state.
+"""ctypes binding to the CPU oracle (oracle/athena_oracle.c, oracle/mg_oracle.c,
+oracle/fft_oracle.cpp) and helpers to run the reference solver on a seeded state.
 
 Test infrastructure only: used by tests/, __graft_entry__.smoke() and bench.py's
 CPU-baseline leg as the checker, never by the product path.
@@ -13,6 +13,7 @@ import numpy as np
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 ORACLE_DIR = os.path.join(ROOT, "oracle")
 LIB_PATH = os.path.join(ORACLE_DIR, "liboracle.so")
+FFT_LIB_PATH = os.path.join(ORACLE_DIR, "liboracle_fft.so")
 
 SOLVERS = {"hlle": 0, "hllc": 1, "hlld": 2, "lhllc": 3, "lhlld": 4}
 INTEGRATORS = {"vl2": 0, "rk1": 1, "rk2": 2, "rk3": 3}
@@ -39,8 +40,20 @@ class MgParams(C.Structure):
 MG_BC = {"periodic": 0, "zerograd": 1, "zerofixed": 2, "multipole": 3}
 
 
+def build_fft_oracle(force=False):
+    """The C++ restatement of the turbulence driver and FFT gravity (std::random engines)."""
+    src = os.path.join(ORACLE_DIR, "fft_oracle.cpp")
+    if not force and os.path.exists(FFT_LIB_PATH) and \
+            os.path.getmtime(FFT_LIB_PATH) > os.path.getmtime(src):
+        return FFT_LIB_PATH
+    subprocess.run(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-fPIC", "-shared", "-o",
+                    FFT_LIB_PATH, src], check=True)
+    return FFT_LIB_PATH
+
+
 def build_oracle(force=False):
     """Compile the oracle with the flags that keep its FP64 arithmetic reproducible."""
+    build_fft_oracle(force)
     src = os.path.join(ORACLE_DIR, "athena_oracle.c")
     if (not force and os.path.exists(LIB_PATH)
             and os.path.getmtime(LIB_PATH) > max(os.path.getmtime(src), os.path.getmtime(
@@ -423,3 +436,64 @@ def run_reference_state(exe, workdir, nx, mb, mhd, u, b1, b2, b3, cfl, tlim, nli
     if r.returncode != 0 or "FATAL" in r.stdout:
         raise RuntimeError("reference run failed:\n" + r.stdout[-2000:] + r.stderr[-2000:])
     return read_state(os.path.join(workdir, "state_out.bin"), nx, mhd, phi=phi)
+
+
+_fft = None
+
+
+def fft_lib():
+    global _fft
+    if _fft is None:
+        build_fft_oracle()
+        L = C.CDLL(FFT_LIB_PATH)
+        L.orc_turb_create.restype = C.c_void_p
+        L.orc_turb_create.argtypes = [C.c_int, C.c_int, C.c_int, C.POINTER(C.c_double),
+                                      C.POINTER(C.c_int), C.POINTER(C.c_double), C.c_int64,
+                                      C.c_double]
+        L.orc_turb_destroy.argtypes = [C.c_void_p]
+        L.orc_turb_drive.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.c_double, C.c_double]
+        L.orc_fft_gravity.argtypes = [C.c_int, C.c_int, C.c_int, C.POINTER(C.c_double),
+                                      C.c_double, C.POINTER(C.c_double), C.POINTER(C.c_double)]
+        _fft = L
+    return _fft
+
+
+def _d(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+class TurbOracle:
+    """TurbulenceDriver on a mesh-wide interior state u[5][n3][n2][n1] (FP64)."""
+
+    def __init__(self, n, lengths, turb_flag, dedt, rseed, nlow=0, nhigh=None, dtdrive=0.0,
+                 tcorr=0.0, f_shear=-1.0, expo=2.0, time=0.0):
+        self.n = tuple(n)
+        nhigh = n[0] // 2 if nhigh is None else nhigh
+        ln = np.asarray(lengths, dtype=np.float64)
+        ic = (C.c_int * 3)(turb_flag, nlow, nhigh)
+        dc = (C.c_double * 5)(dtdrive, tcorr, f_shear, expo, dedt)
+        self.h = fft_lib().orc_turb_create(n[0], n[1], n[2], _d(ln), ic, dc, rseed, time)
+
+    def drive(self, u, time, dt):
+        """Driving at (time, dt) on a copy of u; returns the perturbed state."""
+        u = np.array(u, dtype=np.float64, order="C", copy=True)
+        fft_lib().orc_turb_drive(self.h, _d(u), time, dt)
+        return u
+
+    def close(self):
+        if self.h:
+            fft_lib().orc_turb_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+
+def fft_gravity(rho, lengths, four_pi_G):
+    """FFTGravityDriver::Solve on a periodic mesh: rho[n3][n2][n1] -> phi (same shape)."""
+    rho = np.ascontiguousarray(rho, dtype=np.float64)
+    n3, n2, n1 = rho.shape
+    ln = np.asarray(lengths, dtype=np.float64)
+    phi = np.zeros_like(rho)
+    fft_lib().orc_fft_gravity(n1, n2, n3, _d(ln), four_pi_G, _d(rho), _d(phi))
+    return phi

@@ -65,22 +65,28 @@ def test_adaptive_blast_matches_reference(name, tmp_path):
                                    err_msg=k)
 
 
-def test_adaptive_blast_conserves(tmp_path):
-    """Regrids keep mass, momentum and total energy of the periodic box: prolongation and
-    restriction of the conserved variables conserve them, and fine fluxes replace coarse
-    ones at level boundaries."""
+@pytest.mark.parametrize("name", list(amr_golden.CASES))
+def test_adaptive_blast_history_matches_reference(name, tmp_path):
+    """History sums every 0.002 of time: mass and momenta are conserved to round-off by
+    regrids and level boundaries alike (the reference drifts by 3e-11 in mass over this run
+    and loses 3e-6 of energy to floors in new blocks, and so does this run)."""
     import __graft_entry__ as g
     exe = g.build_driver()
-    name = "amr_mhd_hlld_plm_vl2"
+    mhd = amr_golden.CASES[name][2]
     inp = os.path.join(str(tmp_path), "athinput")
     with open(inp, "w") as f:
-        f.write(amr_golden.athinput(name, host=True))
-    r = subprocess.run([exe, "-i", inp, "output1/dt=-1", "output2/file_type=hst",
-                        "output2/dt=0.002"], cwd=str(tmp_path), capture_output=True, text=True,
+        f.write(amr_golden.athinput_history(name, host=True))
+    r = subprocess.run([exe, "-i", inp], cwd=str(tmp_path), capture_output=True, text=True,
                        timeout=600)
     assert r.returncode == 0, r.stdout[-3000:] + r.stderr[-3000:]
-    rows = np.loadtxt(os.path.join(str(tmp_path), "Blast.hst"))
-    assert len(rows) > 10
-    for col in (2, 3, 4, 5, 9):  # mass, momenta, total energy
-        ref = rows[0, col]
-        np.testing.assert_allclose(rows[:, col], ref, rtol=0, atol=1e-13 * max(1.0, abs(rows[:, 9]).max()))
+    got = np.loadtxt(os.path.join(str(tmp_path), "Blast.hst"))
+    ref = amr_golden.load(name)["hst"]
+    rc, hc = amr_golden.history_columns(mhd)
+    assert got.shape[0] == ref.shape[0]
+    # sums over ~10^5-10^6 cells in another order, of states that agree to round-off
+    scale = np.abs(ref[:, rc]).max(axis=0)
+    np.testing.assert_allclose(got[:, hc], ref[:, rc], rtol=0,
+                               atol=1e-11 * np.maximum(scale, 1.0).max())
+    # mass and momenta conserved to the reference's own drift
+    for c in (2, 3, 4, 5):
+        assert np.abs(got[:, c] - got[0, c]).max() <= 1e-10 * max(1.0, abs(got[0, 2]))

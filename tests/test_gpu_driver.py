@@ -24,7 +24,7 @@ def test_driver_orszag_tang_history_matches_python(tmp_path):
     exe = g.build_driver()
     inp = os.path.join(PKG, "inputs", "athinput.orszag_tang")
     args = [exe, "-i", inp, "mesh/nx1=32", "mesh/nx2=32", "mesh/nx3=32", "meshblock/nx1=16",
-            "meshblock/nx2=16", "meshblock/nx3=16", "time/nlim=4", "output1/dt=-1",
+            "meshblock/nx2=16", "meshblock/nx3=16", "time/nlim=4", "output1/dcycle=1",
             "gb300/precision=fp64"]
     r = subprocess.run(args, cwd=tmp_path, capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stdout + r.stderr
@@ -50,7 +50,7 @@ def test_driver_blast_runs(tmp_path):
     exe = g.build_driver()
     inp = os.path.join(PKG, "inputs", "athinput.blast")
     args = [exe, "-i", inp, "mesh/nx1=32", "mesh/nx2=32", "mesh/nx3=32", "meshblock/nx1=16",
-            "meshblock/nx2=16", "meshblock/nx3=16", "time/nlim=3"]
+            "meshblock/nx2=16", "meshblock/nx3=16", "time/nlim=3", "output1/dcycle=1"]
     r = subprocess.run(args, cwd=tmp_path, capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stdout + r.stderr
     rows = np.loadtxt(os.path.join(tmp_path, "Blast.hst"))
@@ -148,7 +148,7 @@ def test_driver_refined_blast_restart_is_seamless(tmp_path):
     exe = g.build_driver()
     inp = os.path.join(PKG, "inputs", "athinput.blast_smr")
     small = ["mesh/nx1=32", "mesh/nx2=32", "mesh/nx3=32", "meshblock/nx1=8", "meshblock/nx2=8",
-             "meshblock/nx3=8", "output1/dt=-1", "output2/file_type=rst", "output2/dt=100.0"]
+             "meshblock/nx3=8", "output1/dcycle=1", "output2/file_type=rst", "output2/dt=100.0"]
     runs = {}
     for name, extra in (("full", ["time/nlim=4"]), ("half", ["time/nlim=2"])):
         wd = tmp_path / name
@@ -173,3 +173,21 @@ def test_driver_refined_blast_restart_is_seamless(tmp_path):
     for x, y in zip(a["arrays"], b["arrays"]):
         for k in x:
             np.testing.assert_array_equal(x[k], y[k])
+
+
+def test_driver_driven_turbulence_injects_dedt(tmp_path):
+    """athinput.turb (turb_flag 3, solenoidal forcing): the scheme conserves total energy,
+    so the history's total energy grows by exactly dedt * time, with zero net momentum."""
+    import __graft_entry__ as g
+    exe = g.build_driver()
+    inp = os.path.join(PKG, "inputs", "athinput.turb")
+    args = [exe, "-i", inp, "mesh/nx1=32", "mesh/nx2=32", "mesh/nx3=32", "meshblock/nx1=16",
+            "meshblock/nx2=16", "meshblock/nx3=16", "time/nlim=6", "output1/dt=0.0001"]
+    r = subprocess.run(args, cwd=tmp_path, capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    rows = np.loadtxt(os.path.join(tmp_path, "Turb.hst"))
+    assert len(rows) >= 6
+    e0 = rows[0][9]
+    np.testing.assert_allclose(rows[:, 9] - e0, 0.1 * rows[:, 0], rtol=1e-10, atol=1e-14)
+    assert np.abs(rows[:, 3:6]).max() < 1e-12
+    assert rows[-1][6:9].sum() > 0.0  # kinetic energy in the box
