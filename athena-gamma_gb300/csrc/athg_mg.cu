@@ -193,31 +193,6 @@ __global__ void k_fmg_prolong(const T* __restrict__ uc, T* __restrict__ uf, int 
       }
 }
 
-// periodic wrap of every ghost cell of the listed axes (one launch over the shell)
-template <typename T>
-__global__ void k_bc_wrap(T* a, int n, int px, int py, int pz) {
-  const int nt = n + 2;
-  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= 6LL * nt * nt) return;
-  int face = (int)(t / ((long long)nt * nt));
-  long long r = t % ((long long)nt * nt);
-  int p = (int)(r % nt), q = (int)(r / nt);
-  int i, j, k;
-  int ax = face >> 1, side = face & 1;
-  int g = side ? n + 1 : 0;
-  if (ax == 0) { i = g; j = p; k = q; } else if (ax == 1) { j = g; i = p; k = q; } else { k = g; i = p; j = q; }
-  int ii = i, jj = j, kk = k;
-  if (px) ii = i == 0 ? n : (i == n + 1 ? 1 : i);
-  if (py) jj = j == 0 ? n : (j == n + 1 ? 1 : j);
-  if (pz) kk = k == 0 ? n : (k == n + 1 ? 1 : k);
-  if (ii == i && jj == j && kk == k) return;
-  if (ii < 1 || ii > n || jj < 1 || jj > n || kk < 1 || kk > n) {
-    // still a ghost along a non-periodic axis: that face pass fills it
-    return;
-  }
-  a[ix(nt, k, j, i)] = a[ix(nt, kk, jj, ii)];
-}
-
 struct MpCoef {
   double c[25];
   double o[3];
@@ -256,53 +231,95 @@ __device__ inline double xcen(int i, int n, double lo, double hi) {
   return 0.5 * (xface(i, n, lo, hi) + xface(i + 1, n, lo, hi));
 }
 
-struct FaceBC {
-  int type[2];          // inner, outer
-  int lo1, hi1, lo2, hi2;
-  double lo[3], hi[3];  // domain
-  int homogeneous;      // correction equation: multipole faces become zero-fixed
+// Boundary operation of each face (inner x1, outer x1, ..., outer x3)
+enum FaceOp { OP_PERIODIC = 0, OP_COPY = 1, OP_NEGATE = 2, OP_MULTIPOLE = 3 };
+struct FaceOps {
+  int op[6];
+  const double* tab;  // multipole faces: the expansion at each face's ghost positions
 };
 
-// one axis' two faces (bvals_mg.cpp:339-366 extents); a1 runs over the first
-// transverse axis (j for x1, i for x2 and x3), a2 over the second.
-template <typename T>
-__global__ void k_bc_face(T* a, int n, int dir, FaceBC f, MpCoef mp) {
-  const int n1 = f.hi1 - f.lo1 + 1, n2 = f.hi2 - f.lo2 + 1;
-  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= 2LL * n1 * n2) return;
-  int side = (int)(t / ((long long)n1 * n2));
-  long long r = t % ((long long)n1 * n2);
-  int a1 = f.lo1 + (int)(r % n1), a2 = f.lo2 + (int)(r / n1);
+// The multipole expansion at the face positions of one level, for the six faces:
+// tab[(2 ax + side) (n+2)^2 + a2 (n+2) + a1], (a1, a2) = (j, k) on x1 faces, (i, k) on x2
+// faces and (i, j) on x3 faces (level coordinates of multigrid/multigrid.cpp:1321-1346;
+// face-centre positions of bvals/cc/mg/bvals_mg.cpp:339-366 with
+// multigrid/mgbval_multipole.cpp)
+__global__ void k_mp_tab(double* tab, int n, double lo0, double hi0, double lo1, double hi1,
+                         double lo2, double hi2, MpCoef mp) {
   const int nt = n + 2;
-  int gi = side ? n + 1 : 0, si = side ? n : 1;
-  long long g, s;
-  if (dir == 0) {
-    g = ix(nt, a2, a1, gi); s = ix(nt, a2, a1, si);
-  } else if (dir == 1) {
-    g = ix(nt, a2, gi, a1); s = ix(nt, a2, si, a1);
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= 6LL * nt * nt) return;
+  const int face = (int)(t / ((long long)nt * nt));
+  const long long r = t % ((long long)nt * nt);
+  const int a1 = (int)(r % nt), a2 = (int)(r / nt);
+  const int ax = face >> 1, side = face & 1;
+  double px, py, pz;
+  if (ax == 0) {
+    px = xface(side ? n + 1 : 1, n, lo0, hi0); py = xcen(a1, n, lo1, hi1); pz = xcen(a2, n, lo2, hi2);
+  } else if (ax == 1) {
+    px = xcen(a1, n, lo0, hi0); py = xface(side ? n + 1 : 1, n, lo1, hi1); pz = xcen(a2, n, lo2, hi2);
   } else {
-    g = ix(nt, gi, a2, a1); s = ix(nt, si, a2, a1);
+    px = xcen(a1, n, lo0, hi0); py = xcen(a2, n, lo1, hi1); pz = xface(side ? n + 1 : 1, n, lo2, hi2);
   }
-  const int bc = f.type[side];
-  if (bc == ATHG_MG_ZEROGRAD) {
-    a[g] = a[s];
-  } else if (bc == ATHG_MG_ZEROFIXED || (bc == ATHG_MG_MULTIPOLE && f.homogeneous)) {
-    a[g] = -a[s];
-  } else if (bc == ATHG_MG_MULTIPOLE) {
-    // face-centre position (only here: the coordinates cost FP64 divisions)
-    double px, py, pz;
-    if (dir == 0) {
-      px = xface(side ? n + 1 : 1, n, f.lo[0], f.hi[0]);
-      py = xcen(a1, n, f.lo[1], f.hi[1]); pz = xcen(a2, n, f.lo[2], f.hi[2]);
-    } else if (dir == 1) {
-      px = xcen(a1, n, f.lo[0], f.hi[0]);
-      py = xface(side ? n + 1 : 1, n, f.lo[1], f.hi[1]); pz = xcen(a2, n, f.lo[2], f.hi[2]);
-    } else {
-      px = xcen(a1, n, f.lo[0], f.hi[0]); py = xcen(a2, n, f.lo[1], f.hi[1]);
-      pz = xface(side ? n + 1 : 1, n, f.lo[2], f.hi[2]);
+  tab[t] = mp_phi(mp, px - mp.o[0], py - mp.o[1], pz - mp.o[2]);
+}
+
+// Every ghost cell of one level in one launch. The reference fills periodic ghosts first,
+// then the x1 faces, the x2 faces (over the x1 ghosts too) and the x3 faces (over all
+// ghosts), each pass from the value inside its face (bvals/cc/mg/bvals_mg.cpp:321-368):
+// zero gradient copies it, zero-fixed (and a multipole face in the homogeneous correction
+// equation) negates it, a multipole face takes 2 phi_face - value. Composed per ghost cell:
+// start from the interior cell its coordinates wrap (periodic axes) or mirror to, then apply
+// the faces of its non-periodic ghost axes in x1, x2, x3 order, each with phi at the
+// cell's own coordinates on earlier and periodic axes and the mirrored ones on later axes.
+// Each ghost cell has one thread: the x1 faces take all of their (j, k), the x2 faces the
+// interior i, the x3 faces the interior i and j.
+template <typename T>
+__global__ void k_bc_shell(T* a, int n, FaceOps f) {
+  const int nt = n + 2;
+  const long long nx1 = 2LL * nt * nt, nx2 = 2LL * n * nt, nx3 = 2LL * n * n;
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  int c[3];
+  if (t < nx1) {
+    const int side = (int)(t / ((long long)nt * nt));
+    const long long r = t % ((long long)nt * nt);
+    c[0] = side ? n + 1 : 0; c[1] = (int)(r % nt); c[2] = (int)(r / nt);
+  } else if ((t -= nx1) < nx2) {
+    const int side = (int)(t / ((long long)n * nt));
+    const long long r = t % ((long long)n * nt);
+    c[1] = side ? n + 1 : 0; c[0] = 1 + (int)(r % n); c[2] = (int)(r / n);
+  } else if ((t -= nx2) < nx3) {
+    const int side = (int)(t / ((long long)n * n));
+    const long long r = t % ((long long)n * n);
+    c[2] = side ? n + 1 : 0; c[0] = 1 + (int)(r % n); c[1] = 1 + (int)(r / n);
+  } else {
+    return;
+  }
+  int m[3];
+  bool per[3];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    per[d] = f.op[2 * d] == OP_PERIODIC;
+    const int x = c[d];
+    m[d] = (x == 0) ? (per[d] ? n : 1) : (x == n + 1 ? (per[d] ? 1 : n) : x);
+  }
+  T v = a[ix(nt, m[2], m[1], m[0])];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    if (per[d] || (c[d] != 0 && c[d] != n + 1)) continue;
+    const int side = c[d] == n + 1;
+    const int op = f.op[2 * d + side];
+    if (op == OP_NEGATE) {
+      v = -v;
+    } else if (op == OP_MULTIPOLE) {
+      int q[3];
+#pragma unroll
+      for (int e = 0; e < 3; ++e) q[e] = (e < d || per[e]) ? c[e] : m[e];
+      const int a1 = d == 0 ? q[1] : q[0], a2 = d == 2 ? q[1] : q[2];
+      const double phi = f.tab[(long long)(2 * d + side) * nt * nt + (long long)a2 * nt + a1];
+      v = (T)(2.0 * phi - (double)v);
     }
-    a[g] = (T)(2.0 * mp_phi(mp, px - mp.o[0], py - mp.o[1], pz - mp.o[2]) - (double)a[s]);
   }
+  a[ix(nt, c[2], c[1], c[0])] = v;
 }
 
 // ---- reductions (FP64 accumulation) ----
@@ -454,7 +471,9 @@ struct Hier {
   std::vector<T*> u, src, uold;
   std::vector<int> n;
   std::vector<double> dx;
+  std::vector<double*> mptab;  // multipole faces: the expansion at every level's faces
   size_t cells(int L) const { return (size_t)(n[L] + 2) * (n[L] + 2) * (n[L] + 2); }
+  size_t faces(int L) const { return 6 * (size_t)(n[L] + 2) * (n[L] + 2); }
 };
 
 template <typename T>
@@ -500,7 +519,8 @@ void free_hier(Hier<T>& h) {
   for (auto* p : h.u) if (p) cudaFree(p);
   for (auto* p : h.src) if (p) cudaFree(p);
   for (auto* p : h.uold) if (p) cudaFree(p);
-  h.u.clear(); h.src.clear(); h.uold.clear();
+  for (auto* p : h.mptab) if (p) cudaFree(p);
+  h.u.clear(); h.src.clear(); h.uold.clear(); h.mptab.clear();
 }
 
 }  // namespace
@@ -531,40 +551,50 @@ struct athg_mg {
 
 namespace {
 
+#define RC(x) do { int r_ = (x); if (r_) return r_; } while (0)
+
 template <typename T>
 int apply_bc(athg_mg* m, Hier<T>& h, int L, bool homogeneous) {
   const int n = h.n[L];
-  T* a = h.u[L];
-  const int* bc = m->cfg.bc;
-  int px = bc[0] == ATHG_MG_PERIODIC, py = bc[2] == ATHG_MG_PERIODIC, pz = bc[4] == ATHG_MG_PERIODIC;
-  const int nt = n + 2;
-  if (px || py || pz) {
-    k_bc_wrap<T><<<nblk(6LL * nt * nt), TPB, 0, m->st>>>(a, n, px, py, pz);
-    MCKL();
+  FaceOps f;
+  f.tab = nullptr;
+  for (int q = 0; q < 6; ++q) {
+    const int b = m->cfg.bc[q];
+    if (b == ATHG_MG_PERIODIC) f.op[q] = OP_PERIODIC;
+    else if (b == ATHG_MG_ZEROGRAD) f.op[q] = OP_COPY;
+    else if (b == ATHG_MG_ZEROFIXED || homogeneous) f.op[q] = OP_NEGATE;
+    else f.op[q] = OP_MULTIPOLE;
+    if (f.op[q] == OP_MULTIPOLE) {
+      if ((int)h.mptab.size() <= L || !h.mptab[L])
+        return mgfail(ATHG_ERR_STATE, "multipole boundary without its face table");
+      f.tab = h.mptab[L];
+    }
   }
-  if (m->periodic) return ATHG_OK;
-  FaceBC f;
-  f.lo[0] = m->cfg.x1min; f.hi[0] = m->cfg.x1max;
-  f.lo[1] = m->cfg.x2min; f.hi[1] = m->cfg.x2max;
-  f.lo[2] = m->cfg.x3min; f.hi[2] = m->cfg.x3max;
-  f.homogeneous = homogeneous ? 1 : 0;
-  const int bjs = py ? 0 : 1, bje = py ? n + 1 : n, bks = pz ? 0 : 1, bke = pz ? n + 1 : n;
-  if (!px) {
-    f.type[0] = bc[0]; f.type[1] = bc[1];
-    f.lo1 = bjs; f.hi1 = bje; f.lo2 = bks; f.hi2 = bke;
-    k_bc_face<T><<<nblk(2LL * (bje - bjs + 1) * (bke - bks + 1)), TPB, 0, m->st>>>(a, n, 0, f, m->mp);
-    MCKL();
+  const long long cells = 2LL * (n + 2) * (n + 2) + 2LL * n * (n + 2) + 2LL * n * n;
+  k_bc_shell<T><<<nblk(cells), TPB, 0, m->st>>>(h.u[L], n, f);
+  MCKL();
+  return ATHG_OK;
+}
+
+// zeroed face tables of every level (multipole boundaries)
+template <typename T>
+int alloc_mptab(Hier<T>& h) {
+  h.mptab.assign(h.nl, nullptr);
+  for (int L = 0; L < h.nl; ++L) {
+    MCK(cudaMalloc(&h.mptab[L], h.faces(L) * sizeof(double)));
+    MCK(cudaMemset(h.mptab[L], 0, h.faces(L) * sizeof(double)));
   }
-  if (!py) {
-    f.type[0] = bc[2]; f.type[1] = bc[3];
-    f.lo1 = 0; f.hi1 = n + 1; f.lo2 = bks; f.hi2 = bke;
-    k_bc_face<T><<<nblk(2LL * (n + 2) * (bke - bks + 1)), TPB, 0, m->st>>>(a, n, 1, f, m->mp);
-    MCKL();
-  }
-  if (!pz) {
-    f.type[0] = bc[4]; f.type[1] = bc[5];
-    f.lo1 = 0; f.hi1 = n + 1; f.lo2 = 0; f.hi2 = n + 1;
-    k_bc_face<T><<<nblk(2LL * (n + 2) * (n + 2)), TPB, 0, m->st>>>(a, n, 2, f, m->mp);
+  return ATHG_OK;
+}
+
+// The multipole expansion at every level's face positions (after a new expansion)
+template <typename T>
+int tabulate_multipole(athg_mg* m, Hier<T>& h) {
+  if ((int)h.mptab.size() != h.nl) RC(alloc_mptab(h));
+  const athg_mg_config& c = m->cfg;
+  for (int L = 0; L < h.nl; ++L) {
+    k_mp_tab<<<nblk((long long)h.faces(L)), TPB, 0, m->st>>>(
+        h.mptab[L], h.n[L], c.x1min, c.x1max, c.x2min, c.x2max, c.x3min, c.x3max, m->mp);
     MCKL();
   }
   return ATHG_OK;
@@ -598,7 +628,6 @@ int store_old(athg_mg* m, Hier<T>& h, int L) {
   return ATHG_OK;
 }
 
-#define RC(x) do { int r_ = (x); if (r_) return r_; } while (0)
 
 // coarsest level (multigrid_driver.cpp:778-823, ni = 1 on a cubic power-of-two mesh)
 template <typename T>
@@ -751,6 +780,8 @@ int multipole_setup(athg_mg* m) {
   for (int d = 0; d < 3; ++d) m->mp.o[d] = origin[d];
   m->mp.order = c.mporder;
   ++m->mp_version;
+  RC(tabulate_multipole(m, m->h64));
+  if (m->cfg.precision == ATHG_MIXED) RC(tabulate_multipole(m, m->h32));
   return ATHG_OK;
 }
 
@@ -871,6 +902,9 @@ int athg_mg_create(const athg_mg_config* cfg, athg_mg** out) {
   }
   if (!rc && cudaMalloc(&m->red, 32 * sizeof(double)) != cudaSuccess) rc = ATHG_ERR_CUDA;
   if (!rc && cudaMalloc(&m->mpo_d, 4 * sizeof(double)) != cudaSuccess) rc = ATHG_ERR_CUDA;
+  // multipole faces before the first expansion: phi = 0 on every face
+  if (!rc && m->any_mp) rc = alloc_mptab(m->h64);
+  if (!rc && m->any_mp && cfg->precision == ATHG_MIXED) rc = alloc_mptab(m->h32);
   if (rc) {
     athg_mg_destroy(m);
     return mgfail(ATHG_ERR_CUDA, "multigrid allocation failed");
