@@ -58,14 +58,14 @@ __host__ __device__ inline long long ix(int nt, int k, int j, int i) {
 // ------------------------------------------------------------------------- kernels --
 // Red-black Gauss-Seidel half sweep: cells with (color + k + j + i - 1) even in the
 // reference's local indexing (i = is + c, is + c + 2, ...), one thread per updated cell.
-template <typename T>
-__global__ void k_smooth(T* __restrict__ u, const T* __restrict__ src, int n, T dx2, T isix,
-                         int color) {
+// Each kernel's per-cell work is a device function of the thread's index t, called by the
+// kernel (one thread per index) and by k_vcycle_small (a block-strided loop per step).
+template <typename T, typename I>
+__device__ __forceinline__ void smooth_cell(T* u, const T* src, int n, T dx2, T isix, int color,
+                                            I t) {
   const int nh = (n + 1) / 2;
-  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= (long long)nh * n * n) return;
   int ip = (int)(t % nh);
-  long long r = t / nh;
+  I r = t / nh;
   int j = (int)(r % n) + 1, k = (int)(r / n) + 1;
   int c = (color + k + j) & 1;
   int i = 1 + c + 2 * ip;
@@ -75,16 +75,26 @@ __global__ void k_smooth(T* __restrict__ u, const T* __restrict__ src, int n, T 
   u[q] -= ((T(6.0) * u[q] - u[q + sk] - u[q + sj] - u[q + 1] - u[q - sk] - u[q - sj] - u[q - 1]) +
            src[q] * dx2) * isix;
 }
+__host__ __device__ inline long long smooth_count(int n) {
+  return (long long)((n + 1) / 2) * n * n;
+}
+template <typename T>
+__global__ void k_smooth(T* __restrict__ u, const T* __restrict__ src, int n, T dx2, T isix,
+                         int color) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long cnt = smooth_count(n);
+  if (t >= cnt) return;
+  if (cnt <= 0x7fffffffLL) smooth_cell<T, int>(u, src, n, dx2, isix, color, (int)t);
+  else smooth_cell<T, long long>(u, src, n, dx2, isix, color, t);
+}
 
 // defect of the fine level averaged onto the coarse cell (CalculateDefect + Restrict);
 // with FAS the fine solution is restricted too (RestrictBlock).
-template <typename T>
-__global__ void k_defect_restrict(const T* __restrict__ uf, const T* __restrict__ sf,
-                                  T* __restrict__ sc, T* __restrict__ uc, int nc, T idx2, int fas) {
-  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= (long long)nc * nc * nc) return;
+template <typename T, typename I>
+__device__ __forceinline__ void defect_restrict_cell(const T* uf, const T* sf, T* sc, T* uc, int nc,
+                                                     T idx2, int fas, I t) {
   int i = (int)(t % nc) + 1;
-  long long r = t / nc;
+  I r = t / nc;
   int j = (int)(r % nc) + 1, k = (int)(r / nc) + 1;
   const int nf = 2 * nc, ntf = nf + 2, ntc = nc + 2;
   const long long sk = (long long)ntf * ntf, sj = ntf;
@@ -106,6 +116,15 @@ __global__ void k_defect_restrict(const T* __restrict__ uf, const T* __restrict_
                          U(1, 0, 1) + U(1, 1, 0) + U(1, 1, 1));
   }
 }
+template <typename T>
+__global__ void k_defect_restrict(const T* __restrict__ uf, const T* __restrict__ sf,
+                                  T* __restrict__ sc, T* __restrict__ uc, int nc, T idx2, int fas) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long cnt = (long long)nc * nc * nc;
+  if (t >= cnt) return;
+  if (cnt <= 0x7fffffffLL) defect_restrict_cell<T, int>(uf, sf, sc, uc, nc, idx2, fas, (int)t);
+  else defect_restrict_cell<T, long long>(uf, sf, sc, uc, nc, idx2, fas, t);
+}
 
 // plain 8-cell average (RestrictFMGSource)
 template <typename T>
@@ -123,28 +142,32 @@ __global__ void k_restrict(const T* __restrict__ f, T* __restrict__ c, int nc) {
 }
 
 // src -= L'(u) on the interior (CalculateFASRHS)
-template <typename T>
-__global__ void k_fas_rhs(const T* __restrict__ u, T* __restrict__ src, int n, T idx2) {
-  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= (long long)n * n * n) return;
+template <typename T, typename I>
+__device__ __forceinline__ void fas_rhs_cell(const T* u, T* src, int n, T idx2, I t) {
   int i = (int)(t % n) + 1;
-  long long r = t / n;
+  I r = t / n;
   int j = (int)(r % n) + 1, k = (int)(r / n) + 1;
   const int nt = n + 2;
   const long long q = ix(nt, k, j, i), sk = (long long)nt * nt, sj = nt;
   src[q] -= (T(6.0) * u[q] - u[q + sk] - u[q + sj] - u[q + 1] - u[q - sk] - u[q - sj] - u[q - 1]) *
             idx2;
 }
+template <typename T>
+__global__ void k_fas_rhs(const T* __restrict__ u, T* __restrict__ src, int n, T idx2) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long cnt = (long long)n * n * n;
+  if (t >= cnt) return;
+  if (cnt <= 0x7fffffffLL) fas_rhs_cell<T, int>(u, src, n, idx2, (int)t);
+  else fas_rhs_cell<T, long long>(u, src, n, idx2, t);
+}
 
 // trilinear prolongation of the coarse correction, added to the fine level
 // (ProlongateAndCorrect); with FAS the correction is u_c - u_old_c.
-template <typename T>
-__global__ void k_prolong_correct(const T* __restrict__ uc, const T* __restrict__ uold,
-                                  T* __restrict__ uf, int nc) {
-  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= (long long)nc * nc * nc) return;
+template <typename T, typename I>
+__device__ __forceinline__ void prolong_correct_cell(const T* uc, const T* uold, T* uf, int nc,
+                                                     I t) {
   int i = (int)(t % nc) + 1;
-  long long r = t / nc;
+  I r = t / nc;
   int j = (int)(r % nc) + 1, k = (int)(r / nc) + 1;
   const int ntc = nc + 2, ntf = 2 * nc + 2;
   auto S = [&](int kk, int jj, int ii) -> T {
@@ -162,6 +185,15 @@ __global__ void k_prolong_correct(const T* __restrict__ uc, const T* __restrict_
                            T(9.0) * (S(k, j, i + dx) + S(k, j + dy, i) + S(k + dz, j, i)) +
                            T(3.0) * (S(k + dz, j + dy, i) + S(k + dz, j, i + dx) + S(k, j + dy, i + dx)));
       }
+}
+template <typename T>
+__global__ void k_prolong_correct(const T* __restrict__ uc, const T* __restrict__ uold,
+                                  T* __restrict__ uf, int nc) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long cnt = (long long)nc * nc * nc;
+  if (t >= cnt) return;
+  if (cnt <= 0x7fffffffLL) prolong_correct_cell<T, int>(uc, uold, uf, nc, (int)t);
+  else prolong_correct_cell<T, long long>(uc, uold, uf, nc, t);
 }
 
 // FMG prolongation: separable 1-D weights (5,30,-3)/32 per axis, 27 products summed in
@@ -273,24 +305,27 @@ __global__ void k_mp_tab(double* tab, int n, double lo0, double hi0, double lo1,
 // cell's own coordinates on earlier and periodic axes and the mirrored ones on later axes.
 // Each ghost cell has one thread: the x1 faces take all of their (j, k), the x2 faces the
 // interior i, the x3 faces the interior i and j.
+__host__ __device__ inline long long shell_count(int n) {
+  return 2LL * (n + 2) * (n + 2) + 2LL * n * (n + 2) + 2LL * n * n;
+}
 template <typename T>
-__global__ void k_bc_shell(T* a, int n, FaceOps f) {
+__device__ __forceinline__ void bc_shell_cell(T* a, int n, const FaceOps& f, int t) {
+  // the shell of a level up to n = 4096 has fewer than 2^31 cells
   const int nt = n + 2;
-  const long long nx1 = 2LL * nt * nt, nx2 = 2LL * n * nt, nx3 = 2LL * n * n;
-  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int nx1 = 2 * nt * nt, nx2 = 2 * n * nt, nx3 = 2 * n * n;
   int c[3];
   if (t < nx1) {
-    const int side = (int)(t / ((long long)nt * nt));
-    const long long r = t % ((long long)nt * nt);
-    c[0] = side ? n + 1 : 0; c[1] = (int)(r % nt); c[2] = (int)(r / nt);
+    const int side = t / (nt * nt);
+    const int r = t % (nt * nt);
+    c[0] = side ? n + 1 : 0; c[1] = r % nt; c[2] = r / nt;
   } else if ((t -= nx1) < nx2) {
-    const int side = (int)(t / ((long long)n * nt));
-    const long long r = t % ((long long)n * nt);
-    c[1] = side ? n + 1 : 0; c[0] = 1 + (int)(r % n); c[2] = (int)(r / n);
+    const int side = t / (n * nt);
+    const int r = t % (n * nt);
+    c[1] = side ? n + 1 : 0; c[0] = 1 + r % n; c[2] = r / n;
   } else if ((t -= nx2) < nx3) {
-    const int side = (int)(t / ((long long)n * n));
-    const long long r = t % ((long long)n * n);
-    c[2] = side ? n + 1 : 0; c[0] = 1 + (int)(r % n); c[1] = 1 + (int)(r / n);
+    const int side = t / (n * n);
+    const int r = t % (n * n);
+    c[2] = side ? n + 1 : 0; c[0] = 1 + r % n; c[1] = 1 + r / n;
   } else {
     return;
   }
@@ -320,6 +355,135 @@ __global__ void k_bc_shell(T* a, int n, FaceOps f) {
     }
   }
   a[ix(nt, c[2], c[1], c[0])] = v;
+}
+template <typename T>
+__global__ void k_bc_shell(T* a, int n, FaceOps f) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= shell_count(n)) return;
+  bc_shell_cell<T>(a, n, f, (int)t);
+}
+
+// ---- the coarse levels of a V-cycle in one thread block ----
+// Levels 0..ls (at most kSmallLevels, n <= 16) are latency-bound: their ~60 launches of a
+// few microseconds each become one launch. The block stages the levels' arrays in shared
+// memory and runs, step after step with a barrier between them, exactly the sequence of
+// vcycle() for those levels, down to the coarsest level's two smoothing sweeps
+// (multigrid_driver.cpp:778-823, ni = 1 on a cubic power-of-two mesh), calling the same
+// per-cell functions.
+constexpr int kSmallLevels = 5;
+constexpr int kSmallThreads = 1024;
+template <typename T>
+struct SmallV {
+  T* u[kSmallLevels];
+  T* src[kSmallLevels];
+  T* uold[kSmallLevels];
+  const double* tab[kSmallLevels];
+  T dx2[kSmallLevels], idx2[kSmallLevels];
+  int op[6];
+  int ls, top, fas, subtract, coff;
+  T isix;
+};
+
+template <typename T>
+__global__ void __launch_bounds__(kSmallThreads) k_vcycle_small(SmallV<T> v) {
+  extern __shared__ unsigned char sm_raw[];
+  T* sm = reinterpret_cast<T*>(sm_raw);
+  T *u[kSmallLevels], *s[kSmallLevels], *o[kSmallLevels];
+  long long off = 0;
+  for (int L = 0; L <= v.ls; ++L) {
+    const long long c = (long long)((1 << L) + 2) * ((1 << L) + 2) * ((1 << L) + 2);
+    u[L] = sm + off; off += c;
+    s[L] = sm + off; off += c;
+    o[L] = nullptr;
+    if (v.fas) { o[L] = sm + off; off += c; }
+  }
+  const int tid = threadIdx.x, nth = blockDim.x;
+  auto cells = [](int L) { return (long long)((1 << L) + 2) * ((1 << L) + 2) * ((1 << L) + 2); };
+  for (int L = 0; L <= v.ls; ++L)
+    for (long long q = tid; q < cells(L); q += nth) {
+      u[L][q] = v.u[L][q];
+      s[L][q] = v.src[L][q];
+      if (v.fas) o[L][q] = v.uold[L][q];
+    }
+  __syncthreads();
+  auto bc = [&](int L) {
+    FaceOps f;
+    for (int q = 0; q < 6; ++q) f.op[q] = v.op[q];
+    f.tab = v.tab[L];
+    const int n = 1 << L;
+    for (int t = tid; t < (int)shell_count(n); t += nth) bc_shell_cell<T>(u[L], n, f, t);
+    __syncthreads();
+  };
+  auto smooth = [&](int L, int color) {
+    const int n = 1 << L;
+    for (int t = tid; t < (int)smooth_count(n); t += nth)
+      smooth_cell<T, int>(u[L], s[L], n, v.dx2[L], v.isix, color ^ v.coff, t);
+    __syncthreads();
+  };
+  auto store_old = [&](int L) {
+    for (long long q = tid; q < cells(L); q += nth) o[L][q] = u[L][q];
+    __syncthreads();
+  };
+  auto fas_rhs = [&](int L) {
+    const int n = 1 << L;
+    for (int t = tid; t < n * n * n; t += nth) fas_rhs_cell<T, int>(u[L], s[L], n, v.idx2[L], t);
+    __syncthreads();
+  };
+  auto zero = [&](int L) {
+    for (long long q = tid; q < cells(L); q += nth) u[L][q] = T(0.0);
+    __syncthreads();
+  };
+  // down: vcycle() levels ls..1
+  for (int L = v.ls; L > 0; --L) {
+    bc(L);
+    if (v.fas && L < v.top) { store_old(L); fas_rhs(L); }
+    smooth(L, 0);
+    bc(L);
+    smooth(L, 1);
+    bc(L);
+    const int nc = 1 << (L - 1);
+    for (int t = tid; t < nc * nc * nc; t += nth)
+      defect_restrict_cell<T, int>(u[L], s[L], s[L - 1], u[L - 1], nc, v.idx2[L], v.fas, t);
+    __syncthreads();
+    if (!v.fas) zero(L - 1);
+  }
+  // the coarsest level: with a mean to subtract its solution is zero
+  if (v.subtract) {
+    if (v.fas) { bc(0); store_old(0); }
+    zero(0);
+  } else {
+    bc(0);
+    if (v.fas) { store_old(0); fas_rhs(0); }
+    smooth(0, 0);
+    bc(0);
+    smooth(0, 1);
+    bc(0);
+  }
+  // up: vcycle() levels 0..ls-1
+  for (int L = 0; L < v.ls; ++L) {
+    bc(L);
+    const int nc = 1 << L;
+    for (int t = tid; t < nc * nc * nc; t += nth)
+      prolong_correct_cell<T, int>(u[L], v.fas ? o[L] : nullptr, u[L + 1], nc, t);
+    __syncthreads();
+    bc(L + 1);
+    smooth(L + 1, 0);
+    bc(L + 1);
+    smooth(L + 1, 1);
+  }
+  for (int L = 0; L <= v.ls; ++L)
+    for (long long q = tid; q < cells(L); q += nth) {
+      v.u[L][q] = u[L][q];
+      v.src[L][q] = s[L][q];
+      if (v.fas) v.uold[L][q] = o[L][q];
+    }
+}
+
+template <typename T>
+size_t small_smem(int ls, int fas) {
+  size_t c = 0;
+  for (int L = 0; L <= ls; ++L) c += (size_t)((1 << L) + 2) * ((1 << L) + 2) * ((1 << L) + 2);
+  return c * (fas ? 3 : 2) * sizeof(T);
 }
 
 // ---- reductions (FP64 accumulation) ----
@@ -553,25 +717,31 @@ namespace {
 
 #define RC(x) do { int r_ = (x); if (r_) return r_; } while (0)
 
+// the boundary operation of each face; multipole faces need level L's face table
+template <typename T>
+int face_ops(athg_mg* m, Hier<T>& h, int L, bool homogeneous, FaceOps* f) {
+  f->tab = nullptr;
+  for (int q = 0; q < 6; ++q) {
+    const int b = m->cfg.bc[q];
+    if (b == ATHG_MG_PERIODIC) f->op[q] = OP_PERIODIC;
+    else if (b == ATHG_MG_ZEROGRAD) f->op[q] = OP_COPY;
+    else if (b == ATHG_MG_ZEROFIXED || homogeneous) f->op[q] = OP_NEGATE;
+    else f->op[q] = OP_MULTIPOLE;
+    if (f->op[q] == OP_MULTIPOLE) {
+      if ((int)h.mptab.size() <= L || !h.mptab[L])
+        return mgfail(ATHG_ERR_STATE, "multipole boundary without its face table");
+      f->tab = h.mptab[L];
+    }
+  }
+  return ATHG_OK;
+}
+
 template <typename T>
 int apply_bc(athg_mg* m, Hier<T>& h, int L, bool homogeneous) {
   const int n = h.n[L];
   FaceOps f;
-  f.tab = nullptr;
-  for (int q = 0; q < 6; ++q) {
-    const int b = m->cfg.bc[q];
-    if (b == ATHG_MG_PERIODIC) f.op[q] = OP_PERIODIC;
-    else if (b == ATHG_MG_ZEROGRAD) f.op[q] = OP_COPY;
-    else if (b == ATHG_MG_ZEROFIXED || homogeneous) f.op[q] = OP_NEGATE;
-    else f.op[q] = OP_MULTIPOLE;
-    if (f.op[q] == OP_MULTIPOLE) {
-      if ((int)h.mptab.size() <= L || !h.mptab[L])
-        return mgfail(ATHG_ERR_STATE, "multipole boundary without its face table");
-      f.tab = h.mptab[L];
-    }
-  }
-  const long long cells = 2LL * (n + 2) * (n + 2) + 2LL * n * (n + 2) + 2LL * n * n;
-  k_bc_shell<T><<<nblk(cells), TPB, 0, m->st>>>(h.u[L], n, f);
+  RC(face_ops(m, h, L, homogeneous, &f));
+  k_bc_shell<T><<<nblk(shell_count(n)), TPB, 0, m->st>>>(h.u[L], n, f);
   MCKL();
   return ATHG_OK;
 }
@@ -629,20 +799,27 @@ int store_old(athg_mg* m, Hier<T>& h, int L) {
 }
 
 
-// coarsest level (multigrid_driver.cpp:778-823, ni = 1 on a cubic power-of-two mesh)
+// levels 0..ls of a V-cycle from `top` in one launch (k_vcycle_small)
 template <typename T>
-int coarsest(athg_mg* m, Hier<T>& h, bool fas, bool homog, bool subtract, int coff) {
-  if (subtract) {
-    if (fas) { RC(apply_bc(m, h, 0, homog)); RC(store_old(m, h, 0)); }
-    MCK(cudaMemsetAsync(h.u[0], 0, h.cells(0) * sizeof(T), m->st));
-    return ATHG_OK;
+int small_vcycle(athg_mg* m, Hier<T>& h, int ls, int top, bool fas, bool homog, bool subtract,
+                 int coff) {
+  SmallV<T> v{};
+  FaceOps f;
+  for (int L = 0; L <= ls; ++L) {
+    v.u[L] = h.u[L];
+    v.src[L] = h.src[L];
+    v.uold[L] = fas ? h.uold[L] : nullptr;
+    RC(face_ops(m, h, L, homog, &f));
+    v.tab[L] = f.tab;
+    const double dx = h.dx[L];
+    v.dx2[L] = (T)(dx * dx);
+    v.idx2[L] = (T)(1.0 / (dx * dx));
   }
-  RC(apply_bc(m, h, 0, homog));
-  if (fas) { RC(store_old(m, h, 0)); RC(fas_rhs(m, h, 0)); }
-  RC(smooth(m, h, 0, 0, coff));
-  RC(apply_bc(m, h, 0, homog));
-  RC(smooth(m, h, 0, 1, coff));
-  RC(apply_bc(m, h, 0, homog));
+  for (int q = 0; q < 6; ++q) v.op[q] = f.op[q];
+  v.ls = ls; v.top = top; v.fas = fas ? 1 : 0; v.subtract = subtract ? 1 : 0; v.coff = coff;
+  v.isix = (T)(1.15 / 6.0);
+  k_vcycle_small<T><<<1, kSmallThreads, small_smem<T>(ls, v.fas), m->st>>>(v);
+  MCKL();
   return ATHG_OK;
 }
 
@@ -651,7 +828,10 @@ template <typename T>
 int vcycle(athg_mg* m, Hier<T>& h, int top, bool fas, bool homog, bool subtract, int& coffset) {
   coffset ^= 1;
   const int coff = coffset;
-  for (int L = top; L > 0; --L) {
+  // FP32 levels up to n = 16; FP64 ones up to n = 8, since one SM's FP64 rate (1/64 of
+  // FP32 on this GPU) makes the 16^3 level faster as separate multi-SM launches
+  const int ls = std::min(sizeof(T) == 4 ? kSmallLevels - 1 : kSmallLevels - 2, top);
+  for (int L = top; L > ls; --L) {
     RC(apply_bc(m, h, L, homog));
     if (fas && L < top) { RC(store_old(m, h, L)); RC(fas_rhs(m, h, L)); }
     RC(smooth(m, h, L, 0, coff));
@@ -665,8 +845,8 @@ int vcycle(athg_mg* m, Hier<T>& h, int top, bool fas, bool homog, bool subtract,
     MCKL();
     if (!fas) MCK(cudaMemsetAsync(h.u[L - 1], 0, h.cells(L - 1) * sizeof(T), m->st));
   }
-  RC(coarsest(m, h, fas, homog, subtract, coff));
-  for (int L = 0; L < top; ++L) {
+  RC(small_vcycle(m, h, ls, top, fas, homog, subtract, coff));
+  for (int L = ls; L < top; ++L) {
     RC(apply_bc(m, h, L, homog));
     const int nc = h.n[L];
     k_prolong_correct<T><<<nblk((long long)nc * nc * nc), TPB, 0, m->st>>>(
@@ -902,6 +1082,12 @@ int athg_mg_create(const athg_mg_config* cfg, athg_mg** out) {
   }
   if (!rc && cudaMalloc(&m->red, 32 * sizeof(double)) != cudaSuccess) rc = ATHG_ERR_CUDA;
   if (!rc && cudaMalloc(&m->mpo_d, 4 * sizeof(double)) != cudaSuccess) rc = ATHG_ERR_CUDA;
+  // shared memory of the coarse-level kernel (levels up to n = 16, three arrays each)
+  if (!rc && (cudaFuncSetAttribute(k_vcycle_small<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)small_smem<double>(kSmallLevels - 1, 1)) != cudaSuccess ||
+              cudaFuncSetAttribute(k_vcycle_small<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)small_smem<float>(kSmallLevels - 1, 1)) != cudaSuccess))
+    rc = ATHG_ERR_CUDA;
   // multipole faces before the first expansion: phi = 0 on every face
   if (!rc && m->any_mp) rc = alloc_mptab(m->h64);
   if (!rc && m->any_mp && cfg->precision == ATHG_MIXED) rc = alloc_mptab(m->h32);

@@ -17,7 +17,6 @@ import json
 import os
 import subprocess
 import sys
-import threading
 import time
 
 import numpy as np
@@ -54,29 +53,35 @@ class ClockSampler:
          "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
          "clocks_event_reasons.sw_power_cap")
 
-    def __init__(self, index):
-        self.index, self.rows, self.stop = index, [], threading.Event()
-        self.t = threading.Thread(target=self._run, daemon=True)
-
-    def _run(self):
-        while not self.stop.is_set():
-            try:
-                r = subprocess.run(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
-                                    "--format=csv,noheader,nounits"], capture_output=True,
-                                   text=True, timeout=5)
-                if r.returncode == 0:
-                    self.rows.append([x.strip() for x in r.stdout.strip().split(",")])
-            except Exception:
-                pass
-            self.stop.wait(0.2)
+    def __init__(self, index, interval_ms=50):
+        self.index, self.rows, self.interval_ms, self.proc = index, [], interval_ms, None
 
     def __enter__(self):
-        self.t.start()
+        # one nvidia-smi process sampling every interval_ms until the region ends
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                 "--format=csv,noheader,nounits", "-lms", str(self.interval_ms)],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            time.sleep(0.1)  # the first sample lands before the timed work starts
+        except OSError:
+            self.proc = None
         return self
 
     def __exit__(self, *a):
-        self.stop.set()
-        self.t.join(timeout=10)
+        if self.proc is None:
+            return
+        time.sleep(0.06)
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=10)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+            out, _ = self.proc.communicate()
+        for line in out.splitlines():
+            row = [x.strip() for x in line.split(",")]
+            if len(row) >= 4:
+                self.rows.append(row)
 
     def summary(self):
         if not self.rows:
@@ -443,7 +448,7 @@ def run_e2e(athg, torch, u, b1, b2, b3, steps, zones):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-cycles", type=int, default=2)
