@@ -35,30 +35,33 @@ __host__ __device__ inline int64_t ghost_shell_size(const Geom& g) {
   return gk * (g.nc2 + 1) * (g.nc1 + 1) + (int64_t)g.nx3 * gj * (g.nc1 + 1) +
          (int64_t)g.nx3 * g.nx2 * gi;
 }
-__device__ __forceinline__ void ghost_shell_pos(const Geom& g, int64_t t, int& k, int& j, int& i) {
+// t < ghost_shell_size(g), which fits 32 bits for any block that fits in memory: 32-bit
+// index arithmetic (64-bit division is a long instruction sequence)
+__device__ __forceinline__ void ghost_shell_pos(const Geom& g, int t, int& k, int& j, int& i) {
   const int gk = g.nc3 + 1 - g.nx3, gj = g.nc2 + 1 - g.nx2, gi = g.nc1 + 1 - g.nx1;
-  const int64_t na = (int64_t)gk * (g.nc2 + 1) * (g.nc1 + 1);
-  const int64_t nbb = (int64_t)g.nx3 * gj * (g.nc1 + 1);
+  const int w1 = g.nc1 + 1, w2 = g.nc2 + 1;
+  const int na = gk * w2 * w1;
+  const int nbb = g.nx3 * gj * w1;
   if (t < na) {
-    i = (int)(t % (g.nc1 + 1));
-    const int64_t r = t / (g.nc1 + 1);
-    j = (int)(r % (g.nc2 + 1));
-    const int q = (int)(r / (g.nc2 + 1));
+    i = t % w1;
+    const int r = t / w1;
+    j = r % w2;
+    const int q = r / w2;
     k = q < g.ks ? q : q + g.nx3;  // 0..ks-1, then ke+1..nc3
   } else if (t < na + nbb) {
-    const int64_t u = t - na;
-    i = (int)(u % (g.nc1 + 1));
-    const int64_t r = u / (g.nc1 + 1);
-    const int q = (int)(r % gj);
+    const int u = t - na;
+    i = u % w1;
+    const int r = u / w1;
+    const int q = r % gj;
     j = q < g.js ? q : q + g.nx2;
-    k = g.ks + (int)(r / gj);
+    k = g.ks + r / gj;
   } else {
-    const int64_t u = t - na - nbb;
-    const int q = (int)(u % gi);
+    const int u = t - na - nbb;
+    const int q = u % gi;
     i = q < g.is ? q : q + g.nx1;
-    const int64_t r = u / gi;
-    j = g.js + (int)(r % g.nx2);
-    k = g.ks + (int)(r / g.nx2);
+    const int r = u / gi;
+    j = g.js + r % g.nx2;
+    k = g.ks + r / g.nx2;
   }
 }
 
@@ -68,7 +71,7 @@ __global__ void __launch_bounds__(256) k_ghost_same_level(Geom g, GhostPtrs p) {
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= ghost_shell_size(g)) return;
   int k, j, i;
-  ghost_shell_pos(g, t, k, j, i);
+  ghost_shell_pos(g, (int)t, k, j, i);
   const int b = blockIdx.y;
   const int* nb = p.nbr + (int64_t)b * 27;
   // cell-centred variables
@@ -136,7 +139,7 @@ __global__ void __launch_bounds__(256) k_ghost_f32(Geom g, GhostPtrs32 p) {
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= ghost_shell_size(g)) return;
   int k, j, i;
-  ghost_shell_pos(g, t, k, j, i);
+  ghost_shell_pos(g, (int)t, k, j, i);
   const int b = blockIdx.y;
   const int* nb = p.nbr + (int64_t)b * 27;
   const int64_t nc = g.ncell;

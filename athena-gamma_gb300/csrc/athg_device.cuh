@@ -100,9 +100,35 @@ struct MixedGeo {
   double ia[3];    // dx_d / (dx1 dx2 dx3): face-flux change -> face-field change
 };
 
+// Comparisons. FP64 comparisons (and min/max) issue on the FP64 pipe, which runs at 1/64 of
+// the FP32 rate on this GPU and bounds the FP64 flux sweeps, so for doubles they are made
+// on the integer pipe: dkey maps a double to an int64 that orders like the value for every
+// non-NaN double, with -0 equal to +0, so lt/le/gt/ge give the IEEE results. (With a NaN
+// operand IEEE comparisons are all false; these order the NaN instead.)
+__device__ __forceinline__ long long dkey(double x) {
+  long long b = __double_as_longlong(x);
+  b = ((unsigned long long)b << 1) == 0ull ? 0ll : b;
+  return b < 0 ? (b ^ 0x7fffffffffffffffll) : b;
+}
+template <typename T> __device__ __forceinline__ bool lt(T a, T b) {
+  if constexpr (sizeof(T) == 8) return dkey(a) < dkey(b); else return a < b;
+}
+template <typename T> __device__ __forceinline__ bool le(T a, T b) {
+  if constexpr (sizeof(T) == 8) return dkey(a) <= dkey(b); else return a <= b;
+}
+template <typename T> __device__ __forceinline__ bool gt(T a, T b) { return lt(b, a); }
+template <typename T> __device__ __forceinline__ bool ge(T a, T b) { return le(b, a); }
+// |x| by clearing the sign bit (integer pipe for doubles)
+template <typename T> __device__ __forceinline__ T fab(T x) {
+  if constexpr (sizeof(T) == 8)
+    return __longlong_as_double(__double_as_longlong(x) & 0x7fffffffffffffffll);
+  else
+    return fabsf(x);
+}
+
 // std::min / std::max semantics (first argument wins ties)
-template <typename T> __device__ __forceinline__ T mn(T a, T b) { return (b < a) ? b : a; }
-template <typename T> __device__ __forceinline__ T mx(T a, T b) { return (a < b) ? b : a; }
+template <typename T> __device__ __forceinline__ T mn(T a, T b) { return lt(b, a) ? b : a; }
+template <typename T> __device__ __forceinline__ T mx(T a, T b) { return lt(a, b) ? b : a; }
 template <typename T> __device__ __forceinline__ T sq(T x) { return x * x; }
 
 // eos/adiabatic_mhd.cpp:149-156 (fast magnetosonic speed)
@@ -124,7 +150,7 @@ __device__ __forceinline__ T ct_weight(T dflx, T rhol, T rhor, T dx, T dt) {
   return T(0.5) + mx(T(-0.5), tmp_min);
 }
 
-template <typename T> __device__ __forceinline__ T sgn(T x) { return (x < T(0.0)) ? T(-1.0) : T(1.0); }
+template <typename T> __device__ __forceinline__ T sgn(T x) { return lt(x, T(0.0)) ? T(-1.0) : T(1.0); }
 
 // PPM of one cell on a uniform Cartesian axis: Colella-Woodward interface values with the
 // Colella-Sekora extremum-preserving limiter (reference src/reconstruct/ppm.cpp:44-342,
@@ -150,19 +176,26 @@ __device__ __forceinline__ void ppm_cell(T q_im2, T q_im1, T q, T q_ip1, T q_ip2
     T qa_tmp = dph - q_im1, qb_tmp = q - dph;
     T a = T(3.0) * (q_im1 + q - T(2.0) * dph), b = d2qc_im1, c = d2qc;
     T qd = T(0.0);
-    if (sgn(a) == sgn(b) && sgn(a) == sgn(c))
-      qd = sgn(a) * mn(C2 * fabs(b), mn(C2 * fabs(c), fabs(a)));
+    // sgn(a) * min(...) with sgn in {-1, 1}: a sign flip
+    const bool na = lt(a, T(0.0)), nb = lt(b, T(0.0)), ncc = lt(c, T(0.0));
+    if (na == nb && na == ncc) {
+      const T m = mn(C2 * fab(b), mn(C2 * fab(c), fab(a)));
+      qd = na ? -m : m;
+    }
     T dph_tmp = T(0.5) * (q_im1 + q) - qd / T(6.0);
-    if (qa_tmp * qb_tmp < T(0.0)) dph = dph_tmp;
+    if (lt(qa_tmp * qb_tmp, T(0.0))) dph = dph_tmp;
   }
   {
     T qa_tmp = dph_ip1 - q, qb_tmp = q_ip1 - dph_ip1;
     T a = T(3.0) * (q + q_ip1 - T(2.0) * dph_ip1), b = d2qc, c = d2qc_ip1;
     T qd = T(0.0);
-    if (sgn(a) == sgn(b) && sgn(a) == sgn(c))
-      qd = sgn(a) * mn(C2 * fabs(b), mn(C2 * fabs(c), fabs(a)));
+    const bool na = lt(a, T(0.0)), nb = lt(b, T(0.0)), ncc = lt(c, T(0.0));
+    if (na == nb && na == ncc) {
+      const T m = mn(C2 * fab(b), mn(C2 * fab(c), fab(a)));
+      qd = na ? -m : m;
+    }
     T dphip1_tmp = T(0.5) * (q + q_ip1) - qd / T(6.0);
-    if (qa_tmp * qb_tmp < T(0.0)) dph_ip1 = dphip1_tmp;
+    if (lt(qa_tmp * qb_tmp, T(0.0))) dph_ip1 = dphip1_tmp;
   }
   T d2qf = T(6.0) * (dph + dph_ip1 - T(2.0) * q);
   T qminus = dph, qplus = dph_ip1;
@@ -170,22 +203,27 @@ __device__ __forceinline__ void ppm_cell(T q_im2, T q_im1, T q, T q_ip1, T q_ip2
   T qa_tmp = dqf_minus * dqf_plus;
   T qb_tmp = (q_ip1 - q) * (q - q_im1);
   T a = d2qc_im1, b = d2qc, c = d2qc_ip1, d = d2qf, qe = T(0.0);
-  if (sgn(a) == sgn(b) && sgn(a) == sgn(c) && sgn(a) == sgn(d))
-    qe = sgn(d) * mn(mn(C2 * fabs(a), C2 * fabs(b)), mn(C2 * fabs(c), fabs(d)));
-  a = mx(fabs(q_im1), fabs(q_im2));
-  b = mx(mx(fabs(q), fabs(q_ip1)), fabs(q_ip2));
+  {
+    const bool na = lt(a, T(0.0)), nb = lt(b, T(0.0)), ncc = lt(c, T(0.0)), nd = lt(d, T(0.0));
+    if (na == nb && na == ncc && na == nd) {
+      const T m = mn(mn(C2 * fab(a), C2 * fab(b)), mn(C2 * fab(c), fab(d)));
+      qe = nd ? -m : m;
+    }
+  }
+  a = mx(fab(q_im1), fab(q_im2));
+  b = mx(mx(fab(q), fab(q_ip1)), fab(q_ip2));
   T rho = T(0.0);
-  if (fabs(d) > T(1.0e-12) * mx(a, b)) rho = qe / d;
+  if (gt(fab(d), T(1.0e-12) * mx(a, b))) rho = qe / d;
   T tmp_m = q - rho * dqf_minus, tmp_p = q + rho * dqf_plus;
   T tmp2_m = q - T(2.0) * dqf_plus, tmp2_p = q + T(2.0) * dqf_minus;
-  if ((qa_tmp <= T(0.0) || qb_tmp <= T(0.0))) {
-    if (rho <= (T(1.0) - T(1.0e-12))) {
+  if ((le(qa_tmp, T(0.0)) || le(qb_tmp, T(0.0)))) {
+    if (le(rho, (T(1.0) - T(1.0e-12)))) {
       qminus = tmp_m;
       qplus = tmp_p;
     }
   } else {
-    if (fabs(dqf_minus) >= T(2.0) * fabs(dqf_plus)) qminus = tmp2_m;
-    if (fabs(dqf_plus) >= T(2.0) * fabs(dqf_minus)) qplus = tmp2_p;
+    if (ge(fab(dqf_minus), T(2.0) * fab(dqf_plus))) qminus = tmp2_m;
+    if (ge(fab(dqf_plus), T(2.0) * fab(dqf_minus))) qplus = tmp2_p;
   }
   qm = qminus;
   qp = qplus;

@@ -93,6 +93,27 @@ static void flux_dir(const Geom& g, const StagePtrs<T>& p, bool mhd, int solver,
     }
   } else {
   Box b = make_box(il, iu, jl, ju, kl, ku);
+  if constexpr (ORDER == 3) {
+    // PPM: each cell reconstructed once per sweep (k_flux_x1_ppm), when a block's rows fit
+    // the default 48 KB of shared memory
+    const int nw = mhd ? 7 : 5, cells = b.ni + 1;
+    const int rows = std::max(1, 256 / cells);
+    const size_t smem = 2 * (size_t)rows * nw * cells * sizeof(T);
+    if (smem <= 48 * 1024) {
+      const int tpb = std::min(256, ((rows * cells + 31) / 32) * 32);
+      dim3 grid((unsigned)((b.nj * b.nk + rows - 1) / rows), 1, (unsigned)g.nb);
+      if (mhd) {
+        if (solver == HLLD) k_flux_x1_ppm<T, HLLD, true><<<grid, tpb, smem, st>>>(g, p, b, ph, rows);
+        else if (solver == LHLLD) k_flux_x1_ppm<T, LHLLD, true><<<grid, tpb, smem, st>>>(g, p, b, ph, rows);
+        else k_flux_x1_ppm<T, HLLE, true><<<grid, tpb, smem, st>>>(g, p, b, ph, rows);
+      } else {
+        if (solver == HLLC) k_flux_x1_ppm<T, HLLC, false><<<grid, tpb, smem, st>>>(g, p, b, ph, rows);
+        else if (solver == LHLLC) k_flux_x1_ppm<T, LHLLC, false><<<grid, tpb, smem, st>>>(g, p, b, ph, rows);
+        else k_flux_x1_ppm<T, HLLE, false><<<grid, tpb, smem, st>>>(g, p, b, ph, rows);
+      }
+      return;
+    }
+  }
   const int tpb = tune.x1_tpb;
   dim3 grid = box_grid(b, g.nb, tpb);
   if (mhd) {

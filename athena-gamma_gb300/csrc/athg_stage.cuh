@@ -257,6 +257,66 @@ __device__ __forceinline__ void face_solve(const Geom& g, const StagePtrs<T>& p,
   out[IEN * nf + fi] = fx[IEN];
 }
 
+// x1 PPM sweep in two phases: a thread block takes `rows` whole i-rows of the face box;
+// first one thread per cell reconstructs the cell once (ppm_cell gives the states at both
+// of its faces) into shared memory, then one thread per face takes the left state from
+// the cell below and the right state from the cell above and solves. k_flux instead
+// reconstructs both cells of every face, so each cell twice; the states, and so the
+// fluxes, are the same values bit for bit. Shared memory: 2 * rows * NW * (ni + 1) values.
+// (For PLM, whose slope is cheap, the extra pass through shared memory costs more than
+// the second slope: measured slower in FP32 and no faster in FP64.)
+template <typename T, int SOLVER, bool MHD>
+__global__ void __launch_bounds__(256)
+k_flux_x1_ppm(Geom g, StagePtrs<T> p, Box bx, Phys ph, int rows) {
+  constexpr int NW = MHD ? 7 : 5;
+  const int W = bx.ni;     // faces il .. il + W - 1 of a row
+  const int C = W + 1;     // cells il - 1 .. il + W - 1
+  extern __shared__ unsigned char x1_smem[];
+  T* qm = reinterpret_cast<T*>(x1_smem);  // [rows][NW][C]: state at the cell's lower face
+  T* qp = qm + (int64_t)rows * NW * C;    //                 state at its upper face
+  const int b = blockIdx.z;
+  const int nrows = bx.nj * bx.nk;
+  const int r0 = blockIdx.x * rows;
+  const int64_t nc = g.ncell;
+  const T* __restrict__ w = p.w + (int64_t)b * NHYD * nc;
+  const T* __restrict__ bcc = MHD ? p.bcc + (int64_t)b * 3 * nc : nullptr;
+  for (int t = threadIdx.x; t < rows * C; t += blockDim.x) {
+    const int rr = t / C, cc = t - rr * C;
+    const int row = r0 + rr;
+    if (row >= nrows) continue;
+    const int j = bx.jl + row % bx.nj, k = bx.kl + row / bx.nj;
+    const int64_t c = cidx(g, k, j, bx.il - 1 + cc);
+#pragma unroll
+    for (int n = 0; n < NW; ++n) {
+      const T v0 = wave_var<T, 0>(w, bcc, nc, n, c - 2), v1 = wave_var<T, 0>(w, bcc, nc, n, c - 1),
+              v2 = wave_var<T, 0>(w, bcc, nc, n, c), v3 = wave_var<T, 0>(w, bcc, nc, n, c + 1),
+              v4 = wave_var<T, 0>(w, bcc, nc, n, c + 2);
+      T m, q;
+      ppm_cell<T>(v0, v1, v2, v3, v4, m, q);
+      qm[((int64_t)rr * NW + n) * C + cc] = m;
+      qp[((int64_t)rr * NW + n) * C + cc] = q;
+    }
+  }
+  __syncthreads();
+  const T df = ph_dfloor<T>(ph), pf = ph_pfloor<T>(ph);
+  for (int t = threadIdx.x; t < rows * W; t += blockDim.x) {
+    const int rr = t / W, ff = t - rr * W;
+    const int row = r0 + rr;
+    if (row >= nrows) continue;
+    const int j = bx.jl + row % bx.nj, k = bx.kl + row / bx.nj, i = bx.il + ff;
+    T wl[7], wr[7];
+#pragma unroll
+    for (int n = 0; n < NW; ++n) {
+      wl[n] = qp[((int64_t)rr * NW + n) * C + ff];      // cell i - 1
+      wr[n] = qm[((int64_t)rr * NW + n) * C + ff + 1];  // cell i
+    }
+    // density and pressure floors on the PPM states (ppm.cpp:326-332)
+    wl[IDN] = (wl[IDN] > df) ? wl[IDN] : df; wl[IPR] = (wl[IPR] > pf) ? wl[IPR] : pf;
+    wr[IDN] = (wr[IDN] > df) ? wr[IDN] : df; wr[IPR] = (wr[IPR] > pf) ? wr[IPR] : pf;
+    face_solve<T, 0, SOLVER, MHD>(g, p, ph, b, fidx<0>(g, k, j, i), wl, wr, k, j, i);
+  }
+}
+
 // Marching face-flux kernel for the j (DIR=1) and k (DIR=2) sweeps: one thread per
 // pencil along DIR (consecutive threads on consecutive i, so every load is coalesced),
 // walking faces fs..fe with a register window of three cells. Each cell is loaded once
