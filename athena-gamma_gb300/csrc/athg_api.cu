@@ -254,6 +254,10 @@ struct athg_ctx {
   std::vector<int> amr_deref;
   athg_mesh mesh{};
   unsigned long long* amr_bits = nullptr;
+  // mixed precision on a multi-level mesh: FP64 scratch primitives and cell-centred field
+  // the level-boundary lists prolongate through (the working W and bcc are FP32)
+  double* smr_w64 = nullptr;
+  double* smr_bcc64 = nullptr;
   // athg_cycle_timing: events recorded between launch groups, with their names
   std::vector<std::pair<std::string, cudaEvent_t>>* tev = nullptr;
   bool mixed() const { return cfg.precision == ATHG_MIXED; }
@@ -325,17 +329,29 @@ void free_pool(athg_ctx* c) {
   c->smr = nullptr;
   if (c->amr_bits) cudaFree(c->amr_bits);
   c->amr_bits = nullptr;
+  if (c->smr_w64) cudaFree(c->smr_w64);
+  if (c->smr_bcc64) cudaFree(c->smr_bcc64);
+  c->smr_w64 = c->smr_bcc64 = nullptr;
   c->nb = 0;
 }
 
 // the block pool as the SMR work lists see it
 SmrPool smr_pool_of(athg_ctx* c) {
   SmrPool P = athg::smr_pool(c->smr);
-  P.u = c->u; P.w = (double*)c->w;
-  P.b1 = c->b1; P.b2 = c->b2; P.b3 = c->b3; P.bcc = (double*)c->bcc;
-  for (int d = 0; d < 3; ++d) P.flx[d] = (double*)c->flx[d];
+  P.u = c->u;
+  P.b1 = c->b1; P.b2 = c->b2; P.b3 = c->b3;
   P.nflx = c->cfg.magnetic ? 8 : 5;
-  P.edge = (double*)c->edge;
+  if (c->mixed()) {
+    P.w = c->smr_w64;
+    P.bcc = c->smr_bcc64;
+    for (int d = 0; d < 3; ++d) P.flx32[d] = (float*)c->flx[d];
+    P.edge32 = (float*)c->edge;
+  } else {
+    P.w = (double*)c->w;
+    P.bcc = (double*)c->bcc;
+    for (int d = 0; d < 3; ++d) P.flx[d] = (double*)c->flx[d];
+    P.edge = (double*)c->edge;
+  }
   P.gamma = c->cfg.gamma; P.dfloor = c->cfg.dfloor; P.pfloor = c->cfg.pfloor;
   return P;
 }
@@ -554,7 +570,8 @@ int launch_self_gravity(athg_ctx* c, int l) {
 }
 
 bool fused(const athg_ctx* c) {
-  return c->fused_ok && c->mixed() && c->cfg.integrator == ATHG_VL2 && !has_gravity(c);
+  return c->fused_ok && c->mixed() && c->cfg.integrator == ATHG_VL2 && !has_gravity(c) &&
+         !c->smr;
 }
 
 // swap the two state buffers (after a fused cycle the new state is in (u1, r))
@@ -922,8 +939,6 @@ void leaf_coords(const athg_ctx* c, const athg_mesh* m, const std::vector<SmrLoc
 // Allocates the pool for the leaves `loc` of a periodic mesh and plans its level
 // boundaries; coordinates follow the reference's uniform generator per level
 int set_multilevel(athg_ctx* c, const athg_mesh* m, const std::vector<SmrLoc>& loc) {
-  if (c->mixed())
-    return fail(ATHG_ERR_ARG, "multi-level meshes run on the FP64 path (precision ATHG_FP64)");
   for (int d = 0; d < 3; ++d)
     if (!m->periodic[d]) return fail(ATHG_ERR_ARG, "multi-level meshes: periodic boundaries only");
   const Geom& g = c->g;
@@ -965,6 +980,10 @@ int set_multilevel(athg_ctx* c, const athg_mesh* m, const std::vector<SmrLoc>& l
   rc = athg::smr_create(&c->smr, d, nrb, loc, dxv, xvf, xvc, c->cfg.magnetic != 0, c->st, &err);
   if (rc) return fail(rc == -1 ? ATHG_ERR_ARG : ATHG_ERR_CUDA, err);
   CK(cudaMalloc(&c->amr_bits, sizeof(unsigned long long) * nb));
+  if (c->mixed()) {  // FP64 primitives and bcc of the prolongated ghost cells
+    CK(cudaMalloc(&c->smr_w64, sizeof(double) * NHYD * g.ncell * nb));
+    CK(cudaMalloc(&c->smr_bcc64, sizeof(double) * 3 * g.ncell * nb));
+  }
   if ((int)c->amr_deref.size() != nb) c->amr_deref.assign(nb, 0);
   return ATHG_OK;
 }

@@ -30,7 +30,10 @@ __global__ void k_smr_emf_eval(SmrDims d, SmrPool P, const SmrEmf* __restrict__ 
 __global__ void k_smr_emf_store(SmrDims d, SmrPool P, const SmrEmf* __restrict__ e, int64_t n,
                                 const double* __restrict__ tmp) {
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t < n) P.edge[((int64_t)e[t].blk * 3 + e[t].comp) * d.ne + e[t].idx] = tmp[t];
+  if (t >= n) return;
+  const int64_t q = ((int64_t)e[t].blk * 3 + e[t].comp) * d.ne + e[t].idx;
+  if (P.edge32) P.edge32[q] = (float)tmp[t];
+  else P.edge[q] = tmp[t];
 }
 __global__ void k_smr_c2p(SmrDims d, SmrPool P, const SmrPos* __restrict__ p, int64_t n) {
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;

@@ -175,20 +175,26 @@ ATHG_HD double smr_restrict_cc(const SmrDims& d, const double* f, int64_t c, dou
 }
 
 // RestrictFieldX1/X2/X3, 3-D (mesh_refinement.cpp:184-371)
-ATHG_HD double smr_restrict_f1(const SmrDims& d, const double* f, int64_t q, double a) {
+template <typename F>
+ATHG_HD double smr_restrict_f1(const SmrDims& d, const F* f, int64_t q, double a) {
   const int64_t sj = d.nc1 + 1, sk = (int64_t)(d.nc1 + 1) * d.nc2;
   const double tarea = a + a + a + a;
-  return (f[q] * a + f[q + sj] * a + f[q + sk] * a + f[q + sk + sj] * a) / tarea;
+  return ((double)f[q] * a + (double)f[q + sj] * a + (double)f[q + sk] * a +
+          (double)f[q + sk + sj] * a) / tarea;
 }
-ATHG_HD double smr_restrict_f2(const SmrDims& d, const double* f, int64_t q, double a) {
+template <typename F>
+ATHG_HD double smr_restrict_f2(const SmrDims& d, const F* f, int64_t q, double a) {
   const int64_t sk = (int64_t)d.nc1 * (d.nc2 + 1);
   const double tarea = a + a + a + a;
-  return (f[q] * a + f[q + 1] * a + f[q + sk] * a + f[q + sk + 1] * a) / tarea;
+  return ((double)f[q] * a + (double)f[q + 1] * a + (double)f[q + sk] * a +
+          (double)f[q + sk + 1] * a) / tarea;
 }
-ATHG_HD double smr_restrict_f3(const SmrDims& d, const double* f, int64_t q, double a) {
+template <typename F>
+ATHG_HD double smr_restrict_f3(const SmrDims& d, const F* f, int64_t q, double a) {
   const int64_t sj = d.nc1;
   const double tarea = a + a + a + a;
-  return (f[q] * a + f[q + 1] * a + f[q + sj] * a + f[q + sj + 1] * a) / tarea;
+  return ((double)f[q] * a + (double)f[q + 1] * a + (double)f[q + sj] * a +
+          (double)f[q + sj + 1] * a) / tarea;
 }
 
 // minmod-limited slope 0.5 (SIGN(m) + SIGN(p)) min(|m|, |p|) (mesh_refinement.cpp:428-440)
@@ -404,6 +410,10 @@ struct SmrPool {
   double* flx[3];
   int nflx;
   double* edge;
+  // mixed path: the face fluxes and edge EMFs are FP32 (flx / edge then unused); w and bcc
+  // are FP64 scratch for the prolongated ghost cells
+  float* flx32[3];
+  float* edge32;
   const double *dx, *xvf, *xvc;
   int ncmax, nccmax;
   double gamma, dfloor, pfloor;
@@ -446,33 +456,45 @@ ATHG_HD void smr_exec_xfer(const SmrDims& d, const SmrPool& P, const SmrXfer& x)
 }
 
 // hydro flux components of a coarse face from the area-weighted fine fluxes
-ATHG_HD void smr_exec_flux(const SmrDims& d, const SmrPool& P, const SmrFlux& f) {
+template <typename F>
+ATHG_HD void smr_flux_typed(const SmrDims& d, F* base, int nflx, const double* dx,
+                            const SmrFlux& f) {
   const int64_t nf = f.dir == 0 ? d.nf1 : (f.dir == 1 ? d.nf2 : d.nf3);
-  const double* dxs = P.dx + 3 * f.sblk;
-  double* dst = P.flx[f.dir] + (int64_t)f.dblk * P.nflx * nf;
-  const double* src = P.flx[f.dir] + (int64_t)f.sblk * P.nflx * nf;
+  const double* dxs = dx + 3 * f.sblk;
+  F* dst = base + (int64_t)f.dblk * nflx * nf;
+  const F* src = base + (int64_t)f.sblk * nflx * nf;
   for (int n = 0; n < 5; ++n) {
     double v;
     if (f.dir == 0) v = smr_restrict_f1(d, src + n * nf, f.sidx, dxs[1] * dxs[2]);
     else if (f.dir == 1) v = smr_restrict_f2(d, src + n * nf, f.sidx, dxs[0] * dxs[2]);
     else v = smr_restrict_f3(d, src + n * nf, f.sidx, dxs[0] * dxs[1]);
-    dst[n * nf + f.didx] = v;
+    dst[n * nf + f.didx] = (F)v;
   }
+}
+ATHG_HD void smr_exec_flux(const SmrDims& d, const SmrPool& P, const SmrFlux& f) {
+  if (P.flx32[f.dir]) smr_flux_typed(d, P.flx32[f.dir], P.nflx, P.dx, f);
+  else smr_flux_typed(d, P.flx[f.dir], P.nflx, P.dx, f);
 }
 
 // corrected value of one block-boundary edge (reads the uncorrected EMFs only)
-ATHG_HD double smr_exec_emf(const SmrDims& d, const SmrPool& P, const SmrEmf& e,
-                            const SmrEmfAdd* adds) {
-  double v = e.own ? P.edge[((int64_t)e.blk * 3 + e.comp) * d.ne + e.idx] : 0.0;
+template <typename F>
+ATHG_HD double smr_emf_typed(const SmrDims& d, const F* edge, const SmrEmf& e,
+                             const SmrEmfAdd* adds) {
+  double v = e.own ? (double)edge[((int64_t)e.blk * 3 + e.comp) * d.ne + e.idx] : 0.0;
   for (int a = e.add0; a < e.add1; ++a) {
     const SmrEmfAdd& x = adds[a];
-    const double* s = P.edge + ((int64_t)x.sblk * 3 + x.comp) * d.ne;
-    if (x.step == 0) v += s[x.idx];
-    else v += (s[x.idx] * x.len + s[x.idx + x.step] * x.len) / (x.len + x.len);
+    const F* s = edge + ((int64_t)x.sblk * 3 + x.comp) * d.ne;
+    if (x.step == 0) v += (double)s[x.idx];
+    else v += ((double)s[x.idx] * x.len + (double)s[x.idx + x.step] * x.len) / (x.len + x.len);
   }
   v *= e.mul[0];
   v *= e.mul[1];
   return v;
+}
+// (the mixed path sums and scales the FP32 EMFs in FP64 and rounds once when storing)
+ATHG_HD double smr_exec_emf(const SmrDims& d, const SmrPool& P, const SmrEmf& e,
+                            const SmrEmfAdd* adds) {
+  return P.edge32 ? smr_emf_typed(d, P.edge32, e, adds) : smr_emf_typed(d, P.edge, e, adds);
 }
 
 // coarse bcc and W(U) of one coarse-buffer cell

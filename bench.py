@@ -247,8 +247,8 @@ def run_mg_profile(prec, bc, n):
 C3_REF_CPU_ZCPS = 2.10e5
 
 
-def c3_setup(athg, pgens, root=128, mb=16):
-    sim = athg.Sim((root,) * 3, (mb,) * 3, True, "hlld", precision="fp64", xorder=3,
+def c3_setup(athg, pgens, root=128, mb=16, precision="fp64"):
+    sim = athg.Sim((root,) * 3, (mb,) * 3, True, "hlld", precision=precision, xorder=3,
                    integrator="rk3", gamma=5.0 / 3.0, cfl=0.3, tlim=1e30, ng=4,
                    domain=((-1.0, 1.0),) * 3, regions=[(-0.5, 0.5, -0.5, 0.5, -0.5, 0.5, 1)])
     sim.load_blocks(pgens.blast_blocks(sim.leaves, (root,) * 3, (mb,) * 3))
@@ -276,6 +276,26 @@ def run_c3(athg, torch, steps, warmup):
            "reference_cpu_zone_cycles_per_s_1core": C3_REF_CPU_ZCPS,
            "speedup_vs_reference_1core": zcps / C3_REF_CPU_ZCPS}
     sim.close()
+    # the same workload on the mixed path (FP32 fluxes and EMFs, FP64 state and level
+    # boundaries), and how far it is from the FP64 run after the same cycles
+    sim = c3_setup(athg, pgens, precision="mixed")
+    sim.cycles(warmup)
+    sim.synchronize()
+    el_m = timed_cycles(sim, torch, steps)
+    res["mixed"] = {"ms_per_cycle": 1e3 * el_m / steps, "zone_cycles_per_s": cells * steps / el_m,
+                    "launches_per_cycle": sim.launches_per_cycle(), "div_b_max": sim.max_div_b(),
+                    "mixed_over_fp64": el / el_m}
+    sim.close()
+    n_cmp = 2
+    rho = {}
+    for prec in ("fp64", "mixed"):
+        sim = c3_setup(athg, pgens, precision=prec)
+        sim.cycles(n_cmp)
+        blocks = sim.blocks(ghosts=False)
+        rho[prec] = np.concatenate([blocks[b]["u"][0].ravel() for b in sim.leaves])
+        sim.close()
+    res["mixed"]["l1_rho_vs_fp64_after_%d_cycles" % n_cmp] = float(
+        np.abs(rho["mixed"] - rho["fp64"]).sum() / np.abs(rho["fp64"]).sum())
     return res
 
 

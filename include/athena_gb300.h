@@ -103,7 +103,9 @@ int athg_set_uniform_mesh(athg_ctx* ctx, const athg_mesh* mesh);
  * (mesh/mesh.cpp:334-462, mesh/meshblock_tree.cpp) and the level-boundary work of
  * bvals/bvals_refine.cpp, bvals/cc/flux_correction_cc.cpp and bvals/fc/flux_correction_fc.cpp
  * done on the device (ghost fill through coarse buffers, prolongation, flux and EMF
- * correction). FP64 precision and periodic boundaries only. Blocks are ordered by level,
+ * correction). Periodic boundaries only; FP64 or mixed precision (on the mixed path the
+ * level-boundary flux and EMF corrections are FP32, conservative to FP32 rounding of the
+ * boundary fluxes). Blocks are ordered by level,
  * then lx3, lx2, lx1 (athg_block_location gives each one). */
 int athg_set_refined_mesh(athg_ctx* ctx, const athg_mesh* mesh, int nregions,
                           const athg_region* regions);

@@ -82,7 +82,7 @@ int main(int argc, char** argv) {
     fprintf(stderr, "plan: %s\n", err.c_str());
     return 3;
   }
-  SmrPool P;
+  SmrPool P{};
   P.u = u.data(); P.w = w.data(); P.b1 = b1.data(); P.b2 = b2.data(); P.b3 = b3.data();
   P.bcc = bcc.data();
   P.cu = cu.data(); P.cw = cw.data(); P.cb1 = cb1.data(); P.cb2 = cb2.data(); P.cb3 = cb3.data();

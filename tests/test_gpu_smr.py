@@ -21,10 +21,10 @@ import smr_golden  # noqa: E402
 pytestmark = pytest.mark.gpu
 
 
-def make_sim(meta, tlim=100.0):
+def make_sim(meta, tlim=100.0, precision="fp64"):
     regions = [tuple(r) + (1,) for r in meta["regions"]]
     return athg.Sim(tuple(meta["root"]), tuple(meta["meshblock"]), meta["mhd"], meta["solver"],
-                    precision="fp64", xorder=meta["xorder"], integrator=meta["integrator"],
+                    precision=precision, xorder=meta["xorder"], integrator=meta["integrator"],
                     gamma=meta["gamma"], cfl=meta["cfl"], tlim=tlim, ng=meta["nghost"],
                     domain=tuple(tuple(x) for x in meta["domain"]), regions=regions)
 
@@ -93,10 +93,53 @@ def test_conservation_and_div_b():
     sim.close()
 
 
-def test_mixed_precision_rejected():
-    meta, _, _ = smr_golden.load("smr_hydro_hllc_plm_vl2")
-    regions = [tuple(r) + (1,) for r in meta["regions"]]
+@pytest.mark.parametrize("name", smr_golden.CASES)
+def test_mixed_close_to_reference(name):
+    """Mixed precision on the two-level meshes (FP32 fluxes and EMFs with their level-boundary
+    corrections, FP64 state, ghost fill and prolongation) against the reference after the
+    same cycles. PLM: the uniform mixed path's 1e-5 (mixed and FP64 agree to ~1e-7 here).
+    PPM: 3e-4, because fine blocks hold prolongated, piecewise-linear data whose second
+    differences are zero in FP64 but +-rounding in FP32, and PPM's extremum tests
+    (reconstruct/ppm.cpp:150-230) branch on their signs; the difference appears in the first
+    cycle inside fine blocks, not at level boundaries."""
+    meta, blocks, arrs = smr_golden.load(name)
+    sim = make_sim(meta, precision="mixed")
+    sim.load_blocks(smr_golden.states_in(meta, blocks, arrs))
+    sim.initialize()
+    sim.cycles(meta["ncycles"])
+    _, _, nc = sim.get_time()
+    assert nc == meta["ncycle"]
+    got = sim.blocks(ghosts=False)
+    tol = 3e-4 if meta["xorder"] == 3 else 1e-5
+    for k in (("u", "b1", "b2", "b3") if meta["mhd"] else ("u",)):
+        ref = arrs[k + "_out"]
+        g = np.stack([got[b][k] for b in blocks])
+        err = np.abs(g - ref).max() / np.abs(ref).max()
+        assert err < tol, (k, err)
+    sim.close()
+
+
+def test_mixed_conservation_and_div_b():
+    """Mixed precision: div B stays at round-off (CT in FP64 with the corrected FP32 EMFs);
+    mass and energy change only by the FP32 rounding of the coarse-face fluxes that replace
+    the fine ones at level boundaries (2^-24 of the boundary flux per step)."""
+    meta, blocks, arrs = smr_golden.load("smr_mhd_hlld_plm_vl2")
+    sim = make_sim(meta, precision="mixed")
+    sim.load_blocks(smr_golden.states_in(meta, blocks, arrs))
+    sim.initialize()
+    s0 = sim.sum_conserved()
+    sim.cycles(20)
+    s1 = sim.sum_conserved()
+    assert sim.max_div_b() < 1e-12
+    rel = np.abs(s1 - s0) / np.maximum(1.0, np.abs(s0))
+    assert np.all(rel < 1e-7), rel
+    sim.close()
+
+
+def test_adaptive_mixed_rejected():
+    """Adaptive refinement stays on the FP64 path (the reference's precision)."""
+    meta, blocks, arrs = smr_golden.load("smr_hydro_hllc_plm_vl2")
+    sim = make_sim(meta, precision="mixed")
     with pytest.raises(athg.AthgError):
-        athg.Sim(tuple(meta["root"]), tuple(meta["meshblock"]), False, "hllc",
-                 precision="mixed", regions=regions,
-                 domain=tuple(tuple(x) for x in meta["domain"]))
+        sim.amr_enable(0.1, 1)
+    sim.close()
