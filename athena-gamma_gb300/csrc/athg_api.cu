@@ -481,11 +481,10 @@ __global__ void k_scatter_phi(Geom g, double* __restrict__ phi, const int* __res
 
 bool has_gravity(const athg_ctx* c) { return c->grav || c->fgrav; }
 
-// whether a cycle can be captured as a CUDA graph: no host synchronisation (multigrid
-// iterating to a threshold or with multipole boundaries) and no cuFFT call inside
-bool captured(const athg_ctx* c) {
-  return !(c->grav && !athg::mg_solve_capturable(c->grav)) && !c->fgrav;
-}
+// whether a cycle can be captured as a CUDA graph: no host synchronisation inside (a
+// multigrid iterating to a threshold or with multipole boundaries); the FFT solve's cuFFT
+// executions and kernels are captured with the rest
+bool captured(const athg_ctx* c) { return !(c->grav && !athg::mg_solve_capturable(c->grav)); }
 
 // TurbulenceDriver::Driving at the context's current time and dt
 int turb_drive(athg_ctx* c) {
