@@ -38,6 +38,11 @@ CASES = {
                                [(-0.9, -0.1, 0.05, 0.3, 0.05, 0.9)], "vl2", 2, 4, 8, 0.3, True),
     "smr_mhd_hlld_ppm_rk3": ("smr_mhd_hlld_ng4", True, "hlld", (24, 24, 24), (8, 8, 8), 4,
                              [(0.05, 0.3, 0.05, 0.3, 0.05, 0.3)], "rk3", 3, 3, 9, 0.3, False),
+    # three levels: the central half at level 1 and a small central region at level 2
+    "smr3_mhd_hlld_plm_vl2": ("smr_mhd_hlld", True, "hlld", (16, 16, 16), (4, 4, 4), 2,
+                              [(-0.5, 0.5, -0.5, 0.5, -0.5, 0.5, 1),
+                               (-0.05, 0.05, -0.05, 0.05, -0.05, 0.05, 2)], "vl2", 2, 4, 11,
+                              0.3, False),
 }
 GAMMA = 5.0 / 3.0
 

@@ -1,12 +1,13 @@
-"""Loader of the SMR golden fixtures (tests/golden/smr_*.npz, made by
-tests/golden/make_smr_golden.py from the reference)."""
+"""Loader of the SMR golden fixtures (tests/golden/smr_*.npz and smr3_*.npz (three levels),
+made by tests/golden/make_smr_golden.py from the reference)."""
 import json
 import os
 
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-CASES = ["smr_mhd_hlld_plm_vl2", "smr_hydro_hllc_plm_vl2", "smr_mhd_hlld_ppm_rk3"]
+CASES = ["smr_mhd_hlld_plm_vl2", "smr_hydro_hllc_plm_vl2", "smr_mhd_hlld_ppm_rk3",
+         "smr3_mhd_hlld_plm_vl2"]
 
 
 def load(name):

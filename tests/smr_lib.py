@@ -30,45 +30,66 @@ def gen_x(rx, xmin, xmax):
     return 0.5 * (xmin + xmax) + (rx * xmax - rx * xmin)
 
 
+def region_range(reg, level, nrb, domain):
+    """Logical range [a, b) of a region at `level` along each axis, widened to whole parents
+    (mesh/mesh.cpp:334-462)."""
+    rng = []
+    for d in range(3):
+        lo, hi = reg[2 * d], reg[2 * d + 1]
+        lxmax = nrb[d] << level
+        a = 0
+        while a < lxmax:
+            if gen_x(gen_rx(a + 1, lxmax), *domain[d]) > lo:
+                break
+            a += 1
+        b = a
+        while b < lxmax:
+            if gen_x(gen_rx(b + 1, lxmax), *domain[d]) >= hi:
+                break
+            b += 1
+        if a % 2 == 1:
+            a -= 1
+        if b % 2 == 0:
+            b += 1
+        rng.append((a, b))
+    return rng
+
+
 def smr_blocks(root_nx, mb, domain, regions):
     """Sorted list of (level, lx1, lx2, lx3) leaves. regions: [(x1min, x1max, x2min, x2max,
-    x3min, x3max)] at level 1."""
+    x3min, x3max[, level])], level 1 by default. A level-2 region must lie inside the level-1
+    regions with a block of margin, so that splitting its level-1 parents needs no further
+    refinement for the 2:1 rule (MeshBlockTree::Refine then adds nothing)."""
     nrb = [root_nx[d] // mb[d] for d in range(3)]
-    refined = set()
-    for reg in regions:
-        rng = []
-        for d in range(3):
-            lo, hi = reg[2 * d], reg[2 * d + 1]
-            lxmax = nrb[d] * 2
-            a = 0
-            while a < lxmax:
-                if gen_x(gen_rx(a + 1, lxmax), *domain[d]) > lo:
-                    break
-                a += 1
-            b = a
-            while b < lxmax:
-                if gen_x(gen_rx(b + 1, lxmax), *domain[d]) >= hi:
-                    break
-                b += 1
-            if a % 2 == 1:
-                a -= 1
-            if b % 2 == 0:
-                b += 1
-            rng.append((a, b))
-        for k in range(rng[2][0], rng[2][1], 2):
-            for j in range(rng[1][0], rng[1][1], 2):
-                for i in range(rng[0][0], rng[0][1], 2):
-                    refined.add((i // 2, j // 2, k // 2))
-    out = []
-    for k in range(nrb[2]):
-        for j in range(nrb[1]):
-            for i in range(nrb[0]):
-                if (i, j, k) in refined:
-                    for c in range(8):
-                        out.append((1, 2 * i + (c & 1), 2 * j + ((c >> 1) & 1), 2 * k + (c >> 2)))
-                else:
-                    out.append((0, i, j, k))
-    return sorted(out)
+    leaves = {(0, i, j, k) for k in range(nrb[2]) for j in range(nrb[1]) for i in range(nrb[0])}
+    for level in (1, 2):
+        for reg in regions:
+            if (reg[6] if len(reg) > 6 else 1) != level:
+                continue
+            rng = region_range(reg, level, nrb, domain)
+            for k in range(rng[2][0], rng[2][1], 2):
+                for j in range(rng[1][0], rng[1][1], 2):
+                    for i in range(rng[0][0], rng[0][1], 2):
+                        parent = (level - 1, i // 2, j // 2, k // 2)
+                        if parent not in leaves:
+                            assert any(l[0] >= level and (l[1] >> (l[0] - level + 1), l[2] >> (l[0] - level + 1),
+                                       l[3] >> (l[0] - level + 1)) == parent[1:] for l in leaves), parent
+                            continue
+                        leaves.discard(parent)
+                        for c in range(8):
+                            leaves.add((level, i + (c & 1), j + ((c >> 1) & 1), k + (c >> 2)))
+    if any(l[0] == 2 for l in leaves):  # the 2:1 rule: level-2 blocks touch no level-0 block
+        for a in leaves:
+            if a[0] != 2:
+                continue
+            for b in leaves:
+                if b[0] == 0:
+                    lo_a = [x / 4.0 for x in a[1:]]
+                    hi_a = [(x + 1) / 4.0 for x in a[1:]]
+                    lo_b, hi_b = list(b[1:]), [x + 1 for x in b[1:]]
+                    touch = all(lo_a[d] <= hi_b[d] and lo_b[d] <= hi_a[d] for d in range(3))
+                    assert not touch, ("level-2 region too close to level 0", a, b)
+    return sorted(leaves)
 
 
 def block_faces(blk, root_nx, mb, domain, d, ng=0):
@@ -198,7 +219,7 @@ def athinput(root_nx, mb, domain, regions, cfl, nlim, gamma, xorder, integrator,
         s += ["<refinement%d>" % (r + 1)]
         for d in range(3):
             s += ["x%dmin = %r" % (d + 1, reg[2 * d]), "x%dmax = %r" % (d + 1, reg[2 * d + 1])]
-        s += ["level = 1"]
+        s += ["level = %d" % (reg[6] if len(reg) > 6 else 1)]
     s += ["<problem>", "state_in = state_in.bin", "state_out = state_out.bin",
           "ghosts = %s" % ("true" if ghosts else "false")]
     return "\n".join(s) + "\n"

@@ -22,7 +22,8 @@ pytestmark = pytest.mark.gpu
 
 
 def make_sim(meta, tlim=100.0, precision="fp64"):
-    regions = [tuple(r) + (1,) for r in meta["regions"]]
+    # (x1min, x1max, x2min, x2max, x3min, x3max[, level]), level 1 by default
+    regions = [tuple(r) if len(r) > 6 else tuple(r) + (1,) for r in meta["regions"]]
     return athg.Sim(tuple(meta["root"]), tuple(meta["meshblock"]), meta["mhd"], meta["solver"],
                     precision=precision, xorder=meta["xorder"], integrator=meta["integrator"],
                     gamma=meta["gamma"], cfl=meta["cfl"], tlim=tlim, ng=meta["nghost"],
