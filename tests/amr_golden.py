@@ -1,6 +1,6 @@
 """Adaptive mesh refinement fixtures (test infrastructure): the reference's blast wave with
 <mesh> refinement = adaptive on a 16^3 root mesh of 4^3 MeshBlocks (32^3 of 8^3 with four
-ghost cells), two levels, run by the unmodified reference (tests/golden/make_amr_golden.py)
+ghost cells), two levels (and one case with three), run by the unmodified reference (tests/golden/make_amr_golden.py)
 and by the C++ host athg_run.
 
 Each fixture holds the block list of every restart dump (one per 0.01 of time), of the
@@ -15,11 +15,14 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 GOLDEN = os.path.join(HERE, "golden")
 
 # name -> reference build, nghost, mhd, Riemann solver, integrator, xorder, nlim, full arrays,
-# root cells per axis, block cells per axis
+# root cells per axis, block cells per axis, numlevel
 CASES = {
-    "amr_mhd_hlld_plm_vl2": ("blast_mhd_hlld_ng2", 2, True, "hlld", "vl2", 2, 25, True, 16, 4),
-    "amr_hydro_hllc_plm_vl2": ("blast_hydro_hllc_ng2", 2, False, "hllc", "vl2", 2, 25, True, 16, 4),
-    "amr_mhd_hlld_ppm_rk3": ("blast_mhd_hlld", 4, True, "hlld", "rk3", 3, 20, False, 32, 8),
+    "amr_mhd_hlld_plm_vl2": ("blast_mhd_hlld_ng2", 2, True, "hlld", "vl2", 2, 25, True, 16, 4, 2),
+    "amr_hydro_hllc_plm_vl2": ("blast_hydro_hllc_ng2", 2, False, "hllc", "vl2", 2, 25, True, 16, 4,
+                               2),
+    "amr_mhd_hlld_ppm_rk3": ("blast_mhd_hlld", 4, True, "hlld", "rk3", 3, 20, False, 32, 8, 2),
+    # three levels (848 -> 960 blocks of 4^3 in 12 cycles)
+    "amr3_mhd_hlld_plm_vl2": ("blast_mhd_hlld_ng2", 2, True, "hlld", "vl2", 2, 12, False, 16, 4, 3),
 }
 
 
@@ -56,7 +59,7 @@ x3max = 1.0
 ix3_bc = periodic
 ox3_bc = periodic
 refinement = adaptive
-numlevel = 2
+numlevel = {numlevel}
 derefine_count = 3
 <meshblock>
 nx1 = {nblock}
@@ -83,9 +86,9 @@ precision = fp64
 
 
 def athinput(name, host=False):
-    _, ng, mhd, rsolver, integrator, xorder, nlim, _, nroot, nblock = CASES[name]
+    _, ng, mhd, rsolver, integrator, xorder, nlim, _, nroot, nblock, numlevel = CASES[name]
     s = ATHINPUT.format(nlim=nlim, integrator=integrator, xorder=xorder, nroot=nroot,
-                        nblock=nblock)
+                        nblock=nblock, numlevel=numlevel)
     if host:
         s += GB300.format(magnetic=int(mhd), rsolver=rsolver, ng=ng)
     return s

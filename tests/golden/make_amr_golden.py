@@ -26,7 +26,7 @@ WORK = os.path.join(ROOT, "_work", "golden_amr")
 
 
 def make(name):
-    exe_name, ng, mhd, _, _, _, _, full, _, _ = amr_golden.CASES[name]
+    exe_name, ng, mhd, _, _, _, _, full = amr_golden.CASES[name][:8]
     bnx = amr_golden.block_nx(name)
     exe = build_ref.build(exe_name)
     wd = os.path.join(WORK, name)
