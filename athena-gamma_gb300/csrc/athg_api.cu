@@ -1411,7 +1411,8 @@ int athg_amr_enable(athg_ctx* c, const athg_amr_config* cfg) {
     }
     CK(cudaStreamSynchronize(c->st));
     const athg_mesh m = c->mesh;
-    if ((rc = set_multilevel(c, &m, current_leaves(c)))) return rc;
+    rc = set_multilevel(c, &m, current_leaves(c));
+    if (rc) return rc;
     CK(ul(c->u, u, c->st));
     if (mhd) { CK(ul(c->b1, b1, c->st)); CK(ul(c->b2, b2, c->st)); CK(ul(c->b3, b3, c->st)); }
     CK(cudaStreamSynchronize(c->st));
