@@ -303,11 +303,11 @@ def run_c3(athg, torch, steps, warmup):
     return res
 
 
-def run_c3_profile():
+def run_c3_profile(precision="fp64"):
     import torch
     import athg
     import pgens
-    sim = c3_setup(athg, pgens)
+    sim = c3_setup(athg, pgens, precision=precision)
     sim.cycles(2)
     sim.synchronize()
     torch.cuda.profiler.start()
@@ -490,6 +490,8 @@ def main():
     ap.add_argument("--no-c3", action="store_true",
                     help="skip the MHD blast with static refinement")
     ap.add_argument("--c3-steps", type=int, default=5)
+    ap.add_argument("--c3-precision", default="fp64", choices=["fp64", "mixed"],
+                    help="precision of the --c3-profile run")
     ap.add_argument("--c3-profile", action="store_true",
                     help="profiling run: the refined MHD blast, two cycles, then one cycle "
                          "between cudaProfilerStart/Stop")
@@ -510,7 +512,7 @@ def main():
     if args.c5_profile:
         return run_c5_profile(args.c5_profile)
     if args.c3_profile:
-        return run_c3_profile()
+        return run_c3_profile(args.c3_precision)
 
     import torch
     import athg
