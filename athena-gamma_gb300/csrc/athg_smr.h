@@ -511,12 +511,19 @@ ATHG_HD void smr_exec_c2p(const SmrDims& d, const SmrPool& P, const SmrPos& p) {
           bc, P.gamma, P.dfloor, P.pfloor);
 }
 
+// offsets along axis a (0: x1, 1: x2, 2: x3) at the coarse cell of position p. A shared
+// face's index along its normal runs to the last coarse face, one past the last cell whose
+// neighbours the coordinate rows hold, so face prolongation asks only for its two
+// tangential axes.
+ATHG_HD SmrAxis smr_axis_of(const SmrDims& d, const SmrPool& P, const SmrPos& p, int a) {
+  const double* xf = P.xvf + ((int64_t)p.blk * 3 + a) * P.ncmax;
+  const double* xc = P.xvc + ((int64_t)p.blk * 3 + a) * P.nccmax;
+  if (a == 0) return smr_axis(xc, xf, p.i, (p.i - d.cis) * 2 + d.is);
+  if (a == 1) return smr_axis(xc, xf, p.j, (p.j - d.cjs) * 2 + d.js);
+  return smr_axis(xc, xf, p.k, (p.k - d.cks) * 2 + d.ks);
+}
 ATHG_HD void smr_axes(const SmrDims& d, const SmrPool& P, const SmrPos& p, SmrAxis ax[3]) {
-  const double* xf = P.xvf + (int64_t)p.blk * 3 * P.ncmax;
-  const double* xc = P.xvc + (int64_t)p.blk * 3 * P.nccmax;
-  ax[0] = smr_axis(xc, xf, p.i, (p.i - d.cis) * 2 + d.is);
-  ax[1] = smr_axis(xc + P.nccmax, xf + P.ncmax, p.j, (p.j - d.cjs) * 2 + d.js);
-  ax[2] = smr_axis(xc + 2 * P.nccmax, xf + 2 * P.ncmax, p.k, (p.k - d.cks) * 2 + d.ks);
+  for (int a = 0; a < 3; ++a) ax[a] = smr_axis_of(d, P, p, a);
 }
 
 // prolongated primitives of one coarse cell
@@ -531,17 +538,15 @@ ATHG_HD void smr_exec_pcc(const SmrDims& d, const SmrPool& P, const SmrPos& p) {
 
 // prolongated shared faces of one coarse face of component f
 ATHG_HD void smr_exec_psf(const SmrDims& d, const SmrPool& P, int f, const SmrPos& p) {
-  SmrAxis ax[3];
-  smr_axes(d, P, p, ax);
   if (f == 0)
     smr_prolong_f1(d, P.cb1 + (int64_t)p.blk * d.cf1, P.b1 + (int64_t)p.blk * d.nf1, p.k, p.j,
-                   p.i, ax[1], ax[2]);
+                   p.i, smr_axis_of(d, P, p, 1), smr_axis_of(d, P, p, 2));
   else if (f == 1)
     smr_prolong_f2(d, P.cb2 + (int64_t)p.blk * d.cf2, P.b2 + (int64_t)p.blk * d.nf2, p.k, p.j,
-                   p.i, ax[0], ax[2]);
+                   p.i, smr_axis_of(d, P, p, 0), smr_axis_of(d, P, p, 2));
   else
     smr_prolong_f3(d, P.cb3 + (int64_t)p.blk * d.cf3, P.b3 + (int64_t)p.blk * d.nf3, p.k, p.j,
-                   p.i, ax[0], ax[1]);
+                   p.i, smr_axis_of(d, P, p, 0), smr_axis_of(d, P, p, 1));
 }
 
 ATHG_HD void smr_exec_pint(const SmrDims& d, const SmrPool& P, const SmrPos& p) {
