@@ -61,3 +61,22 @@ def test_adaptive_fill_ng2(tmp_path):
     clean(r)
     assert "120 -> 176 blocks (levels 56 56 64)" in r.stdout
     assert "183 -> 127 blocks (levels 55 72 0)" in r.stdout
+
+
+@pytest.mark.parametrize("mhd,nseq", [(True, 2), (False, 1)])
+def test_adaptive_lists_random_sequences_ng2(tmp_path, mhd, nseq):
+    """Every level-boundary work list (ghost fill, restriction, prolongation of cells and
+    faces, internal field, flux and EMF correction) after every regrid of random adaptive
+    sequences on a 32^3 root of 8^3 blocks with two ghost layers, up to three levels: run
+    on host arrays with the device's allocation sizes under the sanitizers, and every
+    entry's block and element indices checked against one block's extent."""
+    exe = build(str(tmp_path), "amr_lists_check", [
+        os.path.join(HERE, "amr_lists_check.cpp"), os.path.join(CSRC, "athg_amr.cpp"),
+        os.path.join(CSRC, "athg_smr_plan.cpp")])
+    r = subprocess.run([exe, "8", "2", "32", "2", str(nseq), "7", "1" if mhd else "0"],
+                       capture_output=True, text=True, timeout=900)
+    clean(r)
+    last = r.stdout.strip().splitlines()[-1]
+    assert last == "checked %d meshes" % (7 * nseq), r.stdout[-2000:]
+    # the sequences reach the third level and derefine
+    assert "levels 0 4" in r.stdout
