@@ -64,7 +64,16 @@ CONFIGS = {
     "jeans_mg": ("jeans.cpp", "hllc", False, 2, 2, False, None),
     "sg_state_mhd_hlld": ("harness:load_state.cpp", "hlld", True, 2, 2, False, None),
     "sg_state_hydro": ("harness:load_state.cpp", "hllc", False, 2, 2, False, None),
+    # FFT drivers (turbulence driving; FFT self-gravity, SELF_GRAVITY_ENABLED = 1), the
+    # FFTW calls served by the test shim in harness/fftw3 (direct transforms)
+    "turb_state_mhd_hlld": ("harness:load_state.cpp", "hlld", True, 2, 0, False, None),
+    "turb_state_hydro_hllc": ("harness:load_state.cpp", "hllc", False, 2, 0, False, None),
+    "fftgrav_state_hydro_hllc": ("harness:load_state.cpp", "hllc", False, 2, 1, False, None),
+    "fftgrav_state_mhd_hlld": ("harness:load_state.cpp", "hlld", True, 2, 1, False, None),
 }
+FFT_BUILDS = {"turb_state_mhd_hlld", "turb_state_hydro_hllc", "fftgrav_state_hydro_hllc",
+              "fftgrav_state_mhd_hlld"}
+SHIM = os.path.join(HERE, "harness", "fftw3")
 
 
 def source_list(pgen):
@@ -88,7 +97,7 @@ def source_list(pgen):
     return s
 
 
-def write_defs(d, pgen, flux, mhd, nghost, grav, omp):
+def write_defs(d, pgen, flux, mhd, nghost, grav, omp, fft=False):
     with open(os.path.join(REF, "src/defs.hpp.in")) as f:
         t = f.read()
     sub = {
@@ -107,7 +116,7 @@ def write_defs(d, pgen, flux, mhd, nghost, grav, omp):
         "FRAME_TRANSFORMATIONS": "0",
         "SINGLE_PRECISION_ENABLED": "0",
         "H5_DOUBLE_PRECISION_ENABLED": "0",
-        "FFT_OPTION": "NO_FFT",
+        "FFT_OPTION": "FFT" if fft else "NO_FFT",
         "MPI_OPTION": "NOT_MPI_PARALLEL",
         "OPENMP_OPTION": "OPENMP_PARALLEL" if omp else "NOT_OPENMP_PARALLEL",
         "HDF5_OPTION": "NO_HDF5OUTPUT",
@@ -140,8 +149,11 @@ def build(name, jobs=8, verbose=False):
     pgen, flux, mhd, nghost, grav, omp, _ = CONFIGS[name]
     d = os.path.join(OUT, name)
     exe = os.path.join(d, "athena")
-    write_defs(d, pgen, flux, mhd, nghost, grav, omp)
+    fft = name in FFT_BUILDS
+    write_defs(d, pgen, flux, mhd, nghost, grav, omp, fft)
     srcs = source_list(pgen)
+    if fft:
+        srcs.append(os.path.join(SHIM, "fftw3_dft.cpp"))
     eos = os.path.join(REF, "src/eos", "adiabatic_mhd.cpp" if mhd else "adiabatic_hydro.cpp")
     srcs += [eos, os.path.join(REF, "src/eos/general/noop.cpp"),
              os.path.join(REF, "src/eos/eos_high_order.cpp"),
@@ -152,6 +164,7 @@ def build(name, jobs=8, verbose=False):
     flags = ["-O3", "-std=c++11", "-I", inc, "-I", os.path.join(inc, "a"),
              "-I", os.path.join(inc, "a", "b"), "-I", os.path.join(inc, "a", "b", "c")]
     flags += ["-fopenmp"] if omp else []
+    flags += ["-I", SHIM] if fft else []
     if pgen.startswith("harness:"):
         flags += ["-I", os.path.join(REF, "src")]
     objdir = os.path.join(d, "obj")

@@ -14,7 +14,10 @@
 //!   same arrays at the end of the run, and, with self-gravity, phi [NX3][NX2][NX1].
 //!
 //! Hook names/signatures are the reference's (src/pgen/default_pgen.cpp:42-107).
-//! Self-gravity runs take <problem> four_pi_G and use the reference's MG driver.
+//! Self-gravity runs take <problem> four_pi_G and use the reference's MG driver (or its
+//! FFT driver when built with SELF_GRAVITY_ENABLED = 1). <problem> turb_flag (default 0)
+//! turns on the reference's turbulence driver with the <turbulence> block, as its own
+//! turb problem generator does (pgen/turb.cpp).
 
 #include <cstdio>
 #include <stdexcept>
@@ -46,6 +49,7 @@ void Mesh::InitUserMeshData(ParameterInput *pin) {
   if (SELF_GRAVITY_ENABLED) {
     SetFourPiG(pin->GetReal("problem", "four_pi_G"));
   }
+  turb_flag = pin->GetOrAddInteger("problem", "turb_flag", 0);
 }
 
 void MeshBlock::ProblemGenerator(ParameterInput *pin) {

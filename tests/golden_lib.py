@@ -14,7 +14,7 @@ def _all():
 
 def cases():
     """Stage-update fixtures (hydro/MHD, no gravity)."""
-    return [c for c in _all() if not c.startswith(("mg_", "sg_", "smr", "rst_", "amr"))]
+    return [c for c in _all() if not c.startswith(("mg_", "sg_", "smr", "rst_", "amr", "fft_"))]
 
 
 def sg_cases():

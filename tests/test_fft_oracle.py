@@ -99,3 +99,54 @@ def test_seeded_sequence_is_reproducible():
     c = spectrum_of(oracle_lib.TurbOracle((n,) * 3, (1.0,) * 3, 1, 1.0, 43), n)[0]
     np.testing.assert_array_equal(a, b)
     assert np.abs(a - c).max() > 1e-3 * np.abs(a).max()
+
+
+# ---- pinned against the reference's own FFT drivers (fixtures from
+# tests/golden/make_fft_golden.py: the unmodified reference built with a direct-DFT stand-in
+# for FFTW; the oracle's direct DFT sums in another order, hence the 1e-12 tolerances) ----
+import golden_lib  # noqa: E402
+
+
+def _fixture(name):
+    return golden_lib.load(name)
+
+
+@pytest.mark.parametrize("name", ["fft_turb_decay_mhd", "fft_turb_decay_hydro"])
+def test_decaying_drive_matches_reference(name):
+    meta, a = _fixture(name)
+    t = meta["turb"]
+    orc = oracle_lib.TurbOracle(tuple(meta["nx"]), (1.0, 1.0, 1.0), t["turb_flag"], t["dedt"],
+                                t["rseed"], nlow=t["nlow"], nhigh=t["nhigh"],
+                                f_shear=t["f_shear"], expo=t["expo"])
+    got = orc.drive(a["u_in"], 0.0, 0.0)
+    ref = a["u_out"]
+    assert np.abs(ref - a["u_in"]).max() > 1e-3
+    np.testing.assert_allclose(got, ref, rtol=0, atol=1e-12 * np.abs(ref).max())
+
+
+def test_continuous_drive_cycles_match_reference():
+    """Three cycles with a drive before each (main.cpp:457): the oracle's stage and
+    driver in the reference's order."""
+    meta, a = _fixture("fft_turb_cont_hydro")
+    t = meta["turb"]
+    n = tuple(meta["nx"])
+    turb = oracle_lib.TurbOracle(n, (1.0, 1.0, 1.0), t["turb_flag"], t["dedt"], t["rseed"],
+                                 nlow=t["nlow"], nhigh=t["nhigh"], tcorr=t["tcorr"],
+                                 f_shear=t["f_shear"], expo=t["expo"])
+    o = oracle_lib.Oracle(n, False, "hllc", cfl=meta["cfl"])
+    o.load_interior(a["u_in"])
+    o.initialize(100.0)
+    for _ in range(meta["nlim"]):
+        u = o.interior()["u"]
+        o.load_interior(turb.drive(u, o.time, o.dt))
+        o.cycle(1, 100.0)
+    got = o.interior()["u"]
+    assert o.time == pytest.approx(meta["time"], rel=1e-13)
+    np.testing.assert_allclose(got, a["u_out"], rtol=0, atol=1e-11 * np.abs(a["u_out"]).max())
+
+
+def test_fft_gravity_potential_matches_reference():
+    meta, a = _fixture("fft_grav_hydro_init")
+    phi = oracle_lib.fft_gravity(a["u_in"][0], (1.0, 1.0, 1.0), meta["four_pi_G"])
+    ref = a["phi"]
+    np.testing.assert_allclose(phi, ref, rtol=0, atol=1e-12 * np.abs(ref).max())
