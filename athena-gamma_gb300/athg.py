@@ -16,7 +16,7 @@ LIB_PATH = os.path.join(HERE, "libathena_gb300.so")
 HLLE, HLLC, HLLD, LHLLC, LHLLD = 0, 1, 2, 3, 4
 SOLVERS = {"hlle": HLLE, "hllc": HLLC, "hlld": HLLD, "lhllc": LHLLC, "lhlld": LHLLD}
 INTEGRATORS = {"vl2": 0, "rk1": 1, "rk2": 2, "rk3": 3}
-PRECISIONS = {"fp64": 0, "mixed": 1}
+PRECISIONS = {"fp64": 0, "mixed": 1, "dfloat": 2}
 VAR_CONS, VAR_B1F, VAR_B2F, VAR_B3F, VAR_PRIM, VAR_BCC, VAR_PHI = range(7)
 # default density/pressure floors of the reference EOS: sqrt(1024*FLT_MIN)
 FLOOR = float(np.sqrt(1024 * np.finfo(np.float32).tiny))
@@ -39,6 +39,7 @@ EXPORTS = [
     "athg_block_cfl_dt_noalloc", "athg_set_refined_mesh", "athg_set_multilevel_blocks",
     "athg_smr_stats", "athg_resume", "athg_cycle_timing", "athg_amr_enable",
     "athg_amr_regrid", "athg_turb_attach", "athg_turb_drive", "athg_attach_fft_gravity",
+    "athg_set_stage_kernel", "athg_get_stage_kernel",
 ]
 MG_BC = {"periodic": 0, "zerograd": 1, "zerofixed": 2, "multipole": 3}
 
@@ -152,6 +153,8 @@ def lib():
         "athg_turb_attach": [vp, C.POINTER(Mesh), C.POINTER(TurbConfig)],
         "athg_turb_drive": [vp],
         "athg_attach_fft_gravity": [vp, C.POINTER(Mesh), d],
+        "athg_set_stage_kernel": [vp, i, i],
+        "athg_get_stage_kernel": [vp, C.POINTER(i), C.POINTER(i)],
     }
     for name, args in sig.items():
         f = getattr(L, name)
@@ -449,6 +452,17 @@ class Sim:
     def set_tuning(self, x1_tpb, march_tpb, seg):
         a = (C.c_int * 3)(x1_tpb, march_tpb, seg)
         check(lib().athg_set_tuning(self.h, a))
+
+    def set_stage_kernel(self, single, nseg=0):
+        """Mixed VL2 MHD stage as one launch (single=True) or as separate sweeps; nseg
+        k-segments per thread block of the single pass (0: autotuned)."""
+        check(lib().athg_set_stage_kernel(self.h, int(bool(single)), int(nseg)))
+
+    def stage_kernel(self):
+        """(whether the next cycle runs the single-pass stage, its k-segments)."""
+        a, b = C.c_int(), C.c_int()
+        check(lib().athg_get_stage_kernel(self.h, C.byref(a), C.byref(b)))
+        return bool(a.value), b.value
 
     def history(self):
         """The 12 history sums of outputs/history.cpp, reduced on the device."""

@@ -15,6 +15,8 @@
 #include "athg_bvals.cuh"
 #include "athg_launch.cuh"
 #include "athg_amr.h"
+#include "athg_single_pass.h"
+#include "athg_df.h"
 #include "athg_fft.h"
 #include "athg_internal.h"
 
@@ -48,7 +50,7 @@ constexpr double kDblMax = 1.79769313486231570815e308;
 // (reference src/mesh/mesh.cpp:1078-1118). The block minimum is read and reset.
 __global__ void k_end_cycle(double* time, double* dt, long long* ncycle,
                             unsigned long long* dtmin, double cfl, double tlim, int advance,
-                            float* dtf) {
+                            float* dtf, unsigned int* err) {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
   double t = *time, d = *dt;
   if (advance) {
@@ -59,6 +61,8 @@ __global__ void k_end_cycle(double* time, double* dt, long long* ncycle,
   d = 2.0 * d;
   d = (bdt < d) ? bdt : d;
   if (t < tlim && (tlim - t) < d) d = tlim - t;
+  // device error word, bit 1: a time step that is not a positive finite number
+  if (!(d > 0.0 && d <= 1.79769313486231570815e308)) atomicOr(err, kErrTimeStep);
   *time = t;
   *dt = d;
   if (dtf) *dtf = (float)d;  // the flux kernels of the mixed path read dt in FP32
@@ -211,6 +215,8 @@ struct athg_ctx {
   double *r1 = nullptr, *r2 = nullptr, *r3 = nullptr;
   void *w = nullptr, *bcc = nullptr, *flx[3] = {nullptr, nullptr, nullptr}, *edge = nullptr;
   float* cce = nullptr;  // mixed MHD: cell-centred EMF written by the primitive recovery
+  float2* cce_df = nullptr;  // double-float MHD: cell-centred EMF as pairs [nb][3][cells]
+  float2* wpair_df = nullptr;  // double-float: W and bcc as pairs [nb][5 or 8][cells]
   BlockGeo* geo = nullptr;
   void* coef = nullptr;        // PLM coefficients in the flux precision
   void* dxT = nullptr;         // cell widths in the flux precision
@@ -258,9 +264,22 @@ struct athg_ctx {
   // the level-boundary lists prolongate through (the working W and bcc are FP32)
   double* smr_w64 = nullptr;
   double* smr_bcc64 = nullptr;
+  // single-pass mixed VL2 MHD stage (athg_single_pass.cu): a second set of FP32 working
+  // arrays (stage 1 reads the first and writes the second, stage 2 the reverse), the TMA
+  // descriptors of both sets' W and bcc, and the k-segments per thread block (autotuned)
+  float *w2 = nullptr, *bcc2 = nullptr, *bf32b[3] = {nullptr, nullptr, nullptr};
+  athg::SinglePassMaps* spm = nullptr;  // [2]: set 1, set 2
+  bool sp_ready = false;
+  bool sp_on = false;     // athg_set_stage_kernel(ctx, 1, ...): one launch per stage
+  bool sp_tuned = false;  // k-segments autotuned (or set by the caller)
+  int sp_nseg = 1;
+  // outflow physical boundaries on the non-periodic axes of a uniform mesh (FP64 arrays)
+  bool outflow = false;
   // athg_cycle_timing: events recorded between launch groups, with their names
   std::vector<std::pair<std::string, cudaEvent_t>>* tev = nullptr;
   bool mixed() const { return cfg.precision == ATHG_MIXED; }
+  // FP64 arrays and FP64 update, reconstruction + Riemann fluxes + corner EMFs in double-float
+  bool dfloat() const { return cfg.precision == ATHG_DFLOAT; }
 };
 
 namespace {
@@ -289,6 +308,23 @@ StagePtrs<T> ptrs(athg_ctx* c) {
     for (int d = 0; d < 3; ++d) p.bfw[d] = nullptr;
   }
   return p;
+}
+
+// the device error word (bits kErr*), in the pool's scalar block
+unsigned int* err_word(const athg_ctx* c) { return reinterpret_cast<unsigned int*>(c->scal + 12); }
+
+// reads and clears the device error word (after the stream was synchronised)
+int device_errors(athg_ctx* c) {
+  unsigned int w = 0;
+  CK(cudaMemcpyAsync(&w, err_word(c), sizeof(w), cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  if (!w) return ATHG_OK;
+  CK(cudaMemsetAsync(err_word(c), 0, sizeof(w), c->st));
+  std::string m = "device error word:";
+  if (w & athg::kErrTmaTimeout) m += " a TMA load of the single-pass stage timed out;";
+  if (w & athg::kErrTimeStep) m += " the new time step is not a positive finite number;";
+  if (w & athg::kErrNonFinite) m += " a non-finite density or pressure was produced;";
+  return fail(ATHG_ERR_DEVICE, m);
 }
 
 Phys phys(const athg_ctx* c) {
@@ -332,6 +368,17 @@ void free_pool(athg_ctx* c) {
   if (c->smr_w64) cudaFree(c->smr_w64);
   if (c->smr_bcc64) cudaFree(c->smr_bcc64);
   c->smr_w64 = c->smr_bcc64 = nullptr;
+  void* sp[] = {c->w2, c->bcc2, c->bf32b[0], c->bf32b[1], c->bf32b[2], c->cce_df,
+                c->wpair_df};
+  c->cce_df = nullptr;
+  c->wpair_df = nullptr;
+  for (void* q : sp)
+    if (q) cudaFree(q);
+  c->w2 = c->bcc2 = nullptr;
+  c->bf32b[0] = c->bf32b[1] = c->bf32b[2] = nullptr;
+  delete[] c->spm;
+  c->spm = nullptr;
+  c->sp_ready = false;
   c->nb = 0;
 }
 
@@ -376,6 +423,9 @@ int launch_fluxes(athg_ctx* c, int order) {
   if (c->mixed())
     Launcher<float>::fluxes(c->g, ptrs<float>(c), mhd, c->cfg.rsolver, order, phys(c), c->tune,
                             c->st);
+  else if (c->dfloat())
+    athg::df_fluxes(c->g, ptrs<double>(c), mhd, c->cfg.rsolver, order, phys(c), c->wpair_df,
+                    c->st);
   else
     Launcher<double>::fluxes(c->g, ptrs<double>(c), mhd, c->cfg.rsolver, order, phys(c),
                              c->tune, c->st);
@@ -389,6 +439,7 @@ int launch_fluxes(athg_ctx* c, int order) {
 int launch_corner(athg_ctx* c) {
   if (!c->cfg.magnetic) return ATHG_OK;
   if (c->mixed()) Launcher<float>::corner_emf(c->g, ptrs<float>(c), c->st);
+  else if (c->dfloat()) athg::df_corner_emf(c->g, ptrs<double>(c), c->cce_df, c->st);
   else Launcher<double>::corner_emf(c->g, ptrs<double>(c), c->st);
   c->counting += 1;
   // EMF correction at block boundaries (time_integrator.cpp: SEND_FLDFLX, RECV_FLDFLX)
@@ -427,6 +478,14 @@ int launch_c2p(athg_ctx* c) {
   if (c->mixed()) Launcher<float>::c2p(c->g, ptrs<float>(c), mhd, phys(c), c->st);
   else Launcher<double>::c2p(c->g, ptrs<double>(c), mhd, phys(c), c->st);
   c->counting += 1;
+  if (c->outflow) {  // ApplyPhysicalBoundaries after the primitives (FP64 arrays)
+    OutflowPtrs op{c->u, (double*)c->w, c->b1, c->b2, c->b3, (double*)c->bcc, c->nbr,
+                   mhd ? 1 : 0, 1.0 / (c->cfg.gamma - 1.0)};
+    const dim3 grid((unsigned)((ghost_shell_size(c->g) + 255) / 256), (unsigned)c->nb);
+    k_outflow_copy<<<grid, 256, 0, c->st>>>(c->g, op);
+    k_outflow_cons<<<grid, 256, 0, c->st>>>(c->g, op);
+    c->counting += 2;
+  }
   CKL();
   return ATHG_OK;
 }
@@ -444,7 +503,7 @@ int launch_block_dt(athg_ctx* c) {
 int launch_end(athg_ctx* c, int advance) {
   k_end_cycle<<<1, 32, 0, c->st>>>(c->scal, c->scal + 1, (long long*)(c->scal + 2),
                                    (unsigned long long*)(c->scal + 3), c->cfg.cfl_number,
-                                   c->cfg.tlim, advance, c->dtf);
+                                   c->cfg.tlim, advance, c->dtf, err_word(c));
   c->counting += 1;
   CKL();
   return ATHG_OK;
@@ -573,6 +632,92 @@ bool fused(const athg_ctx* c) {
          !c->smr;
 }
 
+// The single-pass stage kernel (opt-in: athg_set_stage_kernel) covers the fused path for
+// MHD with PLM (donor cell in the first VL2 stage), HLLD or HLLE, on meshes whose blocks it
+// tiles
+bool single_pass(const athg_ctx* c) {
+  return fused(c) && c->cfg.magnetic && c->cfg.xorder == 2 &&
+         (c->cfg.rsolver == ATHG_HLLD || c->cfg.rsolver == ATHG_HLLE) && c->sp_on &&
+         athg::single_pass_fits(c->g, 1);
+}
+
+// the second set of FP32 working arrays and the TMA descriptors of both sets (allocates:
+// called outside stream capture)
+int sp_prepare(athg_ctx* c) {
+  if (c->sp_ready) return ATHG_OK;
+  const Geom& g = c->g;
+  if (int e = athg::single_pass_setup())
+    return fail(ATHG_ERR_CUDA, std::string("single-pass kernel attributes: ") +
+                                   cudaGetErrorString((cudaError_t)e));
+  const size_t nb = (size_t)c->nb;
+  CK(cudaMalloc(&c->w2, sizeof(float) * NHYD * g.ncell * nb));
+  CK(cudaMalloc(&c->bcc2, sizeof(float) * 3 * g.ncell * nb));
+  const int64_t nf[3] = {g.nf1, g.nf2, g.nf3};
+  for (int d = 0; d < 3; ++d) CK(cudaMalloc(&c->bf32b[d], sizeof(float) * nf[d] * nb));
+  // the second set starts as a copy (its ghost zones are rewritten after every stage)
+  CK(cudaMemcpyAsync(c->w2, c->w, sizeof(float) * NHYD * g.ncell * nb, cudaMemcpyDeviceToDevice, c->st));
+  CK(cudaMemcpyAsync(c->bcc2, c->bcc, sizeof(float) * 3 * g.ncell * nb, cudaMemcpyDeviceToDevice, c->st));
+  for (int d = 0; d < 3; ++d)
+    CK(cudaMemcpyAsync(c->bf32b[d], c->bf32[d], sizeof(float) * nf[d] * nb,
+                       cudaMemcpyDeviceToDevice, c->st));
+  c->spm = new athg::SinglePassMaps[2];
+  std::string err;
+  if (athg::single_pass_maps((const float*)c->w, (const float*)c->bcc, g, &c->spm[0], &err) ||
+      athg::single_pass_maps(c->w2, c->bcc2, g, &c->spm[1], &err))
+    return fail(ATHG_ERR_CUDA, err);
+  c->sp_ready = true;
+  return ATHG_OK;
+}
+
+// one stage of the single-pass kernel: stage 1 reads FP32 set 1 and writes set 2, stage 2
+// the reverse, so after a whole VL2 cycle the current W is in set 1 again; then the ghost
+// exchange of the set just written. order_override > 0 replaces the stage's reconstruction
+// order (the autotuner times the second stage's PLM kernel in the first stage's direction,
+// which writes only scratch: the other state buffer and FP32 set 2).
+int launch_single_pass(athg_ctx* c, int l, bool dt_too, int order_override = 0) {
+  const bool first = (l == 0);
+  const int order = order_override > 0 ? order_override : (first ? 1 : c->cfg.xorder);
+  StagePtrs<float> p = ptrs<float>(c);
+  float* set1w = (float*)c->w;
+  float* set1b = (float*)c->bcc;
+  float* const set1f[3] = {c->bf32[0], c->bf32[1], c->bf32[2]};
+  float* const set2f[3] = {c->bf32b[0], c->bf32b[1], c->bf32b[2]};
+  if (!first) {
+    p.w = c->w2; p.bcc = c->bcc2;
+    for (int d = 0; d < 3; ++d) p.bf[d] = c->bf32b[d];
+  }
+  StateBufs sb;
+  sb.u_in = c->u; sb.u_out = c->u1;
+  sb.b_in[0] = c->b1; sb.b_in[1] = c->b2; sb.b_in[2] = c->b3;
+  sb.b_out[0] = c->r1; sb.b_out[1] = c->r2; sb.b_out[2] = c->r3;
+  const int e = athg::single_pass_launch(
+      c->spm[first ? 0 : 1], c->g, p, first ? c->w2 : set1w, first ? c->bcc2 : set1b,
+      first ? set2f : set1f, sb, stage_weights(c, l), phys(c),
+      dt_too ? (unsigned long long*)(c->scal + 3) : nullptr, err_word(c), order,
+      c->cfg.rsolver == ATHG_HLLD ? HLLD : HLLE, c->sp_nseg, c->st);
+  if (e) return fail(ATHG_ERR_CUDA, std::string("single-pass stage: ") +
+                                        cudaGetErrorString((cudaError_t)e));
+  c->counting += 1;
+  return ATHG_OK;
+}
+
+int launch_ghosts_set(athg_ctx* c, float* w, float* bcc, float* const bf[3], float* cce) {
+  const Geom& g = c->g;
+  GhostPtrs32 gp;
+  const bool mhd = c->cfg.magnetic != 0;
+  gp.cell[0] = w; gp.ncomp[0] = NHYD;
+  gp.cell[1] = mhd ? bcc : nullptr; gp.ncomp[1] = 3;
+  gp.cell[2] = mhd ? cce : nullptr; gp.ncomp[2] = 3;
+  for (int d = 0; d < 3; ++d) gp.face[d] = mhd ? bf[d] : nullptr;
+  gp.nbr = c->nbr;
+  dim3 grid((unsigned)((ghost_shell_size(g) + 255) / 256), (unsigned)c->nb);
+  if (mhd) k_ghost_f32<true><<<grid, 256, 0, c->st>>>(g, gp);
+  else k_ghost_f32<false><<<grid, 256, 0, c->st>>>(g, gp);
+  c->counting += 1;
+  CKL();
+  return ATHG_OK;
+}
+
 // swap the two state buffers (after a fused cycle the new state is in (u1, r))
 void swap_state(athg_ctx* c) {
   std::swap(c->u, c->u1);
@@ -596,20 +741,8 @@ int launch_update_c2p(athg_ctx* c, int l, bool dt_too) {
 }
 
 int launch_ghosts_f32(athg_ctx* c) {
-  const Geom& g = c->g;
-  GhostPtrs32 gp;
-  const bool mhd = c->cfg.magnetic != 0;
-  gp.cell[0] = (float*)c->w; gp.ncomp[0] = NHYD;
-  gp.cell[1] = mhd ? (float*)c->bcc : nullptr; gp.ncomp[1] = 3;
-  gp.cell[2] = mhd ? c->cce : nullptr; gp.ncomp[2] = 3;
-  for (int d = 0; d < 3; ++d) gp.face[d] = mhd ? c->bf32[d] : nullptr;
-  gp.nbr = c->nbr;
-  dim3 grid((unsigned)((ghost_shell_size(g) + 255) / 256), (unsigned)c->nb);
-  if (mhd) k_ghost_f32<true><<<grid, 256, 0, c->st>>>(g, gp);
-  else k_ghost_f32<false><<<grid, 256, 0, c->st>>>(g, gp);
-  c->counting += 1;
-  CKL();
-  return ATHG_OK;
+  float* const bf[3] = {c->bf32[0], c->bf32[1], c->bf32[2]};
+  return launch_ghosts_set(c, (float*)c->w, (float*)c->bcc, bf, c->cce);
 }
 
 // FP64 ghost zones of the current state, when a fused cycle left them behind
@@ -654,6 +787,21 @@ int do_stage(athg_ctx* c, int stage) {
   const int l = stage - 1;
   int order = (c->cfg.integrator == ATHG_VL2 && l == 0) ? 1 : c->cfg.xorder;
   int rc;
+  if (single_pass(c) && c->sp_ready) {
+    if ((rc = launch_single_pass(c, l, stage == c->integ.nstages))) return rc;
+    mark(c, stage, "single-pass stage (k_single_pass)");
+    if (l == 0) {
+      float* const bf[3] = {c->bf32b[0], c->bf32b[1], c->bf32b[2]};
+      rc = launch_ghosts_set(c, c->w2, c->bcc2, bf, nullptr);
+    } else {
+      float* const bf[3] = {c->bf32[0], c->bf32[1], c->bf32[2]};
+      rc = launch_ghosts_set(c, (float*)c->w, (float*)c->bcc, bf, nullptr);
+    }
+    if (rc) return rc;
+    mark(c, stage, "ghost exchange");
+    c->ghosts_stale = true;
+    return ATHG_OK;
+  }
   if (fused(c)) {
     if ((rc = launch_fluxes(c, order))) return rc;
     mark(c, stage, "flux sweeps");
@@ -732,12 +880,22 @@ int capture_cycle(athg_ctx* c, cudaGraph_t* graph, cudaGraphExec_t* exec) {
 // CUDA events on the context's stream; the fastest median wins. Mixed path only (the FP64
 // path is the reference-order check, not the fast path); runs once, before the first
 // captured cycle.
+int autotune_single_pass(athg_ctx* c);
+
 int autotune(athg_ctx* c) {
-  if (c->tuned || !c->mixed()) return ATHG_OK;
-  c->tuned = true;
+  if (!c->mixed()) return ATHG_OK;
   cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
   CK(cudaStreamIsCapturing(c->st, &cs));
   if (cs != cudaStreamCaptureStatusNone) return ATHG_OK;
+  if (single_pass(c)) {
+    int rc = sp_prepare(c);
+    if (rc) return rc;
+    if (c->sp_tuned) return ATHG_OK;
+    c->sp_tuned = true;
+    return autotune_single_pass(c);
+  }
+  if (c->tuned) return ATHG_OK;
+  c->tuned = true;
   const int tpbs[2] = {64, 128}, segs[4] = {8, 16, 32, 0};
   cudaEvent_t e0, e1;
   CK(cudaEventCreate(&e0));
@@ -772,6 +930,42 @@ int autotune(athg_ctx* c) {
   cudaEventDestroy(e1);
   c->counting = saved;
   if (!rc) c->tune = best;
+  return rc;
+}
+
+// k-segments per thread block of the single-pass stage: each candidate (1, 2, 4 segments
+// where they divide the block) runs the PLM kernel on the context's own state three times
+// in the first stage's direction (reading FP32 set 1, writing only the other state buffer
+// and FP32 set 2, which the next real stage overwrites), timed with CUDA events; the
+// fastest median wins.
+int autotune_single_pass(athg_ctx* c) {
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  const int saved = c->counting;
+  int best = 1;
+  float best_ms = 1e30f;
+  int rc = ATHG_OK;
+  for (int nseg = 1; nseg <= 4 && !rc; nseg *= 2) {
+    if (!athg::single_pass_fits(c->g, nseg)) continue;
+    c->sp_nseg = nseg;
+    float ms[3];
+    for (int r = 0; r < 3 && !rc; ++r) {
+      cudaEventRecord(e0, c->st);
+      rc = launch_single_pass(c, 0, false, c->cfg.xorder);
+      cudaEventRecord(e1, c->st);
+      if (!rc && (cudaEventSynchronize(e1) != cudaSuccess || cudaGetLastError() != cudaSuccess))
+        rc = fail(ATHG_ERR_CUDA, "autotune launch failed");
+      if (!rc) cudaEventElapsedTime(&ms[r], e0, e1);
+    }
+    if (rc) break;
+    std::sort(ms, ms + 3);
+    if (ms[1] < best_ms) { best_ms = ms[1]; best = nseg; }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  c->counting = saved;
+  c->sp_nseg = best;
   return rc;
 }
 
@@ -1120,8 +1314,13 @@ int athg_create(const athg_config* cfg, athg_ctx** out) {
   if (!cfg->magnetic &&
       !(cfg->rsolver == ATHG_HLLC || cfg->rsolver == ATHG_HLLE || cfg->rsolver == ATHG_LHLLC))
     return fail(ATHG_ERR_ARG, "hydro needs the HLLC, LHLLC or HLLE solver");
-  if (cfg->precision != ATHG_FP64 && cfg->precision != ATHG_MIXED)
-    return fail(ATHG_ERR_ARG, "precision must be ATHG_FP64 or ATHG_MIXED");
+  if (cfg->precision != ATHG_FP64 && cfg->precision != ATHG_MIXED &&
+      cfg->precision != ATHG_DFLOAT)
+    return fail(ATHG_ERR_ARG, "precision must be ATHG_FP64, ATHG_MIXED or ATHG_DFLOAT");
+  if (cfg->precision == ATHG_DFLOAT &&
+      !athg::df_supported(cfg->magnetic, cfg->rsolver, cfg->xorder))
+    return fail(ATHG_ERR_ARG, "ATHG_DFLOAT supports donor cell or PLM with HLLC/HLLE (hydro) "
+                              "or HLLD/HLLE (MHD)");
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
     return fail(ATHG_ERR_CUDA, "no CUDA device available");
@@ -1161,6 +1360,7 @@ int athg_destroy(athg_ctx* c) {
 
 int athg_set_blocks(athg_ctx* c, int nblocks, const athg_block* blocks) {
   if (!c || nblocks <= 0 || !blocks) return fail(ATHG_ERR_ARG, "bad block list");
+  c->outflow = false;  // athg_set_uniform_mesh turns it on for its non-periodic axes
   if (nblocks > 65535) return fail(ATHG_ERR_ARG, "at most 65535 blocks per context");
   for (int b = 0; b < nblocks; ++b) {
     if (!blocks[b].x1f || !blocks[b].x2f || !blocks[b].x3f)
@@ -1180,6 +1380,8 @@ int athg_set_blocks(athg_ctx* c, int nblocks, const athg_block* blocks) {
   const int NF = mhd ? 8 : 5;
   CK(cudaMalloc(&c->u, sizeof(double) * NHYD * g.ncell * nb));
   CK(cudaMalloc(&c->u1, sizeof(double) * NHYD * g.ncell * nb));
+  if (c->dfloat())
+    CK(cudaMalloc(&c->wpair_df, sizeof(float2) * (c->cfg.magnetic ? 8 : 5) * g.ncell * nb));
   CK(cudaMalloc(&c->w, tsz * NHYD * g.ncell * nb));
   CK(cudaMalloc(&c->flx[0], tsz * NF * g.nf1 * nb));
   CK(cudaMalloc(&c->flx[1], tsz * NF * g.nf2 * nb));
@@ -1203,6 +1405,7 @@ int athg_set_blocks(athg_ctx* c, int nblocks, const athg_block* blocks) {
       CK(cudaMemsetAsync(c->bf32[1], 0, sizeof(float) * g.nf2 * nb, c->st));
       CK(cudaMemsetAsync(c->bf32[2], 0, sizeof(float) * g.nf3 * nb, c->st));
     }
+    if (c->dfloat()) CK(cudaMalloc(&c->cce_df, sizeof(float2) * 3 * g.ncell * nb));
     CK(cudaMemsetAsync(c->b1, 0, sizeof(double) * g.nf1 * nb, c->st));
     CK(cudaMemsetAsync(c->b2, 0, sizeof(double) * g.nf2 * nb, c->st));
     CK(cudaMemsetAsync(c->b3, 0, sizeof(double) * g.nf3 * nb, c->st));
@@ -1217,6 +1420,7 @@ int athg_set_blocks(athg_ctx* c, int nblocks, const athg_block* blocks) {
   if (c->mixed()) CK(cudaMalloc(&c->dtf, sizeof(float)));
   CK(cudaMalloc(&c->nbr, sizeof(int) * 27 * nb));
   CK(cudaMalloc(&c->scal, sizeof(double) * 16));
+  CK(cudaMemsetAsync(c->scal, 0, sizeof(double) * 16, c->st));
   // host-side per-block tables
   std::vector<BlockGeo> hgeo(nb);
   std::vector<double> hcoef(nb * 3 * 2 * g.ncmax, 0.0);
@@ -1300,6 +1504,11 @@ int athg_set_uniform_mesh(athg_ctx* c, const athg_mesh* m) {
   for (int d = 0; d < 3; ++d) {
     if (nmx[d] % nbx[d] != 0)
       return fail(ATHG_ERR_ARG, "mesh size must be a multiple of the MeshBlock size");
+    if (m->periodic[d] != 0 && m->periodic[d] != 1)
+      return fail(ATHG_ERR_ARG, "periodic[d] must be 1 (periodic) or 0 (outflow)");
+    if (!m->periodic[d] && c->mixed())
+      return fail(ATHG_ERR_ARG, "outflow boundaries run on the FP64 and double-float paths "
+                                "(precision ATHG_FP64 or ATHG_DFLOAT)");
     nrb[d] = nmx[d] / nbx[d];
   }
   const int nblocks = nrb[0] * nrb[1] * nrb[2];
@@ -1353,7 +1562,10 @@ int athg_set_uniform_mesh(athg_ctx* c, const athg_mesh* m) {
       }
   const athg_mesh mcopy = *m;
   int rc = athg_set_blocks(c, nblocks, bl.data());
-  if (!rc) c->mesh = mcopy;
+  if (!rc) {
+    c->mesh = mcopy;
+    c->outflow = !(m->periodic[0] && m->periodic[1] && m->periodic[2]);
+  }
   return rc;
 }
 
@@ -1761,6 +1973,7 @@ int athg_get_time(athg_ctx* c, double* time, double* dt, int64_t* ncycle) {
   double hs[3];
   CK(cudaMemcpyAsync(hs, c->scal, sizeof(hs), cudaMemcpyDeviceToHost, c->st));
   CK(cudaStreamSynchronize(c->st));
+  if ((rc = device_errors(c))) return rc;
   if (time) *time = hs[0];
   if (dt) *dt = hs[1];
   long long nc;
@@ -1786,7 +1999,7 @@ int athg_set_time(athg_ctx* c, double time, double dt, int64_t ncycle) {
 int athg_synchronize(athg_ctx* c) {
   if (!c) return fail(ATHG_ERR_ARG, "null context");
   CK(cudaStreamSynchronize(c->st));
-  return ATHG_OK;
+  return c->nb > 0 ? device_errors(c) : ATHG_OK;
 }
 
 int athg_stream(athg_ctx* c, void** stream) {
@@ -1897,6 +2110,27 @@ int athg_set_tuning(athg_ctx* c, const int* in3) {
   drop_graphs(c);  // captured cycles hold the old launch shape
   c->tune.x1_tpb = in3[0]; c->tune.march_tpb = in3[1]; c->tune.seg = in3[2];
   c->tuned = true;
+  return ATHG_OK;
+}
+
+int athg_set_stage_kernel(athg_ctx* c, int single, int nseg) {
+  int rc = need_pool(c);
+  if (rc) return rc;
+  if (nseg < 0 || (nseg > 0 && !athg::single_pass_fits(c->g, nseg)))
+    return fail(ATHG_ERR_ARG, "k-segments must divide the block's nx3 (0: autotuned)");
+  drop_graphs(c);  // captured cycles hold the old stage sequence
+  c->sp_on = (single != 0);
+  if (nseg > 0) { c->sp_nseg = nseg; c->sp_tuned = true; }
+  else c->sp_tuned = false;
+  return ATHG_OK;
+}
+
+int athg_get_stage_kernel(athg_ctx* c, int* single, int* nseg) {
+  int rc = need_pool(c);
+  if (rc) return rc;
+  if (!single || !nseg) return fail(ATHG_ERR_ARG, "null argument");
+  *single = single_pass(c) ? 1 : 0;
+  *nseg = c->sp_nseg;
   return ATHG_OK;
 }
 

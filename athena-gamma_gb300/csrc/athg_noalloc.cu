@@ -1,8 +1,8 @@
 // athg_noalloc.cu -- CFL time step of one caller-owned MeshBlock without any device
 // allocation (athg_block_cfl_dt_noalloc, declared in include/athena_gb300.h).
 //
-// Some callers cannot allocate device memory: code running while a stream is being
-// captured into a CUDA graph, hosts whose device memory is handed out by their own pool
+// Some callers cannot allocate device memory: code that must not synchronise the device
+// (cudaMalloc and cudaFree may), hosts whose device memory is handed out by their own pool
 // and must not be touched by a library, or drivers with a fixed memory budget set up
 // before the run. This entry point computes the same minimum as athg_new_block_dt (the
 // reference's Hydro::NewBlockTimeStep for one block), but takes the block's arrays from
@@ -35,9 +35,6 @@ constexpr int kMaxPartials = 8192;
 
 static __device__ __align__(256) double g_dt_partials[kMaxPartials];
 
-// device address of g_dt_partials per device, looked up once with that device current
-constexpr int kMaxDevices = 64;
-double* g_partials_addr[kMaxDevices] = {nullptr};
 
 int fail(int code, const std::string& msg) {
   set_last_error(msg);
@@ -140,14 +137,15 @@ extern "C" int athg_block_cfl_dt_noalloc(const athg_config* cfg, const double* w
                     " interior cells, at most " + std::to_string((long long)kMaxPartials * per_block));
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return fail(ATHG_ERR_CUDA, "no current CUDA device");
-  if (dev < 0 || dev >= kMaxDevices) return fail(ATHG_ERR_ARG, "device index out of range");
-  if (!g_partials_addr[dev]) {
-    // first call on this device: find the device address of the scratch array
-    double* p = nullptr;
-    cudaError_t e = cudaGetSymbolAddress((void**)&p, g_dt_partials);
+  // the scratch array's address in the current device's context, looked up on every call
+  // (a host-side lookup, no allocation): a cached address would go stale when the context
+  // is replaced (cudaDeviceReset), and nothing is shared between host threads. The first
+  // call on a device loads this library's device code there.
+  double* partials = nullptr;
+  {
+    cudaError_t e = cudaGetSymbolAddress((void**)&partials, g_dt_partials);
     if (e != cudaSuccess)
       return fail(ATHG_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
-    g_partials_addr[dev] = p;
   }
   BlockArgs a;
   a.w = w; a.bcc = bcc; a.b1 = b1f; a.b2 = b2f; a.b3 = b3f;
@@ -161,8 +159,8 @@ extern "C" int athg_block_cfl_dt_noalloc(const athg_config* cfg, const double* w
   a.gamma = cfg->gamma;
   a.dx1 = dx1; a.dx2 = dx2; a.dx3 = dx3;
   cudaStream_t st = (cudaStream_t)stream;
-  k_dt_partials<<<(unsigned)nparts, kThreads, 0, st>>>(a, g_partials_addr[dev]);
-  k_dt_final<<<1, kThreads, 0, st>>>(g_partials_addr[dev], (int)nparts, cfg->cfl_number, dt_out);
+  k_dt_partials<<<(unsigned)nparts, kThreads, 0, st>>>(a, partials);
+  k_dt_final<<<1, kThreads, 0, st>>>(partials, (int)nparts, cfg->cfl_number, dt_out);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess)
     return fail(ATHG_ERR_CUDA, std::string("kernel launch: ") + cudaGetErrorString(e));

@@ -239,30 +239,44 @@ def turbulent_box(nx, seed=20261203, mach=5.0, beta=1.0, gamma=1.0001, kmin=1, k
     """Magnetised self-gravitating turbulent box (no reference problem generator: the
     reference's turbulence driver needs FFTW). rho = 1, p = 1/gamma (c_s = 1), uniform
     B along z with plasma beta = 2 p / B^2, and a seeded Gaussian random solenoidal
-    velocity: white noise filtered to a 3-D power spectrum |v_k|^2 ~ k^expo on the
-    integer shells kmin <= |k| <= kmax, projected divergence-free, mean removed and
-    scaled to rms Mach number `mach`. Returns (u, b1, b2, b3, four_pi_G, sha256 of the
+    velocity: independent complex Gaussian amplitudes on the integer wavevectors of the
+    shells kmin <= |k| <= kmax (Hermitian, so the field is real) with |v_k|^2 ~ k^expo,
+    projected divergence-free, synthesised by three separable 1-D sums (only the few
+    hundred modes of the shells exist, so no full-grid transform is needed), mean removed
+    and scaled to rms Mach number `mach`. Returns (u, b1, b2, b3, four_pi_G, sha256 of the
     velocity field), with G set for the Jeans number n_J = L / lambda_J,
     lambda_J = c_s sqrt(pi / (G rho)):  G = pi n_J^2 c_s^2 / (rho L^2)."""
     import hashlib
     n1, n2, n3 = nx
     rng = np.random.default_rng(seed)
-    k1 = np.fft.fftfreq(n1, 1.0 / n1)
-    k2 = np.fft.fftfreq(n2, 1.0 / n2)
-    k3 = np.fft.fftfreq(n3, 1.0 / n3)
-    K3, K2, K1 = np.meshgrid(k3, k2, k1, indexing="ij")
+    kr = np.arange(-kmax, kmax + 1)
+    nk = kr.size
+    K3, K2, K1 = np.meshgrid(kr, kr, kr, indexing="ij")
     kk = np.sqrt(K1 ** 2 + K2 ** 2 + K3 ** 2)
     shell = (kk >= kmin - 1e-9) & (kk <= kmax + 1e-9)
-    amp = np.zeros_like(kk)
-    amp[shell] = kk[shell] ** (0.5 * expo)
+    amp = np.where(shell, np.where(kk > 0, kk, 1.0) ** (0.5 * expo), 0.0)
     vk = []
     for _ in range(3):
-        noise = rng.standard_normal((n3, n2, n1))
-        vk.append(np.fft.fftn(noise) * amp)
+        a = (rng.standard_normal(kk.shape) + 1j * rng.standard_normal(kk.shape)) * amp
+        a = 0.5 * (a + np.conj(a[::-1, ::-1, ::-1]))  # a(-k) = conj(a(k)): a real field
+        vk.append(a)
     ksq = np.where(kk > 0, kk ** 2, 1.0)
     div = (K1 * vk[0] + K2 * vk[1] + K3 * vk[2]) / ksq
     vk = [vk[0] - K1 * div, vk[1] - K2 * div, vk[2] - K3 * div]
-    v = [np.real(np.fft.ifftn(a)) for a in vk]
+
+    def synth(a):
+        # v(x3, x2, x1) = Re sum_k a(k) exp(2 pi i k.x), cell centres of the unit cube
+        e1 = np.exp(2j * np.pi * np.outer(kr, (np.arange(n1) + 0.5) / n1))  # [nk, n1]
+        e2 = np.exp(2j * np.pi * np.outer(kr, (np.arange(n2) + 0.5) / n2))
+        e3 = np.exp(2j * np.pi * np.outer(kr, (np.arange(n3) + 0.5) / n3))
+        t = np.einsum("cba,cz->zba", a, e3)                     # [n3, nk2, nk1]
+        t = np.einsum("zba,by->zya", t, e2)                     # [n3, n2, nk1]
+        out = np.empty((n3, n2, n1))
+        for z in range(n3):                                     # [n2, nk1] @ [nk1, n1]
+            out[z] = np.real(t[z] @ e1)
+        return out
+
+    v = [synth(a) for a in vk]
     v = [a - a.mean() for a in v]
     rms = math.sqrt(float(np.mean(v[0] ** 2 + v[1] ** 2 + v[2] ** 2)))
     cs = 1.0

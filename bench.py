@@ -28,11 +28,9 @@ NX = (256, 256, 256)
 MB = (64, 64, 64)
 CFL = 0.4
 BYTES_PER_ZC = 384  # VL2 MHD: 2 stages x (read 2 + write 1) x (40 B U + 24 B face B)
-# algorithmic bytes of one launch of the fused update + primitive recovery (k_update_c2p),
-# per cell: FP64 U in and out (80 B), the cell's three FP64 lower faces in and out (48 B),
-# FP32 hydro fluxes of its three lower faces (60 B), its three FP32 edge EMFs (12 B), FP32
-# W, bcc, cell-centred EMF and face copies out (56 B)
-BYTES_UPDATE_C2P = 256
+# algorithmic bytes of one stage per cell (MHD, FP64 state): two register reads and one
+# write of 40 B U + 24 B face B; one launch of the stage's update kernel covers one stage
+BYTES_PER_CELL_STAGE = 192
 METRIC = "zone-cycles/s"
 WORKLOAD = "orszag_tang_256^3_mhd_plm_hlld_vl2"
 
@@ -116,44 +114,65 @@ def dist_env():
         int(os.environ.get("LOCAL_RANK", 0))
 
 
-def cpu_reference(steps_cells, sample_cycles):
-    """Times the oracle port (FP64 CPU restatement) on this host's cores."""
+def workload_config():
+    """The `config` object both arms print: the workload itself, not how it is laid out."""
+    return {"workload": WORKLOAD, "cells": list(NX), "domain": [-0.5, 0.5],
+            "physics": "ideal MHD, gamma 5/3, PLM + HLLD + CT, VL2, CFL %.1f" % CFL,
+            "initial_state": "Orszag-Tang (pgen/orszag_tang.cpp), z-invariant"}
+
+
+def cpu_oracle(nx):
+    """The oracle port (FP64 CPU restatement of the reference's stage, OpenMP) on the
+    Orszag-Tang initial state, initialised (ghosts, W(U), first dt)."""
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     import oracle_lib as ol
     import pgens
-    nx = steps_cells
     u, b1, b2, b3 = pgens.orszag_tang(nx)
     o = ol.Oracle(nx, True, "hlld", cfl=CFL, domain=((-0.5, 0.5),) * 3)
     o.load_interior(u, b1, b2, b3)
     o.initialize(100.0)
+    return o, ol.lib().orc_num_threads()
+
+
+def cpu_reference(steps_cells, sample_cycles):
+    """Times `sample_cycles` cycles of the oracle port on this host's cores; returns the
+    throughput, the threads used, the seconds and the oracle (its state after the sample,
+    which the parity check compares with the GPU's)."""
+    o, cores = cpu_oracle(steps_cells)
     t0 = time.perf_counter()
     o.cycle(sample_cycles, 100.0)
     el = time.perf_counter() - t0
-    zc = float(np.prod(nx)) * sample_cycles
-    return zc / el, ol.lib().orc_num_threads(), el
+    zc = float(np.prod(steps_cells)) * sample_cycles
+    return zc / el, cores, el, o
 
 
 def run_reference(args):
+    """Reference arm: the oracle port on all host cores, one VL2 cycle of the 256^3
+    Orszag-Tang update per step (about 0.7 s on 16 cores), W warm-up cycles, then K timed
+    cycles continuing the same run; ranks other than 0 exit without work."""
     rank, world, _ = dist_env()
     if rank != 0:
         return
-    cycles = max(1, args.cpu_cycles)
-    # warm-up samples of one cycle each (page-in, OpenMP thread start), at most three
-    warm = min(max(0, args.warmup), 3)
-    for _ in range(warm):
-        cpu_reference(NX, 1)
-    vals = []
-    for _ in range(max(1, args.steps if args.steps <= 3 else 3)):
-        v, cores, _ = cpu_reference(NX, cycles)
-        vals.append(v)
-    v = float(np.median(vals))
+    o, cores = cpu_oracle(NX)
+    o.cycle(max(0, args.warmup), 100.0)
+    per = []
+    for _ in range(max(1, args.steps)):
+        t0 = time.perf_counter()
+        o.cycle(1, 100.0)
+        per.append(time.perf_counter() - t0)
+    el = float(sum(per))
+    v = float(np.prod(NX)) * len(per) / el
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": METRIC, "n_gpus": args.gpus,
-            "steps": len(vals), "warmup": warm, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic (Orszag-Tang initial state)",
-            "config": {"workload": WORKLOAD, "cells": list(NX), "meshblock": list(MB)},
+            "steps": len(per), "warmup": max(0, args.warmup), "ms_per_step": 1e3 * el / len(per),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (Orszag-Tang initial state, %d^3)" % NX[0],
+            "config": workload_config(),
+            "layout": {"blocks": 1, "meshblock": list(NX),
+                       "note": "the oracle port runs the mesh as one periodic block"},
             "cpu_baseline": {"value": v, "unit": METRIC, "cores": cores, "kind": "port",
-                             "sample": "%d VL2 cycle(s) of the 256^3 Orszag-Tang update per "
-                                       "step, FP64 oracle port, OpenMP" % cycles},
+                             "sample": "one VL2 cycle of the %d^3 Orszag-Tang update per step "
+                                       "(%d steps, %.1f s), FP64 oracle port, OpenMP on %d "
+                                       "threads" % (NX[0], len(per), el, cores)},
             "e2e": {"value": v, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -245,10 +264,8 @@ def run_mg_profile(prec, bc, n):
 
 # MHD blast with static refinement (the reference's athinput.blast with <refinement1>):
 # root 128^3 on [-1,1]^3, the central half refined one level, 16^3 blocks (960 of them),
-# PPM + HLLD + RK3, NGHOST 4, FP64 (the precision of the reference). The reference's own
-# CPU throughput on this configuration, measured with its binary on one core, is
-# 2.10e5 zone-cycles/s.
-C3_REF_CPU_ZCPS = 2.10e5
+# PPM + HLLD + RK3, NGHOST 4, FP64 (the precision of the reference). The oracle port is a
+# single uniform block, so this workload has no CPU figure measured on the same host.
 
 
 def c3_setup(athg, pgens, root=128, mb=16, precision="fp64"):
@@ -276,9 +293,7 @@ def run_c3(athg, torch, steps, warmup):
            "smr_lists": dict(zip(("ghost_fill", "same_level_restrict", "flux_corr", "emf_corr",
                                   "coarse_c2p", "prolong_cells", "internal_field",
                                   "fine_rebuild"), sim.smr_stats())),
-           "div_b_max": sim.max_div_b(),
-           "reference_cpu_zone_cycles_per_s_1core": C3_REF_CPU_ZCPS,
-           "speedup_vs_reference_1core": zcps / C3_REF_CPU_ZCPS}
+           "div_b_max": sim.max_div_b()}
     sim.close()
     # the same workload on the mixed path (FP32 fluxes and EMFs, FP64 state and level
     # boundaries), and how far it is from the FP64 run after the same cycles
@@ -454,6 +469,14 @@ def run_c5(args):
             "fp64": {"value": res["fp64"]["zcps"], "steps": res["fp64"]["steps"],
                      "ms_per_step": 1e3 * res["fp64"]["el"] / res["fp64"]["steps"]},
             "mixed_over_fp64": m["zcps"] / res["fp64"]["zcps"],
+        "dfloat": {"value": res["dfloat"]["zcps"],
+                   "ms_per_step": 1e3 * res["dfloat"]["el"] / res["dfloat"]["steps"],
+                   "steps": res["dfloat"]["steps"],
+                   "over_fp64": res["dfloat"]["zcps"] / res["fp64"]["zcps"],
+                   "note": "double-float reconstruction, Riemann fluxes and corner EMFs, "
+                           "FP64 state and update (the FP64 path's accuracy)"},
+        "linear_waves_equal_l1": lwres,
+        "single_pass_stage": spres,
             "vcycle_ms": {"mixed": m["vcycle_ms"], "fp64": res["fp64"]["vcycle_ms"]},
             "l1_rho_mixed_vs_fp64": {"cycles": args.c5_fp64_steps, "rel": l1,
                                      "mg": "iterated to convergence (threshold 0)"},
@@ -461,9 +484,78 @@ def run_c5(args):
     print(json.dumps(line), flush=True)
 
 
+def run_linear_waves(athg):
+    """The metric's "at equal L1 error" on the reference's own linear waves (C1 hydro HLLC,
+    C2 MHD fast wave HLLD; 64x32x32, one block, amplitude 1e-6, one period / tlim 0.5):
+    zone-cycles/s of the whole run (every cycle followed by the time read-back of the main
+    loop) and the L1 error against the initial state, for the FP64 path, the double-float
+    flux path and the FP32 flux path. The reference's L1 values (linearwave-errors.dat)
+    are 4.611e-08 and 5.973e-08."""
+    import pgens
+    out = {}
+    dom = ((0.0, 3.0), (0.0, 1.5), (0.0, 1.5))
+    nx = (64, 32, 32)
+    for key, mhd, solver, tlim, cfl in (("c1_hydro_hllc", False, "hllc", 1.0, 0.4),
+                                        ("c2_mhd_fast_hlld", True, "hlld", 0.5, 0.3)):
+        lw = pgens.LinearWave(nx, dom, mhd)
+        u, b1, b2, b3 = lw.initial_state()
+        res = {}
+        for prec in ("fp64", "dfloat", "mixed"):
+            sim = athg.Sim(nx, nx, mhd=mhd, solver=solver, precision=prec, cfl=cfl,
+                           gamma=1.666666666666667, tlim=tlim, domain=dom)
+            sim.load_interior(u, b1, b2, b3)
+            sim.initialize()
+            sim.cycles(1)  # graph capture and autotuning outside the timed run
+            sim.load_interior(u, b1, b2, b3)
+            sim.set_time(0.0, 0.0, 0)
+            sim.initialize()
+            sim.synchronize()
+            t0 = time.perf_counter()
+            n = sim.run(tlim)
+            el = time.perf_counter() - t0
+            o = sim.interior()
+            sim.close()
+            l1 = lw.l1_errors(o["u"], o.get("b1"), o.get("b2"), o.get("b3"))[0]
+            res[prec] = {"cycles": n, "zone_cycles_per_s": float(np.prod(nx)) * n / el,
+                         "l1_rms": float(l1)}
+        res["l1_ratio_to_fp64"] = {p: res[p]["l1_rms"] / res["fp64"]["l1_rms"]
+                                   for p in ("dfloat", "mixed")}
+        res["speed_over_fp64"] = {p: res[p]["zone_cycles_per_s"] / res["fp64"]["zone_cycles_per_s"]
+                                  for p in ("dfloat", "mixed")}
+        out[key] = res
+    return out
+
+
+SINGLE_PASS = False  # --single-pass: the mixed runs use the single-pass stage kernel
+
+
 def make_sim(athg, precision):
-    return athg.Sim(NX, MB, mhd=True, solver="hlld", precision=precision, cfl=CFL, tlim=1e30,
-                    domain=((-0.5, 0.5),) * 3)
+    sim = athg.Sim(NX, MB, mhd=True, solver="hlld", precision=precision, cfl=CFL, tlim=1e30,
+                   domain=((-0.5, 0.5),) * 3)
+    if SINGLE_PASS and precision == "mixed":
+        sim.set_stage_kernel(True)
+    return sim
+
+
+def run_single_pass(athg, torch, u, b1, b2, b3, steps):
+    """The same mixed cycles with the single-pass stage kernel (one launch per stage, W/bcc
+    planes staged by TMA): ms per cycle, and per launch group."""
+    sim = athg.Sim(NX, MB, mhd=True, solver="hlld", precision="mixed", cfl=CFL, tlim=1e30,
+                   domain=((-0.5, 0.5),) * 3)
+    sim.load_interior(u, b1, b2, b3)
+    sim.initialize()
+    sim.set_stage_kernel(True)
+    on, nseg = sim.stage_kernel()
+    sim.cycles(3)
+    sim.synchronize()
+    el = timed_cycles(sim, torch, steps)
+    groups = {}
+    for _ in range(3):
+        for name, t in sim.cycle_timing():
+            groups.setdefault(name, []).append(t)
+    sim.close()
+    return {"active": on, "k_segments": nseg, "ms_per_step": 1e3 * el / steps,
+            "cycle_breakdown_ms": {k: float(np.median(v)) for k, v in groups.items()}}
 
 
 def timed_cycles(sim, torch, steps):
@@ -528,6 +620,9 @@ def main():
     ap.add_argument("--nx", type=int, default=256, help="cells per side (profiling: 128)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-mg", action="store_true")
+    ap.add_argument("--no-lw", action="store_true", help="skip the linear-wave equal-L1 leg")
+    ap.add_argument("--single-pass", action="store_true",
+                    help="the mixed runs use the single-pass stage kernel (profiling)")
     ap.add_argument("--mg-profile", nargs=3, metavar=("PREC", "BC", "N"), default=None,
                     help="profiling run: solve the uniform sphere once, then one V-cycle "
                          "between cudaProfilerStart/Stop (for ncu --profile-from-start off)")
@@ -547,8 +642,9 @@ def main():
     ap.add_argument("--c5-nx", type=int, default=512)
     ap.add_argument("--c5-fp64-steps", type=int, default=10)
     args = ap.parse_args()
-    global NX, WORKLOAD
+    global NX, WORKLOAD, SINGLE_PASS
     NX = (args.nx,) * 3
+    SINGLE_PASS = args.single_pass
     WORKLOAD = "orszag_tang_%d^3_mhd_plm_hlld_vl2" % args.nx
     if args.impl == "reference":
         return run_reference(args)
@@ -575,7 +671,8 @@ def main():
 
     # ---------------- device-resident throughput, mixed (headline) and FP64 -------------
     res = {}
-    for prec, steps in (("mixed", args.steps), ("fp64", args.fp64_steps)):
+    for prec, steps in (("mixed", args.steps), ("fp64", args.fp64_steps),
+                        ("dfloat", args.fp64_steps)):
         sim = make_sim(athg, prec)
         sim.load_interior(u, b1, b2, b3)
         sim.initialize()
@@ -605,7 +702,8 @@ def main():
         del sim
 
     # L1 deviation of the mixed path from the FP64 path after the same number of cycles
-    n_cmp = 4
+    # (the cycles of the CPU sample, so both states are also compared with the oracle's)
+    n_cmp = max(1, args.cpu_cycles)
     devs = {}
     for prec in ("mixed", "fp64"):
         sim = make_sim(athg, prec)
@@ -621,6 +719,16 @@ def main():
     e2e = None
     if not args.no_e2e:
         e2e = run_e2e(athg, torch, u, b1, b2, b3, args.steps, zones)
+
+    # ---------------- the single-pass stage kernel on the same workload ---------------
+    spres = None
+    if not args.single_pass:
+        spres = run_single_pass(athg, torch, u, b1, b2, b3, min(args.steps, 20))
+
+    # ---------------- linear waves at the reference's amplitude (equal L1) ------------
+    lwres = None
+    if not args.no_lw:
+        lwres = run_linear_waves(athg)
 
     # ---------------- multigrid (uniform sphere, multipole boundaries) ----------------
     mgres = None
@@ -639,29 +747,49 @@ def main():
 
     # ---------------- CPU baseline (oracle port) ----------------
     cpu = None
+    parity = None
     if rank == 0 and not args.no_cpu_baseline:
-        v, cores, el = cpu_reference(NX, args.cpu_cycles)
+        v, cores, el, orc = cpu_reference(NX, n_cmp)
         cpu = {"value": v, "unit": METRIC, "cores": cores, "kind": "port",
-               "sample": "%d VL2 cycles of the 256^3 Orszag-Tang update, FP64 oracle port "
-                         "(OpenMP), %.1f s" % (args.cpu_cycles, el)}
+               "sample": "%d VL2 cycles of the %d^3 Orszag-Tang update, FP64 oracle port "
+                         "(OpenMP), %.1f s" % (n_cmp, NX[0], el)}
+        # parity at the headline size: the GPU states after the same cycles against the
+        # oracle's (FP64 to 1e-13 of each field's magnitude, mixed to 2e-6)
+        ref = orc.interior()
+        del orc
+        parity = {"cycles": n_cmp, "tolerance": {"fp64": 1e-13, "mixed": 2e-6}}
+        ok = True
+        bmax = max(float(np.abs(ref[k]).max()) for k in ("b1", "b2", "b3"))
+        for prec in ("fp64", "mixed"):
+            # face fields against the largest field component (b3 is zero up to round-off
+            # in the z-invariant vortex)
+            errs = {k: float(np.abs(devs[prec][k] - ref[k]).max() /
+                             (np.abs(ref[k]).max() if k == "u" else bmax)) for k in ref}
+            parity[prec + "_max_rel_diff"] = errs
+            ok = ok and max(errs.values()) <= parity["tolerance"][prec]
+        parity["ok"] = bool(ok)
 
     peak, peak_kind = peaks()
     m = res["mixed"]
     sec_per_cycle = m["el"] / m["steps"]
     achieved = BYTES_PER_ZC * zones / sec_per_cycle / 1e9
-    # the dominant kernel, k_update_c2p: median over the three timed cycles of its mean
-    # launch time (two launches per cycle)
+    # the dominant kernel (the single-pass stage kernel, or k_update_c2p of the separate
+    # kernels): median over the three timed cycles of its mean launch time (one launch per
+    # stage, two per cycle)
+    kname = "k_single_pass" if any("k_single_pass" in n for n, _ in m["timing"][0]) \
+        else "k_update_c2p"
     upd = []
     groups = {}
     for rep in m["timing"]:
-        ts = [t for name, t in rep if "k_update_c2p" in name]
+        ts = [t for name, t in rep if kname in name]
         upd.append(sum(ts) / len(ts))
         for name, t in rep:
             groups.setdefault(name, []).append(t)
     t_upd = float(np.median(upd)) / 1e3
-    k_achieved = BYTES_UPDATE_C2P * zones / t_upd / 1e9
+    k_achieved = BYTES_PER_CELL_STAGE * zones / t_upd / 1e9
     k_traffic = None
-    kpath = os.path.join(ROOT, "profiles", "update_c2p_fused_ncu_192.md")
+    kpath = os.path.join(ROOT, "profiles", "single_pass_stage_ncu_128.md"
+                         if kname == "k_single_pass" else "update_c2p_fused_ncu_192.md")
     if os.path.exists(kpath):
         with open(kpath) as f:
             for ln in f:
@@ -676,25 +804,37 @@ def main():
             for ln in f:
                 if ln.startswith("bytes_per_zone_cycle:"):
                     traffic = float(ln.split(":")[1]) * zones
+    value = m["zcps"]
+    if parity is not None and not parity["ok"]:
+        value = 0.0  # a result that differs from the oracle's is not a throughput
     line = {
-        "metric": METRIC, "value": m["zcps"], "unit": METRIC, "n_gpus": world,
+        "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world,
         "steps": m["steps"], "warmup": args.warmup, "ms_per_step": 1e3 * sec_per_cycle,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
         "data": "synthetic (Orszag-Tang initial state, 256^3)",
-        "config": {"workload": WORKLOAD, "cells": list(NX), "meshblock": list(MB),
-                   "blocks": int(np.prod([a // b for a, b in zip(NX, MB)])),
+        "config": workload_config(),
+        "layout": {"meshblock": list(MB), "blocks": int(np.prod([a // b for a, b in zip(NX, MB)])),
                    "precision": "mixed: FP32 reconstruction+Riemann, FP64 U/B/CT",
                    "flux_launch_shape": dict(zip(("x1_tpb", "march_tpb", "march_segment"),
                                                  m["tuning"])),
                    "l2": "working set (~2.9 GB) far larger than L2; no flush needed",
                    "parallelism": "replicas" if world > 1 else "1 GPU"},
+        "parity_vs_oracle": parity,
         "fp64": {"value": res["fp64"]["zcps"], "ms_per_step": 1e3 * res["fp64"]["el"] / res["fp64"]["steps"],
                  "steps": res["fp64"]["steps"]},
         "mixed_over_fp64": m["zcps"] / res["fp64"]["zcps"],
+        "dfloat": {"value": res["dfloat"]["zcps"],
+                   "ms_per_step": 1e3 * res["dfloat"]["el"] / res["dfloat"]["steps"],
+                   "steps": res["dfloat"]["steps"],
+                   "over_fp64": res["dfloat"]["zcps"] / res["fp64"]["zcps"],
+                   "note": "double-float reconstruction, Riemann fluxes and corner EMFs, "
+                           "FP64 state and update (the FP64 path's accuracy)"},
+        "linear_waves_equal_l1": lwres,
+        "single_pass_stage": spres,
         "l1_rho_mixed_vs_fp64": {"cycles": n_cmp, "abs": l1_dev, "rel": l1_rel},
         "div_b_max": {"mixed": m["divb"], "fp64": res["fp64"]["divb"]},
-        "roofline": {"bound": "hbm", "kernel": "k_update_c2p (fused VL2 update + primitive "
-                               "recovery, 44% of the cycle)",
+        "roofline": {"bound": "hbm", "kernel": kname + " (%.0f%% of the cycle)" % (
+                         100.0 * 2 * t_upd / sec_per_cycle),
                      "achieved": k_achieved, "peak": peak, "unit": "GB/s",
                      "frac": k_achieved / peak, "traffic": k_traffic,
                      "launch_ms": 1e3 * t_upd,
@@ -702,7 +842,7 @@ def main():
                              "from CUDA events between launch groups on the context stream "
                              "(athg_cycle_timing, median of 3 cycles); peak %s copy bandwidth; "
                              "traffic = ncu DRAM bytes per launch (192^3 capture scaled to the "
-                             "cells)" % (BYTES_UPDATE_C2P, zones, peak_kind)},
+                             "cells)" % (BYTES_PER_CELL_STAGE, zones, peak_kind)},
         "cycle_roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                            "frac": achieved / peak, "traffic": traffic,
                            "note": "one launch = one captured VL2 cycle (graph); algorithmic "

@@ -26,14 +26,22 @@ extern "C" {
 #define ATHG_ERR_ARG (-1)    /* invalid argument or unsupported configuration */
 #define ATHG_ERR_CUDA (-2)   /* CUDA runtime error */
 #define ATHG_ERR_STATE (-3)  /* call out of order (e.g. no blocks yet) */
-#define ATHG_ERR_DEVICE (-4) /* a kernel reported an error through the device error word */
+#define ATHG_ERR_DEVICE (-4) /* a kernel reported an error through the device error word
+                                (a TMA load that timed out, a time step that is not a
+                                positive finite number, a non-finite density or pressure);
+                                reported by the next call that synchronises the context's
+                                stream: athg_get_time, athg_synchronize */
 
 /* Riemann solvers (configure.py --flux) */
 enum { ATHG_HLLE = 0, ATHG_HLLC = 1, ATHG_HLLD = 2, ATHG_LHLLC = 3, ATHG_LHLLD = 4 };
 /* time integrators (<time> integrator) */
 enum { ATHG_VL2 = 0, ATHG_RK1 = 1, ATHG_RK2 = 2, ATHG_RK3 = 3 };
-/* arithmetic of reconstruction/Riemann fluxes: FP64, or FP32 with FP64 state + CT */
-enum { ATHG_FP64 = 0, ATHG_MIXED = 1 };
+/* arithmetic of reconstruction/Riemann fluxes: FP64 (the reference's, bit for bit); FP32
+ * with FP64 state + CT (mixed); or double-float (pairs of FP32 values, ~48 bits, on the FP32
+ * pipe) with FP64 state, update and CT: the FP64 path's accuracy, including for waves near
+ * the FP32 resolution of their background (donor cell or PLM; HLLC/HLLE hydro, HLLD/HLLE
+ * MHD). ATHG_DFLOAT has no counterpart in the reference. */
+enum { ATHG_FP64 = 0, ATHG_MIXED = 1, ATHG_DFLOAT = 2 };
 /* arrays exchanged with the host, per block, AthenaArray layout with ghosts:
  * CONS (5,nc3,nc2,nc1)  B1F (nc3,nc2,nc1+1)  B2F (nc3,nc2+1,nc1)  B3F (nc3+1,nc2,nc1)
  * PRIM (5,nc3,nc2,nc1)  BCC (3,nc3,nc2,nc1)  PHI (nc3,nc2,nc1)   nc = nx + 2*nghost */
@@ -79,7 +87,12 @@ typedef struct {
 typedef struct {
   int nx1, nx2, nx3;                         /* <mesh> nx1..nx3 */
   double x1min, x1max, x2min, x2max, x3min, x3max;
-  int periodic[3];                           /* 1 if ix/ox bc are periodic on this axis */
+  int periodic[3];                           /* per axis: 1 periodic (ix/ox_bc = periodic);
+                                                0 outflow on both sides (ix/ox_bc = outflow,
+                                                bvals/cc/outflow_cc.cpp, bvals/fc/
+                                                outflow_fc.cpp; precision ATHG_FP64 or
+                                                ATHG_DFLOAT, uniform meshes). Other
+                                                values are rejected with ATHG_ERR_ARG */
 } athg_mesh;
 
 /* A static-refinement region (<refinementN> x1min..x3max, level >= 1). */
@@ -287,6 +300,18 @@ int athg_mg_multipole(athg_mg* mg, double* out28);
 int athg_get_tuning(athg_ctx* ctx, int* out3);
 int athg_set_tuning(athg_ctx* ctx, const int* in3);
 
+/* Stage kernel of the mixed-precision VL2 MHD path (PLM, HLLD or HLLE) on a uniform mesh:
+ * single = 1 runs each stage as one launch (reconstruction, Riemann fluxes, corner EMFs,
+ * flux divergence, CT and primitive recovery on chip, W/bcc staged by TMA; where it
+ * applies: two ghost layers, MeshBlock nx1 a multiple of 32 and nx2 of 8), single = 0 (the
+ * default, faster on this GPU) the separate sweep, corner-EMF and update kernels. nseg:
+ * k-segments per thread block of the single pass (a divisor of nx3; 0 = autotuned before
+ * the first captured cycle). No counterpart in the reference (its stage is one loop nest
+ * per MeshBlock). athg_get_stage_kernel reports whether the next cycle runs the single
+ * pass. */
+int athg_set_stage_kernel(athg_ctx* ctx, int single, int nseg);
+int athg_get_stage_kernel(athg_ctx* ctx, int* single, int* nseg);
+
 /* HistoryOutput::WriteOutputFile sums (outputs/history.cpp:45-130), reduced on the
  * device over all blocks' interior cells: out[0] mass, [1..3] momenta, [4..6] kinetic
  * energy per direction, [7] total energy, [8] 1/2 rho phi (0 without self-gravity),
@@ -308,8 +333,8 @@ int athg_attach_gravity(athg_ctx* ctx, athg_mg* mg, double four_pi_G);
 
 /* ---- CFL time step of one caller-owned block, with no device allocation ------------
  * No counterpart in the reference: an addition for callers that cannot allocate device
- * memory (a stream being captured into a CUDA graph, a host whose device memory belongs
- * to its own pool, a fixed memory budget). Computes the same minimum as
+ * memory (code that must not synchronise the device, which cudaMalloc and cudaFree may
+ * do; a host whose device memory belongs to its own pool; a fixed memory budget). Computes the same minimum as
  * athg_new_block_dt (dx / (|v| + c_f) over the interior, times cfg->cfl_number) for ONE
  * block whose device arrays the caller owns, in the AthenaArray layout with ghosts, FP64:
  *   w (5,nc3,nc2,nc1) primitives; for MHD also bcc (3,nc3,nc2,nc1) and the face fields
@@ -319,8 +344,10 @@ int athg_attach_gravity(athg_ctx* ctx, athg_mg* mg, double four_pi_G);
  * Only cfg->nx1..nx3, nghost, magnetic, gamma and cfl_number are read.
  * Scratch is a fixed file-scope device array of 8192 doubles (64 KiB) that every GPU
  * loading this library keeps until exit; blocks of more than 16,777,216 interior cells
- * are rejected with ATHG_ERR_ARG. The first call on a device looks up the array's device
- * address (cudaGetSymbolAddress), so make that first call before any stream capture.
+ * are rejected with ATHG_ERR_ARG. Every call looks up the array's device address in the
+ * current context (cudaGetSymbolAddress, no allocation), so the entry point stays valid
+ * after cudaDeviceReset; the first call on a device also loads this library's device code
+ * there, so make that first call before any stream capture.
  * All calls share the array: calls that overlap on the GPU (e.g. on two streams) race. */
 int athg_block_cfl_dt_noalloc(const athg_config* cfg, const double* w, const double* bcc,
                               const double* b1f, const double* b2f, const double* b3f,

@@ -46,14 +46,23 @@ CASES = {
     "mhd_lhlld_plm_rk2": ("state_mhd_lhlld", True, "lhlld", (16, 8, 8), (16, 8, 8), "rk2", 2, 3, 44, 0.8),
 }
 NGHOST = {"state_hydro_hllc_ng4": 4, "state_mhd_hlld_ng4": 4}
+# outflow physical boundaries on every face (bvals/cc/outflow_cc.cpp, bvals/fc/outflow_fc.cpp):
+# two blocks along x1, so the same-level exchange and the physical boundaries both act
+OUTFLOW = {"hydro_hllc_plm_vl2_outflow", "mhd_hlld_plm_vl2_outflow"}
+CASES["hydro_hllc_plm_vl2_outflow"] = ("state_hydro_hllc", False, "hllc", (16, 8, 8), (8, 8, 8),
+                                       "vl2", 2, 3, 51, 0.4)
+CASES["mhd_hlld_plm_vl2_outflow"] = ("state_mhd_hlld", True, "hlld", (16, 8, 8), (8, 8, 8),
+                                     "vl2", 2, 3, 52, 0.4)
 
 
 def make_case(name, spec):
     exe_cfg, mhd, solver, nx, mb, integ, xorder, ncyc, seed, cfl = spec
     exe = build_ref.build(exe_cfg)
     u, b1, b2, b3 = ol.smooth_random_state(nx, mhd, seed=seed)
+    bc = "outflow" if name in OUTFLOW else "periodic"
     out = ol.run_reference_state(exe, os.path.join(WORK, name), nx, mb, mhd, u, b1, b2, b3,
-                                 cfl=cfl, tlim=100.0, nlim=ncyc, xorder=xorder, integrator=integ)
+                                 cfl=cfl, tlim=100.0, nlim=ncyc, xorder=xorder, integrator=integ,
+                                 mesh_bc=bc)
     arrays = {"u_in": u, "u_out": out["u"]}
     if mhd:
         arrays.update(b1_in=b1, b2_in=b2, b3_in=b3, b1_out=out["b1"], b2_out=out["b2"],
@@ -61,7 +70,7 @@ def make_case(name, spec):
     meta = dict(mhd=mhd, solver=solver, nx=list(nx), meshblock=list(mb), integrator=integ,
                 xorder=xorder, ncycles=ncyc, seed=seed, cfl=cfl, gamma=5.0 / 3.0,
                 time=out["time"], dt=out["dt"], ncycle=out["ncycle"],
-                nghost=NGHOST.get(exe_cfg, 2))
+                nghost=NGHOST.get(exe_cfg, 2), bc=bc)
     np.savez_compressed(os.path.join(HERE, name + ".npz"), meta=json.dumps(meta), **arrays)
     print("wrote", name, "t=%.6g ncycle=%d" % (out["time"], out["ncycle"]))
 

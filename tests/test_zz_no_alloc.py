@@ -1,8 +1,8 @@
 """athg_block_cfl_dt_noalloc: the CFL time step of one block whose device arrays the
 caller owns, computed without any device allocation (scratch is a fixed device array in
-the library). It is for callers that cannot allocate device memory -- code running while
-a stream is captured into a CUDA graph, or hosts whose device memory is managed by their
-own pool. Its result must equal the pool entry point athg_new_block_dt on the same state.
+the library). It is for callers that cannot allocate device memory -- code that must not
+synchronise the device (cudaMalloc and cudaFree may), or hosts whose device memory is
+managed by their own pool. Its result must equal the pool entry point athg_new_block_dt on the same state.
 
 This file is collected last on purpose. It runs alone in a fresh process as well as after
 the other tests.
