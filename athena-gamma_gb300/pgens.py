@@ -271,6 +271,13 @@ def turbulent_box(nx, seed=20261203, mach=5.0, beta=1.0, gamma=1.0001, kmin=1, k
         e3 = np.exp(2j * np.pi * np.outer(kr, (np.arange(n3) + 0.5) / n3))
         t = np.einsum("cba,cz->zba", a, e3)                     # [n3, nk2, nk1]
         t = np.einsum("zba,by->zya", t, e2)                     # [n3, n2, nk1]
+        try:  # the last sum is the large one: on the GPU when there is one
+            import torch
+            if torch.cuda.is_available():
+                tt = torch.from_numpy(t).cuda()
+                return (tt @ torch.from_numpy(e1).cuda()).real.cpu().numpy()
+        except ImportError:
+            pass
         out = np.empty((n3, n2, n1))
         for z in range(n3):                                     # [n2, nk1] @ [nk1, n1]
             out[z] = np.real(t[z] @ e1)

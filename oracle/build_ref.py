@@ -74,6 +74,15 @@ CONFIGS = {
 FFT_BUILDS = {"turb_state_mhd_hlld", "turb_state_hydro_hllc", "fftgrav_state_hydro_hllc",
               "fftgrav_state_mhd_hlld"}
 SHIM = os.path.join(HERE, "harness", "fftw3")
+# the reference-side binding of the GB300 library (INTEGRATION.md's shim), compiled into the
+# reference against its own headers and linked with the in-tree libathena_gb300.so
+REPO = os.path.dirname(HERE)
+PKG = os.path.join(REPO, "athena-gamma_gb300")
+CONFIGS["shim_mhd_hlld"] = ("harness:shim_driver.cpp", "hlld", True, 2, 0, False, None)
+LINKED = {"shim_mhd_hlld": {
+    "srcs": [os.path.join(HERE, "harness", "gb300_shim.cpp")],
+    "inc": [os.path.join(REPO, "include")],
+    "ld": ["-L", PKG, "-lathena_gb300", "-Wl,-rpath," + PKG]}}
 
 
 def source_list(pgen):
@@ -154,6 +163,8 @@ def build(name, jobs=8, verbose=False):
     srcs = source_list(pgen)
     if fft:
         srcs.append(os.path.join(SHIM, "fftw3_dft.cpp"))
+    extra = LINKED.get(name, {})
+    srcs += extra.get("srcs", [])
     eos = os.path.join(REF, "src/eos", "adiabatic_mhd.cpp" if mhd else "adiabatic_hydro.cpp")
     srcs += [eos, os.path.join(REF, "src/eos/general/noop.cpp"),
              os.path.join(REF, "src/eos/eos_high_order.cpp"),
@@ -165,6 +176,8 @@ def build(name, jobs=8, verbose=False):
              "-I", os.path.join(inc, "a", "b"), "-I", os.path.join(inc, "a", "b", "c")]
     flags += ["-fopenmp"] if omp else []
     flags += ["-I", SHIM] if fft else []
+    for d in extra.get("inc", []):
+        flags += ["-I", d]
     if pgen.startswith("harness:"):
         flags += ["-I", os.path.join(REF, "src")]
     objdir = os.path.join(d, "obj")
@@ -185,7 +198,8 @@ def build(name, jobs=8, verbose=False):
     with cf.ThreadPoolExecutor(jobs) as ex:
         objs = list(ex.map(one, srcs))
     if (not os.path.exists(exe)) or any(os.path.getmtime(o) > os.path.getmtime(exe) for o in objs):
-        r = subprocess.run(["g++"] + flags + ["-o", exe] + objs, capture_output=True, text=True)
+        r = subprocess.run(["g++"] + flags + ["-o", exe] + objs + extra.get("ld", []),
+                           capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("link failed:\n" + r.stderr[-3000:])
     if verbose:
