@@ -706,11 +706,10 @@ struct athg_mg {
   int iterations = 0;
   double last_norm = 0.0;
   // one captured cycle per colour-offset parity (the kernels take colour ^ offset); the
-  // multipole coefficients are kernel arguments, so a new expansion invalidates them
+  // multipole boundaries read the face tables, rewritten in place by every new expansion,
+  // so the captured cycles stay valid from solve to solve
   cudaGraph_t cyc_graph[2] = {nullptr, nullptr};
   cudaGraphExec_t cyc_exec[2] = {nullptr, nullptr};
-  int cyc_mp[2] = {-1, -1};
-  int mp_version = 0;
 };
 
 namespace {
@@ -959,7 +958,6 @@ int multipole_setup(athg_mg* m) {
   for (int q = 0; q < 25; ++q) m->mp.c[q] = q < nc ? mm[q] * sc[q] : 0.0;
   for (int d = 0; d < 3; ++d) m->mp.o[d] = origin[d];
   m->mp.order = c.mporder;
-  ++m->mp_version;
   RC(tabulate_multipole(m, m->h64));
   if (m->cfg.precision == ATHG_MIXED) RC(tabulate_multipole(m, m->h32));
   return ATHG_OK;
@@ -1000,11 +998,7 @@ int cycle(athg_mg* m) {
   const bool mixed = m->cfg.precision == ATHG_MIXED;
   int& coff = mixed ? m->coffset32 : m->coffset;
   const int par = coff & 1;
-  if (!m->cyc_exec[par] || m->cyc_mp[par] != m->mp_version) {
-    if (m->cyc_exec[par]) cudaGraphExecDestroy(m->cyc_exec[par]);
-    if (m->cyc_graph[par]) cudaGraphDestroy(m->cyc_graph[par]);
-    m->cyc_exec[par] = nullptr;
-    m->cyc_graph[par] = nullptr;
+  if (!m->cyc_exec[par]) {
     const int c32 = m->coffset32, c64 = m->coffset;
     MCK(cudaStreamBeginCapture(m->st, cudaStreamCaptureModeThreadLocal));
     int rc = one_cycle(m);
@@ -1019,7 +1013,6 @@ int cycle(athg_mg* m) {
     if (e != cudaSuccess) return mgfail(ATHG_ERR_CUDA, "multigrid cycle capture failed");
     m->cyc_graph[par] = gr;
     MCK(cudaGraphInstantiate(&m->cyc_exec[par], gr, 0));
-    m->cyc_mp[par] = m->mp_version;
   }
   MCK(cudaGraphLaunch(m->cyc_exec[par], m->st));
   coff ^= 1;  // what the captured cycle did to the host-side colour offset
