@@ -461,8 +461,15 @@ __global__ void __launch_bounds__(128) k_corner_emf(Geom g, StagePtrs<T> p, Box 
   const T* w = p.w + (int64_t)b * NHYD * nc;
   const T* bc = p.bcc + (int64_t)b * 3 * nc;
   const T* ce = kMixed<T> ? p.cce + (int64_t)b * 3 * nc : nullptr;
-  auto cce = [&](int n, int kk, int jj, int ii) -> T {
-    int64_t c = cidx(g, kk, jj, ii);
+  // Every value sits at this corner's index or one below it along some axes: the
+  // accessors take those offsets (0 or -1 per axis), so each load is a base pointer plus
+  // a stride combination formed once, not a fresh 64-bit index polynomial.
+  const int64_t c0 = cidx(g, k, j, i), q1 = f1idx(g, k, j, i), q2 = f2idx(g, k, j, i);
+  const int64_t jc = g.nc1, kc = (int64_t)g.nc1 * g.nc2;             // cells, x3 faces
+  const int64_t j1 = g.nc1 + 1, k1 = (int64_t)(g.nc1 + 1) * g.nc2;   // x1 faces
+  const int64_t j2 = g.nc1, k2 = (int64_t)g.nc1 * (g.nc2 + 1);       // x2 faces
+  auto cce = [&](int n, int dk, int dj, int di) -> T {
+    const int64_t c = c0 + dk * kc + dj * jc + di;
     if constexpr (kMixed<T>) return ce[n * nc + c];
     T vx = w[IVX * nc + c], vy = w[IVY * nc + c], vz = w[IVZ * nc + c];
     T bx1 = bc[c], by1 = bc[nc + c], bz1 = bc[2 * nc + c];
@@ -471,57 +478,60 @@ __global__ void __launch_bounds__(128) k_corner_emf(Geom g, StagePtrs<T> p, Box 
     return vy * bx1 - vx * by1;
   };
   const int64_t n1 = g.nf1, n2 = g.nf2, n3 = g.nf3;
-  const T* F1 = p.flx[0] + (int64_t)b * 8 * n1;
-  const T* F2 = p.flx[1] + (int64_t)b * 8 * n2;
-  const T* F3 = p.flx[2] + (int64_t)b * 8 * n3;
+  const T* F1 = p.flx[0] + (int64_t)b * 8 * n1 + q1;
+  const T* F2 = p.flx[1] + (int64_t)b * 8 * n2 + q2;
+  const T* F3 = p.flx[2] + (int64_t)b * 8 * n3 + c0;
   // face EMFs: x1 faces carry (e3, e2), x2 faces (e1, e3), x3 faces (e2, e1)
-  auto e3x1 = [&](int kk, int jj, int ii) { return F1[5 * n1 + f1idx(g, kk, jj, ii)]; };
-  auto e2x1 = [&](int kk, int jj, int ii) { return F1[6 * n1 + f1idx(g, kk, jj, ii)]; };
-  auto wx1 = [&](int kk, int jj, int ii) { return F1[7 * n1 + f1idx(g, kk, jj, ii)]; };
-  auto e1x2 = [&](int kk, int jj, int ii) { return F2[5 * n2 + f2idx(g, kk, jj, ii)]; };
-  auto e3x2 = [&](int kk, int jj, int ii) { return F2[6 * n2 + f2idx(g, kk, jj, ii)]; };
-  auto wx2 = [&](int kk, int jj, int ii) { return F2[7 * n2 + f2idx(g, kk, jj, ii)]; };
-  auto e2x3 = [&](int kk, int jj, int ii) { return F3[5 * n3 + f3idx(g, kk, jj, ii)]; };
-  auto e1x3 = [&](int kk, int jj, int ii) { return F3[6 * n3 + f3idx(g, kk, jj, ii)]; };
-  auto wx3 = [&](int kk, int jj, int ii) { return F3[7 * n3 + f3idx(g, kk, jj, ii)]; };
+  auto o1 = [&](int dk, int dj, int di) { return dk * k1 + dj * j1 + di; };
+  auto o2 = [&](int dk, int dj, int di) { return dk * k2 + dj * j2 + di; };
+  auto o3 = [&](int dk, int dj, int di) { return dk * kc + dj * jc + di; };
+  auto e3x1 = [&](int dk, int dj, int di) { return F1[5 * n1 + o1(dk, dj, di)]; };
+  auto e2x1 = [&](int dk, int dj, int di) { return F1[6 * n1 + o1(dk, dj, di)]; };
+  auto wx1 = [&](int dk, int dj, int di) { return F1[7 * n1 + o1(dk, dj, di)]; };
+  auto e1x2 = [&](int dk, int dj, int di) { return F2[5 * n2 + o2(dk, dj, di)]; };
+  auto e3x2 = [&](int dk, int dj, int di) { return F2[6 * n2 + o2(dk, dj, di)]; };
+  auto wx2 = [&](int dk, int dj, int di) { return F2[7 * n2 + o2(dk, dj, di)]; };
+  auto e2x3 = [&](int dk, int dj, int di) { return F3[5 * n3 + o3(dk, dj, di)]; };
+  auto e1x3 = [&](int dk, int dj, int di) { return F3[6 * n3 + o3(dk, dj, di)]; };
+  auto wx3 = [&](int dk, int dj, int di) { return F3[7 * n3 + o3(dk, dj, di)]; };
   const T one = T(1.0), q = T(0.25);
   T* E = p.edge + (int64_t)b * 3 * g.ne;
   const int64_t ei = eidx(g, k, j, i);
   {
-    T de1_l3 = (one - wx2(k - 1, j, i)) * (e1x3(k, j, i) - cce(0, k - 1, j, i)) +
-               (wx2(k - 1, j, i)) * (e1x3(k, j - 1, i) - cce(0, k - 1, j - 1, i));
-    T de1_r3 = (one - wx2(k, j, i)) * (e1x3(k, j, i) - cce(0, k, j, i)) +
-               (wx2(k, j, i)) * (e1x3(k, j - 1, i) - cce(0, k, j - 1, i));
-    T de1_l2 = (one - wx3(k, j - 1, i)) * (e1x2(k, j, i) - cce(0, k, j - 1, i)) +
-               (wx3(k, j - 1, i)) * (e1x2(k - 1, j, i) - cce(0, k - 1, j - 1, i));
-    T de1_r2 = (one - wx3(k, j, i)) * (e1x2(k, j, i) - cce(0, k, j, i)) +
-               (wx3(k, j, i)) * (e1x2(k - 1, j, i) - cce(0, k - 1, j, i));
-    E[ei] = q * (de1_l3 + de1_r3 + de1_l2 + de1_r2 + e1x2(k - 1, j, i) +
-                 e1x2(k, j, i) + e1x3(k, j - 1, i) + e1x3(k, j, i));
+    T de1_l3 = (one - wx2(-1, 0, 0)) * (e1x3(0, 0, 0) - cce(0, -1, 0, 0)) +
+               (wx2(-1, 0, 0)) * (e1x3(0, -1, 0) - cce(0, -1, -1, 0));
+    T de1_r3 = (one - wx2(0, 0, 0)) * (e1x3(0, 0, 0) - cce(0, 0, 0, 0)) +
+               (wx2(0, 0, 0)) * (e1x3(0, -1, 0) - cce(0, 0, -1, 0));
+    T de1_l2 = (one - wx3(0, -1, 0)) * (e1x2(0, 0, 0) - cce(0, 0, -1, 0)) +
+               (wx3(0, -1, 0)) * (e1x2(-1, 0, 0) - cce(0, -1, -1, 0));
+    T de1_r2 = (one - wx3(0, 0, 0)) * (e1x2(0, 0, 0) - cce(0, 0, 0, 0)) +
+               (wx3(0, 0, 0)) * (e1x2(-1, 0, 0) - cce(0, -1, 0, 0));
+    E[ei] = q * (de1_l3 + de1_r3 + de1_l2 + de1_r2 + e1x2(-1, 0, 0) +
+                 e1x2(0, 0, 0) + e1x3(0, -1, 0) + e1x3(0, 0, 0));
   }
   {
-    T de2_l3 = (one - wx1(k - 1, j, i)) * (e2x3(k, j, i) - cce(1, k - 1, j, i)) +
-               (wx1(k - 1, j, i)) * (e2x3(k, j, i - 1) - cce(1, k - 1, j, i - 1));
-    T de2_r3 = (one - wx1(k, j, i)) * (e2x3(k, j, i) - cce(1, k, j, i)) +
-               (wx1(k, j, i)) * (e2x3(k, j, i - 1) - cce(1, k, j, i - 1));
-    T de2_l1 = (one - wx3(k, j, i - 1)) * (e2x1(k, j, i) - cce(1, k, j, i - 1)) +
-               (wx3(k, j, i - 1)) * (e2x1(k - 1, j, i) - cce(1, k - 1, j, i - 1));
-    T de2_r1 = (one - wx3(k, j, i)) * (e2x1(k, j, i) - cce(1, k, j, i)) +
-               (wx3(k, j, i)) * (e2x1(k - 1, j, i) - cce(1, k - 1, j, i));
-    E[g.ne + ei] = q * (de2_l3 + de2_r3 + de2_l1 + de2_r1 + e2x3(k, j, i - 1) +
-                        e2x3(k, j, i) + e2x1(k - 1, j, i) + e2x1(k, j, i));
+    T de2_l3 = (one - wx1(-1, 0, 0)) * (e2x3(0, 0, 0) - cce(1, -1, 0, 0)) +
+               (wx1(-1, 0, 0)) * (e2x3(0, 0, -1) - cce(1, -1, 0, -1));
+    T de2_r3 = (one - wx1(0, 0, 0)) * (e2x3(0, 0, 0) - cce(1, 0, 0, 0)) +
+               (wx1(0, 0, 0)) * (e2x3(0, 0, -1) - cce(1, 0, 0, -1));
+    T de2_l1 = (one - wx3(0, 0, -1)) * (e2x1(0, 0, 0) - cce(1, 0, 0, -1)) +
+               (wx3(0, 0, -1)) * (e2x1(-1, 0, 0) - cce(1, -1, 0, -1));
+    T de2_r1 = (one - wx3(0, 0, 0)) * (e2x1(0, 0, 0) - cce(1, 0, 0, 0)) +
+               (wx3(0, 0, 0)) * (e2x1(-1, 0, 0) - cce(1, -1, 0, 0));
+    E[g.ne + ei] = q * (de2_l3 + de2_r3 + de2_l1 + de2_r1 + e2x3(0, 0, -1) +
+                        e2x3(0, 0, 0) + e2x1(-1, 0, 0) + e2x1(0, 0, 0));
   }
   {
-    T de3_l2 = (one - wx1(k, j - 1, i)) * (e3x2(k, j, i) - cce(2, k, j - 1, i)) +
-               (wx1(k, j - 1, i)) * (e3x2(k, j, i - 1) - cce(2, k, j - 1, i - 1));
-    T de3_r2 = (one - wx1(k, j, i)) * (e3x2(k, j, i) - cce(2, k, j, i)) +
-               (wx1(k, j, i)) * (e3x2(k, j, i - 1) - cce(2, k, j, i - 1));
-    T de3_l1 = (one - wx2(k, j, i - 1)) * (e3x1(k, j, i) - cce(2, k, j, i - 1)) +
-               (wx2(k, j, i - 1)) * (e3x1(k, j - 1, i) - cce(2, k, j - 1, i - 1));
-    T de3_r1 = (one - wx2(k, j, i)) * (e3x1(k, j, i) - cce(2, k, j, i)) +
-               (wx2(k, j, i)) * (e3x1(k, j - 1, i) - cce(2, k, j - 1, i));
-    E[2 * g.ne + ei] = q * (de3_l1 + de3_r1 + de3_l2 + de3_r2 + e3x2(k, j, i - 1) +
-                            e3x2(k, j, i) + e3x1(k, j - 1, i) + e3x1(k, j, i));
+    T de3_l2 = (one - wx1(0, -1, 0)) * (e3x2(0, 0, 0) - cce(2, 0, -1, 0)) +
+               (wx1(0, -1, 0)) * (e3x2(0, 0, -1) - cce(2, 0, -1, -1));
+    T de3_r2 = (one - wx1(0, 0, 0)) * (e3x2(0, 0, 0) - cce(2, 0, 0, 0)) +
+               (wx1(0, 0, 0)) * (e3x2(0, 0, -1) - cce(2, 0, 0, -1));
+    T de3_l1 = (one - wx2(0, 0, -1)) * (e3x1(0, 0, 0) - cce(2, 0, 0, -1)) +
+               (wx2(0, 0, -1)) * (e3x1(0, -1, 0) - cce(2, 0, -1, -1));
+    T de3_r1 = (one - wx2(0, 0, 0)) * (e3x1(0, 0, 0) - cce(2, 0, 0, 0)) +
+               (wx2(0, 0, 0)) * (e3x1(0, -1, 0) - cce(2, 0, -1, 0));
+    E[2 * g.ne + ei] = q * (de3_l1 + de3_r1 + de3_l2 + de3_r2 + e3x2(0, 0, -1) +
+                            e3x2(0, 0, 0) + e3x1(0, -1, 0) + e3x1(0, 0, 0));
   }
 }
 

@@ -18,8 +18,10 @@ run. Instead this script
 3. optionally adds a harness problem generator from ``oracle/harness/``
    (own code) in place of a reference ``src/pgen/*.cpp``.
 
-``oracle/_ref/`` is git-ignored. The reference tree is only present in the
-development container, so this runs there (``build()`` skips it elsewhere).
+``oracle/_ref/`` is git-ignored. The reference tree is read from the directory
+named by the environment variable ``ATHG_REFERENCE`` (default: the development
+container's checkout). It is only present in the development container, so this
+runs there (``build()`` skips it elsewhere).
 """
 import argparse
 import concurrent.futures as cf
