@@ -96,7 +96,9 @@ struct ff {
 // Split binary64 x into hi = x rounded to binary32 and lo ~ x - hi, on the integer pipe:
 // the 29 mantissa bits that rounding drops become a signed integer r, |r| <= 2^28, kept
 // to 22 bits and scaled by the exponent. |x| outside [2^-80, 2^120]: lo = 0.
-ATHG_HD ff split_ff(double x) {
+// split_ff_general handles every input; split_ff below takes a short path for the usual
+// range and gives the same bits.
+ATHG_HD ff split_ff_general(double x) {
   // the rounding of d2f_int, and its remainder, on the 32-bit halves
   const uint64_t b = bits_d(x);
   const uint32_t hi32 = (uint32_t)(b >> 32), lo32 = (uint32_t)b;
@@ -122,6 +124,27 @@ ATHG_HD ff split_ff(double x) {
   const bool ok = se > 0 && se < 255 && ed >= 943u && ed <= 1143u;
   const float scale = from_bits_f((uint32_t)(ok ? se : 1) << 23);
   const float lo = ok ? q * scale : 0.0f;
+  o.lo = s ? -lo : lo;
+  return o;
+}
+
+ATHG_HD ff split_ff(double x) {
+  const uint64_t b = bits_d(x);
+  const uint32_t hi32 = (uint32_t)(b >> 32), lo32 = (uint32_t)b;
+  const uint32_t a = hi32 & 0x7fffffffu;
+  // 2^-80 <= |x| < 2^120 (binary64 exponent 943..1142): hi is a normal binary32 whatever
+  // the rounding, and the remainder's scale is a normal binary32 too
+  if (a - 0x3af00000u >= 0x0c800000u) return split_ff_general(x);
+  // exponent rebiased and the 23 kept mantissa bits, in one word
+  const uint32_t m = ((a - 0x38000000u) << 3) | (lo32 >> 29);
+  const uint32_t rb = lo32 & 0x1fffffffu;
+  const uint32_t up = (rb > 0x10000000u || (rb == 0x10000000u && (m & 1u))) ? 1u : 0u;
+  const uint32_t s = hi32 & 0x80000000u;
+  ff o;
+  o.hi = from_bits_f(s | (m + up));
+  const int32_t r = (int32_t)rb - (int32_t)(up << 29);
+  const float q = from_bits_f(0x4b400000u + (uint32_t)(r >> 6)) - 12582912.0f;
+  const float lo = q * from_bits_f(((a >> 20) - 942u) << 23);
   o.lo = s ? -lo : lo;
   return o;
 }

@@ -124,6 +124,23 @@ int main(int argc, char** argv) {
     double ep = (double)(std::fabs((long double)pp.hi + pp.lo - pex) / (gm1 * (long double)E));
     if (ep > worst_p) worst_p = ep;
   }
+  // the short path of split_ff gives the general routine's bits: random patterns across
+  // every exponent, and the edges of its range (zeros, subnormals, infinities, NaNs and
+  // the binary64 exponents 942..943 and 1142..1143 around 2^-80 and 2^120)
+  for (long t = 0; t < n; ++t) {
+    uint64_t u = rng();
+    if (t % 3 == 1) {  // exponent near the range edges
+      static const uint64_t eds[] = {0, 1, 941, 942, 943, 944, 1141, 1142, 1143, 1144, 2046, 2047};
+      u = (u & 0x800fffffffffffffull) | (eds[rng() % 12] << 52);
+    } else if (t % 3 == 2) {  // mantissas with ties and near-ties at the 29 dropped bits
+      const uint64_t tail = (rng() & 3) == 0 ? 0x10000000ull : (rng() & 0x1fffffffull);
+      u = (u & ~0x1fffffffull) | tail;
+    }
+    const double x = from_bits_d(u);
+    const ff a = split_ff(x), g = split_ff_general(x);
+    CHECK(bits_f(a.hi) == bits_f(g.hi) && bits_f(a.lo) == bits_f(g.lo),
+          "split short path %016llx", (unsigned long long)u);
+  }
   CHECK(worst_split <= std::ldexp(1.0, -45), "split error %g", worst_split);
   CHECK(worst_p <= std::ldexp(1.0, -42), "pressure error %g", worst_p);
   std::printf("split=%.3g pressure(rel. to (g-1)E)=%.3g\n", worst_split, worst_p);
