@@ -547,8 +547,13 @@ __global__ void k_defect_sq(const double* u, const double* src, int n, double id
   block_add<1>(v, out);
 }
 
-// FP64 defect of the FP64 solution, narrowed to the FP32 correction source
-__global__ void k_defect_to32(const double* u, const double* src, int n, double idx2, float* r32) {
+// Defect of the FP64 solution, narrowed to the FP32 correction source (mixed path only).
+// FP64 issues at 1/64 of the FP32 rate here, so the seven-point sum is formed exactly in
+// 64-bit integers (athg::lap7_ff, more accurate than six FP64 roundings) and scaled and
+// added to the source in double-float arithmetic; values outside the integer form's range
+// (or not finite) take the FP64 formula.
+__global__ void k_defect_to32(const double* u, const double* src, int n, double idx2,
+                              float idx2_hi, float idx2_lo, float* r32) {
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= (long long)n * n * n) return;
   int i = (int)(t % n) + 1;
@@ -556,10 +561,17 @@ __global__ void k_defect_to32(const double* u, const double* src, int n, double 
   int j = (int)(r % n) + 1, k = (int)(r / n) + 1;
   const int nt = n + 2;
   const long long q = ix(nt, k, j, i), sk = (long long)nt * nt, sj = nt;
-  // mixed path only: FP64 is 1/64 of the FP32 rate here, so the defect is formed with
-  // fused operations (7 FP64 instructions) and converted on the integer pipe
-  const double s = ((u[q + sk] + u[q - sk]) + (u[q + sj] + u[q - sj])) + (u[q + 1] + u[q - 1]);
-  r32[q] = athg::d2f_int(fma(fma(6.0, u[q], -s), idx2, src[q]));
+  const double c = u[q];
+  const double nb[6] = {u[q + sk], u[q - sk], u[q + sj], u[q - sj], u[q + 1], u[q - 1]};
+  athg::ff lap;
+  if (athg::lap7_ff(c, nb, lap)) {
+    const athg::ff d = athg::ff_add(athg::ff_mul(lap, athg::ff{idx2_hi, idx2_lo}),
+                                    athg::split_ff(src[q]));
+    r32[q] = athg::ff_f(d);
+  } else {
+    const double s = ((nb[0] + nb[1]) + (nb[2] + nb[3])) + (nb[4] + nb[5]);
+    r32[q] = athg::d2f_int(fma(fma(6.0, c, -s), idx2, src[q]));
+  }
 }
 
 __global__ void k_add_correction(double* u, const float* e, long long cnt) {
@@ -971,8 +983,10 @@ int refine_once(athg_mg* m) {
   const int top = h.nl - 1, n = h.n[top];
   RC(apply_bc(m, H, top, false));
   const double dx = H.dx[top];
-  k_defect_to32<<<nblk((long long)n * n * n), TPB, 0, m->st>>>(H.u[top], H.src[top], n,
-                                                               1.0 / (dx * dx), h.src[top]);
+  const double idx2 = 1.0 / (dx * dx);
+  const float idx2_hi = (float)idx2, idx2_lo = (float)(idx2 - (double)idx2_hi);
+  k_defect_to32<<<nblk((long long)n * n * n), TPB, 0, m->st>>>(H.u[top], H.src[top], n, idx2,
+                                                               idx2_hi, idx2_lo, h.src[top]);
   MCKL();
   MCK(cudaMemsetAsync(h.u[top], 0, h.cells(top) * sizeof(float), m->st));
   RC(vcycle(m, h, top, false, true, m->subtract, m->coffset32));

@@ -213,4 +213,42 @@ ATHG_HD float ff_f(ff a) { return a.hi + a.lo; }
 // a > b for double-float values (normalised: |lo| <= ulp(hi) / 2)
 ATHG_HD bool ff_gt(ff a, ff b) { return a.hi > b.hi || (a.hi == b.hi && a.lo > b.lo); }
 
+// 6 c - (n[0] + ... + n[5]) of seven binary64 values, as a double-float pair, without FP64
+// instructions. Each value becomes a 64-bit integer in units of 2^(emax - 1081), emax the
+// largest of the seven binary64 exponents, so the largest mantissa sits below bit 59; a
+// value loses only the bits below that unit (at most 2^-58 of the largest |value|). The
+// seven-point sum is then exact in the integer (|sum| < 1.5 * 2^62) and is rounded once
+// into hi + lo (|error| <= about 2^-47 |sum|), where FP64 would round after each of six
+// operations. Returns false, with out untouched, for values that are not finite or whose
+// scale falls outside [2^-126, 2^64] (|c| and |n| roughly outside [2^-68, 2^122]); the
+// caller then takes FP64.
+ATHG_HD bool lap7_ff(double c, const double* n, ff& out) {
+  uint64_t b[7];
+  b[0] = bits_d(c);
+  for (int q = 0; q < 6; ++q) b[q + 1] = bits_d(n[q]);
+  int ex[7];
+  int emax = 1;
+  for (int q = 0; q < 7; ++q) {
+    const int e = (int)((b[q] >> 52) & 0x7ffu);
+    ex[q] = e ? e : 1;  // subnormals: the exponent of the smallest normals
+    emax = ex[q] > emax ? ex[q] : emax;
+  }
+  if (emax < 955 || emax > 1145) return false;  // also excludes infinities and NaNs
+  int64_t x[7];
+  for (int q = 0; q < 7; ++q) {
+    const uint64_t mant = (b[q] & 0x000fffffffffffffull) |
+                          (((b[q] >> 52) & 0x7ffu) ? 0x0010000000000000ull : 0ull);
+    const int sh = emax - ex[q];
+    const uint64_t m = sh < 64 ? ((mant << 6) >> sh) : 0ull;
+    x[q] = (b[q] >> 63) ? -(int64_t)m : (int64_t)m;
+  }
+  const int64_t sum = 6 * x[0] - (((x[1] + x[2]) + (x[3] + x[4])) + (x[5] + x[6]));
+  const float hi = (float)sum;                        // rounded to nearest
+  const float lo = (float)(sum - (int64_t)hi);        // the remainder, |.| <= 2^38
+  const float scale = from_bits_f((uint32_t)(emax - 1081 + 127) << 23);
+  out.hi = hi * scale;
+  out.lo = lo * scale;
+  return true;
+}
+
 }  // namespace athg

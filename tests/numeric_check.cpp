@@ -141,6 +141,49 @@ int main(int argc, char** argv) {
     CHECK(bits_f(a.hi) == bits_f(g.hi) && bits_f(a.lo) == bits_f(g.lo),
           "split short path %016llx", (unsigned long long)u);
   }
+  // seven-point sum 6c - sum(n) in 64-bit integers: smooth fields (neighbours within a
+  // few percent of the centre, the multigrid's case, where FP64 cancels most digits),
+  // independent values over many exponents, zeros and sign changes; against long double
+  double worst_lap = 0.0;
+  std::uniform_int_distribution<int> ex2(-60, 60);
+  for (long t = 0; t < n / 4; ++t) {
+    const int kind = (int)(t % 3);
+    const double c = std::ldexp(0.5 + ud01(rng), ex2(rng)) * ((rng() & 1) ? 1 : -1);
+    double nb[6];
+    for (int q = 0; q < 6; ++q) {
+      if (kind == 0) nb[q] = c * (1.0 + 0.05 * (ud01(rng) - 0.5));
+      else if (kind == 1) nb[q] = std::ldexp(0.5 + ud01(rng), ex2(rng)) * ((rng() & 1) ? 1 : -1);
+      else nb[q] = (q == (int)(rng() % 6)) ? 0.0 : c * (ud01(rng) - 0.5);
+    }
+    ff L;
+    const bool ok = lap7_ff(c, nb, L);
+    CHECK(ok, "lap7 refused %a", c);
+    if (!ok) continue;
+    long double ex = 6.0L * c, mag = 6.0L * std::fabs((long double)c), mx = std::fabs((long double)c);
+    for (int q = 0; q < 6; ++q) {
+      ex -= nb[q];
+      mag += std::fabs((long double)nb[q]);
+      if (std::fabs((long double)nb[q]) > mx) mx = std::fabs((long double)nb[q]);
+    }
+    const long double err = std::fabs((long double)L.hi + L.lo - ex);
+    const long double bound = std::ldexp(1.0L, -46) * std::fabs(ex) + std::ldexp(1.0L, -54) * mx;
+    CHECK(err <= bound, "lap7 error %Lg bound %Lg (c %a)", err, bound, c);
+    const double rel = (double)(err / mag);
+    if (rel > worst_lap) worst_lap = rel;
+  }
+  {
+    const double inf = INFINITY, nan = NAN, z6[6] = {0, 0, 0, 0, 0, 0};
+    const double in6[6] = {1.0, 1.0, inf, 1.0, 1.0, 1.0}, nn6[6] = {1.0, nan, 1.0, 1.0, 1.0, 1.0};
+    ff L = {7.0f, 7.0f};
+    CHECK(!lap7_ff(1.0, in6, L) && !lap7_ff(1.0, nn6, L) && !lap7_ff(0.0, z6, L) &&
+              !lap7_ff(1e-30, z6, L) && !lap7_ff(1e40, z6, L) && L.hi == 7.0f,
+          "lap7 outside its range must refuse and leave the result");
+    const double small = 1e-20;
+    CHECK(lap7_ff(small, z6, L) &&
+              std::fabs((long double)L.hi + L.lo - 6.0L * small) <= std::ldexp(6.0L * small, -46),
+          "lap7 small");
+  }
+  std::printf("lap7 worst error / (6|c| + sum|n|) = %.3g\n", worst_lap);
   CHECK(worst_split <= std::ldexp(1.0, -45), "split error %g", worst_split);
   CHECK(worst_p <= std::ldexp(1.0, -42), "pressure error %g", worst_p);
   std::printf("split=%.3g pressure(rel. to (g-1)E)=%.3g\n", worst_split, worst_p);
