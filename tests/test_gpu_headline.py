@@ -77,3 +77,18 @@ def test_headline_mixed_close_to_oracle(reference_state):
         err = float(np.abs(out[k] - ref[k]).max()) / scale
         assert err < 2e-6, (k, err)
     assert divb < 1e-13
+
+
+def test_headline_dfloat_matches_oracle(reference_state):
+    """The double-float flux path (FP64 state, fluxes and EMFs in FP32 pairs) at the
+    headline size: within 1e-11 of the oracle, like the single-block fixtures."""
+    init, ref, t_ref = reference_state
+    out, (t, _, n), divb = _gpu_run(init, "dfloat")
+    assert n == CYCLES
+    assert abs(t - t_ref) <= 1e-12 * t_ref, (t, t_ref)
+    bmax = max(float(np.abs(ref[k]).max()) for k in ("b1", "b2", "b3"))
+    for k in ("u", "b1", "b2", "b3"):
+        scale = float(np.abs(ref[k]).max()) if k == "u" else bmax
+        err = float(np.abs(out[k] - ref[k]).max()) / scale
+        assert err < 1e-11, (k, err)
+    assert divb < 1e-13
