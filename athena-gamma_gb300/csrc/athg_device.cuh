@@ -520,6 +520,154 @@ __device__ __forceinline__ void rs_hlld(const T* wli, const T* wri, T bxi, T gam
   }
 }
 
+// ---- HLLD for the FP32 flux path on packed FP32 instructions ---------------------------
+// Blackwell issues two FP32 additions, multiplications or FMAs per instruction on float2
+// operands (__fadd2_rn, __fmul2_rn, __ffma2_rn; each lane rounds as the scalar operation
+// does). Most of HLLD is the same arithmetic on the left and right states, so here lane x
+// carries the left state and lane y the right one, and the L/R-symmetric parts (the
+// conserved states, fast speeds, outer fluxes, single- and double-star states) take half
+// the issue slots. Divisions and square roots stay scalar; the few L-R mixed expressions
+// (the contact speed, the double-star averages) are scalar too. Same formulas as rs_hlld
+// above (hydro/rsolvers/mhd/hlld.cpp:56-371); the results agree to FP32 rounding (the FP32
+// flux path's tolerance), not bit for bit, because products that the scalar code rounds
+// separately may be fused here.
+namespace pk {
+__device__ __forceinline__ float2 S(float s) { return make_float2(s, s); }
+__device__ __forceinline__ float2 P(float l, float r) { return make_float2(l, r); }
+__device__ __forceinline__ float2 add(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 mul(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+// a - b, rounded once (b times -1 is exact)
+__device__ __forceinline__ float2 sub(float2 a, float2 b) { return __ffma2_rn(b, S(-1.0f), a); }
+__device__ __forceinline__ float2 rcp(float2 a) { return make_float2(1.0f / a.x, 1.0f / a.y); }
+__device__ __forceinline__ float2 sqrt2(float2 a) { return make_float2(sqrtf(a.x), sqrtf(a.y)); }
+__device__ __forceinline__ float2 sel(bool l, bool r, float2 a, float2 b) {
+  return make_float2(l ? a.x : b.x, r ? a.y : b.y);
+}
+}  // namespace pk
+
+template <>
+__device__ __forceinline__ void rs_hlld<float>(const float* wli, const float* wri, float bxi,
+                                               float gamma, float* flxi) {
+  using namespace pk;
+  const float SMALLN = 1.0e-8f;
+  const float igm1 = 1.0f / (gamma - 1.0f);
+  const float bxsq = bxi * bxi;
+  const float2 d = P(wli[IDN], wri[IDN]), vx = P(wli[IVX], wri[IVX]),
+               vy = P(wli[IVY], wri[IVY]), vz = P(wli[IVZ], wri[IVZ]),
+               p = P(wli[IPR], wri[IPR]), by = P(wli[IBY], wri[IBY]), bz = P(wli[IBZ], wri[IBZ]);
+  // magnetic and kinetic energy densities, conserved states
+  const float2 bt2 = fma(by, by, mul(bz, bz));
+  const float2 pb = mul(S(0.5f), add(S(bxsq), bt2));
+  const float2 ke = mul(mul(S(0.5f), d), fma(vx, vx, fma(vy, vy, mul(vz, vz))));
+  const float2 umx = mul(vx, d), umy = mul(vy, d), umz = mul(vz, d);
+  const float2 ue = add(fma(p, S(igm1), ke), pb);
+  // fast magnetosonic speeds (fast_speed)
+  const float2 asq = mul(S(gamma), p);
+  const float2 qsq = add(add(S(bxsq), bt2), asq);
+  const float2 tmq = sub(add(S(bxsq), bt2), asq);
+  const float2 disc = sqrt2(fma(tmq, tmq, mul(S(4.0f), mul(asq, bt2))));
+  const float2 cf2 = mul(S(0.5f), add(qsq, disc));
+  const float2 cf = sqrt2(P(cf2.x / d.x, cf2.y / d.y));
+  const float2 vm = sub(vx, cf), vp = add(vx, cf);
+  const float spd0 = mn(vm.x, vm.y), spd4 = mx(vp.x, vp.y);
+  const float2 pt = add(p, pb);
+  // outer fluxes F(U_L), F(U_R)
+  const float2 nbx = S(-bxi);
+  const float2 fmx = add(fma(umx, vx, pt), S(-bxsq));
+  const float2 fmy = fma(umy, vx, mul(nbx, by));
+  const float2 fmz = fma(umz, vx, mul(nbx, bz));
+  const float2 fe = fma(vx, add(add(ue, pt), S(-bxsq)), mul(nbx, fma(vy, by, mul(vz, bz))));
+  const float2 fby = fma(by, vx, mul(nbx, vy));
+  const float2 fbz = fma(bz, vx, mul(nbx, vz));
+  // contact speed (L-R mixed: scalar)
+  const float2 sd = sub(P(spd0, spd4), vx);  // (sdl, sdr)
+  const float spd2 = (sd.y * umx.y - sd.x * umx.x + (pt.x - pt.y)) / (sd.y * d.y - sd.x * d.x);
+  const float2 sdm = sub(P(spd0, spd4), S(spd2));
+  const float2 sdm_inv = rcp(sdm);
+  // single-star states
+  const float2 dsd = mul(d, sd);
+  const float2 std_ = mul(dsd, sdm_inv);  // rho*
+  const float2 std_inv = rcp(std_);
+  const float2 sqrtd = sqrt2(std_);
+  const float abx = fabsf(bxi);
+  const float spd1 = spd2 - abx / sqrtd.x;
+  const float spd3 = spd2 + abx / sqrtd.y;
+  const float2 ptstlr = fma(dsd, sub(S(spd2), vx), pt);
+  const float ptst = 0.5f * (ptstlr.y + ptstlr.x);
+  const float2 stmx = mul(std_, S(spd2));
+  const float2 den = add(mul(dsd, sdm), S(-bxsq));
+  const bool degl = fabsf(den.x) < SMALLN * ptst, degr = fabsf(den.y) < SMALLN * ptst;
+  const float2 iden = rcp(den);
+  const float2 tmp1 = mul(mul(S(bxi), sub(sd, sdm)), iden);
+  const float2 tmp2 = mul(add(mul(dsd, sd), S(-bxsq)), iden);
+  const float2 stmy = sel(degl, degr, mul(std_, vy), mul(std_, sub(vy, mul(by, tmp1))));
+  const float2 stmz = sel(degl, degr, mul(std_, vz), mul(std_, sub(vz, mul(bz, tmp1))));
+  const float2 stby = sel(degl, degr, by, mul(by, tmp2));
+  const float2 stbz = sel(degl, degr, bz, mul(bz, tmp2));
+  const float2 vbst = mul(fma(stmx, S(bxi), fma(stmy, stby, mul(stmz, stbz))), std_inv);
+  const float2 vbu = fma(vy, by, mul(vz, bz));
+  const float2 ste = mul(add(add(sub(mul(sd, ue), mul(pt, vx)), S(ptst * spd2)),
+                             mul(S(bxi), sub(fma(vx, S(bxi), vbu), vbst))),
+                         sdm_inv);
+  // double-star states (L-R averages: scalar where they mix)
+  float2 dsmy = stmy, dsmz = stmz, dsby = stby, dsbz = stbz, dse = ste;
+  if (!(0.5f * bxsq < SMALLN * ptst)) {
+    const float invsumd = 1.0f / (sqrtd.x + sqrtd.y);
+    const float bxsig = (bxi > 0.0f ? 1.0f : -1.0f);
+    const float2 vyst = mul(stmy, std_inv), vzst = mul(stmz, std_inv);
+    const float ty = invsumd * (sqrtd.x * vyst.x + sqrtd.y * vyst.y + bxsig * (stby.y - stby.x));
+    const float tz = invsumd * (sqrtd.x * vzst.x + sqrtd.y * vzst.y + bxsig * (stbz.y - stbz.x));
+    dsmy = mul(std_, S(ty));
+    dsmz = mul(std_, S(tz));
+    const float sq2 = bxsig * sqrtd.x * sqrtd.y;
+    const float tby = invsumd * (sqrtd.x * stby.y + sqrtd.y * stby.x + sq2 * (vyst.y - vyst.x));
+    const float tbz = invsumd * (sqrtd.x * stbz.y + sqrtd.y * stbz.x + sq2 * (vzst.y - vzst.x));
+    dsby = S(tby);
+    dsbz = S(tbz);
+    const float tv = spd2 * bxi + (dsmy.x * tby + dsmz.x * tbz) / std_.x;
+    const float2 sgn = P(-sqrtd.x * bxsig, sqrtd.y * bxsig);
+    dse = fma(sgn, sub(vbst, S(tv)), ste);
+  }
+  // the region of the fan that contains x/t = 0
+  const bool left = spd2 >= 0.0f;
+  auto L = [](float2 a) { return a.x; };
+  auto R = [](float2 a) { return a.y; };
+  if (spd0 >= 0.0f) {
+    flxi[IDN] = umx.x; flxi[IVX] = fmx.x; flxi[IVY] = fmy.x; flxi[IVZ] = fmz.x;
+    flxi[IEN] = fe.x; flxi[IBY] = fby.x; flxi[IBZ] = fbz.x;
+    return;
+  }
+  if (spd4 <= 0.0f) {
+    flxi[IDN] = umx.y; flxi[IVX] = fmx.y; flxi[IVY] = fmy.y; flxi[IVZ] = fmz.y;
+    flxi[IEN] = fe.y; flxi[IBY] = fby.y; flxi[IBZ] = fbz.y;
+    return;
+  }
+  // one side's outer state U, star state U*, double-star state U**, outer flux F and the
+  // wave speeds: F + s_o (U* - U) [+ s_i (U** - U*)], two components per instruction
+  const bool inner = left ? !(spd1 >= 0.0f) : (spd3 > 0.0f);
+  const float so = left ? spd0 : spd4, si = left ? spd1 : spd3;
+  auto pick = [&](float2 a) { return left ? L(a) : R(a); };
+  const float2 u01 = P(pick(d), pick(umx)), u23 = P(pick(umy), pick(umz)),
+               u45 = P(pick(ue), pick(by)), u6 = P(pick(bz), 0.0f);
+  const float2 s01 = P(pick(std_), pick(stmx)), s23 = P(pick(stmy), pick(stmz)),
+               s45 = P(pick(ste), pick(stby)), s6 = P(pick(stbz), 0.0f);
+  const float2 f01 = P(pick(umx), pick(fmx)), f23 = P(pick(fmy), pick(fmz)),
+               f45 = P(pick(fe), pick(fby)), f6 = P(pick(fbz), 0.0f);
+  float2 r01 = fma(S(so), sub(s01, u01), f01), r23 = fma(S(so), sub(s23, u23), f23),
+         r45 = fma(S(so), sub(s45, u45), f45), r6 = fma(S(so), sub(s6, u6), f6);
+  if (inner) {
+    const float2 d01 = P(pick(std_), pick(stmx)), d23 = P(pick(dsmy), pick(dsmz)),
+                 d45 = P(pick(dse), pick(dsby)), d6 = P(pick(dsbz), 0.0f);
+    r01 = fma(S(si), sub(d01, s01), r01);
+    r23 = fma(S(si), sub(d23, s23), r23);
+    r45 = fma(S(si), sub(d45, s45), r45);
+    r6 = fma(S(si), sub(d6, s6), r6);
+  }
+  flxi[IDN] = r01.x; flxi[IVX] = r01.y; flxi[IVY] = r23.x; flxi[IVZ] = r23.y;
+  flxi[IEN] = r45.x; flxi[IBY] = r45.y; flxi[IBZ] = r6.x;
+}
+
 // LHLLC, the fork's low-dissipation HLLC (hydro/rsolvers/hydro/lhllc.cpp:26-180): PVRS
 // wave speeds, the shock detector th = min(1, (cmax - min(dvn,0)) / (cmax - min(dvt,0)))^4
 // on the pressure jump of the contact speed and the low-Mach factor phi = chi (2 - chi) on
