@@ -237,7 +237,7 @@ struct athg_ctx {
   cudaGraph_t graph2 = nullptr;
   cudaGraphExec_t gexec2 = nullptr;
   const double* graph_src = nullptr;  // state buffer the first captured cycle reads
-  FluxTune tune;        // launch shape of the flux sweeps
+  FluxTune tune[4];     // launch shape of the flux sweeps, per reconstruction order 1..3
   bool tuned = false;   // autotuned (or set by the caller)
   int launches_per_cycle = 0;
   int counting = 0;
@@ -418,17 +418,19 @@ int launch_ghosts(athg_ctx* c) {
   return ATHG_OK;
 }
 
+bool df_fast(const athg_ctx* c);
+
 int launch_fluxes(athg_ctx* c, int order) {
   bool mhd = c->cfg.magnetic != 0;
   if (c->mixed())
-    Launcher<float>::fluxes(c->g, ptrs<float>(c), mhd, c->cfg.rsolver, order, phys(c), c->tune,
-                            c->st);
+    Launcher<float>::fluxes(c->g, ptrs<float>(c), mhd, c->cfg.rsolver, order, phys(c),
+                            c->tune[order], c->st);
   else if (c->dfloat())
     athg::df_fluxes(c->g, ptrs<double>(c), mhd, c->cfg.rsolver, order, phys(c), c->wpair_df,
-                    c->st);
+                    df_fast(c), c->st);
   else
     Launcher<double>::fluxes(c->g, ptrs<double>(c), mhd, c->cfg.rsolver, order, phys(c),
-                             c->tune, c->st);
+                             c->tune[order], c->st);
   c->counting += 3;
   // SendFluxCorrection / ReceiveFluxCorrection (time_integrator.cpp: SEND_HYDFLX, RECV_HYDFLX)
   if (c->smr) c->counting += athg::smr_correct_flux(c->smr, smr_pool_of(c), c->st);
@@ -439,7 +441,8 @@ int launch_fluxes(athg_ctx* c, int order) {
 int launch_corner(athg_ctx* c) {
   if (!c->cfg.magnetic) return ATHG_OK;
   if (c->mixed()) Launcher<float>::corner_emf(c->g, ptrs<float>(c), c->st);
-  else if (c->dfloat()) athg::df_corner_emf(c->g, ptrs<double>(c), c->cce_df, c->st);
+  else if (c->dfloat())
+    athg::df_corner_emf(c->g, ptrs<double>(c), c->cce_df, c->wpair_df, df_fast(c), c->st);
   else Launcher<double>::corner_emf(c->g, ptrs<double>(c), c->st);
   c->counting += 1;
   // EMF correction at block boundaries (time_integrator.cpp: SEND_FLDFLX, RECV_FLDFLX)
@@ -467,6 +470,7 @@ int launch_update(athg_ctx* c, int l) {
   StageW sw = stage_weights(c, l);
   bool mhd = c->cfg.magnetic != 0;
   if (c->mixed()) Launcher<float>::update(c->g, ptrs<float>(c), mhd, sw, c->st);
+  else if (df_fast(c)) athg::df_update(c->g, ptrs<double>(c), mhd, sw, c->st);
   else Launcher<double>::update(c->g, ptrs<double>(c), mhd, sw, c->st);
   c->counting += 1;
   CKL();
@@ -476,6 +480,7 @@ int launch_update(athg_ctx* c, int l) {
 int launch_c2p(athg_ctx* c) {
   bool mhd = c->cfg.magnetic != 0;
   if (c->mixed()) Launcher<float>::c2p(c->g, ptrs<float>(c), mhd, phys(c), c->st);
+  else if (df_fast(c)) athg::df_c2p(c->g, ptrs<double>(c), mhd, phys(c), c->wpair_df, c->st);
   else Launcher<double>::c2p(c->g, ptrs<double>(c), mhd, phys(c), c->st);
   c->counting += 1;
   if (c->outflow) {  // ApplyPhysicalBoundaries after the primitives (FP64 arrays)
@@ -494,6 +499,8 @@ int launch_block_dt(athg_ctx* c) {
   bool mhd = c->cfg.magnetic != 0;
   unsigned long long* dm = (unsigned long long*)(c->scal + 3);
   if (c->mixed()) Launcher<float>::block_dt(c->g, ptrs<float>(c), mhd, phys(c), dm, c->st);
+  else if (df_fast(c))
+    athg::df_block_dt(c->g, ptrs<double>(c), mhd, phys(c), c->wpair_df, dm, c->st);
   else Launcher<double>::block_dt(c->g, ptrs<double>(c), mhd, phys(c), dm, c->st);
   c->counting += 1;
   CKL();
@@ -539,6 +546,13 @@ __global__ void k_scatter_phi(Geom g, double* __restrict__ phi, const int* __res
 }
 
 bool has_gravity(const athg_ctx* c) { return c->grav || c->fgrav; }
+
+// The double-float path without FP64 arithmetic in the update, primitive recovery and time
+// step (df_update, df_c2p, df_block_dt): uniform periodic meshes without source terms, where
+// nothing but those kernels writes the primitives the flux sweeps read as pairs
+bool df_fast(const athg_ctx* c) {
+  return c->dfloat() && !c->smr && !has_gravity(c) && !c->outflow && !c->turb;
+}
 
 // whether a cycle can be captured as a CUDA graph: no host synchronisation inside (a
 // multigrid iterating to a threshold or with multipole boundaries); the FFT solve's cuFFT
@@ -875,9 +889,10 @@ int capture_cycle(athg_ctx* c, cudaGraph_t* graph, cudaGraphExec_t* exec) {
 }
 
 // Autotuner of the flux sweeps' launch shape (threads per block of the x1 and marching
-// sweeps, faces per marching segment): every candidate runs the three sweeps of one stage
-// on the context's own state (they only write the flux arrays) three times, timed with
-// CUDA events on the context's stream; the fastest median wins. Mixed path only (the FP64
+// sweeps, faces per marching segment), one shape per reconstruction order the integrator
+// uses: every candidate runs the three sweeps of one stage on the context's own state
+// (they only write the flux arrays) three times, timed with CUDA events on the context's
+// stream; the fastest median wins. Mixed path only (the FP64
 // path is the reference-order check, not the fast path); runs once, before the first
 // captured cycle.
 int autotune_single_pass(athg_ctx* c);
@@ -896,40 +911,47 @@ int autotune(athg_ctx* c) {
   }
   if (c->tuned) return ATHG_OK;
   c->tuned = true;
-  const int tpbs[2] = {64, 128}, segs[4] = {8, 16, 32, 0};
+  const int tpbs[2] = {64, 128}, segs[5] = {4, 8, 16, 32, 0};
   cudaEvent_t e0, e1;
   CK(cudaEventCreate(&e0));
   CK(cudaEventCreate(&e1));
   const bool mhd = c->cfg.magnetic != 0;
   const int saved = c->counting;
-  FluxTune best = c->tune;
-  float best_ms = 1e30f;
   int rc = ATHG_OK;
-  for (int a = 0; a < 2 && !rc; ++a)
-    for (int m = 0; m < 2 && !rc; ++m)
-      for (int q = 0; q < 4 && !rc; ++q) {
-        FluxTune t;
-        t.x1_tpb = tpbs[a]; t.march_tpb = tpbs[m]; t.seg = segs[q];
-        float ms[3];
-        for (int r = 0; r < 3; ++r) {
-          cudaEventRecord(e0, c->st);
-          Launcher<float>::fluxes(c->g, ptrs<float>(c), mhd, c->cfg.rsolver, c->cfg.xorder,
-                                  phys(c), t, c->st);
-          cudaEventRecord(e1, c->st);
-          if (cudaEventSynchronize(e1) != cudaSuccess || cudaGetLastError() != cudaSuccess) {
-            rc = fail(ATHG_ERR_CUDA, "autotune launch failed");
-            break;
+  // each reconstruction order the integrator uses (VL2: donor cell, then xorder) has its
+  // own registers per thread, so its own best shape
+  const int orders[2] = {c->cfg.integrator == ATHG_VL2 ? 1 : c->cfg.xorder, c->cfg.xorder};
+  for (int oi = 0; oi < 2 && !rc; ++oi) {
+    const int order = orders[oi];
+    if (oi == 1 && order == orders[0]) break;
+    FluxTune best = c->tune[order];
+    float best_ms = 1e30f;
+    for (int a = 0; a < 2 && !rc; ++a)
+      for (int m = 0; m < 2 && !rc; ++m)
+        for (int q = 0; q < 5 && !rc; ++q) {
+          FluxTune t;
+          t.x1_tpb = tpbs[a]; t.march_tpb = tpbs[m]; t.seg = segs[q];
+          float ms[3];
+          for (int r = 0; r < 3; ++r) {
+            cudaEventRecord(e0, c->st);
+            Launcher<float>::fluxes(c->g, ptrs<float>(c), mhd, c->cfg.rsolver, order, phys(c),
+                                    t, c->st);
+            cudaEventRecord(e1, c->st);
+            if (cudaEventSynchronize(e1) != cudaSuccess || cudaGetLastError() != cudaSuccess) {
+              rc = fail(ATHG_ERR_CUDA, "autotune launch failed");
+              break;
+            }
+            cudaEventElapsedTime(&ms[r], e0, e1);
           }
-          cudaEventElapsedTime(&ms[r], e0, e1);
+          if (rc) break;
+          std::sort(ms, ms + 3);
+          if (ms[1] < best_ms) { best_ms = ms[1]; best = t; }
         }
-        if (rc) break;
-        std::sort(ms, ms + 3);
-        if (ms[1] < best_ms) { best_ms = ms[1]; best = t; }
-      }
+    if (!rc) c->tune[order] = best;
+  }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   c->counting = saved;
-  if (!rc) c->tune = best;
   return rc;
 }
 
@@ -1466,6 +1488,9 @@ int athg_set_blocks(athg_ctx* c, int nblocks, const athg_block* blocks) {
       hmg[b].idx[d] = (float)(1.0 / dx[d]);
       hmg[b].dx[d] = (float)dx[d];
       hmg[b].ia[d] = dx[d] / vol;
+      const double idx = 1.0 / dx[d];
+      hmg[b].idxh[d] = (float)idx;
+      hmg[b].idxl[d] = (float)(idx - (double)hmg[b].idxh[d]);
     }
   }
   if (c->mixed()) {
@@ -2097,7 +2122,8 @@ int athg_get_tuning(athg_ctx* c, int* out3) {
   int rc = need_pool(c);
   if (rc) return rc;
   if (!out3) return fail(ATHG_ERR_ARG, "null argument");
-  out3[0] = c->tune.x1_tpb; out3[1] = c->tune.march_tpb; out3[2] = c->tune.seg;
+  const FluxTune& t = c->tune[c->cfg.xorder];
+  out3[0] = t.x1_tpb; out3[1] = t.march_tpb; out3[2] = t.seg;
   return ATHG_OK;
 }
 
@@ -2108,7 +2134,9 @@ int athg_set_tuning(athg_ctx* c, const int* in3) {
   if ((in3[0] != 64 && in3[0] != 128) || (in3[1] != 64 && in3[1] != 128) || in3[2] < 0)
     return fail(ATHG_ERR_ARG, "threads per block must be 64 or 128, segment length >= 0");
   drop_graphs(c);  // captured cycles hold the old launch shape
-  c->tune.x1_tpb = in3[0]; c->tune.march_tpb = in3[1]; c->tune.seg = in3[2];
+  for (FluxTune& t : c->tune) {
+    t.x1_tpb = in3[0]; t.march_tpb = in3[1]; t.seg = in3[2];
+  }
   c->tuned = true;
   return ATHG_OK;
 }

@@ -98,6 +98,7 @@ struct MixedGeo {
   float idx[3];    // 1 / dx_d
   float dx[3];     // dx_d
   double ia[3];    // dx_d / (dx1 dx2 dx3): face-flux change -> face-field change
+  float idxh[3], idxl[3];  // 1 / dx_d as a double-float pair (double-float path)
 };
 
 // Comparisons. FP64 comparisons (and min/max) issue on the FP64 pipe, which runs at 1/64 of

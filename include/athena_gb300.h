@@ -294,9 +294,11 @@ int athg_mg_multipole(athg_mg* mg, double* out28);
 
 /* Launch shape of the flux sweeps: out3/in3 = {threads per block of the x1 sweep (64 or
  * 128), of the marching x2/x3 sweeps (64 or 128), faces per marching segment (0: whole
- * pencil)}. No counterpart in the reference. The mixed path autotunes it before its first
- * captured cycle (every candidate timed on the context's own state); setting it disables
- * the autotuner. Results do not depend on it. */
+ * pencil)}. No counterpart in the reference. The mixed path autotunes one shape per
+ * reconstruction order its integrator uses (VL2: donor cell, then xorder) before its first
+ * captured cycle, every candidate timed on the context's own state; get returns the
+ * xorder shape, set applies to every order and disables the autotuner. Results do not
+ * depend on it. */
 int athg_get_tuning(athg_ctx* ctx, int* out3);
 int athg_set_tuning(athg_ctx* ctx, const int* in3);
 

@@ -239,13 +239,14 @@ def test_flux_launch_shape_does_not_change_results():
         sim.close()
     for k in out[0]:
         assert np.array_equal(out[0][k], out[1][k]), k
-    # the autotuner picks one of its candidates
+    # the autotuner picks one of its candidates (for each reconstruction order the
+    # integrator uses; the reported shape is the second VL2 stage's)
     sim = athg.Sim(nx, mb, mhd=True, solver="hlld", precision="mixed", cfl=0.4, tlim=100.0)
     sim.load_interior(u, b1, b2, b3)
     sim.initialize()
     sim.cycles(1)
     x1, mt, seg = sim.tuning()
-    assert x1 in (64, 128) and mt in (64, 128) and seg in (8, 16, 32, 0)
+    assert x1 in (64, 128) and mt in (64, 128) and seg in (4, 8, 16, 32, 0)
     sim.close()
 
 
