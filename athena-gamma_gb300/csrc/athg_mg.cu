@@ -530,19 +530,43 @@ __global__ void k_sub_const(T* a, long long cnt, const double* tot, double scale
   a[t] -= (T)ave;
 }
 
-// sum of squared FP64 defects of the finest level
-__global__ void k_defect_sq(const double* u, const double* src, int n, double idx2, double* out) {
+// Column sums: one thread per (i, j) column and run of kColK cells along k, then one block
+// reduction (a block reduction per cell cost more than the summed terms themselves).
+constexpr int kColK = 32;
+__host__ __device__ inline int col_chunks(int n) { return (n + kColK - 1) / kColK; }
+
+// Sum of squared defects of the finest level, as column sums. FP64
+// path: the FP64 defect. Mixed path (dfl): the seven-point sum exactly in integers and the
+// rest in double-float, as k_defect_to32 forms it (the norm only steers the iteration).
+__global__ void k_defect_sq(const double* u, const double* src, int n, double idx2,
+                            float idx2_hi, float idx2_lo, int dfl, double* out) {
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   double v[1] = {0.0};
-  if (t < (long long)n * n * n) {
-    int i = (int)(t % n) + 1;
-    long long r = t / n;
-    int j = (int)(r % n) + 1, k = (int)(r / n) + 1;
+  if (t < (long long)n * n * col_chunks(n)) {
+    const int i = (int)(t % n) + 1, j = (int)((t / n) % n) + 1;
+    const int k0 = 1 + (int)(t / ((long long)n * n)) * kColK, k1 = min(n, k0 + kColK - 1);
     const int nt = n + 2;
-    const long long q = ix(nt, k, j, i), sk = (long long)nt * nt, sj = nt;
-    double d = (6.0 * u[q] - u[q + sk] - u[q + sj] - u[q + 1] - u[q - sk] - u[q - sj] - u[q - 1]) *
-                   idx2 + src[q];
-    v[0] = d * d;
+    const long long sk = (long long)nt * nt, sj = nt;
+    athg::ff acc = {0.0f, 0.0f};
+    double accd = 0.0;
+    for (int k = k0; k <= k1; ++k) {
+      const long long q = ix(nt, k, j, i);
+      if (dfl) {
+        const double nb[6] = {u[q + sk], u[q - sk], u[q + sj], u[q - sj], u[q + 1], u[q - 1]};
+        athg::ff lap;
+        if (athg::lap7_ff(u[q], nb, lap)) {
+          const athg::ff d = athg::ff_add(athg::ff_mul(lap, athg::ff{idx2_hi, idx2_lo}),
+                                          athg::split_ff(src[q]));
+          acc = athg::ff_add(acc, athg::ff_sqr(d));
+          continue;
+        }
+      }
+      const double d =
+          (6.0 * u[q] - u[q + sk] - u[q + sj] - u[q + 1] - u[q - sk] - u[q - sj] - u[q - 1]) *
+              idx2 + src[q];
+      accd += d * d;
+    }
+    v[0] = accd + (athg::f2d_int(acc.hi) + athg::f2d_int(acc.lo));
   }
   block_add<1>(v, out);
 }
@@ -587,18 +611,20 @@ __global__ void k_narrow(const double* a, float* b, long long cnt) {
   if (t < cnt) b[t] = athg::d2f_int(a[t]);
 }
 
-// multipole moments (and the centre of mass) of the finest source, FP64
+// multipole moments (and the centre of mass) of the finest source, FP64, as column sums (x
+// and y fixed per thread): per-cell reductions of 25 sums cost ten times the moments.
 __global__ void k_com(const double* src, int n, double lo0, double hi0, double lo1, double hi1,
                       double lo2, double hi2, double vol, double* out) {
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   double v[4] = {0, 0, 0, 0};
-  if (t < (long long)n * n * n) {
-    int i = (int)(t % n) + 1;
-    long long r = t / n;
-    int j = (int)(r % n) + 1, k = (int)(r / n) + 1;
-    double s = src[ix(n + 2, k, j, i)] * vol;
-    v[0] = s; v[1] = s * xcen(j, n, lo1, hi1); v[2] = s * xcen(k, n, lo2, hi2);
-    v[3] = s * xcen(i, n, lo0, hi0);
+  if (t < (long long)n * n * col_chunks(n)) {
+    const int i = (int)(t % n) + 1, j = (int)((t / n) % n) + 1;
+    const int k0 = 1 + (int)(t / ((long long)n * n)) * kColK, k1 = min(n, k0 + kColK - 1);
+    const double x = xcen(i, n, lo0, hi0), y = xcen(j, n, lo1, hi1);
+    for (int k = k0; k <= k1; ++k) {
+      const double s = src[ix(n + 2, k, j, i)] * vol;
+      v[0] += s; v[1] += s * y; v[2] += s * xcen(k, n, lo2, hi2); v[3] += s * x;
+    }
   }
   block_add<4>(v, out);
 }
@@ -609,32 +635,34 @@ __global__ void k_moments(const double* src, int n, double lo0, double hi0, doub
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   double m[25];
   for (int q = 0; q < 25; ++q) m[q] = 0.0;
-  if (t < (long long)n * n * n) {
-    int i = (int)(t % n) + 1;
-    long long r = t / n;
-    int j = (int)(r % n) + 1, k = (int)(r / n) + 1;
-    double z = xcen(k, n, lo2, hi2) - origin[2], z2 = z * z;
-    double y = xcen(j, n, lo1, hi1) - origin[1], y2 = y * y, yz = y * z;
-    double x = xcen(i, n, lo0, hi0) - origin[0];
-    double x2 = x * x, xy = x * y, zx = z * x;
-    double r2 = x2 + y2 + z2;
-    double s = src[ix(n + 2, k, j, i)] * vol;
-    m[0] = s;
-    if (!nodipole) { m[1] = s * y; m[2] = s * z; m[3] = s * x; }
-    m[4] = s * xy; m[5] = s * yz; m[6] = s * (3.0 * z2 - r2); m[7] = s * zx;
-    if (order == 4) {
-      double hx2my2 = 0.5 * (x2 - y2), x2mty2 = x2 - 3.0 * y2, tx2my2 = 3.0 * x2 - y2;
-      double fz2mr2 = 5.0 * z2 - r2, sz2mr2 = 7.0 * z2 - r2, sz2mtr2 = 7.0 * z2 - 3.0 * r2;
-      m[8] = s * hx2my2;
-      m[9] = s * y * tx2my2; m[10] = s * xy * z; m[11] = s * y * fz2mr2;
-      m[12] = s * z * (z2 - 3.0 * r2); m[13] = s * x * fz2mr2; m[14] = s * z * hx2my2;
-      m[15] = s * x * x2mty2; m[16] = s * xy * hx2my2; m[17] = s * yz * tx2my2;
-      m[18] = s * xy * sz2mr2; m[19] = s * yz * sz2mtr2;
-      m[20] = s * (35.0 * z2 * z2 - 30.0 * z2 * r2 + 3.0 * r2 * r2);
-      m[21] = s * zx * sz2mtr2; m[22] = s * hx2my2 * sz2mr2; m[23] = s * zx * x2mty2;
-      m[24] = s * 0.125 * (x2 * x2mty2 - y2 * tx2my2);
-    } else {
-      m[8] = s * 0.5 * (x2 - y2);
+  if (t < (long long)n * n * col_chunks(n)) {
+    const int i = (int)(t % n) + 1, j = (int)((t / n) % n) + 1;
+    const int k0 = 1 + (int)(t / ((long long)n * n)) * kColK, k1 = min(n, k0 + kColK - 1);
+    const double y = xcen(j, n, lo1, hi1) - origin[1], y2 = y * y;
+    const double x = xcen(i, n, lo0, hi0) - origin[0];
+    const double x2 = x * x, xy = x * y;
+    for (int k = k0; k <= k1; ++k) {
+      double z = xcen(k, n, lo2, hi2) - origin[2], z2 = z * z;
+      double yz = y * z, zx = z * x;
+      double r2 = x2 + y2 + z2;
+      double s = src[ix(n + 2, k, j, i)] * vol;
+      m[0] += s;
+      if (!nodipole) { m[1] += s * y; m[2] += s * z; m[3] += s * x; }
+      m[4] += s * xy; m[5] += s * yz; m[6] += s * (3.0 * z2 - r2); m[7] += s * zx;
+      if (order == 4) {
+        double hx2my2 = 0.5 * (x2 - y2), x2mty2 = x2 - 3.0 * y2, tx2my2 = 3.0 * x2 - y2;
+        double fz2mr2 = 5.0 * z2 - r2, sz2mr2 = 7.0 * z2 - r2, sz2mtr2 = 7.0 * z2 - 3.0 * r2;
+        m[8] += s * hx2my2;
+        m[9] += s * y * tx2my2; m[10] += s * xy * z; m[11] += s * y * fz2mr2;
+        m[12] += s * z * (z2 - 3.0 * r2); m[13] += s * x * fz2mr2; m[14] += s * z * hx2my2;
+        m[15] += s * x * x2mty2; m[16] += s * xy * hx2my2; m[17] += s * yz * tx2my2;
+        m[18] += s * xy * sz2mr2; m[19] += s * yz * sz2mtr2;
+        m[20] += s * (35.0 * z2 * z2 - 30.0 * z2 * r2 + 3.0 * r2 * r2);
+        m[21] += s * zx * sz2mtr2; m[22] += s * hx2my2 * sz2mr2; m[23] += s * zx * x2mty2;
+        m[24] += s * 0.125 * (x2 * x2mty2 - y2 * tx2my2);
+      } else {
+        m[8] += s * 0.5 * (x2 - y2);
+      }
     }
   }
   block_add<25>(m, out);
@@ -915,8 +943,11 @@ int defect_norm64(athg_mg* m, double* out) {
   RC(apply_bc(m, h, L, false));
   MCK(cudaMemsetAsync(m->red, 0, sizeof(double), m->st));
   const double dx = h.dx[L];
-  k_defect_sq<<<nblk((long long)n * n * n), TPB, 0, m->st>>>(h.u[L], h.src[L], n, 1.0 / (dx * dx),
-                                                             m->red);
+  const double idx2 = 1.0 / (dx * dx);
+  const float idx2_hi = (float)idx2, idx2_lo = (float)(idx2 - (double)idx2_hi);
+  k_defect_sq<<<nblk((long long)n * n * col_chunks(n)), TPB, 0, m->st>>>(
+      h.u[L], h.src[L], n, idx2, idx2_hi, idx2_lo, m->cfg.precision == ATHG_MIXED ? 1 : 0,
+      m->red);
   MCKL();
   double s;
   MCK(cudaMemcpyAsync(&s, m->red, sizeof(double), cudaMemcpyDeviceToHost, m->st));
@@ -940,8 +971,8 @@ int multipole_setup(athg_mg* m) {
   double origin[3] = {c.mporigin[0], c.mporigin[1], c.mporigin[2]};
   if (c.auto_mporigin) {
     MCK(cudaMemsetAsync(m->red, 0, 4 * sizeof(double), m->st));
-    k_com<<<nblk((long long)n * n * n), TPB, 0, m->st>>>(h.src[L], n, c.x1min, c.x1max, c.x2min,
-                                                         c.x2max, c.x3min, c.x3max, vol, m->red);
+    k_com<<<nblk((long long)n * n * col_chunks(n)), TPB, 0, m->st>>>(
+        h.src[L], n, c.x1min, c.x1max, c.x2min, c.x2max, c.x3min, c.x3max, vol, m->red);
     MCKL();
     double s[4];
     MCK(cudaMemcpyAsync(s, m->red, sizeof(s), cudaMemcpyDeviceToHost, m->st));
@@ -951,9 +982,9 @@ int multipole_setup(athg_mg* m) {
   }
   MCK(cudaMemcpyAsync(m->mpo_d, origin, sizeof(origin), cudaMemcpyHostToDevice, m->st));
   MCK(cudaMemsetAsync(m->red, 0, 25 * sizeof(double), m->st));
-  k_moments<<<nblk((long long)n * n * n), TPB, 0, m->st>>>(h.src[L], n, c.x1min, c.x1max, c.x2min,
-                                                           c.x2max, c.x3min, c.x3max, vol, m->mpo_d,
-                                                           c.mporder, c.nodipole, m->red);
+  k_moments<<<nblk((long long)n * n * col_chunks(n)), TPB, 0, m->st>>>(
+      h.src[L], n, c.x1min, c.x1max, c.x2min, c.x2max, c.x3min, c.x3max, vol, m->mpo_d,
+      c.mporder, c.nodipole, m->red);
   MCKL();
   double mm[25];
   MCK(cudaMemcpyAsync(mm, m->red, sizeof(mm), cudaMemcpyDeviceToHost, m->st));
