@@ -909,8 +909,9 @@ def main():
                    "ms_per_step": 1e3 * res["dfloat"]["el"] / res["dfloat"]["steps"],
                    "steps": res["dfloat"]["steps"],
                    "over_fp64": res["dfloat"]["zcps"] / res["fp64"]["zcps"],
-                   "note": "double-float reconstruction, Riemann fluxes and corner EMFs, "
-                           "FP64 state and update (the FP64 path's accuracy)"},
+                   "note": "double-float reconstruction, Riemann fluxes, corner EMFs, "
+                           "update, primitive recovery and time step; FP64 state (the FP64 "
+                           "path's accuracy)"},
         "linear_waves_equal_l1": lwres,
         "single_pass_stage": spres,
         "l1_rho_mixed_vs_fp64": {"cycles": n_cmp, "abs": l1_dev, "rel": l1_rel},
