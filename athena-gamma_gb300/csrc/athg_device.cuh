@@ -521,152 +521,174 @@ __device__ __forceinline__ void rs_hlld(const T* wli, const T* wri, T bxi, T gam
   }
 }
 
-// ---- HLLD for the FP32 flux path on packed FP32 instructions ---------------------------
-// Blackwell issues two FP32 additions, multiplications or FMAs per instruction on float2
-// operands (__fadd2_rn, __fmul2_rn, __ffma2_rn; each lane rounds as the scalar operation
-// does). Most of HLLD is the same arithmetic on the left and right states, so here lane x
-// carries the left state and lane y the right one, and the L/R-symmetric parts (the
-// conserved states, fast speeds, outer fluxes, single- and double-star states) take half
-// the issue slots. Divisions and square roots stay scalar; the few L-R mixed expressions
-// (the contact speed, the double-star averages) are scalar too. Same formulas as rs_hlld
-// above (hydro/rsolvers/mhd/hlld.cpp:56-371); the results agree to FP32 rounding (the FP32
-// flux path's tolerance), not bit for bit, because products that the scalar code rounds
-// separately may be fused here.
-namespace pk {
-__device__ __forceinline__ float2 S(float s) { return make_float2(s, s); }
-__device__ __forceinline__ float2 P(float l, float r) { return make_float2(l, r); }
-__device__ __forceinline__ float2 add(float2 a, float2 b) { return __fadd2_rn(a, b); }
-__device__ __forceinline__ float2 mul(float2 a, float2 b) { return __fmul2_rn(a, b); }
-__device__ __forceinline__ float2 fma(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
-// a - b, rounded once (b times -1 is exact)
-__device__ __forceinline__ float2 sub(float2 a, float2 b) { return __ffma2_rn(b, S(-1.0f), a); }
-__device__ __forceinline__ float2 rcp(float2 a) { return make_float2(1.0f / a.x, 1.0f / a.y); }
-__device__ __forceinline__ float2 sqrt2(float2 a) { return make_float2(sqrtf(a.x), sqrtf(a.y)); }
-__device__ __forceinline__ float2 sel(bool l, bool r, float2 a, float2 b) {
-  return make_float2(l ? a.x : b.x, r ? a.y : b.y);
+// ---- HLLD on left/right lane pairs ------------------------------------------------------
+// Most of HLLD is the same arithmetic on the left and right states, so hlld_lr carries the
+// left state in one lane and the right one in the other of a pair type K::P and does the
+// L/R-symmetric parts (the conserved states, fast speeds, outer fluxes, single- and
+// double-star states, the final flux sums two components at a time) on both lanes at once.
+// The few L-R mixed expressions (the contact speed, the double-star averages) and the
+// divisions and square roots are per lane. Same formulas as rs_hlld above
+// (hydro/rsolvers/mhd/hlld.cpp:56-371); the results agree to the arithmetic's rounding,
+// not bit for bit, where a product and a sum are fused.
+//
+// PkF: FP32, on Blackwell's packed instructions (__fadd2_rn, __fmul2_rn, __ffma2_rn issue
+// two FP32 operations per instruction, each lane rounded as the scalar operation). The
+// double-float path (athg_df.cu) supplies its own K with pairs of double-float numbers.
+struct PkF {
+  using S = float;
+  using P = float2;
+  static __device__ __forceinline__ S sc(double v) { return (float)v; }
+  static __device__ __forceinline__ P splat(S s) { return make_float2(s, s); }
+  static __device__ __forceinline__ P pair(S l, S r) { return make_float2(l, r); }
+  static __device__ __forceinline__ S L(P a) { return a.x; }
+  static __device__ __forceinline__ S R(P a) { return a.y; }
+  static __device__ __forceinline__ P add(P a, P b) { return __fadd2_rn(a, b); }
+  static __device__ __forceinline__ P mul(P a, P b) { return __fmul2_rn(a, b); }
+  static __device__ __forceinline__ P fma(P a, P b, P c) { return __ffma2_rn(a, b, c); }
+  // a - b, rounded once (b times -1 is exact)
+  static __device__ __forceinline__ P sub(P a, P b) { return __ffma2_rn(b, splat(-1.0f), a); }
+  static __device__ __forceinline__ P div(P a, P b) { return make_float2(a.x / b.x, a.y / b.y); }
+  static __device__ __forceinline__ P sqrt2(P a) { return make_float2(sqrtf(a.x), sqrtf(a.y)); }
+  static __device__ __forceinline__ P sel(bool l, bool r, P a, P b) {
+    return make_float2(l ? a.x : b.x, r ? a.y : b.y);
+  }
+  static __device__ __forceinline__ S abs(S a) { return fabsf(a); }
+};
+
+template <class K>
+__device__ __forceinline__ void hlld_lr(const typename K::S* wli, const typename K::S* wri,
+                                        typename K::S bxi, typename K::S gamma,
+                                        typename K::S* flxi) {
+  using S = typename K::S;
+  using P = typename K::P;
+  auto sp = [](S v) { return K::splat(v); };
+  const S zero = K::sc(0.0), half = K::sc(0.5), one = K::sc(1.0);
+  const S SMALLN = K::sc(1.0e-8);
+  const S igm1 = one / (gamma - one);
+  const S bxsq = bxi * bxi;
+  const P d = K::pair(wli[IDN], wri[IDN]), vx = K::pair(wli[IVX], wri[IVX]),
+          vy = K::pair(wli[IVY], wri[IVY]), vz = K::pair(wli[IVZ], wri[IVZ]),
+          p = K::pair(wli[IPR], wri[IPR]), by = K::pair(wli[IBY], wri[IBY]),
+          bz = K::pair(wli[IBZ], wri[IBZ]);
+  // magnetic and kinetic energy densities, conserved states
+  const P bt2 = K::fma(by, by, K::mul(bz, bz));
+  const P pb = K::mul(sp(half), K::add(sp(bxsq), bt2));
+  const P ke = K::mul(K::mul(sp(half), d), K::fma(vx, vx, K::fma(vy, vy, K::mul(vz, vz))));
+  const P umx = K::mul(vx, d), umy = K::mul(vy, d), umz = K::mul(vz, d);
+  const P ue = K::add(K::fma(p, sp(igm1), ke), pb);
+  // fast magnetosonic speeds (fast_speed)
+  const P asq = K::mul(sp(gamma), p);
+  const P qsq = K::add(K::add(sp(bxsq), bt2), asq);
+  const P tmq = K::sub(K::add(sp(bxsq), bt2), asq);
+  const P disc = K::sqrt2(K::fma(tmq, tmq, K::mul(sp(K::sc(4.0)), K::mul(asq, bt2))));
+  const P cf = K::sqrt2(K::div(K::mul(sp(half), K::add(qsq, disc)), d));
+  const P vm = K::sub(vx, cf), vp = K::add(vx, cf);
+  const S spd0 = mn(K::L(vm), K::R(vm)), spd4 = mx(K::L(vp), K::R(vp));
+  const P pt = K::add(p, pb);
+  // outer fluxes F(U_L), F(U_R)
+  const P nbx = sp(-bxi);
+  const P fmx = K::add(K::fma(umx, vx, pt), sp(-bxsq));
+  const P fmy = K::fma(umy, vx, K::mul(nbx, by));
+  const P fmz = K::fma(umz, vx, K::mul(nbx, bz));
+  const P fe = K::fma(vx, K::add(K::add(ue, pt), sp(-bxsq)),
+                      K::mul(nbx, K::fma(vy, by, K::mul(vz, bz))));
+  const P fby = K::fma(by, vx, K::mul(nbx, vy));
+  const P fbz = K::fma(bz, vx, K::mul(nbx, vz));
+  // contact speed (L-R mixed: per lane)
+  const P sd = K::sub(K::pair(spd0, spd4), vx);  // (sdl, sdr)
+  const S spd2 = (K::R(sd) * K::R(umx) - K::L(sd) * K::L(umx) + (K::L(pt) - K::R(pt))) /
+                 (K::R(sd) * K::R(d) - K::L(sd) * K::L(d));
+  const P sdm = K::sub(K::pair(spd0, spd4), sp(spd2));
+  const P sdm_inv = K::div(sp(one), sdm);
+  // single-star states
+  const P dsd = K::mul(d, sd);
+  const P std_ = K::mul(dsd, sdm_inv);  // rho*
+  const P std_inv = K::div(sp(one), std_);
+  const P sqrtd = K::sqrt2(std_);
+  const S abx = K::abs(bxi);
+  const S spd1 = spd2 - abx / K::L(sqrtd);
+  const S spd3 = spd2 + abx / K::R(sqrtd);
+  const P ptstlr = K::fma(dsd, K::sub(sp(spd2), vx), pt);
+  const S ptst = half * (K::R(ptstlr) + K::L(ptstlr));
+  const P stmx = K::mul(std_, sp(spd2));
+  const P den = K::add(K::mul(dsd, sdm), sp(-bxsq));
+  const bool degl = K::abs(K::L(den)) < SMALLN * ptst, degr = K::abs(K::R(den)) < SMALLN * ptst;
+  const P iden = K::div(sp(one), den);
+  const P tmp1 = K::mul(K::mul(sp(bxi), K::sub(sd, sdm)), iden);
+  const P tmp2 = K::mul(K::add(K::mul(dsd, sd), sp(-bxsq)), iden);
+  const P stmy = K::sel(degl, degr, K::mul(std_, vy), K::mul(std_, K::sub(vy, K::mul(by, tmp1))));
+  const P stmz = K::sel(degl, degr, K::mul(std_, vz), K::mul(std_, K::sub(vz, K::mul(bz, tmp1))));
+  const P stby = K::sel(degl, degr, by, K::mul(by, tmp2));
+  const P stbz = K::sel(degl, degr, bz, K::mul(bz, tmp2));
+  const P vbst = K::mul(K::fma(stmx, sp(bxi), K::fma(stmy, stby, K::mul(stmz, stbz))), std_inv);
+  const P vbu = K::fma(vy, by, K::mul(vz, bz));
+  const P ste = K::mul(K::add(K::add(K::sub(K::mul(sd, ue), K::mul(pt, vx)), sp(ptst * spd2)),
+                              K::mul(sp(bxi), K::sub(K::fma(vx, sp(bxi), vbu), vbst))),
+                       sdm_inv);
+  // double-star states (L-R averages: per lane where they mix)
+  P dsmy = stmy, dsmz = stmz, dsby = stby, dsbz = stbz, dse = ste;
+  if (!(half * bxsq < SMALLN * ptst)) {
+    const S invsumd = one / (K::L(sqrtd) + K::R(sqrtd));
+    const S bxsig = (bxi > zero ? one : -one);
+    const P vyst = K::mul(stmy, std_inv), vzst = K::mul(stmz, std_inv);
+    const S ty = invsumd * (K::L(sqrtd) * K::L(vyst) + K::R(sqrtd) * K::R(vyst) +
+                            bxsig * (K::R(stby) - K::L(stby)));
+    const S tz = invsumd * (K::L(sqrtd) * K::L(vzst) + K::R(sqrtd) * K::R(vzst) +
+                            bxsig * (K::R(stbz) - K::L(stbz)));
+    dsmy = K::mul(std_, sp(ty));
+    dsmz = K::mul(std_, sp(tz));
+    const S sq2 = bxsig * K::L(sqrtd) * K::R(sqrtd);
+    const S tby = invsumd * (K::L(sqrtd) * K::R(stby) + K::R(sqrtd) * K::L(stby) +
+                             sq2 * (K::R(vyst) - K::L(vyst)));
+    const S tbz = invsumd * (K::L(sqrtd) * K::R(stbz) + K::R(sqrtd) * K::L(stbz) +
+                             sq2 * (K::R(vzst) - K::L(vzst)));
+    dsby = sp(tby);
+    dsbz = sp(tbz);
+    const S tv = spd2 * bxi + (K::L(dsmy) * tby + K::L(dsmz) * tbz) / K::L(std_);
+    const P sgn = K::pair(-K::L(sqrtd) * bxsig, K::R(sqrtd) * bxsig);
+    dse = K::fma(sgn, K::sub(vbst, sp(tv)), ste);
+  }
+  // the region of the fan that contains x/t = 0
+  if (spd0 >= zero) {
+    flxi[IDN] = K::L(umx); flxi[IVX] = K::L(fmx); flxi[IVY] = K::L(fmy); flxi[IVZ] = K::L(fmz);
+    flxi[IEN] = K::L(fe); flxi[IBY] = K::L(fby); flxi[IBZ] = K::L(fbz);
+    return;
+  }
+  if (spd4 <= zero) {
+    flxi[IDN] = K::R(umx); flxi[IVX] = K::R(fmx); flxi[IVY] = K::R(fmy); flxi[IVZ] = K::R(fmz);
+    flxi[IEN] = K::R(fe); flxi[IBY] = K::R(fby); flxi[IBZ] = K::R(fbz);
+    return;
+  }
+  // one side's outer state U, star state U*, double-star state U**, outer flux F and the
+  // wave speeds: F + s_o (U* - U) [+ s_i (U** - U*)], two components per operation
+  const bool left = spd2 >= zero;
+  const bool inner = left ? !(spd1 >= zero) : (spd3 > zero);
+  const S so = left ? spd0 : spd4, si = left ? spd1 : spd3;
+  auto pick = [&](P a) { return left ? K::L(a) : K::R(a); };
+  const P u01 = K::pair(pick(d), pick(umx)), u23 = K::pair(pick(umy), pick(umz)),
+          u45 = K::pair(pick(ue), pick(by)), u6 = K::pair(pick(bz), zero);
+  const P s01 = K::pair(pick(std_), pick(stmx)), s23 = K::pair(pick(stmy), pick(stmz)),
+          s45 = K::pair(pick(ste), pick(stby)), s6 = K::pair(pick(stbz), zero);
+  const P f01 = K::pair(pick(umx), pick(fmx)), f23 = K::pair(pick(fmy), pick(fmz)),
+          f45 = K::pair(pick(fe), pick(fby)), f6 = K::pair(pick(fbz), zero);
+  P r01 = K::fma(sp(so), K::sub(s01, u01), f01), r23 = K::fma(sp(so), K::sub(s23, u23), f23),
+    r45 = K::fma(sp(so), K::sub(s45, u45), f45), r6 = K::fma(sp(so), K::sub(s6, u6), f6);
+  if (inner) {
+    const P d01 = K::pair(pick(std_), pick(stmx)), d23 = K::pair(pick(dsmy), pick(dsmz)),
+            d45 = K::pair(pick(dse), pick(dsby)), d6 = K::pair(pick(dsbz), zero);
+    r01 = K::fma(sp(si), K::sub(d01, s01), r01);
+    r23 = K::fma(sp(si), K::sub(d23, s23), r23);
+    r45 = K::fma(sp(si), K::sub(d45, s45), r45);
+    r6 = K::fma(sp(si), K::sub(d6, s6), r6);
+  }
+  flxi[IDN] = K::L(r01); flxi[IVX] = K::R(r01); flxi[IVY] = K::L(r23); flxi[IVZ] = K::R(r23);
+  flxi[IEN] = K::L(r45); flxi[IBY] = K::R(r45); flxi[IBZ] = K::L(r6);
 }
-}  // namespace pk
 
 template <>
 __device__ __forceinline__ void rs_hlld<float>(const float* wli, const float* wri, float bxi,
                                                float gamma, float* flxi) {
-  using namespace pk;
-  const float SMALLN = 1.0e-8f;
-  const float igm1 = 1.0f / (gamma - 1.0f);
-  const float bxsq = bxi * bxi;
-  const float2 d = P(wli[IDN], wri[IDN]), vx = P(wli[IVX], wri[IVX]),
-               vy = P(wli[IVY], wri[IVY]), vz = P(wli[IVZ], wri[IVZ]),
-               p = P(wli[IPR], wri[IPR]), by = P(wli[IBY], wri[IBY]), bz = P(wli[IBZ], wri[IBZ]);
-  // magnetic and kinetic energy densities, conserved states
-  const float2 bt2 = fma(by, by, mul(bz, bz));
-  const float2 pb = mul(S(0.5f), add(S(bxsq), bt2));
-  const float2 ke = mul(mul(S(0.5f), d), fma(vx, vx, fma(vy, vy, mul(vz, vz))));
-  const float2 umx = mul(vx, d), umy = mul(vy, d), umz = mul(vz, d);
-  const float2 ue = add(fma(p, S(igm1), ke), pb);
-  // fast magnetosonic speeds (fast_speed)
-  const float2 asq = mul(S(gamma), p);
-  const float2 qsq = add(add(S(bxsq), bt2), asq);
-  const float2 tmq = sub(add(S(bxsq), bt2), asq);
-  const float2 disc = sqrt2(fma(tmq, tmq, mul(S(4.0f), mul(asq, bt2))));
-  const float2 cf2 = mul(S(0.5f), add(qsq, disc));
-  const float2 cf = sqrt2(P(cf2.x / d.x, cf2.y / d.y));
-  const float2 vm = sub(vx, cf), vp = add(vx, cf);
-  const float spd0 = mn(vm.x, vm.y), spd4 = mx(vp.x, vp.y);
-  const float2 pt = add(p, pb);
-  // outer fluxes F(U_L), F(U_R)
-  const float2 nbx = S(-bxi);
-  const float2 fmx = add(fma(umx, vx, pt), S(-bxsq));
-  const float2 fmy = fma(umy, vx, mul(nbx, by));
-  const float2 fmz = fma(umz, vx, mul(nbx, bz));
-  const float2 fe = fma(vx, add(add(ue, pt), S(-bxsq)), mul(nbx, fma(vy, by, mul(vz, bz))));
-  const float2 fby = fma(by, vx, mul(nbx, vy));
-  const float2 fbz = fma(bz, vx, mul(nbx, vz));
-  // contact speed (L-R mixed: scalar)
-  const float2 sd = sub(P(spd0, spd4), vx);  // (sdl, sdr)
-  const float spd2 = (sd.y * umx.y - sd.x * umx.x + (pt.x - pt.y)) / (sd.y * d.y - sd.x * d.x);
-  const float2 sdm = sub(P(spd0, spd4), S(spd2));
-  const float2 sdm_inv = rcp(sdm);
-  // single-star states
-  const float2 dsd = mul(d, sd);
-  const float2 std_ = mul(dsd, sdm_inv);  // rho*
-  const float2 std_inv = rcp(std_);
-  const float2 sqrtd = sqrt2(std_);
-  const float abx = fabsf(bxi);
-  const float spd1 = spd2 - abx / sqrtd.x;
-  const float spd3 = spd2 + abx / sqrtd.y;
-  const float2 ptstlr = fma(dsd, sub(S(spd2), vx), pt);
-  const float ptst = 0.5f * (ptstlr.y + ptstlr.x);
-  const float2 stmx = mul(std_, S(spd2));
-  const float2 den = add(mul(dsd, sdm), S(-bxsq));
-  const bool degl = fabsf(den.x) < SMALLN * ptst, degr = fabsf(den.y) < SMALLN * ptst;
-  const float2 iden = rcp(den);
-  const float2 tmp1 = mul(mul(S(bxi), sub(sd, sdm)), iden);
-  const float2 tmp2 = mul(add(mul(dsd, sd), S(-bxsq)), iden);
-  const float2 stmy = sel(degl, degr, mul(std_, vy), mul(std_, sub(vy, mul(by, tmp1))));
-  const float2 stmz = sel(degl, degr, mul(std_, vz), mul(std_, sub(vz, mul(bz, tmp1))));
-  const float2 stby = sel(degl, degr, by, mul(by, tmp2));
-  const float2 stbz = sel(degl, degr, bz, mul(bz, tmp2));
-  const float2 vbst = mul(fma(stmx, S(bxi), fma(stmy, stby, mul(stmz, stbz))), std_inv);
-  const float2 vbu = fma(vy, by, mul(vz, bz));
-  const float2 ste = mul(add(add(sub(mul(sd, ue), mul(pt, vx)), S(ptst * spd2)),
-                             mul(S(bxi), sub(fma(vx, S(bxi), vbu), vbst))),
-                         sdm_inv);
-  // double-star states (L-R averages: scalar where they mix)
-  float2 dsmy = stmy, dsmz = stmz, dsby = stby, dsbz = stbz, dse = ste;
-  if (!(0.5f * bxsq < SMALLN * ptst)) {
-    const float invsumd = 1.0f / (sqrtd.x + sqrtd.y);
-    const float bxsig = (bxi > 0.0f ? 1.0f : -1.0f);
-    const float2 vyst = mul(stmy, std_inv), vzst = mul(stmz, std_inv);
-    const float ty = invsumd * (sqrtd.x * vyst.x + sqrtd.y * vyst.y + bxsig * (stby.y - stby.x));
-    const float tz = invsumd * (sqrtd.x * vzst.x + sqrtd.y * vzst.y + bxsig * (stbz.y - stbz.x));
-    dsmy = mul(std_, S(ty));
-    dsmz = mul(std_, S(tz));
-    const float sq2 = bxsig * sqrtd.x * sqrtd.y;
-    const float tby = invsumd * (sqrtd.x * stby.y + sqrtd.y * stby.x + sq2 * (vyst.y - vyst.x));
-    const float tbz = invsumd * (sqrtd.x * stbz.y + sqrtd.y * stbz.x + sq2 * (vzst.y - vzst.x));
-    dsby = S(tby);
-    dsbz = S(tbz);
-    const float tv = spd2 * bxi + (dsmy.x * tby + dsmz.x * tbz) / std_.x;
-    const float2 sgn = P(-sqrtd.x * bxsig, sqrtd.y * bxsig);
-    dse = fma(sgn, sub(vbst, S(tv)), ste);
-  }
-  // the region of the fan that contains x/t = 0
-  const bool left = spd2 >= 0.0f;
-  auto L = [](float2 a) { return a.x; };
-  auto R = [](float2 a) { return a.y; };
-  if (spd0 >= 0.0f) {
-    flxi[IDN] = umx.x; flxi[IVX] = fmx.x; flxi[IVY] = fmy.x; flxi[IVZ] = fmz.x;
-    flxi[IEN] = fe.x; flxi[IBY] = fby.x; flxi[IBZ] = fbz.x;
-    return;
-  }
-  if (spd4 <= 0.0f) {
-    flxi[IDN] = umx.y; flxi[IVX] = fmx.y; flxi[IVY] = fmy.y; flxi[IVZ] = fmz.y;
-    flxi[IEN] = fe.y; flxi[IBY] = fby.y; flxi[IBZ] = fbz.y;
-    return;
-  }
-  // one side's outer state U, star state U*, double-star state U**, outer flux F and the
-  // wave speeds: F + s_o (U* - U) [+ s_i (U** - U*)], two components per instruction
-  const bool inner = left ? !(spd1 >= 0.0f) : (spd3 > 0.0f);
-  const float so = left ? spd0 : spd4, si = left ? spd1 : spd3;
-  auto pick = [&](float2 a) { return left ? L(a) : R(a); };
-  const float2 u01 = P(pick(d), pick(umx)), u23 = P(pick(umy), pick(umz)),
-               u45 = P(pick(ue), pick(by)), u6 = P(pick(bz), 0.0f);
-  const float2 s01 = P(pick(std_), pick(stmx)), s23 = P(pick(stmy), pick(stmz)),
-               s45 = P(pick(ste), pick(stby)), s6 = P(pick(stbz), 0.0f);
-  const float2 f01 = P(pick(umx), pick(fmx)), f23 = P(pick(fmy), pick(fmz)),
-               f45 = P(pick(fe), pick(fby)), f6 = P(pick(fbz), 0.0f);
-  float2 r01 = fma(S(so), sub(s01, u01), f01), r23 = fma(S(so), sub(s23, u23), f23),
-         r45 = fma(S(so), sub(s45, u45), f45), r6 = fma(S(so), sub(s6, u6), f6);
-  if (inner) {
-    const float2 d01 = P(pick(std_), pick(stmx)), d23 = P(pick(dsmy), pick(dsmz)),
-                 d45 = P(pick(dse), pick(dsby)), d6 = P(pick(dsbz), 0.0f);
-    r01 = fma(S(si), sub(d01, s01), r01);
-    r23 = fma(S(si), sub(d23, s23), r23);
-    r45 = fma(S(si), sub(d45, s45), r45);
-    r6 = fma(S(si), sub(d6, s6), r6);
-  }
-  flxi[IDN] = r01.x; flxi[IVX] = r01.y; flxi[IVY] = r23.x; flxi[IVZ] = r23.y;
-  flxi[IEN] = r45.x; flxi[IBY] = r45.y; flxi[IBZ] = r6.x;
+  hlld_lr<PkF>(wli, wri, bxi, gamma, flxi);
 }
 
 // LHLLC, the fork's low-dissipation HLLC (hydro/rsolvers/hydro/lhllc.cpp:26-180): PVRS

@@ -23,6 +23,66 @@
 
 namespace athg {
 
+// HLLD of this path on left/right lane pairs (hlld_lr in athg_device.cuh): pairs of
+// double-float numbers whose hi and lo parts are float2 lanes, with the operations of
+// athg_dfloat.cuh done on both lanes by Blackwell's packed FP32 instructions (the same
+// operation sequence per lane; divisions and square roots per lane).
+struct D2 {
+  float2 hi, lo;
+};
+struct PkD {
+  using S = dfl;
+  using P = D2;
+  static __device__ __forceinline__ S sc(double v) { return dfl(v); }
+  static __device__ __forceinline__ P splat(S s) {
+    return D2{make_float2(s.hi, s.hi), make_float2(s.lo, s.lo)};
+  }
+  static __device__ __forceinline__ P pair(S l, S r) {
+    return D2{make_float2(l.hi, r.hi), make_float2(l.lo, r.lo)};
+  }
+  static __device__ __forceinline__ S L(P a) { return dfl(a.hi.x, a.lo.x); }
+  static __device__ __forceinline__ S R(P a) { return dfl(a.hi.y, a.lo.y); }
+  static __device__ __forceinline__ float2 ad(float2 a, float2 b) { return __fadd2_rn(a, b); }
+  static __device__ __forceinline__ float2 sb(float2 a, float2 b) {  // a - b, one rounding
+    return __ffma2_rn(b, make_float2(-1.0f, -1.0f), a);
+  }
+  static __device__ __forceinline__ P fast(float2 s, float2 e) {  // df_fast on both lanes
+    const float2 h = ad(s, e);
+    return D2{h, sb(e, sb(h, s))};
+  }
+  static __device__ __forceinline__ P add(P a, P b) {  // dfl operator+ (TwoSum, renorm)
+    const float2 s = ad(a.hi, b.hi);
+    const float2 bp = sb(s, a.hi);
+    float2 e = ad(sb(a.hi, sb(s, bp)), sb(b.hi, bp));
+    e = ad(e, ad(a.lo, b.lo));
+    return fast(s, e);
+  }
+  static __device__ __forceinline__ P neg(P a) {
+    return D2{make_float2(-a.hi.x, -a.hi.y), make_float2(-a.lo.x, -a.lo.y)};
+  }
+  static __device__ __forceinline__ P sub(P a, P b) { return add(a, neg(b)); }
+  static __device__ __forceinline__ P mul(P a, P b) {  // dfl operator* (TwoProduct)
+    const float2 p = __fmul2_rn(a.hi, b.hi);
+    float2 e = __ffma2_rn(a.hi, b.hi, make_float2(-p.x, -p.y));
+    e = __ffma2_rn(a.hi, b.lo, e);
+    e = __ffma2_rn(a.lo, b.hi, e);
+    return fast(p, e);
+  }
+  static __device__ __forceinline__ P fma(P a, P b, P c) { return add(mul(a, b), c); }
+  static __device__ __forceinline__ P div(P a, P b) { return pair(L(a) / L(b), R(a) / R(b)); }
+  static __device__ __forceinline__ P sqrt2(P a) { return pair(sqrt(L(a)), sqrt(R(a))); }
+  static __device__ __forceinline__ P sel(bool l, bool r, P a, P b) {
+    return pair(l ? L(a) : L(b), r ? R(a) : R(b));
+  }
+  static __device__ __forceinline__ S abs(S a) { return fabs(a); }
+};
+
+template <>
+__device__ __forceinline__ void rs_hlld<dfl>(const dfl* wli, const dfl* wri, dfl bxi, dfl gamma,
+                                             dfl* flxi) {
+  hlld_lr<PkD>(wli, wri, bxi, gamma, flxi);
+}
+
 namespace {
 
 constexpr int kThreads = 128;
