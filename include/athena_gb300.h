@@ -38,9 +38,11 @@ enum { ATHG_HLLE = 0, ATHG_HLLC = 1, ATHG_HLLD = 2, ATHG_LHLLC = 3, ATHG_LHLLD =
 enum { ATHG_VL2 = 0, ATHG_RK1 = 1, ATHG_RK2 = 2, ATHG_RK3 = 3 };
 /* arithmetic of reconstruction/Riemann fluxes: FP64 (the reference's, bit for bit); FP32
  * with FP64 state + CT (mixed); or double-float (pairs of FP32 values, ~48 bits, on the FP32
- * pipe) with FP64 state, update and CT: the FP64 path's accuracy, including for waves near
- * the FP32 resolution of their background (donor cell or PLM; HLLC/HLLE hydro, HLLD/HLLE
- * MHD). ATHG_DFLOAT has no counterpart in the reference. */
+ * pipe) with FP64 state (on uniform periodic meshes without source terms the update,
+ * primitive recovery and time step in double-float too, each new state value FP64 base
+ * minus a double-float increment): the FP64 path's accuracy, including for waves near the
+ * FP32 resolution of their background (donor cell or PLM; HLLC/HLLE hydro, HLLD/HLLE MHD).
+ * ATHG_DFLOAT has no counterpart in the reference. */
 enum { ATHG_FP64 = 0, ATHG_MIXED = 1, ATHG_DFLOAT = 2 };
 /* arrays exchanged with the host, per block, AthenaArray layout with ghosts:
  * CONS (5,nc3,nc2,nc1)  B1F (nc3,nc2,nc1+1)  B2F (nc3,nc2+1,nc1)  B3F (nc3+1,nc2,nc1)
