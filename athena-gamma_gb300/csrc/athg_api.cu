@@ -246,6 +246,7 @@ struct athg_ctx {
   athg_mg* grav = nullptr;
   double four_pi_G = 0.0;
   double* phi = nullptr;
+  float2* phi2 = nullptr;  // mixed path: the same potential as FP32 pairs hi + lo
   int* boff = nullptr;
   // FFT self-gravity (SELF_GRAVITY_ENABLED == 1) in place of the multigrid, and the
   // turbulence driver; both transform the whole mesh (blocks placed by boff)
@@ -353,8 +354,9 @@ void free_pool(athg_ctx* c) {
   c->gexec2 = nullptr; c->graph2 = nullptr;
   c->ghosts_stale = false;
   if (c->phi) cudaFree(c->phi);
+  if (c->phi2) cudaFree(c->phi2);
   if (c->boff) cudaFree(c->boff);
-  c->phi = nullptr; c->boff = nullptr;
+  c->phi = nullptr; c->phi2 = nullptr; c->boff = nullptr;
   if (c->grav) athg::mg_bind_stream(c->grav, nullptr);
   c->grav = nullptr;
   athg::fftgrav_destroy(c->fgrav);
@@ -532,8 +534,10 @@ __global__ void k_gather_rho(Geom g, const double* __restrict__ u, const int* __
 
 // Multigrid::RetrieveResult (multigrid.cpp:269-286) with one ghost layer: the solver's
 // finest level, whose ghost layer holds the final boundary fill, into every block's phi
-__global__ void k_scatter_phi(Geom g, double* __restrict__ phi, const int* __restrict__ boff,
-                              const double* __restrict__ um, int n) {
+// (and, for the mixed path's source term, into phi2 as FP32 pairs)
+__global__ void k_scatter_phi(Geom g, double* __restrict__ phi, float2* __restrict__ phi2,
+                              const int* __restrict__ boff, const double* __restrict__ um,
+                              int n) {
   const int b = blockIdx.z, k = blockIdx.y;  // k over nx3 + 2
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   const int w1 = g.nx1 + 2, w2 = g.nx2 + 2;
@@ -541,8 +545,13 @@ __global__ void k_scatter_phi(Geom g, double* __restrict__ phi, const int* __res
   const int j = t / w1, i = t - j * w1;
   const int64_t nt = n + 2;
   const int I = boff[3 * b] + i, J = boff[3 * b + 1] + j, K = boff[3 * b + 2] + k;
-  phi[(int64_t)b * g.ncell + cidx(g, k + g.ks - 1, j + g.js - 1, i + g.is - 1)] =
-      um[((int64_t)K * nt + J) * nt + I];
+  const int64_t q = (int64_t)b * g.ncell + cidx(g, k + g.ks - 1, j + g.js - 1, i + g.is - 1);
+  const double v = um[((int64_t)K * nt + J) * nt + I];
+  phi[q] = v;
+  if (phi2) {
+    const athg::ff f = athg::split_ff(v);
+    phi2[q] = make_float2(f.hi, f.lo);
+  }
 }
 
 bool has_gravity(const athg_ctx* c) { return c->grav || c->fgrav; }
@@ -600,16 +609,22 @@ int tile_blocks(athg_ctx* c, int n1, int n2, int n3) {
     CK(cudaMalloc(&c->phi, sizeof(double) * g.ncell * c->nb));
     CK(cudaMemsetAsync(c->phi, 0, sizeof(double) * g.ncell * c->nb, c->st));
   }
+  if (c->mixed() && !c->phi2) {
+    CK(cudaMalloc(&c->phi2, sizeof(float2) * g.ncell * c->nb));
+    CK(cudaMemsetAsync(c->phi2, 0, sizeof(float2) * g.ncell * c->nb, c->st));
+  }
   CK(cudaMemcpyAsync(c->boff, hb.data(), sizeof(int) * hb.size(), cudaMemcpyHostToDevice, c->st));
   CK(cudaStreamSynchronize(c->st));
   return ATHG_OK;
 }
 
-// MGGravityDriver::Solve (gravity/mg_gravity.cpp:166-211) on the context's stream
-int gravity_solve(athg_ctx* c) {
+// MGGravityDriver::Solve (gravity/mg_gravity.cpp:166-211) on the context's stream, from
+// the density of `ucons` (the current state, or the fused stage's output buffer)
+int gravity_solve(athg_ctx* c, const double* ucons) {
   if (c->fgrav) {  // FFTGravityDriver::Solve (gravity/fft_gravity.cpp:58-100)
     std::string err;
-    if (athg::fftgrav_solve(c->fgrav, c->g, c->nb, c->u, c->boff, c->phi, c->st, &err))
+    if (athg::fftgrav_solve(c->fgrav, c->g, c->nb, ucons, c->boff, c->phi, c->phi2, c->st,
+                            &err))
       return fail(ATHG_ERR_CUDA, err);
     c->counting += 4;
     return ATHG_OK;
@@ -620,12 +635,12 @@ int gravity_solve(athg_ctx* c) {
   if (rc) return rc;
   const Geom& g = c->g;
   dim3 gg((unsigned)((g.nx1 * g.nx2 + 255) / 256), (unsigned)g.nx3, (unsigned)c->nb);
-  k_gather_rho<<<gg, 256, 0, c->st>>>(g, c->u, c->boff, src, n, c->four_pi_G);
+  k_gather_rho<<<gg, 256, 0, c->st>>>(g, ucons, c->boff, src, n, c->four_pi_G);
   CKL();
   if ((rc = athg::mg_solve(c->grav, false, nullptr, nullptr))) return rc;
   dim3 gs((unsigned)(((g.nx1 + 2) * (g.nx2 + 2) + 255) / 256), (unsigned)(g.nx3 + 2),
           (unsigned)c->nb);
-  k_scatter_phi<<<gs, 256, 0, c->st>>>(g, c->phi, c->boff, um, n);
+  k_scatter_phi<<<gs, 256, 0, c->st>>>(g, c->phi, c->phi2, c->boff, um, n);
   CKL();
   c->counting += 2;
   return ATHG_OK;
@@ -642,15 +657,14 @@ int launch_self_gravity(athg_ctx* c, int l) {
 }
 
 bool fused(const athg_ctx* c) {
-  return c->fused_ok && c->mixed() && c->cfg.integrator == ATHG_VL2 && !has_gravity(c) &&
-         !c->smr;
+  return c->fused_ok && c->mixed() && c->cfg.integrator == ATHG_VL2 && !c->smr;
 }
 
 // The single-pass stage kernel (opt-in: athg_set_stage_kernel) covers the fused path for
 // MHD with PLM (donor cell in the first VL2 stage), HLLD or HLLE, on meshes whose blocks it
 // tiles
 bool single_pass(const athg_ctx* c) {
-  return fused(c) && c->cfg.magnetic && c->cfg.xorder == 2 &&
+  return fused(c) && !has_gravity(c) && c->cfg.magnetic && c->cfg.xorder == 2 &&
          (c->cfg.rsolver == ATHG_HLLD || c->cfg.rsolver == ATHG_HLLE) && c->sp_on &&
          athg::single_pass_fits(c->g, 1);
 }
@@ -748,7 +762,8 @@ int launch_update_c2p(athg_ctx* c, int l, bool dt_too) {
   sb.b_in[0] = c->b1; sb.b_in[1] = c->b2; sb.b_in[2] = c->b3;
   sb.b_out[0] = c->r1; sb.b_out[1] = c->r2; sb.b_out[2] = c->r3;
   Launcher<float>::update_c2p(c->g, ptrs<float>(c), c->cfg.magnetic != 0, sw, phys(c), sb,
-                              dt_too ? (unsigned long long*)(c->scal + 3) : nullptr, c->st);
+                              dt_too ? (unsigned long long*)(c->scal + 3) : nullptr,
+                              has_gravity(c) ? c->phi2 : nullptr, c->st);
   c->counting += 1;
   CKL();
   return ATHG_OK;
@@ -826,6 +841,9 @@ int do_stage(athg_ctx* c, int stage) {
     if ((rc = launch_ghosts_f32(c))) return rc;
     mark(c, stage, "ghost exchange");
     c->ghosts_stale = true;
+    // the potential of the new state for the next stage (main.cpp:461-466)
+    if (has_gravity(c) && (rc = gravity_solve(c, c->u1))) return rc;
+    if (has_gravity(c)) mark(c, stage, "gravity solve");
     return ATHG_OK;
   }
   if ((rc = launch_fluxes(c, order))) return rc;
@@ -841,7 +859,7 @@ int do_stage(athg_ctx* c, int stage) {
   mark(c, stage, "ghost exchange");
   if ((rc = launch_c2p(c))) return rc;
   mark(c, stage, "primitives (k_c2p)");
-  if (has_gravity(c) && (rc = gravity_solve(c))) return rc;  // main.cpp:461-466
+  if (has_gravity(c) && (rc = gravity_solve(c, c->u))) return rc;  // main.cpp:461-466
   if (has_gravity(c)) mark(c, stage, "gravity solve");
   if (stage == c->integ.nstages) {
     if ((rc = launch_block_dt(c))) return rc;
@@ -1016,6 +1034,20 @@ int run_cycle_graph(athg_ctx* c) {
     c->ghosts_stale = true;
   } else {
     CK(cudaGraphLaunch(c->gexec, c->st));
+  }
+  return ATHG_OK;
+}
+
+// one whole cycle launched kernel by kernel (a cycle that cannot be captured: a multigrid
+// iterating to a threshold or with multipole boundaries); in the fused path the new state
+// is then in the other buffer, as after run_cycle_graph
+int run_cycle_direct(athg_ctx* c) {
+  int rc = autotune(c);
+  if (rc) return rc;
+  if ((rc = do_cycle(c))) return rc;
+  if (fused(c)) {
+    swap_state(c);
+    c->ghosts_stale = true;
   }
   return ATHG_OK;
 }
@@ -1787,7 +1819,7 @@ int athg_initialize(athg_ctx* c) {
   CK(cudaMemcpyAsync(c->scal, hs, sizeof(hs), cudaMemcpyHostToDevice, c->st));
   // the first perturbation of decaying or impulsive turbulence (mesh/mesh.cpp:1383-1384)
   if (c->turb && athg::turb_flag(c->turb) <= 2 && (rc = turb_drive(c))) return rc;
-  if (has_gravity(c) && (rc = gravity_solve(c))) return rc;  // mesh/mesh.cpp:1398-1402
+  if (has_gravity(c) && (rc = gravity_solve(c, c->u))) return rc;  // mesh/mesh.cpp:1398-1402
   if ((rc = launch_ghosts(c))) return rc;
   c->ghosts_stale = false;
   if ((rc = launch_c2p(c))) return rc;
@@ -1805,7 +1837,7 @@ int athg_resume(athg_ctx* c) {
   unsigned long long big;
   std::memcpy(&big, &kDblMax, 8);
   CK(cudaMemcpyAsync(c->scal + 3, &big, 8, cudaMemcpyHostToDevice, c->st));
-  if (has_gravity(c) && (rc = gravity_solve(c))) return rc;
+  if (has_gravity(c) && (rc = gravity_solve(c, c->u))) return rc;
   if ((rc = launch_ghosts(c))) return rc;
   c->ghosts_stale = false;
   if ((rc = launch_c2p(c))) return rc;
@@ -1839,7 +1871,7 @@ int athg_cycles(athg_ctx* c, int n) {
     for (int q = 0; q < n; ++q) {
       if ((rc = turb_drive(c))) return rc;
       if (!captured(c)) {
-        if ((rc = do_cycle(c))) return rc;
+        if ((rc = run_cycle_direct(c))) return rc;
       } else {
         if ((rc = build_graph(c))) return rc;
         if ((rc = run_cycle_graph(c))) return rc;
@@ -1851,7 +1883,7 @@ int athg_cycles(athg_ctx* c, int n) {
     // the solve iterates to a threshold or sets up multipole moments on the host, or
     // runs cuFFT
     for (int q = 0; q < n; ++q)
-      if ((rc = do_cycle(c))) return rc;
+      if ((rc = run_cycle_direct(c))) return rc;
     return ATHG_OK;
   }
   if (c->amr) {  // the refinement check after every cycle (main.cpp:470-477)
@@ -1939,6 +1971,7 @@ int athg_attach_gravity(athg_ctx* c, athg_mg* mg, double four_pi_G) {
   // one uniform level tiling the solver's n^3 root grid
   if ((rc = tile_blocks(c, n, n, n))) return rc;
   CK(cudaMemsetAsync(c->phi, 0, sizeof(double) * c->g.ncell * c->nb, c->st));
+  if (c->phi2) CK(cudaMemsetAsync(c->phi2, 0, sizeof(float2) * c->g.ncell * c->nb, c->st));
   if ((rc = athg::mg_bind_stream(mg, c->st))) return rc;
   c->grav = mg;
   c->four_pi_G = four_pi_G;
@@ -1958,6 +1991,7 @@ int athg_attach_fft_gravity(athg_ctx* c, const athg_mesh* mesh, double four_pi_G
   if (!mesh) return fail(ATHG_ERR_ARG, "null argument");
   if ((rc = tile_blocks(c, mesh->nx1, mesh->nx2, mesh->nx3))) return rc;
   CK(cudaMemsetAsync(c->phi, 0, sizeof(double) * c->g.ncell * c->nb, c->st));
+  if (c->phi2) CK(cudaMemsetAsync(c->phi2, 0, sizeof(float2) * c->g.ncell * c->nb, c->st));
   athg::FftMesh fm{{mesh->nx1, mesh->nx2, mesh->nx3},
                    {mesh->x1max - mesh->x1min, mesh->x2max - mesh->x2min, mesh->x3max - mesh->x3min}};
   std::string err;

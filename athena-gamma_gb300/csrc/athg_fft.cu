@@ -11,6 +11,7 @@
 #include <vector>
 
 #include "athg_fft.h"
+#include "athg_numeric.h"
 
 namespace athg {
 namespace {
@@ -105,9 +106,11 @@ __global__ void k_fg_kernel(cufftDoubleComplex* __restrict__ c, const double* __
 }
 
 // FFTBlock::RetrieveResult (athena_fft.cpp:133-162) times the normalisation, plus the one
-// ghost layer the gravity boundary exchange fills from the periodic neighbours
-__global__ void k_fg_scatter(Geom g, double* __restrict__ phi, const int* __restrict__ boff,
-                             const double* __restrict__ r, int n1, int n2, int n3, double norm) {
+// ghost layer the gravity boundary exchange fills from the periodic neighbours (and, for
+// the mixed path's source term, the same potential as FP32 pairs in phi2)
+__global__ void k_fg_scatter(Geom g, double* __restrict__ phi, float2* __restrict__ phi2,
+                             const int* __restrict__ boff, const double* __restrict__ r, int n1,
+                             int n2, int n3, double norm) {
   const int b = blockIdx.z, k = blockIdx.y;  // k over nx3 + 2
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   const int w1 = g.nx1 + 2, w2 = g.nx2 + 2;
@@ -117,8 +120,13 @@ __global__ void k_fg_scatter(Geom g, double* __restrict__ phi, const int* __rest
   I = (I + n1) % n1;
   J = (J + n2) % n2;
   K = (K + n3) % n3;
-  phi[(int64_t)b * g.ncell + cidx(g, k + g.ks - 1, j + g.js - 1, i + g.is - 1)] =
-      r[((int64_t)K * n2 + J) * n1 + I] * norm;
+  const int64_t q = (int64_t)b * g.ncell + cidx(g, k + g.ks - 1, j + g.js - 1, i + g.is - 1);
+  const double v = r[((int64_t)K * n2 + J) * n1 + I] * norm;
+  phi[q] = v;
+  if (phi2) {
+    const ff f = split_ff(v);
+    phi2[q] = make_float2(f.hi, f.lo);
+  }
 }
 
 // ---- turbulence ----------------------------------------------------------------------
@@ -317,7 +325,7 @@ int fftgrav_create(const FftMesh& m, double four_pi_G, FftGravity** out, std::st
 }
 
 int fftgrav_solve(FftGravity* f, const Geom& g, int nb, const double* u, const int* boff,
-                  double* phi, cudaStream_t st, std::string* err) {
+                  double* phi, float2* phi2, cudaStream_t st, std::string* err) {
   const int n1 = f->m.n[0], n2 = f->m.n[1], n3 = f->m.n[2];
   dim3 gg((unsigned)((g.nx1 * g.nx2 + kThreads - 1) / kThreads), (unsigned)g.nx3, (unsigned)nb);
   k_fg_gather<<<gg, kThreads, 0, st>>>(g, u, boff, f->r, n1, n2);
@@ -333,7 +341,7 @@ int fftgrav_solve(FftGravity* f, const Geom& g, int nb, const double* u, const i
     return -1;
   dim3 gs((unsigned)(((g.nx1 + 2) * (g.nx2 + 2) + kThreads - 1) / kThreads),
           (unsigned)(g.nx3 + 2), (unsigned)nb);
-  k_fg_scatter<<<gs, kThreads, 0, st>>>(g, phi, boff, f->r, n1, n2, n3, f->norm);
+  k_fg_scatter<<<gs, kThreads, 0, st>>>(g, phi, phi2, boff, f->r, n1, n2, n3, f->norm);
   if (!cu_ok(cudaGetLastError(), "fft gravity scatter", err)) return -1;
   return 0;
 }

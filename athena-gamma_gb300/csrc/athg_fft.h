@@ -32,9 +32,9 @@ int fftgrav_create(const FftMesh& m, double four_pi_G, FftGravity** out, std::st
 void fftgrav_destroy(FftGravity* f);
 // rho of every block (u, interior) -> phi of every block with one ghost layer (periodic
 // wrap, as the gravity boundary exchange fills it). boff: each block's cell offset in the
-// mesh (3 ints per block, device).
+// mesh (3 ints per block, device). phi2 (or nullptr): the same potential as FP32 pairs.
 int fftgrav_solve(FftGravity* f, const Geom& g, int nb, const double* u, const int* boff,
-                  double* phi, cudaStream_t st, std::string* err);
+                  double* phi, float2* phi2, cudaStream_t st, std::string* err);
 
 // Driver state at Mesh construction: `time` is the mesh time then (tdrive starts there).
 // Returns 0, 1 for an invalid configuration, -1 for a CUDA or cuFFT failure.

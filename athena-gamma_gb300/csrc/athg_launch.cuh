@@ -41,10 +41,11 @@ struct Launcher {
   static void c2p(const Geom& g, const StagePtrs<T>& p, bool mhd, const Phys& ph,
                   cudaStream_t st);
   // Mixed VL2: update + interior primitive recovery from `sb.in` into `sb.out`
-  // (k_update_c2p; no-op for the FP64 path, which never takes this route).
+  // (k_update_c2p; no-op for the FP64 path, which never takes this route). phi2: the
+  // potential as FP32 pairs [nb][cells] for the self-gravity source, or nullptr.
   static void update_c2p(const Geom& g, const StagePtrs<T>& p, bool mhd, const StageW& sw,
                          const Phys& ph, const StateBufs& sb, unsigned long long* dtmin,
-                         cudaStream_t st);
+                         const float2* phi2, cudaStream_t st);
   // HydroSourceTerms::SelfGravity over every block (phi: [nb][cells] potential).
   static void self_gravity(const Geom& g, const StagePtrs<T>& p, bool mhd, const StageW& sw,
                            const double* phi, cudaStream_t st);
@@ -164,17 +165,19 @@ void Launcher<T>::update(const Geom& g, const StagePtrs<T>& p, bool mhd, const S
 template <typename T>
 void Launcher<T>::update_c2p(const Geom& g, const StagePtrs<T>& p, bool mhd, const StageW& sw,
                              const Phys& ph, const StateBufs& sb, unsigned long long* dtmin,
-                             cudaStream_t st) {
+                             const float2* phi2, cudaStream_t st) {
   if constexpr (kMixed<T>) {
     Box b = make_box(g.is, g.ie, g.js, g.je, g.ks, g.ke);
     const dim3 gr = box_grid(b, g.nb, 128);
-    if (mhd) {
-      if (dtmin) k_update_c2p<true, true><<<gr, 128, 0, st>>>(g, p, b, sw, ph, sb, dtmin);
-      else k_update_c2p<true, false><<<gr, 128, 0, st>>>(g, p, b, sw, ph, sb, dtmin);
+#define ATHG_UC2P(M, D, S) k_update_c2p<M, D, S><<<gr, 128, 0, st>>>(g, p, b, sw, ph, sb, dtmin, phi2)
+    if (phi2) {
+      if (mhd) { if (dtmin) ATHG_UC2P(true, true, true); else ATHG_UC2P(true, false, true); }
+      else { if (dtmin) ATHG_UC2P(false, true, true); else ATHG_UC2P(false, false, true); }
     } else {
-      if (dtmin) k_update_c2p<false, true><<<gr, 128, 0, st>>>(g, p, b, sw, ph, sb, dtmin);
-      else k_update_c2p<false, false><<<gr, 128, 0, st>>>(g, p, b, sw, ph, sb, dtmin);
+      if (mhd) { if (dtmin) ATHG_UC2P(true, true, false); else ATHG_UC2P(true, false, false); }
+      else { if (dtmin) ATHG_UC2P(false, true, false); else ATHG_UC2P(false, false, false); }
     }
+#undef ATHG_UC2P
   }
 }
 

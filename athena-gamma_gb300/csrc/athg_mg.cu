@@ -56,46 +56,93 @@ __host__ __device__ inline long long ix(int nt, int k, int j, int i) {
 }
 
 // ------------------------------------------------------------------------- kernels --
+// With every face periodic and n even, a ghost cell holds a copy of the interior cell it
+// wraps to, and that cell has the ghost's red-black colour. So a smoothing sweep can also
+// write the periodic images of the cells it updates (push_images): it reads only cells of
+// the other colour, so nothing it reads changes, and the level's ghost layer then needs no
+// separate boundary fill.
+template <typename T>
+__device__ __forceinline__ void push_images(T* u, int n, int k, int j, int i, T v) {
+  const int oi = i == 1 ? n + 1 : (i == n ? 0 : -1);
+  const int oj = j == 1 ? n + 1 : (j == n ? 0 : -1);
+  const int ok = k == 1 ? n + 1 : (k == n ? 0 : -1);
+  if ((oi & oj & ok) == -1) return;  // not next to a face
+  const int nt = n + 2;
+  for (int s = 1; s < 8; ++s) {
+    const int x = (s & 1) ? oi : i, y = (s & 2) ? oj : j, z = (s & 4) ? ok : k;
+    if (x < 0 || y < 0 || z < 0) continue;
+    u[ix(nt, z, y, x)] = v;
+  }
+}
+
 // Red-black Gauss-Seidel half sweep: cells with (color + k + j + i - 1) even in the
 // reference's local indexing (i = is + c, is + c + 2, ...), one thread per updated cell.
 // Each kernel's per-cell work is a device function of the thread's index t, called by the
 // kernel (one thread per index) and by k_vcycle_small (a block-strided loop per step).
-template <typename T, typename I>
+// P2: n = 2^lg (the one-block levels), so t decodes with shifts and masks instead of the
+// integer divisions that otherwise take most of a small level's instructions.
+template <typename T, typename I, bool PUSH = false, bool P2 = false>
 __device__ __forceinline__ void smooth_cell(T* u, const T* src, int n, T dx2, T isix, int color,
-                                            I t) {
-  const int nh = (n + 1) / 2;
-  int ip = (int)(t % nh);
-  I r = t / nh;
-  int j = (int)(r % n) + 1, k = (int)(r / n) + 1;
+                                            I t, int lg = 0) {
+  int ip, j, k;
+  if constexpr (P2) {
+    const int lh = lg > 0 ? lg - 1 : 0;  // nh = (n + 1) / 2 = 2^lh
+    ip = (int)t & ((1 << lh) - 1);
+    const int r = (int)t >> lh;
+    j = (r & (n - 1)) + 1;
+    k = (r >> lg) + 1;
+  } else {
+    const int nh = (n + 1) / 2;
+    ip = (int)(t % nh);
+    I r = t / nh;
+    j = (int)(r % n) + 1;
+    k = (int)(r / n) + 1;
+  }
   int c = (color + k + j) & 1;
   int i = 1 + c + 2 * ip;
   if (i > n) return;
   const int nt = n + 2;
   const long long q = ix(nt, k, j, i), sk = (long long)nt * nt, sj = nt;
-  u[q] -= ((T(6.0) * u[q] - u[q + sk] - u[q + sj] - u[q + 1] - u[q - sk] - u[q - sj] - u[q - 1]) +
-           src[q] * dx2) * isix;
+  const T v = u[q] - ((T(6.0) * u[q] - u[q + sk] - u[q + sj] - u[q + 1] - u[q - sk] - u[q - sj] -
+                       u[q - 1]) + src[q] * dx2) * isix;
+  u[q] = v;
+  if constexpr (PUSH) push_images(u, n, k, j, i, v);
 }
 __host__ __device__ inline long long smooth_count(int n) {
   return (long long)((n + 1) / 2) * n * n;
 }
-template <typename T>
+template <typename T, bool PUSH>
 __global__ void k_smooth(T* __restrict__ u, const T* __restrict__ src, int n, T dx2, T isix,
                          int color) {
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const long long cnt = smooth_count(n);
   if (t >= cnt) return;
-  if (cnt <= 0x7fffffffLL) smooth_cell<T, int>(u, src, n, dx2, isix, color, (int)t);
-  else smooth_cell<T, long long>(u, src, n, dx2, isix, color, t);
+  if (cnt <= 0x7fffffffLL) smooth_cell<T, int, PUSH>(u, src, n, dx2, isix, color, (int)t);
+  else smooth_cell<T, long long, PUSH>(u, src, n, dx2, isix, color, t);
+}
+
+// interior cell (k, j, i) of an n^3 box from a thread index t, i fastest; P2: n = 2^lg
+template <bool P2, typename I>
+__device__ __forceinline__ void box_cell(I t, int n, int lg, int& k, int& j, int& i) {
+  if constexpr (P2) {
+    i = ((int)t & (n - 1)) + 1;
+    j = (((int)t >> lg) & (n - 1)) + 1;
+    k = ((int)t >> (2 * lg)) + 1;
+  } else {
+    i = (int)(t % n) + 1;
+    I r = t / n;
+    j = (int)(r % n) + 1;
+    k = (int)(r / n) + 1;
+  }
 }
 
 // defect of the fine level averaged onto the coarse cell (CalculateDefect + Restrict);
 // with FAS the fine solution is restricted too (RestrictBlock).
-template <typename T, typename I>
+template <typename T, typename I, bool P2 = false>
 __device__ __forceinline__ void defect_restrict_cell(const T* uf, const T* sf, T* sc, T* uc, int nc,
-                                                     T idx2, int fas, I t) {
-  int i = (int)(t % nc) + 1;
-  I r = t / nc;
-  int j = (int)(r % nc) + 1, k = (int)(r / nc) + 1;
+                                                     T idx2, int fas, I t, int lg = 0) {
+  int i, j, k;
+  box_cell<P2>(t, nc, lg, k, j, i);
   const int nf = 2 * nc, ntf = nf + 2, ntc = nc + 2;
   const long long sk = (long long)ntf * ntf, sj = ntf;
   const int fk = 2 * k - 1, fj = 2 * j - 1, fi = 2 * i - 1;
@@ -142,11 +189,10 @@ __global__ void k_restrict(const T* __restrict__ f, T* __restrict__ c, int nc) {
 }
 
 // src -= L'(u) on the interior (CalculateFASRHS)
-template <typename T, typename I>
-__device__ __forceinline__ void fas_rhs_cell(const T* u, T* src, int n, T idx2, I t) {
-  int i = (int)(t % n) + 1;
-  I r = t / n;
-  int j = (int)(r % n) + 1, k = (int)(r / n) + 1;
+template <typename T, typename I, bool P2 = false>
+__device__ __forceinline__ void fas_rhs_cell(const T* u, T* src, int n, T idx2, I t, int lg = 0) {
+  int i, j, k;
+  box_cell<P2>(t, n, lg, k, j, i);
   const int nt = n + 2;
   const long long q = ix(nt, k, j, i), sk = (long long)nt * nt, sj = nt;
   src[q] -= (T(6.0) * u[q] - u[q + sk] - u[q + sj] - u[q + 1] - u[q - sk] - u[q - sj] - u[q - 1]) *
@@ -163,12 +209,11 @@ __global__ void k_fas_rhs(const T* __restrict__ u, T* __restrict__ src, int n, T
 
 // trilinear prolongation of the coarse correction, added to the fine level
 // (ProlongateAndCorrect); with FAS the correction is u_c - u_old_c.
-template <typename T, typename I>
+template <typename T, typename I, bool P2 = false>
 __device__ __forceinline__ void prolong_correct_cell(const T* uc, const T* uold, T* uf, int nc,
-                                                     I t) {
-  int i = (int)(t % nc) + 1;
-  I r = t / nc;
-  int j = (int)(r % nc) + 1, k = (int)(r / nc) + 1;
+                                                     I t, int lg = 0) {
+  int i, j, k;
+  box_cell<P2>(t, nc, lg, k, j, i);
   const int ntc = nc + 2, ntf = 2 * nc + 2;
   auto S = [&](int kk, int jj, int ii) -> T {
     long long q = ix(ntc, kk, jj, ii);
@@ -308,24 +353,31 @@ __global__ void k_mp_tab(double* tab, int n, double lo0, double hi0, double lo1,
 __host__ __device__ inline long long shell_count(int n) {
   return 2LL * (n + 2) * (n + 2) + 2LL * n * (n + 2) + 2LL * n * n;
 }
-template <typename T>
-__device__ __forceinline__ void bc_shell_cell(T* a, int n, const FaceOps& f, int t) {
+// P2 (the one-block levels, n = 2^lg <= 16): the quotients by n + 2 and (n + 2)^2 come
+// from FP32 reciprocals (div_small; rnt = 1 / (n + 2), rnt2 = 1 / (n + 2)^2), the others
+// from shifts.
+template <typename T, bool P2 = false>
+__device__ __forceinline__ void bc_shell_cell(T* a, int n, const FaceOps& f, int t, int lg = 0,
+                                              float rnt = 0.0f, float rnt2 = 0.0f) {
   // the shell of a level up to n = 4096 has fewer than 2^31 cells
   const int nt = n + 2;
   const int nx1 = 2 * nt * nt, nx2 = 2 * n * nt, nx3 = 2 * n * n;
   int c[3];
   if (t < nx1) {
-    const int side = t / (nt * nt);
-    const int r = t % (nt * nt);
-    c[0] = side ? n + 1 : 0; c[1] = r % nt; c[2] = r / nt;
+    const int side = P2 ? athg::div_small(t, rnt2) : t / (nt * nt);
+    const int r = t - side * (nt * nt);
+    const int rq = P2 ? athg::div_small(r, rnt) : r / nt;
+    c[0] = side ? n + 1 : 0; c[1] = r - rq * nt; c[2] = rq;
   } else if ((t -= nx1) < nx2) {
-    const int side = t / (n * nt);
-    const int r = t % (n * nt);
-    c[1] = side ? n + 1 : 0; c[0] = 1 + r % n; c[2] = r / n;
+    const int side = P2 ? athg::div_small(t >> lg, rnt) : t / (n * nt);
+    const int r = t - side * (n * nt);
+    const int rq = P2 ? (r >> lg) : r / n;
+    c[1] = side ? n + 1 : 0; c[0] = 1 + (r - rq * n); c[2] = rq;
   } else if ((t -= nx2) < nx3) {
-    const int side = t / (n * n);
-    const int r = t % (n * n);
-    c[2] = side ? n + 1 : 0; c[0] = 1 + r % n; c[1] = 1 + r / n;
+    const int side = P2 ? (t >> (2 * lg)) : t / (n * n);
+    const int r = t - side * (n * n);
+    const int rq = P2 ? (r >> lg) : r / n;
+    c[2] = side ? n + 1 : 0; c[0] = 1 + (r - rq * n); c[1] = 1 + rq;
   } else {
     return;
   }
@@ -397,10 +449,12 @@ __global__ void __launch_bounds__(kSmallThreads) k_vcycle_small(SmallV<T> v) {
     o[L] = nullptr;
     if (v.fas) { o[L] = sm + off; off += c; }
   }
+  // every level here is n = 2^L <= 16: int indices, and the per-cell functions decode
+  // their thread index with shifts (P2)
   const int tid = threadIdx.x, nth = blockDim.x;
-  auto cells = [](int L) { return (long long)((1 << L) + 2) * ((1 << L) + 2) * ((1 << L) + 2); };
+  auto cells = [](int L) { return ((1 << L) + 2) * ((1 << L) + 2) * ((1 << L) + 2); };
   for (int L = 0; L <= v.ls; ++L)
-    for (long long q = tid; q < cells(L); q += nth) {
+    for (int q = tid; q < cells(L); q += nth) {
       u[L][q] = v.u[L][q];
       s[L][q] = v.src[L][q];
       if (v.fas) o[L][q] = v.uold[L][q];
@@ -410,27 +464,30 @@ __global__ void __launch_bounds__(kSmallThreads) k_vcycle_small(SmallV<T> v) {
     FaceOps f;
     for (int q = 0; q < 6; ++q) f.op[q] = v.op[q];
     f.tab = v.tab[L];
-    const int n = 1 << L;
-    for (int t = tid; t < (int)shell_count(n); t += nth) bc_shell_cell<T>(u[L], n, f, t);
+    const int n = 1 << L, nt = n + 2;
+    const float rnt = 1.0f / (float)nt, rnt2 = 1.0f / (float)(nt * nt);
+    for (int t = tid; t < (int)shell_count(n); t += nth)
+      bc_shell_cell<T, true>(u[L], n, f, t, L, rnt, rnt2);
     __syncthreads();
   };
   auto smooth = [&](int L, int color) {
     const int n = 1 << L;
     for (int t = tid; t < (int)smooth_count(n); t += nth)
-      smooth_cell<T, int>(u[L], s[L], n, v.dx2[L], v.isix, color ^ v.coff, t);
+      smooth_cell<T, int, false, true>(u[L], s[L], n, v.dx2[L], v.isix, color ^ v.coff, t, L);
     __syncthreads();
   };
   auto store_old = [&](int L) {
-    for (long long q = tid; q < cells(L); q += nth) o[L][q] = u[L][q];
+    for (int q = tid; q < cells(L); q += nth) o[L][q] = u[L][q];
     __syncthreads();
   };
   auto fas_rhs = [&](int L) {
     const int n = 1 << L;
-    for (int t = tid; t < n * n * n; t += nth) fas_rhs_cell<T, int>(u[L], s[L], n, v.idx2[L], t);
+    for (int t = tid; t < n * n * n; t += nth)
+      fas_rhs_cell<T, int, true>(u[L], s[L], n, v.idx2[L], t, L);
     __syncthreads();
   };
   auto zero = [&](int L) {
-    for (long long q = tid; q < cells(L); q += nth) u[L][q] = T(0.0);
+    for (int q = tid; q < cells(L); q += nth) u[L][q] = T(0.0);
     __syncthreads();
   };
   // down: vcycle() levels ls..1
@@ -443,7 +500,8 @@ __global__ void __launch_bounds__(kSmallThreads) k_vcycle_small(SmallV<T> v) {
     bc(L);
     const int nc = 1 << (L - 1);
     for (int t = tid; t < nc * nc * nc; t += nth)
-      defect_restrict_cell<T, int>(u[L], s[L], s[L - 1], u[L - 1], nc, v.idx2[L], v.fas, t);
+      defect_restrict_cell<T, int, true>(u[L], s[L], s[L - 1], u[L - 1], nc, v.idx2[L], v.fas, t,
+                                         L - 1);
     __syncthreads();
     if (!v.fas) zero(L - 1);
   }
@@ -464,7 +522,7 @@ __global__ void __launch_bounds__(kSmallThreads) k_vcycle_small(SmallV<T> v) {
     bc(L);
     const int nc = 1 << L;
     for (int t = tid; t < nc * nc * nc; t += nth)
-      prolong_correct_cell<T, int>(u[L], v.fas ? o[L] : nullptr, u[L + 1], nc, t);
+      prolong_correct_cell<T, int, true>(u[L], v.fas ? o[L] : nullptr, u[L + 1], nc, t, L);
     __syncthreads();
     bc(L + 1);
     smooth(L + 1, 0);
@@ -472,7 +530,7 @@ __global__ void __launch_bounds__(kSmallThreads) k_vcycle_small(SmallV<T> v) {
     smooth(L + 1, 1);
   }
   for (int L = 0; L <= v.ls; ++L)
-    for (long long q = tid; q < cells(L); q += nth) {
+    for (int q = tid; q < cells(L); q += nth) {
       v.u[L][q] = u[L][q];
       v.src[L][q] = s[L][q];
       if (v.fas) v.uold[L][q] = o[L][q];
@@ -510,19 +568,6 @@ __device__ void block_add(double (&v)[NV], double* out) {
 }
 
 template <typename T>
-__global__ void k_sum(const T* a, int n, double* out) {
-  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  double v[1] = {0.0};
-  if (t < (long long)n * n * n) {
-    int i = (int)(t % n) + 1;
-    long long r = t / n;
-    int j = (int)(r % n) + 1, k = (int)(r / n) + 1;
-    v[0] = (double)a[ix(n + 2, k, j, i)];
-  }
-  block_add<1>(v, out);
-}
-
-template <typename T>
 __global__ void k_sub_const(T* a, long long cnt, const double* tot, double scale) {
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= cnt) return;
@@ -534,6 +579,27 @@ __global__ void k_sub_const(T* a, long long cnt, const double* tot, double scale
 // reduction (a block reduction per cell cost more than the summed terms themselves).
 constexpr int kColK = 32;
 __host__ __device__ inline int col_chunks(int n) { return (n + kColK - 1) / kColK; }
+
+// Sum of the interior cells of one level (Multigrid::CalculateTotal), as column sums.
+template <typename T>
+__global__ void k_sum(const T* a, int n, double* out) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  double v[1] = {0.0};
+  if (t < (long long)n * n * col_chunks(n)) {
+    const int i = (int)(t % n) + 1, j = (int)((t / n) % n) + 1;
+    const int k0 = 1 + (int)(t / ((long long)n * n)) * kColK, k1 = min(n, k0 + kColK - 1);
+    const long long sk = (long long)(n + 2) * (n + 2);
+    const T* p = a + ix(n + 2, k0, j, i);
+    double acc = 0.0;
+    // FP32 values widen on the integer pipe (f2d_int): only the addition is an FP64 instruction
+    for (int k = k0; k <= k1; ++k, p += sk) {
+      if constexpr (sizeof(T) == 4) acc += athg::f2d_int(*p);
+      else acc += (double)*p;
+    }
+    v[0] = acc;
+  }
+  block_add<1>(v, out);
+}
 
 // Sum of squared defects of the finest level, as column sums. FP64
 // path: the FP64 defect. Mixed path (dfl): the seven-point sum exactly in integers and the
@@ -609,6 +675,21 @@ __global__ void k_widen(const float* a, double* b, long long cnt) {
 __global__ void k_narrow(const double* a, float* b, long long cnt) {
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t < cnt) b[t] = athg::d2f_int(a[t]);
+}
+// the mean subtraction of the FP64 source (k_sub_const) and its narrowing in one pass
+__global__ void k_sub_narrow(double* a, float* b, long long cnt, const double* tot,
+                             double scale) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= cnt) return;
+  const double v = a[t] - (*tot) * scale;
+  a[t] = v;
+  b[t] = athg::d2f_int(v);
+}
+// the widening of the FP32 FMG solution and its mean subtraction (k_sub_const) in one pass
+__global__ void k_widen_sub(const float* a, double* b, long long cnt, const double* tot,
+                            double scale) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < cnt) b[t] = athg::f2d_int(a[t]) - (*tot) * scale;
 }
 
 // multipole moments (and the centre of mass) of the finest source, FP64, as column sums (x
@@ -809,14 +890,27 @@ int tabulate_multipole(athg_mg* m, Hier<T>& h) {
   return ATHG_OK;
 }
 
+// whether the smoothing sweeps of an n^3 level also write its periodic ghost images
+// (push_images): every face periodic, n even, and n <= 128. On a GB300 the pushes add
+// 0.6-2.3 us to a sweep up to n = 128 against 3.2-3.7 us for a boundary-fill launch, but
+// 12.5 us at n = 256 against 6.2 us.
+constexpr int kPushMaxN = 128;
+bool pushes(const athg_mg* m, int n) {
+  return m->periodic && n >= 2 && n % 2 == 0 && n <= kPushMaxN;
+}
+
 template <typename T>
 int smooth(athg_mg* m, Hier<T>& h, int L, int color, int coff) {
   const int n = h.n[L];
   const double dx = h.dx[L];
   const double isix = 1.15 / 6.0;
   long long nth = (long long)((n + 1) / 2) * n * n;
-  k_smooth<T><<<nblk(nth), TPB, 0, m->st>>>(h.u[L], h.src[L], n, (T)(dx * dx), (T)isix,
-                                            color ^ coff);
+  if (pushes(m, n))
+    k_smooth<T, true><<<nblk(nth), TPB, 0, m->st>>>(h.u[L], h.src[L], n, (T)(dx * dx), (T)isix,
+                                                    color ^ coff);
+  else
+    k_smooth<T, false><<<nblk(nth), TPB, 0, m->st>>>(h.u[L], h.src[L], n, (T)(dx * dx), (T)isix,
+                                                     color ^ coff);
   MCKL();
   return ATHG_OK;
 }
@@ -870,13 +964,17 @@ int vcycle(athg_mg* m, Hier<T>& h, int top, bool fas, bool homog, bool subtract,
   // FP32 levels up to n = 16; FP64 ones up to n = 8, since one SM's FP64 rate (1/64 of
   // FP32 on this GPU) makes the 16^3 level faster as separate multi-SM launches
   const int ls = std::min(sizeof(T) == 4 ? kSmallLevels - 1 : kSmallLevels - 2, top);
+  // Periodic levels (pushes): the smoothing sweeps keep the ghost layer filled and a level
+  // zeroed on the way down has zero ghosts, so the boundary fills left there are the top
+  // level's first one, the one after the one-block levels and those after prolongation.
   for (int L = top; L > ls; --L) {
-    RC(apply_bc(m, h, L, homog));
+    const bool p = pushes(m, h.n[L]);
+    if (!p || fas || L == top) RC(apply_bc(m, h, L, homog));
     if (fas && L < top) { RC(store_old(m, h, L)); RC(fas_rhs(m, h, L)); }
     RC(smooth(m, h, L, 0, coff));
-    RC(apply_bc(m, h, L, homog));
+    if (!p) RC(apply_bc(m, h, L, homog));
     RC(smooth(m, h, L, 1, coff));
-    RC(apply_bc(m, h, L, homog));
+    if (!p) RC(apply_bc(m, h, L, homog));
     const int nc = h.n[L - 1];
     const double dx = h.dx[L];
     k_defect_restrict<T><<<nblk((long long)nc * nc * nc), TPB, 0, m->st>>>(
@@ -886,29 +984,39 @@ int vcycle(athg_mg* m, Hier<T>& h, int top, bool fas, bool homog, bool subtract,
   }
   RC(small_vcycle(m, h, ls, top, fas, homog, subtract, coff));
   for (int L = ls; L < top; ++L) {
-    RC(apply_bc(m, h, L, homog));
+    if (L == ls || !pushes(m, h.n[L])) RC(apply_bc(m, h, L, homog));
     const int nc = h.n[L];
+    const bool p = pushes(m, h.n[L + 1]);
     k_prolong_correct<T><<<nblk((long long)nc * nc * nc), TPB, 0, m->st>>>(
         h.u[L], fas ? h.uold[L] : nullptr, h.u[L + 1], nc);
     MCKL();
     RC(apply_bc(m, h, L + 1, homog));
     RC(smooth(m, h, L + 1, 0, coff));
-    RC(apply_bc(m, h, L + 1, homog));
+    if (!p) RC(apply_bc(m, h, L + 1, homog));
     RC(smooth(m, h, L + 1, 1, coff));
   }
-  RC(apply_bc(m, h, top, homog));
+  // the ghost layer of the result (callers read it: FMG prolongation, the next cycle)
+  if (top == ls || !pushes(m, h.n[top])) RC(apply_bc(m, h, top, homog));
+  return ATHG_OK;
+}
+
+// the sum of level L's interior into m->red; *scale turns it into the mean: total = sum *
+// dx^3 (Multigrid::CalculateTotal), average = total / volume
+template <typename T>
+int level_sum(athg_mg* m, Hier<T>& h, const T* a, int L, double* scale) {
+  const int n = h.n[L];
+  MCK(cudaMemsetAsync(m->red, 0, sizeof(double), m->st));
+  k_sum<T><<<nblk((long long)n * n * col_chunks(n)), TPB, 0, m->st>>>(a, n, m->red);
+  MCKL();
+  const double dxl = h.dx[L];
+  *scale = dxl * dxl * dxl / m->vol;
   return ATHG_OK;
 }
 
 template <typename T>
 int subtract_mean(athg_mg* m, Hier<T>& h, T* a, int L) {
-  const int n = h.n[L];
-  MCK(cudaMemsetAsync(m->red, 0, sizeof(double), m->st));
-  k_sum<T><<<nblk((long long)n * n * n), TPB, 0, m->st>>>(a, n, m->red);
-  MCKL();
-  const double dxl = h.dx[L];
-  // total = sum * dx^3 (Multigrid::CalculateTotal), average = total / volume
-  const double scale = dxl * dxl * dxl / m->vol;
+  double scale;
+  RC(level_sum(m, h, a, L, &scale));
   k_sub_const<T><<<nblk((long long)h.cells(L)), TPB, 0, m->st>>>(a, (long long)h.cells(L), m->red,
                                                                 scale);
   MCKL();
@@ -926,9 +1034,9 @@ int fmg(athg_mg* m, Hier<T>& h, bool fas, bool subtract, int& coffset) {
     MCKL();
   }
   for (int f = 0; f <= top; ++f) {
+    // vcycle() leaves level f's ghost layer filled for the FMG prolongation
     RC(vcycle(m, h, f, fas, false, subtract, coffset));
     if (f != top) {
-      RC(apply_bc(m, h, f, false));
       const int nc = h.n[f];
       k_fmg_prolong<T><<<nblk((long long)nc * nc * nc), TPB, 0, m->st>>>(h.u[f], h.u[f + 1], nc);
       MCKL();
@@ -1222,21 +1330,37 @@ int mg_solve(athg_mg* m, bool want_norm, int* iterations, double* defect_norm) {
   const int top = m->lmax;
   Hier<double>& H = m->h64;
   m->iterations = 0;
-  if (m->subtract) RC(subtract_mean(m, H, H.src[top], top));
+  // mixed FMG: the mean subtractions of the source and of the FMG solution ride on the
+  // narrowing and widening passes (k_sub_narrow, k_widen_sub)
+  const bool mixed_fmg = m->cfg.mode == ATHG_MG_FMG && m->cfg.precision == ATHG_MIXED;
+  double scale = 0.0;
+  if (m->subtract) {
+    if (mixed_fmg) RC(level_sum(m, H, H.src[top], top, &scale));
+    else RC(subtract_mean(m, H, H.src[top], top));
+  }
   if (m->any_mp) RC(multipole_setup(m));
   if (m->cfg.mode == ATHG_MG_FMG) {
-    if (m->cfg.precision == ATHG_MIXED) {
+    if (mixed_fmg) {
       Hier<float>& h = m->h32;
       const long long c = (long long)h.cells(top);
-      k_narrow<<<nblk(c), TPB, 0, m->st>>>(H.src[top], h.src[top], c);
+      if (m->subtract) {
+        k_sub_narrow<<<nblk(c), TPB, 0, m->st>>>(H.src[top], h.src[top], c, m->red, scale);
+      } else {
+        k_narrow<<<nblk(c), TPB, 0, m->st>>>(H.src[top], h.src[top], c);
+      }
       MCKL();
       RC(fmg(m, h, m->fas, m->subtract, m->coffset32));
-      k_widen<<<nblk(c), TPB, 0, m->st>>>(h.u[top], H.u[top], c);
+      if (m->subtract) {
+        RC(level_sum(m, h, h.u[top], top, &scale));
+        k_widen_sub<<<nblk(c), TPB, 0, m->st>>>(h.u[top], H.u[top], c, m->red, scale);
+      } else {
+        k_widen<<<nblk(c), TPB, 0, m->st>>>(h.u[top], H.u[top], c);
+      }
       MCKL();
     } else {
       RC(fmg(m, H, m->fas, m->subtract, m->coffset));
+      if (m->subtract) RC(subtract_mean(m, H, H.u[top], top));
     }
-    if (m->subtract) RC(subtract_mean(m, H, H.u[top], top));
   }
   double def = 0.0;
   if (m->cfg.threshold >= 0.0) {  // SolveIterative (multigrid_driver.cpp:721-760)

@@ -251,4 +251,10 @@ ATHG_HD bool lap7_ff(double c, const double* n, ff& out) {
   return true;
 }
 
+// Quotient a / b for 0 <= a < 2^12 and 1 <= b <= 2^10, given rb = 1 / b rounded to binary32:
+// one FP32 multiply in place of an integer division. (a + 0.5) / b lies at least 0.5 / b
+// from every integer, and the two roundings move (a + 0.5) * rb by at most about
+// 2^-23 (a + 0.5) / b, below 2^-12 / b, so truncation gives the exact quotient.
+ATHG_HD int div_small(int a, float rb) { return (int)(((float)a + 0.5f) * rb); }
+
 }  // namespace athg

@@ -882,12 +882,26 @@ struct StateBufs {
   double* b_out[3];
 };
 
+// (a.hi + a.lo) - (b.hi + b.lo) rounded to binary32: TwoSum of the leading parts, so the
+// difference of two nearby FP64 potentials keeps its FP32 precision
+__device__ __forceinline__ float pair_diff(float2 a, float2 b) {
+  float s, e;
+  two_sum(a.x, -b.x, s, e);
+  return s + (e + (a.y - b.y));
+}
+
 // One cell of k_update_c2p; returns the cell's CFL time step (new_blockdt.cpp:58-158,
 // as k_block_dt computes it) when DT, so the last stage folds the time-step kernel in.
-template <bool MHD, bool DT>
+// SG: the self-gravity source (hydro/srcterms/self_gravity.cpp:35-125) joins the
+// momentum and energy increments before they reach the FP64 state: momentum from the
+// potential differences times the stage-start density, energy from this stage's mass
+// fluxes. phi2 holds the potential as FP32 pairs hi + lo (one ghost layer), so the
+// differences take no FP64 instructions.
+template <bool MHD, bool DT, bool SG>
 __device__ __forceinline__ float update_c2p_cell(const Geom& g, const StagePtrs<float>& p,
                                                  int i, int j, int k, int b, const StageW& sw,
-                                                 const Phys& ph, const StateBufs& sb) {
+                                                 const Phys& ph, const StateBufs& sb,
+                                                 const float2* __restrict__ phi2) {
   const MixedGeo mg = p.mg[b];
   const float wf = __fmul_rn(sw.betaf, __ldg(p.dtT));
   const int64_t nc = g.ncell;
@@ -900,6 +914,28 @@ __device__ __forceinline__ float update_c2p_cell(const Geom& g, const StagePtrs<
   const float* __restrict__ F3 = p.flx[2] + (int64_t)b * NF * g.nf3;
   const int64_t q1 = f1idx(g, k, j, i), q2 = f2idx(g, k, j, i), q3 = f3idx(g, k, j, i);
   const int64_t s2 = g.nc1, s3 = (int64_t)g.nc1 * g.nc2;
+  const float cw1 = __fmul_rn(wf, mg.idx[0]), cw2 = __fmul_rn(wf, mg.idx[1]),
+              cw3 = __fmul_rn(wf, mg.idx[2]);
+  float* __restrict__ w = p.w + (int64_t)b * NHYD * nc;
+  float sgs[NHYD] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f};  // source terms, subtracted below
+  if constexpr (SG) {
+    // first, while few values are live: the density the stage's fluxes were computed
+    // from (this thread's own cell of W, read before it is overwritten below), the
+    // potential differences and the mass fluxes of the six faces
+    const float rho = w[c];
+    const float2* __restrict__ pp = phi2 + (int64_t)b * nc;
+    const float2 pc = __ldg(pp + c);
+    const int64_t sd[3] = {1, s2, s3};
+    const float cw[3] = {cw1, cw2, cw3};
+    const float* __restrict__ Fd[3] = {F1 + q1, F2 + q2, F3 + q3};
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      const float dl = pair_diff(pc, __ldg(pp + c - sd[d]));
+      const float dr = pair_diff(__ldg(pp + c + sd[d]), pc);
+      sgs[1 + d] = cw[d] * rho * (0.5f * (dl + dr));
+      sgs[4] += cw[d] * (0.5f * (__ldg(Fd[d]) * dl + __ldg(Fd[d] + sd[d]) * dr));
+    }
+  }
   float fx[NHYD][6];
   double uo[NHYD];
 #pragma unroll
@@ -938,14 +974,17 @@ __device__ __forceinline__ float update_c2p_cell(const Geom& g, const StagePtrs<
       }
   }
   // conserved update (base = the state at the start of the cycle)
-  const float cw1 = __fmul_rn(wf, mg.idx[0]), cw2 = __fmul_rn(wf, mg.idx[1]),
-              cw3 = __fmul_rn(wf, mg.idx[2]);
   double un[NHYD];
 #pragma unroll
   for (int n = 0; n < NHYD; ++n) {
     float hi, lo;
     sum3diff(__fmul_rn(cw1, fx[n][0]), __fmul_rn(cw1, fx[n][1]), __fmul_rn(cw2, fx[n][2]),
              __fmul_rn(cw2, fx[n][3]), __fmul_rn(cw3, fx[n][4]), __fmul_rn(cw3, fx[n][5]), hi, lo);
+    if (SG && n > 0) {
+      float e;
+      two_sum(hi, sgs[n], hi, e);
+      lo += e;
+    }
     un[n] = (uo[n] - f2d_int(hi)) - f2d_int(lo);
   }
   ff ss = {0.0f, 0.0f};
@@ -988,7 +1027,6 @@ __device__ __forceinline__ float update_c2p_cell(const Geom& g, const StagePtrs<
     ss = ff_add(ff_add(ff_sqr(s1), ff_sqr(s2f)), ff_sqr(s3f));
   }
   // primitive recovery (the mixed k_c2p)
-  float* __restrict__ w = p.w + (int64_t)b * NHYD * nc;
   double ud = un[0];
   const uint64_t ub = bits_d(ud);
   if (!((ub >> 63) == 0 && ub > bits_d(ph.dfloor) && ub <= 0x7ff0000000000000ull)) ud = ph.dfloor;
@@ -1048,14 +1086,14 @@ __device__ __forceinline__ float update_c2p_cell(const Geom& g, const StagePtrs<
   return 3.402823466e38f;
 }
 
-template <bool MHD, bool DT>
+template <bool MHD, bool DT, bool SG>
 __global__ void __launch_bounds__(128, 8)
 k_update_c2p(Geom g, StagePtrs<float> p, Box bx, StageW sw, Phys ph, StateBufs sb,
-             unsigned long long* dtmin) {
+             unsigned long long* dtmin, const float2* __restrict__ phi2) {
   int i, j, k, b;
   const bool active = box_coords(bx, i, j, k, b);
   float mindt = 3.402823466e38f;
-  if (active) mindt = update_c2p_cell<MHD, DT>(g, p, i, j, k, b, sw, ph, sb);
+  if (active) mindt = update_c2p_cell<MHD, DT, SG>(g, p, i, j, k, b, sw, ph, sb, phi2);
   if constexpr (DT) {  // block minimum, then one 64-bit atomicMin (as k_block_dt)
     for (int o = 16; o > 0; o >>= 1) mindt = mn(mindt, __shfl_xor_sync(0xffffffffu, mindt, o));
     __shared__ float red[32];

@@ -344,8 +344,8 @@ def run_next_rows(athg, torch):
         out["fft_gravity"] = {"workload": WORKLOAD + "_fft_self_gravity", "precision": "mixed",
                               "ms_per_cycle": ms, "ms_per_solve": float(np.median(solve)),
                               "note": "one FFT Poisson solve per stage (256^3 real-to-complex "
-                                      "and back, kernel, gather, scatter); self-gravity runs "
-                                      "the unfused mixed stage"}
+                                      "and back, kernel, gather, scatter); the source term "
+                                      "runs inside the fused mixed update (k_update_c2p)"}
     except Exception as e:  # noqa: BLE001 - reported, the bench line still prints
         out["fft_gravity"] = {"error": str(e)[:200]}
     try:

@@ -14,6 +14,11 @@ static int fails = 0;
 int main(int argc, char** argv) {
   const long n = argc > 1 ? std::atol(argv[1]) : 2000000;
   std::mt19937_64 rng(12345);
+  // small-range quotients by an FP32 reciprocal: every a < 2^12, every b <= 2^10
+  for (int b = 1; b <= 1024; ++b) {
+    const float rb = 1.0f / (float)b;
+    for (int a = 0; a < 4096; ++a) CHECK(div_small(a, rb) == a / b, "div_small %d / %d", a, b);
+  }
   // binary32 -> binary64: every normal float, sampled across all bit patterns
   for (long t = 0; t < n; ++t) {
     uint32_t u = (uint32_t)rng();

@@ -84,3 +84,48 @@ def test_turbulent_box_mixed_tracks_fp64():
         mg.close()
     l1 = np.mean(np.abs(rho["mixed"] - rho["fp64"])) / np.mean(np.abs(rho["fp64"]))
     assert l1 < 1e-5, l1
+
+
+@pytest.mark.parametrize("mhd", [True, False])
+@pytest.mark.parametrize("threshold", [-1.0, 0.0])
+def test_fused_mixed_sg_tracks_fp64(mhd, threshold):
+    """The fused mixed VL2 stage with the self-gravity source inside the update (potential
+    read as FP32 pairs) against the separate-kernel mixed path (k_update, k_self_gravity,
+    k_c2p), both measured from the FP64 run, on 8 blocks over five cycles. The two mixed
+    paths round the source term differently (by an FP32 ulp), so they agree to the mixed
+    path's noise, not bit for bit: the fused one must stay as close to FP64 as the other.
+    threshold -1: a fixed cycle count per solve, the cycles run as captured graphs;
+    threshold 0: the solve iterates to convergence and the cycles run kernel by kernel.
+    Both mixed runs leave the state in the other buffer (odd cycle count)."""
+    import oracle_lib as ol
+    n, mb = 32, (16, 16, 16)
+    u, b1, b2, b3 = ol.smooth_random_state((n, n, n), mhd, seed=29, amp=0.3)
+    out = {}
+    for mode in ("fp64", "fused", "unfused"):
+        sim = athg.Sim((n, n, n), mb, mhd=mhd, solver="hlld" if mhd else "hllc",
+                       precision="fp64" if mode == "fp64" else "mixed", cfl=0.4, tlim=100.0)
+        mg = athg.Multigrid(n, domain=((0.0, 1.0),) * 3, bc="periodic", mode="FMG",
+                            threshold=threshold, niteration=2, precision="fp64")
+        sim.attach_gravity(mg, 4.0)
+        sim.load_interior(u, b1, b2, b3)
+        sim.initialize()
+        if mode == "unfused":
+            # any single-step entry point leaves the fused path for good
+            athg.check(athg.lib().athg_exchange_ghosts(sim.h))
+        sim.cycles(5)
+        out[mode] = (sim.interior(), sim.phi(), sim.get_time())
+        sim.attach_gravity(None, 0.0)
+        sim.close()
+        mg.close()
+    ref, rphi, rt = out["fp64"]
+    err = {}
+    for mode in ("fused", "unfused"):
+        st, phi, t = out[mode]
+        assert t[2] == rt[2]
+        assert t[0] == pytest.approx(rt[0], rel=1e-6)
+        e = {k: np.abs(st[k] - ref[k]).max() / np.abs(ref[k]).max() for k in ref}
+        e["phi"] = np.abs(phi - rphi).max() / np.abs(rphi).max()
+        err[mode] = e
+    for k, e in err["fused"].items():
+        assert e < 5e-6, (k, err)
+        assert e <= 2.0 * err["unfused"][k] + 1e-9, (k, err)
