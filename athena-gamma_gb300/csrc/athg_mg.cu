@@ -433,6 +433,8 @@ struct SmallV {
   T dx2[kSmallLevels], idx2[kSmallLevels];
   int op[6];
   int ls, top, fas, subtract, coff;
+  int push;    // every face periodic: the sweeps of levels L >= 1 write their ghost images
+  int anyper;  // some face periodic
   T isix;
 };
 
@@ -470,10 +472,18 @@ __global__ void __launch_bounds__(kSmallThreads) k_vcycle_small(SmallV<T> v) {
       bc_shell_cell<T, true>(u[L], n, f, t, L, rnt, rnt2);
     __syncthreads();
   };
+  // pushes and boundary fills between colour sweeps as in vcycle() (pushes, mid_fill)
+  auto pushL = [&](int L) { return v.push && L >= 1; };
+  auto midfill = [&](int L) { return v.anyper && !pushL(L); };
   auto smooth = [&](int L, int color) {
     const int n = 1 << L;
-    for (int t = tid; t < (int)smooth_count(n); t += nth)
-      smooth_cell<T, int, false, true>(u[L], s[L], n, v.dx2[L], v.isix, color ^ v.coff, t, L);
+    if (pushL(L)) {
+      for (int t = tid; t < (int)smooth_count(n); t += nth)
+        smooth_cell<T, int, true, true>(u[L], s[L], n, v.dx2[L], v.isix, color ^ v.coff, t, L);
+    } else {
+      for (int t = tid; t < (int)smooth_count(n); t += nth)
+        smooth_cell<T, int, false, true>(u[L], s[L], n, v.dx2[L], v.isix, color ^ v.coff, t, L);
+    }
     __syncthreads();
   };
   auto store_old = [&](int L) {
@@ -492,12 +502,13 @@ __global__ void __launch_bounds__(kSmallThreads) k_vcycle_small(SmallV<T> v) {
   };
   // down: vcycle() levels ls..1
   for (int L = v.ls; L > 0; --L) {
-    bc(L);
+    // a level below the top was zeroed (ghosts included) unless FAS
+    if (!(pushL(L) && !v.fas && L < v.top)) bc(L);
     if (v.fas && L < v.top) { store_old(L); fas_rhs(L); }
     smooth(L, 0);
-    bc(L);
+    if (midfill(L)) bc(L);
     smooth(L, 1);
-    bc(L);
+    if (!pushL(L)) bc(L);
     const int nc = 1 << (L - 1);
     for (int t = tid; t < nc * nc * nc; t += nth)
       defect_restrict_cell<T, int, true>(u[L], s[L], s[L - 1], u[L - 1], nc, v.idx2[L], v.fas, t,
@@ -513,20 +524,20 @@ __global__ void __launch_bounds__(kSmallThreads) k_vcycle_small(SmallV<T> v) {
     bc(0);
     if (v.fas) { store_old(0); fas_rhs(0); }
     smooth(0, 0);
-    bc(0);
+    if (midfill(0)) bc(0);
     smooth(0, 1);
     bc(0);
   }
   // up: vcycle() levels 0..ls-1
   for (int L = 0; L < v.ls; ++L) {
-    bc(L);
+    if (L == 0 || !pushL(L)) bc(L);
     const int nc = 1 << L;
     for (int t = tid; t < nc * nc * nc; t += nth)
       prolong_correct_cell<T, int, true>(u[L], v.fas ? o[L] : nullptr, u[L + 1], nc, t, L);
     __syncthreads();
     bc(L + 1);
     smooth(L + 1, 0);
-    bc(L + 1);
+    if (midfill(L + 1)) bc(L + 1);
     smooth(L + 1, 1);
   }
   for (int L = 0; L <= v.ls; ++L)
@@ -814,6 +825,7 @@ struct athg_mg {
   athg_mg_config cfg{};
   int lmax = 0;
   bool periodic = true, subtract = true, fas = false, any_mp = false;
+  bool any_periodic = false;  // some face periodic
   double rdx = 0.0, vol = 0.0;
   cudaStream_t st = nullptr;
   cudaStream_t own_st = nullptr;  // the stream created with the solver
@@ -899,6 +911,14 @@ bool pushes(const athg_mg* m, int n) {
   return m->periodic && n >= 2 && n % 2 == 0 && n <= kPushMaxN;
 }
 
+// whether the two colour sweeps of a smoothing step need a boundary fill between them.
+// A ghost next to a non-periodic face (zero gradient, zero-fixed, multipole: a function of
+// the interior cell it mirrors) is read only by that cell, which the other colour's sweep
+// does not change, so it is filled again before the next sweep of its own colour anyway;
+// only periodic ghosts, the images of cells of the other colour, change in between, and
+// pushes keep those filled.
+bool mid_fill(const athg_mg* m, int n) { return m->any_periodic && !pushes(m, n); }
+
 template <typename T>
 int smooth(athg_mg* m, Hier<T>& h, int L, int color, int coff) {
   const int n = h.n[L];
@@ -950,6 +970,8 @@ int small_vcycle(athg_mg* m, Hier<T>& h, int ls, int top, bool fas, bool homog, 
   }
   for (int q = 0; q < 6; ++q) v.op[q] = f.op[q];
   v.ls = ls; v.top = top; v.fas = fas ? 1 : 0; v.subtract = subtract ? 1 : 0; v.coff = coff;
+  v.push = m->periodic ? 1 : 0;  // pushes(m, 2^L) for every L >= 1 here
+  v.anyper = m->any_periodic ? 1 : 0;
   v.isix = (T)(1.15 / 6.0);
   k_vcycle_small<T><<<1, kSmallThreads, small_smem<T>(ls, v.fas), m->st>>>(v);
   MCKL();
@@ -966,13 +988,13 @@ int vcycle(athg_mg* m, Hier<T>& h, int top, bool fas, bool homog, bool subtract,
   const int ls = std::min(sizeof(T) == 4 ? kSmallLevels - 1 : kSmallLevels - 2, top);
   // Periodic levels (pushes): the smoothing sweeps keep the ghost layer filled and a level
   // zeroed on the way down has zero ghosts, so the boundary fills left there are the top
-  // level's first one, the one after the one-block levels and those after prolongation.
+  // level's first one and those after prolongation.
   for (int L = top; L > ls; --L) {
     const bool p = pushes(m, h.n[L]);
     if (!p || fas || L == top) RC(apply_bc(m, h, L, homog));
     if (fas && L < top) { RC(store_old(m, h, L)); RC(fas_rhs(m, h, L)); }
     RC(smooth(m, h, L, 0, coff));
-    if (!p) RC(apply_bc(m, h, L, homog));
+    if (mid_fill(m, h.n[L])) RC(apply_bc(m, h, L, homog));
     RC(smooth(m, h, L, 1, coff));
     if (!p) RC(apply_bc(m, h, L, homog));
     const int nc = h.n[L - 1];
@@ -984,19 +1006,19 @@ int vcycle(athg_mg* m, Hier<T>& h, int top, bool fas, bool homog, bool subtract,
   }
   RC(small_vcycle(m, h, ls, top, fas, homog, subtract, coff));
   for (int L = ls; L < top; ++L) {
-    if (L == ls || !pushes(m, h.n[L])) RC(apply_bc(m, h, L, homog));
+    // the one-block levels' last sweep pushed too when pushes(): n = 2^ls <= 16
+    if (!pushes(m, h.n[L])) RC(apply_bc(m, h, L, homog));
     const int nc = h.n[L];
-    const bool p = pushes(m, h.n[L + 1]);
     k_prolong_correct<T><<<nblk((long long)nc * nc * nc), TPB, 0, m->st>>>(
         h.u[L], fas ? h.uold[L] : nullptr, h.u[L + 1], nc);
     MCKL();
     RC(apply_bc(m, h, L + 1, homog));
     RC(smooth(m, h, L + 1, 0, coff));
-    if (!p) RC(apply_bc(m, h, L + 1, homog));
+    if (mid_fill(m, h.n[L + 1])) RC(apply_bc(m, h, L + 1, homog));
     RC(smooth(m, h, L + 1, 1, coff));
   }
   // the ghost layer of the result (callers read it: FMG prolongation, the next cycle)
-  if (top == ls || !pushes(m, h.n[top])) RC(apply_bc(m, h, top, homog));
+  if (!pushes(m, h.n[top])) RC(apply_bc(m, h, top, homog));
   return ATHG_OK;
 }
 
@@ -1201,6 +1223,7 @@ int athg_mg_create(const athg_mg_config* cfg, athg_mg** out) {
   m->lmax = lmax;
   for (int f = 0; f < 6; ++f) {
     if (cfg->bc[f] != ATHG_MG_PERIODIC) m->periodic = false;
+    else m->any_periodic = true;
     if (cfg->bc[f] == ATHG_MG_MULTIPOLE) m->any_mp = true;
   }
   if (m->any_mp && cfg->mporder != 2 && cfg->mporder != 4) {
