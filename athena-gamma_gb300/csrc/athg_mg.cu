@@ -56,6 +56,11 @@ __host__ __device__ inline long long ix(int nt, int k, int j, int i) {
 }
 
 // ------------------------------------------------------------------------- kernels --
+// Every level is n = 2^lg cells per side (a power of two is checked when the solver is
+// made), so the kernels decode thread indices with shifts and masks: a division by a
+// runtime n is a long instruction sequence, 64-bit ones longer still.
+__device__ __forceinline__ int lg2(int n) { return __ffs(n) - 1; }
+
 // With every face periodic and n even, a ghost cell holds a copy of the interior cell it
 // wraps to, and that cell has the ghost's red-black colour. So a smoothing sweep can also
 // write the periodic images of the cells it updates (push_images): it reads only cells of
@@ -79,25 +84,14 @@ __device__ __forceinline__ void push_images(T* u, int n, int k, int j, int i, T 
 // reference's local indexing (i = is + c, is + c + 2, ...), one thread per updated cell.
 // Each kernel's per-cell work is a device function of the thread's index t, called by the
 // kernel (one thread per index) and by k_vcycle_small (a block-strided loop per step).
-// P2: n = 2^lg (the one-block levels), so t decodes with shifts and masks instead of the
-// integer divisions that otherwise take most of a small level's instructions.
-template <typename T, typename I, bool PUSH = false, bool P2 = false>
+template <typename T, typename I, bool PUSH = false>
 __device__ __forceinline__ void smooth_cell(T* u, const T* src, int n, T dx2, T isix, int color,
-                                            I t, int lg = 0) {
-  int ip, j, k;
-  if constexpr (P2) {
-    const int lh = lg > 0 ? lg - 1 : 0;  // nh = (n + 1) / 2 = 2^lh
-    ip = (int)t & ((1 << lh) - 1);
-    const int r = (int)t >> lh;
-    j = (r & (n - 1)) + 1;
-    k = (r >> lg) + 1;
-  } else {
-    const int nh = (n + 1) / 2;
-    ip = (int)(t % nh);
-    I r = t / nh;
-    j = (int)(r % n) + 1;
-    k = (int)(r / n) + 1;
-  }
+                                            I t, int lg) {
+  const int lh = lg > 0 ? lg - 1 : 0;  // (n + 1) / 2 = 2^lh cells of one colour per row
+  const int ip = (int)(t & (I)((1 << lh) - 1));
+  const I r = t >> lh;
+  const int j = (int)(r & (I)(n - 1)) + 1;
+  const int k = (int)(r >> lg) + 1;
   int c = (color + k + j) & 1;
   int i = 1 + c + 2 * ip;
   if (i > n) return;
@@ -117,32 +111,26 @@ __global__ void k_smooth(T* __restrict__ u, const T* __restrict__ src, int n, T 
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const long long cnt = smooth_count(n);
   if (t >= cnt) return;
-  if (cnt <= 0x7fffffffLL) smooth_cell<T, int, PUSH>(u, src, n, dx2, isix, color, (int)t);
-  else smooth_cell<T, long long, PUSH>(u, src, n, dx2, isix, color, t);
+  if (cnt <= 0x7fffffffLL)
+    smooth_cell<T, int, PUSH>(u, src, n, dx2, isix, color, (int)t, lg2(n));
+  else smooth_cell<T, long long, PUSH>(u, src, n, dx2, isix, color, t, lg2(n));
 }
 
-// interior cell (k, j, i) of an n^3 box from a thread index t, i fastest; P2: n = 2^lg
-template <bool P2, typename I>
+// interior cell (k, j, i) of an n^3 box (n = 2^lg) from a thread index t, i fastest
+template <typename I>
 __device__ __forceinline__ void box_cell(I t, int n, int lg, int& k, int& j, int& i) {
-  if constexpr (P2) {
-    i = ((int)t & (n - 1)) + 1;
-    j = (((int)t >> lg) & (n - 1)) + 1;
-    k = ((int)t >> (2 * lg)) + 1;
-  } else {
-    i = (int)(t % n) + 1;
-    I r = t / n;
-    j = (int)(r % n) + 1;
-    k = (int)(r / n) + 1;
-  }
+  i = (int)(t & (I)(n - 1)) + 1;
+  j = (int)((t >> lg) & (I)(n - 1)) + 1;
+  k = (int)(t >> (2 * lg)) + 1;
 }
 
 // defect of the fine level averaged onto the coarse cell (CalculateDefect + Restrict);
 // with FAS the fine solution is restricted too (RestrictBlock).
-template <typename T, typename I, bool P2 = false>
+template <typename T, typename I>
 __device__ __forceinline__ void defect_restrict_cell(const T* uf, const T* sf, T* sc, T* uc, int nc,
-                                                     T idx2, int fas, I t, int lg = 0) {
+                                                     T idx2, int fas, I t, int lg) {
   int i, j, k;
-  box_cell<P2>(t, nc, lg, k, j, i);
+  box_cell(t, nc, lg, k, j, i);
   const int nf = 2 * nc, ntf = nf + 2, ntc = nc + 2;
   const long long sk = (long long)ntf * ntf, sj = ntf;
   const int fk = 2 * k - 1, fj = 2 * j - 1, fi = 2 * i - 1;
@@ -169,8 +157,9 @@ __global__ void k_defect_restrict(const T* __restrict__ uf, const T* __restrict_
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const long long cnt = (long long)nc * nc * nc;
   if (t >= cnt) return;
-  if (cnt <= 0x7fffffffLL) defect_restrict_cell<T, int>(uf, sf, sc, uc, nc, idx2, fas, (int)t);
-  else defect_restrict_cell<T, long long>(uf, sf, sc, uc, nc, idx2, fas, t);
+  if (cnt <= 0x7fffffffLL)
+    defect_restrict_cell<T, int>(uf, sf, sc, uc, nc, idx2, fas, (int)t, lg2(nc));
+  else defect_restrict_cell<T, long long>(uf, sf, sc, uc, nc, idx2, fas, t, lg2(nc));
 }
 
 // plain 8-cell average (RestrictFMGSource)
@@ -178,9 +167,8 @@ template <typename T>
 __global__ void k_restrict(const T* __restrict__ f, T* __restrict__ c, int nc) {
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= (long long)nc * nc * nc) return;
-  int i = (int)(t % nc) + 1;
-  long long r = t / nc;
-  int j = (int)(r % nc) + 1, k = (int)(r / nc) + 1;
+  int i, j, k;
+  box_cell(t, nc, lg2(nc), k, j, i);
   const int ntf = 2 * nc + 2;
   const int fk = 2 * k - 1, fj = 2 * j - 1, fi = 2 * i - 1;
   auto F = [&](int a, int b, int cc) { return f[ix(ntf, fk + a, fj + b, fi + cc)]; };
@@ -189,10 +177,10 @@ __global__ void k_restrict(const T* __restrict__ f, T* __restrict__ c, int nc) {
 }
 
 // src -= L'(u) on the interior (CalculateFASRHS)
-template <typename T, typename I, bool P2 = false>
-__device__ __forceinline__ void fas_rhs_cell(const T* u, T* src, int n, T idx2, I t, int lg = 0) {
+template <typename T, typename I>
+__device__ __forceinline__ void fas_rhs_cell(const T* u, T* src, int n, T idx2, I t, int lg) {
   int i, j, k;
-  box_cell<P2>(t, n, lg, k, j, i);
+  box_cell(t, n, lg, k, j, i);
   const int nt = n + 2;
   const long long q = ix(nt, k, j, i), sk = (long long)nt * nt, sj = nt;
   src[q] -= (T(6.0) * u[q] - u[q + sk] - u[q + sj] - u[q + 1] - u[q - sk] - u[q - sj] - u[q - 1]) *
@@ -203,17 +191,17 @@ __global__ void k_fas_rhs(const T* __restrict__ u, T* __restrict__ src, int n, T
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const long long cnt = (long long)n * n * n;
   if (t >= cnt) return;
-  if (cnt <= 0x7fffffffLL) fas_rhs_cell<T, int>(u, src, n, idx2, (int)t);
-  else fas_rhs_cell<T, long long>(u, src, n, idx2, t);
+  if (cnt <= 0x7fffffffLL) fas_rhs_cell<T, int>(u, src, n, idx2, (int)t, lg2(n));
+  else fas_rhs_cell<T, long long>(u, src, n, idx2, t, lg2(n));
 }
 
 // trilinear prolongation of the coarse correction, added to the fine level
 // (ProlongateAndCorrect); with FAS the correction is u_c - u_old_c.
-template <typename T, typename I, bool P2 = false>
+template <typename T, typename I>
 __device__ __forceinline__ void prolong_correct_cell(const T* uc, const T* uold, T* uf, int nc,
-                                                     I t, int lg = 0) {
+                                                     I t, int lg) {
   int i, j, k;
-  box_cell<P2>(t, nc, lg, k, j, i);
+  box_cell(t, nc, lg, k, j, i);
   const int ntc = nc + 2, ntf = 2 * nc + 2;
   auto S = [&](int kk, int jj, int ii) -> T {
     long long q = ix(ntc, kk, jj, ii);
@@ -237,8 +225,8 @@ __global__ void k_prolong_correct(const T* __restrict__ uc, const T* __restrict_
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const long long cnt = (long long)nc * nc * nc;
   if (t >= cnt) return;
-  if (cnt <= 0x7fffffffLL) prolong_correct_cell<T, int>(uc, uold, uf, nc, (int)t);
-  else prolong_correct_cell<T, long long>(uc, uold, uf, nc, t);
+  if (cnt <= 0x7fffffffLL) prolong_correct_cell<T, int>(uc, uold, uf, nc, (int)t, lg2(nc));
+  else prolong_correct_cell<T, long long>(uc, uold, uf, nc, t, lg2(nc));
 }
 
 // FMG prolongation: separable 1-D weights (5,30,-3)/32 per axis, 27 products summed in
@@ -247,9 +235,8 @@ template <typename T>
 __global__ void k_fmg_prolong(const T* __restrict__ uc, T* __restrict__ uf, int nc) {
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= (long long)nc * nc * nc) return;
-  int i = (int)(t % nc) + 1;
-  long long r = t / nc;
-  int j = (int)(r % nc) + 1, k = (int)(r / nc) + 1;
+  int i, j, k;
+  box_cell(t, nc, lg2(nc), k, j, i);
   const int ntc = nc + 2, ntf = 2 * nc + 2;
   T s[27];
   for (int a = 0; a < 3; ++a)
@@ -451,8 +438,8 @@ __global__ void __launch_bounds__(kSmallThreads) k_vcycle_small(SmallV<T> v) {
     o[L] = nullptr;
     if (v.fas) { o[L] = sm + off; off += c; }
   }
-  // every level here is n = 2^L <= 16: int indices, and the per-cell functions decode
-  // their thread index with shifts (P2)
+  // every level here is n = 2^L <= 16: int indices, and the boundary fill's quotients by
+  // n + 2 from FP32 reciprocals (bc_shell_cell's P2)
   const int tid = threadIdx.x, nth = blockDim.x;
   auto cells = [](int L) { return ((1 << L) + 2) * ((1 << L) + 2) * ((1 << L) + 2); };
   for (int L = 0; L <= v.ls; ++L)
@@ -479,10 +466,10 @@ __global__ void __launch_bounds__(kSmallThreads) k_vcycle_small(SmallV<T> v) {
     const int n = 1 << L;
     if (pushL(L)) {
       for (int t = tid; t < (int)smooth_count(n); t += nth)
-        smooth_cell<T, int, true, true>(u[L], s[L], n, v.dx2[L], v.isix, color ^ v.coff, t, L);
+        smooth_cell<T, int, true>(u[L], s[L], n, v.dx2[L], v.isix, color ^ v.coff, t, L);
     } else {
       for (int t = tid; t < (int)smooth_count(n); t += nth)
-        smooth_cell<T, int, false, true>(u[L], s[L], n, v.dx2[L], v.isix, color ^ v.coff, t, L);
+        smooth_cell<T, int, false>(u[L], s[L], n, v.dx2[L], v.isix, color ^ v.coff, t, L);
     }
     __syncthreads();
   };
@@ -493,7 +480,7 @@ __global__ void __launch_bounds__(kSmallThreads) k_vcycle_small(SmallV<T> v) {
   auto fas_rhs = [&](int L) {
     const int n = 1 << L;
     for (int t = tid; t < n * n * n; t += nth)
-      fas_rhs_cell<T, int, true>(u[L], s[L], n, v.idx2[L], t, L);
+      fas_rhs_cell<T, int>(u[L], s[L], n, v.idx2[L], t, L);
     __syncthreads();
   };
   auto zero = [&](int L) {
@@ -511,7 +498,7 @@ __global__ void __launch_bounds__(kSmallThreads) k_vcycle_small(SmallV<T> v) {
     if (!pushL(L)) bc(L);
     const int nc = 1 << (L - 1);
     for (int t = tid; t < nc * nc * nc; t += nth)
-      defect_restrict_cell<T, int, true>(u[L], s[L], s[L - 1], u[L - 1], nc, v.idx2[L], v.fas, t,
+      defect_restrict_cell<T, int>(u[L], s[L], s[L - 1], u[L - 1], nc, v.idx2[L], v.fas, t,
                                          L - 1);
     __syncthreads();
     if (!v.fas) zero(L - 1);
@@ -533,7 +520,7 @@ __global__ void __launch_bounds__(kSmallThreads) k_vcycle_small(SmallV<T> v) {
     if (L == 0 || !pushL(L)) bc(L);
     const int nc = 1 << L;
     for (int t = tid; t < nc * nc * nc; t += nth)
-      prolong_correct_cell<T, int, true>(u[L], v.fas ? o[L] : nullptr, u[L + 1], nc, t, L);
+      prolong_correct_cell<T, int>(u[L], v.fas ? o[L] : nullptr, u[L + 1], nc, t, L);
     __syncthreads();
     bc(L + 1);
     smooth(L + 1, 0);
@@ -597,8 +584,9 @@ __global__ void k_sum(const T* a, int n, double* out) {
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   double v[1] = {0.0};
   if (t < (long long)n * n * col_chunks(n)) {
-    const int i = (int)(t % n) + 1, j = (int)((t / n) % n) + 1;
-    const int k0 = 1 + (int)(t / ((long long)n * n)) * kColK, k1 = min(n, k0 + kColK - 1);
+    const int lg = lg2(n);
+    const int i = (int)(t & (n - 1)) + 1, j = (int)((t >> lg) & (n - 1)) + 1;
+    const int k0 = 1 + (int)(t >> (2 * lg)) * kColK, k1 = min(n, k0 + kColK - 1);
     const long long sk = (long long)(n + 2) * (n + 2);
     const T* p = a + ix(n + 2, k0, j, i);
     double acc = 0.0;
@@ -620,8 +608,9 @@ __global__ void k_defect_sq(const double* u, const double* src, int n, double id
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   double v[1] = {0.0};
   if (t < (long long)n * n * col_chunks(n)) {
-    const int i = (int)(t % n) + 1, j = (int)((t / n) % n) + 1;
-    const int k0 = 1 + (int)(t / ((long long)n * n)) * kColK, k1 = min(n, k0 + kColK - 1);
+    const int lg = lg2(n);
+    const int i = (int)(t & (n - 1)) + 1, j = (int)((t >> lg) & (n - 1)) + 1;
+    const int k0 = 1 + (int)(t >> (2 * lg)) * kColK, k1 = min(n, k0 + kColK - 1);
     const int nt = n + 2;
     const long long sk = (long long)nt * nt, sj = nt;
     athg::ff acc = {0.0f, 0.0f};
@@ -657,9 +646,8 @@ __global__ void k_defect_to32(const double* u, const double* src, int n, double 
                               float idx2_hi, float idx2_lo, float* r32) {
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= (long long)n * n * n) return;
-  int i = (int)(t % n) + 1;
-  long long r = t / n;
-  int j = (int)(r % n) + 1, k = (int)(r / n) + 1;
+  int i, j, k;
+  box_cell(t, n, lg2(n), k, j, i);
   const int nt = n + 2;
   const long long q = ix(nt, k, j, i), sk = (long long)nt * nt, sj = nt;
   const double c = u[q];
@@ -710,8 +698,9 @@ __global__ void k_com(const double* src, int n, double lo0, double hi0, double l
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   double v[4] = {0, 0, 0, 0};
   if (t < (long long)n * n * col_chunks(n)) {
-    const int i = (int)(t % n) + 1, j = (int)((t / n) % n) + 1;
-    const int k0 = 1 + (int)(t / ((long long)n * n)) * kColK, k1 = min(n, k0 + kColK - 1);
+    const int lg = lg2(n);
+    const int i = (int)(t & (n - 1)) + 1, j = (int)((t >> lg) & (n - 1)) + 1;
+    const int k0 = 1 + (int)(t >> (2 * lg)) * kColK, k1 = min(n, k0 + kColK - 1);
     const double x = xcen(i, n, lo0, hi0), y = xcen(j, n, lo1, hi1);
     for (int k = k0; k <= k1; ++k) {
       const double s = src[ix(n + 2, k, j, i)] * vol;
@@ -728,8 +717,9 @@ __global__ void k_moments(const double* src, int n, double lo0, double hi0, doub
   double m[25];
   for (int q = 0; q < 25; ++q) m[q] = 0.0;
   if (t < (long long)n * n * col_chunks(n)) {
-    const int i = (int)(t % n) + 1, j = (int)((t / n) % n) + 1;
-    const int k0 = 1 + (int)(t / ((long long)n * n)) * kColK, k1 = min(n, k0 + kColK - 1);
+    const int lg = lg2(n);
+    const int i = (int)(t & (n - 1)) + 1, j = (int)((t >> lg) & (n - 1)) + 1;
+    const int k0 = 1 + (int)(t >> (2 * lg)) * kColK, k1 = min(n, k0 + kColK - 1);
     const double y = xcen(j, n, lo1, hi1) - origin[1], y2 = y * y;
     const double x = xcen(i, n, lo0, hi0) - origin[0];
     const double x2 = x * x, xy = x * y;
