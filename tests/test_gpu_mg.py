@@ -28,15 +28,16 @@ def test_mg_fp64_matches_reference(name):
     assert err < 1e-12, err
 
 
+# n = 128 takes the one-pass smoothing step (k_smooth_rb) on its finest level
+@pytest.mark.parametrize("n", [64, 128])
 @pytest.mark.parametrize("bc", ["periodic", "multipole", "zerograd"])
-def test_mg_fp64_matches_oracle_converged(bc):
-    n = 64
+def test_mg_fp64_matches_oracle_converged(bc, n):
     x = (np.arange(n) + 0.5) / n - 0.5
     Z, Y, X = np.meshgrid(x, x, x, indexing="ij")
     r = np.sqrt(X ** 2 + Y ** 2 + Z ** 2)
     rho = np.where(r < 0.25, 1.0, 1.0e-6) + 0.1 * np.cos(2 * np.pi * X) * np.sin(4 * np.pi * Y)
     src = 4 * np.pi * rho
-    o = ol.MgOracle(6, bc=bc, fmg=True, eps=-1.0, niter=8, mporder=4)
+    o = ol.MgOracle(n.bit_length() - 1, bc=bc, fmg=True, eps=-1.0, niter=8, mporder=4)
     o.load_source(src)
     o.solve()
     mg = athg.Multigrid(n, bc=bc, mode="FMG", threshold=-1.0, niteration=8, precision="fp64")
@@ -47,10 +48,10 @@ def test_mg_fp64_matches_oracle_converged(bc):
     assert err < 1e-11, err
 
 
+@pytest.mark.parametrize("n", [64, 128])
 @pytest.mark.parametrize("bc", ["periodic", "multipole"])
-def test_mg_mixed_reaches_fp64_solution(bc):
+def test_mg_mixed_reaches_fp64_solution(bc, n):
     """Iterative refinement: FP32 cycles, FP64 defect, relative residual 1e-10."""
-    n = 64
     x = (np.arange(n) + 0.5) / n - 0.5
     Z, Y, X = np.meshgrid(x, x, x, indexing="ij")
     r = np.sqrt(X ** 2 + Y ** 2 + Z ** 2)
