@@ -1400,6 +1400,11 @@ int athg_create(const athg_config* cfg, athg_ctx** out) {
   g.nf3 = (int64_t)(g.nc3 + 1) * g.nc2 * g.nc1;
   g.ne = (int64_t)(g.nc3 + 1) * (g.nc2 + 1) * (g.nc1 + 1);
   g.ncmax = std::max(g.nc1, std::max(g.nc2, g.nc3));
+  g.dw1 = fastdiv_make((uint32_t)(g.nc1 + 1));
+  g.dw2 = fastdiv_make((uint32_t)(g.nc2 + 1));
+  g.dgj = fastdiv_make((uint32_t)(g.nc2 + 1 - g.nx2));
+  g.dgi = fastdiv_make((uint32_t)(g.nc1 + 1 - g.nx1));
+  g.dnx2 = fastdiv_make((uint32_t)g.nx2);
   *out = c;
   return ATHG_OK;
 }

@@ -42,26 +42,29 @@ __device__ __forceinline__ void ghost_shell_pos(const Geom& g, int t, int& k, in
   const int w1 = g.nc1 + 1, w2 = g.nc2 + 1;
   const int na = gk * w2 * w1;
   const int nbb = g.nx3 * gj * w1;
+  // quotients by multiply and shift (FastDiv), remainders from them
   if (t < na) {
-    i = t % w1;
-    const int r = t / w1;
-    j = r % w2;
-    const int q = r / w2;
+    const int r = fastdiv(t, g.dw1);
+    i = t - r * w1;
+    const int q = fastdiv(r, g.dw2);
+    j = r - q * w2;
     k = q < g.ks ? q : q + g.nx3;  // 0..ks-1, then ke+1..nc3
   } else if (t < na + nbb) {
     const int u = t - na;
-    i = u % w1;
-    const int r = u / w1;
-    const int q = r % gj;
+    const int r = fastdiv(u, g.dw1);
+    i = u - r * w1;
+    const int rk = fastdiv(r, g.dgj);
+    const int q = r - rk * gj;
     j = q < g.js ? q : q + g.nx2;
-    k = g.ks + r / gj;
+    k = g.ks + rk;
   } else {
     const int u = t - na - nbb;
-    const int q = u % gi;
+    const int r = fastdiv(u, g.dgi);
+    const int q = u - r * gi;
     i = q < g.is ? q : q + g.nx1;
-    const int r = u / gi;
-    j = g.js + r % g.nx2;
-    k = g.ks + r / g.nx2;
+    const int rk = fastdiv(r, g.dnx2);
+    j = g.js + (r - rk * g.nx2);
+    k = g.ks + rk;
   }
 }
 

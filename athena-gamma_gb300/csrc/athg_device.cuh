@@ -30,6 +30,9 @@ struct Geom {
   int64_t ncell, nf1, nf2, nf3, ne;
   int nb;
   int ncmax;  // max(nc1, nc2, nc3), stride of the per-block coefficient arrays
+  // divisions of the ghost-shell index (ghost_shell_pos): by nc1 + 1, nc2 + 1, the ghost
+  // rows and columns per side pair (nc2 + 1 - nx2, nc1 + 1 - nx1) and nx2
+  FastDiv dw1, dw2, dgj, dgi, dnx2;
 };
 
 __host__ __device__ inline int64_t cidx(const Geom& g, int k, int j, int i) {

@@ -501,10 +501,7 @@ __global__ void __launch_bounds__(256) k_dt_df(Geom g, StagePtrs<double> p, Box 
 }
 
 Box box_of(int il, int iu, int jl, int ju, int kl, int ku) {
-  Box b;
-  b.il = il; b.jl = jl; b.kl = kl;
-  b.ni = iu - il + 1; b.nj = ju - jl + 1; b.nk = ku - kl + 1;
-  return b;
+  return box_make(il, iu, jl, ju, kl, ku);
 }
 dim3 grid_of(const Box& b, int nb) {
   return dim3((unsigned)((b.ni * b.nj + kThreads - 1) / kThreads), (unsigned)b.nk, (unsigned)nb);

@@ -9,10 +9,7 @@
 namespace athg {
 
 inline Box make_box(int il, int iu, int jl, int ju, int kl, int ku) {
-  Box b;
-  b.il = il; b.jl = jl; b.kl = kl;
-  b.ni = iu - il + 1; b.nj = ju - jl + 1; b.nk = ku - kl + 1;
-  return b;
+  return box_make(il, iu, jl, ju, kl, ku);
 }
 inline dim3 box_grid(const Box& b, int nblocks, int tpb) {
   return dim3((unsigned)((b.ni * b.nj + tpb - 1) / tpb), (unsigned)b.nk, (unsigned)nblocks);
@@ -150,7 +147,11 @@ void Launcher<T>::fluxes(const Geom& g, const StagePtrs<T>& p, bool mhd, int sol
 template <typename T>
 void Launcher<T>::corner_emf(const Geom& g, const StagePtrs<T>& p, cudaStream_t st) {
   Box b = make_box(g.is, g.ie + 1, g.js, g.je + 1, g.ks, g.ke + 1);
-  k_corner_emf<T><<<box_grid(b, g.nb, 128), 128, 0, st>>>(g, p, b);
+  // 64^3 blocks with two ghost layers (68^3 cells) take the fixed-size instantiation
+  if (kMixed<T> && g.nc1 == 68 && g.nc2 == 68 && g.nc3 == 68)
+    k_corner_emf<T, 68><<<box_grid(b, g.nb, 128), 128, 0, st>>>(g, p, b);
+  else
+    k_corner_emf<T, 0><<<box_grid(b, g.nb, 128), 128, 0, st>>>(g, p, b);
 }
 
 template <typename T>

@@ -251,6 +251,32 @@ ATHG_HD bool lap7_ff(double c, const double* n, ff& out) {
   return true;
 }
 
+// Division by an invariant d (1 <= d < 2^31) for numerators 0 <= a < 2^31 with the high
+// half of one 32 x 32-bit product and a shift (Granlund and Montgomery's round-up method):
+// with l = ceil(log2 d) and m = ceil(2^(31 + l) / d) < 2^32,
+// a m / 2^(31 + l) = a / d + a r / (d 2^(31 + l)) with 0 <= r < d, and the second term is
+// below 2^-l <= 1 / d, so it never reaches the next integer: floor(a m / 2^(31 + l)) =
+// floor(a / d). As 2a < 2^32, that quotient is the high word of (2a) m shifted by l.
+struct FastDiv {
+  uint32_t mul;
+  uint32_t shift;  // l
+};
+inline FastDiv fastdiv_make(uint32_t d) {
+  uint32_t l = 0;
+  while ((1ull << l) < d) ++l;
+  const uint64_t m = ((1ull << (31 + l)) + d - 1) / d;
+  return FastDiv{(uint32_t)m, l};
+}
+ATHG_HD int fastdiv(int a, FastDiv f) {
+  const uint32_t a2 = (uint32_t)a << 1;
+#ifdef __CUDA_ARCH__
+  const uint32_t hi = __umulhi(a2, f.mul);
+#else
+  const uint32_t hi = (uint32_t)(((uint64_t)a2 * f.mul) >> 32);
+#endif
+  return (int)(hi >> f.shift);
+}
+
 // Quotient a / b for 0 <= a < 2^12 and 1 <= b <= 2^10, given rb = 1 / b rounded to binary32:
 // one FP32 multiply in place of an integer division. (a + 0.5) / b lies at least 0.5 / b
 // from every integer, and the two roundings move (a + 0.5) * rb by at most about

@@ -41,11 +41,19 @@ template <typename T> constexpr bool kMixed = std::is_same<T, float>::value;
 // like is..ie+1 do not leave idle half-warps), grid.y runs over k, grid.z over blocks.
 struct Box {
   int il, jl, kl, ni, nj, nk;
+  FastDiv dni;  // division by ni
 };
+inline Box box_make(int il, int iu, int jl, int ju, int kl, int ku) {
+  Box b;
+  b.il = il; b.jl = jl; b.kl = kl;
+  b.ni = iu - il + 1; b.nj = ju - jl + 1; b.nk = ku - kl + 1;
+  b.dni = fastdiv_make((uint32_t)b.ni);
+  return b;
+}
 __device__ __forceinline__ bool box_coords(const Box& bx, int& i, int& j, int& k, int& b) {
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= bx.ni * bx.nj) return false;
-  int jj = t / bx.ni;
+  int jj = fastdiv(t, bx.dni);
   i = bx.il + (t - jj * bx.ni);
   j = bx.jl + jj;
   k = bx.kl + blockIdx.y;
@@ -463,22 +471,29 @@ k_flux_march(Geom g, StagePtrs<T> p, Box bx, Phys ph, int fs, int fe) {
 // Corner EMFs (Gardiner & Stone upwind integration), one thread per corner location
 // (k,j,i) in [ks,ke+1]x[js,je+1]x[is,ie+1] computing e1, e2, e3 there.
 // Reference src/field/calculate_corner_e.cpp:129-229 (3-D, Newtonian). The cell-centred
-// E = -v x B is recomputed from W and bcc where needed instead of being stored.
-template <typename T>
+// E = -v x B is recomputed from W and bcc where needed instead of being stored (the mixed
+// path reads it from cce, written by the update).
+// SNC > 0: blocks of SNC^3 cells (ghosts included), a compile-time size, so the strides
+// fold into the loads' immediate offsets; 0: any size (the same arithmetic either way).
+template <typename T, int SNC>
 __global__ void __launch_bounds__(128) k_corner_emf(Geom g, StagePtrs<T> p, Box bx) {
   int i, j, k, b;
   if (!box_coords(bx, i, j, k, b)) return;
-  const int64_t nc = g.ncell;
+  const int nc1 = SNC ? SNC : g.nc1, nc2 = SNC ? SNC : g.nc2;
+  constexpr int64_t S = SNC;
+  const int64_t nc = SNC ? S * S * S : g.ncell;
   const T* w = p.w + (int64_t)b * NHYD * nc;
   const T* bc = p.bcc + (int64_t)b * 3 * nc;
   const T* ce = kMixed<T> ? p.cce + (int64_t)b * 3 * nc : nullptr;
   // Every value sits at this corner's index or one below it along some axes: the
   // accessors take those offsets (0 or -1 per axis), so each load is a base pointer plus
   // a stride combination formed once, not a fresh 64-bit index polynomial.
-  const int64_t c0 = cidx(g, k, j, i), q1 = f1idx(g, k, j, i), q2 = f2idx(g, k, j, i);
-  const int64_t jc = g.nc1, kc = (int64_t)g.nc1 * g.nc2;             // cells, x3 faces
-  const int64_t j1 = g.nc1 + 1, k1 = (int64_t)(g.nc1 + 1) * g.nc2;   // x1 faces
-  const int64_t j2 = g.nc1, k2 = (int64_t)g.nc1 * (g.nc2 + 1);       // x2 faces
+  const int64_t c0 = ((int64_t)k * nc2 + j) * nc1 + i;
+  const int64_t q1 = ((int64_t)k * nc2 + j) * (nc1 + 1) + i;
+  const int64_t q2 = ((int64_t)k * (nc2 + 1) + j) * nc1 + i;
+  const int64_t jc = nc1, kc = (int64_t)nc1 * nc2;             // cells, x3 faces
+  const int64_t j1 = nc1 + 1, k1 = (int64_t)(nc1 + 1) * nc2;   // x1 faces
+  const int64_t j2 = nc1, k2 = (int64_t)nc1 * (nc2 + 1);       // x2 faces
   auto cce = [&](int n, int dk, int dj, int di) -> T {
     const int64_t c = c0 + dk * kc + dj * jc + di;
     if constexpr (kMixed<T>) return ce[n * nc + c];
@@ -488,7 +503,8 @@ __global__ void __launch_bounds__(128) k_corner_emf(Geom g, StagePtrs<T> p, Box 
     if (n == 1) return vx * bz1 - vz * bx1;
     return vy * bx1 - vx * by1;
   };
-  const int64_t n1 = g.nf1, n2 = g.nf2, n3 = g.nf3;
+  const int64_t n1 = SNC ? S * S * (S + 1) : g.nf1, n2 = SNC ? S * S * (S + 1) : g.nf2,
+                n3 = SNC ? S * S * (S + 1) : g.nf3;
   const T* F1 = p.flx[0] + (int64_t)b * 8 * n1 + q1;
   const T* F2 = p.flx[1] + (int64_t)b * 8 * n2 + q2;
   const T* F3 = p.flx[2] + (int64_t)b * 8 * n3 + c0;
@@ -506,8 +522,9 @@ __global__ void __launch_bounds__(128) k_corner_emf(Geom g, StagePtrs<T> p, Box 
   auto e1x3 = [&](int dk, int dj, int di) { return F3[6 * n3 + o3(dk, dj, di)]; };
   auto wx3 = [&](int dk, int dj, int di) { return F3[7 * n3 + o3(dk, dj, di)]; };
   const T one = T(1.0), q = T(0.25);
-  T* E = p.edge + (int64_t)b * 3 * g.ne;
-  const int64_t ei = eidx(g, k, j, i);
+  const int64_t ne = SNC ? (S + 1) * (S + 1) * (S + 1) : g.ne;
+  T* E = p.edge + (int64_t)b * 3 * ne;
+  const int64_t ei = ((int64_t)k * (nc2 + 1) + j) * (nc1 + 1) + i;
   {
     T de1_l3 = (one - wx2(-1, 0, 0)) * (e1x3(0, 0, 0) - cce(0, -1, 0, 0)) +
                (wx2(-1, 0, 0)) * (e1x3(0, -1, 0) - cce(0, -1, -1, 0));
@@ -529,7 +546,7 @@ __global__ void __launch_bounds__(128) k_corner_emf(Geom g, StagePtrs<T> p, Box 
                (wx3(0, 0, -1)) * (e2x1(-1, 0, 0) - cce(1, -1, 0, -1));
     T de2_r1 = (one - wx3(0, 0, 0)) * (e2x1(0, 0, 0) - cce(1, 0, 0, 0)) +
                (wx3(0, 0, 0)) * (e2x1(-1, 0, 0) - cce(1, -1, 0, 0));
-    E[g.ne + ei] = q * (de2_l3 + de2_r3 + de2_l1 + de2_r1 + e2x3(0, 0, -1) +
+    E[ne + ei] = q * (de2_l3 + de2_r3 + de2_l1 + de2_r1 + e2x3(0, 0, -1) +
                         e2x3(0, 0, 0) + e2x1(-1, 0, 0) + e2x1(0, 0, 0));
   }
   {
@@ -541,7 +558,7 @@ __global__ void __launch_bounds__(128) k_corner_emf(Geom g, StagePtrs<T> p, Box 
                (wx2(0, 0, -1)) * (e3x1(0, -1, 0) - cce(2, 0, -1, -1));
     T de3_r1 = (one - wx2(0, 0, 0)) * (e3x1(0, 0, 0) - cce(2, 0, 0, 0)) +
                (wx2(0, 0, 0)) * (e3x1(0, -1, 0) - cce(2, 0, -1, 0));
-    E[2 * g.ne + ei] = q * (de3_l1 + de3_r1 + de3_l2 + de3_r2 + e3x2(0, 0, -1) +
+    E[2 * ne + ei] = q * (de3_l1 + de3_r1 + de3_l2 + de3_r2 + e3x2(0, 0, -1) +
                             e3x2(0, 0, 0) + e3x1(0, -1, 0) + e3x1(0, 0, 0));
   }
 }

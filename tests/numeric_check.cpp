@@ -14,6 +14,30 @@ static int fails = 0;
 int main(int argc, char** argv) {
   const long n = argc > 1 ? std::atol(argv[1]) : 2000000;
   std::mt19937_64 rng(12345);
+  // division by an invariant: every d up to 2^17 against a spread of numerators (both ends
+  // of the range, around multiples of d, random), and every a < 2^20 for a few d
+  for (uint32_t d = 1; d <= (1u << 17); ++d) {
+    const FastDiv f = fastdiv_make(d);
+    const uint32_t hi = 0x7fffffffu;
+    const uint32_t probe[8] = {0u, 1u, d - 1u, d, d + 1u, hi, hi - 1u, hi - (hi % d)};
+    for (uint32_t a : probe)
+      if (a <= hi) CHECK(fastdiv((int)a, f) == (int)(a / d), "fastdiv %u / %u", a, d);
+    for (int r = 0; r < 16; ++r) {
+      const uint32_t a = (uint32_t)(rng() & hi);
+      CHECK(fastdiv((int)a, f) == (int)(a / d), "fastdiv %u / %u", a, d);
+      const uint32_t q = a / d, b = q * d;  // around a multiple of d
+      CHECK(fastdiv((int)b, f) == (int)q, "fastdiv %u / %u", b, d);
+      if (b) CHECK(fastdiv((int)(b - 1), f) == (int)((b - 1) / d), "fastdiv %u / %u", b - 1, d);
+    }
+  }
+  {
+    const uint32_t ds[6] = {3, 7, 65, 69, 1000, 65537};
+    for (uint32_t d : ds) {
+      const FastDiv f = fastdiv_make(d);
+      for (uint32_t a = 0; a < (1u << 20); ++a)
+        CHECK(fastdiv((int)a, f) == (int)(a / d), "fastdiv %u / %u", a, d);
+    }
+  }
   // small-range quotients by an FP32 reciprocal: every a < 2^12, every b <= 2^10
   for (int b = 1; b <= 1024; ++b) {
     const float rb = 1.0f / (float)b;
