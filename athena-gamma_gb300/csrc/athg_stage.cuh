@@ -61,6 +61,36 @@ __device__ __forceinline__ bool box_coords(const Box& bx, int& i, int& j, int& k
   return true;
 }
 
+// Block sizes of a launch: compile-time constants for SNC > 0 (blocks of SNC^3 cells, ghosts
+// included, so strides fold into the loads' immediate offsets), else the context's.
+template <int SNC>
+struct BlockDims {
+  int64_t nc1, nc2, ncell, nf1, nf2, nf3, ne;
+  __device__ __forceinline__ explicit BlockDims(const Geom& g) {
+    if constexpr (SNC > 0) {
+      constexpr int64_t S = SNC;
+      nc1 = S; nc2 = S; ncell = S * S * S;
+      nf1 = nf2 = nf3 = S * S * (S + 1);
+      ne = (S + 1) * (S + 1) * (S + 1);
+    } else {
+      nc1 = g.nc1; nc2 = g.nc2; ncell = g.ncell;
+      nf1 = g.nf1; nf2 = g.nf2; nf3 = g.nf3; ne = g.ne;
+    }
+  }
+  __device__ __forceinline__ int64_t cell(int k, int j, int i) const {
+    return ((int64_t)k * nc2 + j) * nc1 + i;
+  }
+  __device__ __forceinline__ int64_t f1(int k, int j, int i) const {
+    return ((int64_t)k * nc2 + j) * (nc1 + 1) + i;
+  }
+  __device__ __forceinline__ int64_t f2(int k, int j, int i) const {
+    return ((int64_t)k * (nc2 + 1) + j) * nc1 + i;
+  }
+  __device__ __forceinline__ int64_t edge(int k, int j, int i) const {
+    return ((int64_t)k * (nc2 + 1) + j) * (nc1 + 1) + i;
+  }
+};
+
 // Wave variable n of cell c for a sweep along DIR (transverse B in the cyclic order of
 // reference src/reconstruct/plm.cpp:44-55 (x1), :156-170 (x2), :268-282 (x3)).
 template <typename T, int DIR>
@@ -110,18 +140,20 @@ __device__ __forceinline__ void velocity_differences(const Geom& g, const T* __r
 // reference src/reconstruct/dc.cpp, src/reconstruct/plm.cpp uniform branch) fused with
 // the Riemann solve. Face (k,j,i) along DIR separates cell index-1 from cell index.
 // Loop extents per direction follow src/hydro/calculate_fluxes.cpp:63-74,164-172,274-279.
-template <typename T, int DIR, int ORDER, int SOLVER, bool MHD>
+// SNC > 0: blocks of SNC^3 cells (BlockDims), compile-time strides.
+template <typename T, int DIR, int ORDER, int SOLVER, bool MHD, int SNC = 0>
 __global__ void __launch_bounds__(128)
 k_flux(Geom g, StagePtrs<T> p, Box bx, Phys ph) {
   int i, j, k, b;
   if (!box_coords(bx, i, j, k, b)) return;
   constexpr int NW = MHD ? 7 : 5;
   constexpr int NF = MHD ? 8 : 5;
-  const int64_t nc = g.ncell;
+  const BlockDims<SNC> d(g);
+  const int64_t nc = d.ncell;
   const T* __restrict__ w = p.w + (int64_t)b * NHYD * nc;
   const T* __restrict__ bcc = MHD ? p.bcc + (int64_t)b * 3 * nc : nullptr;
-  const int64_t st = DIR == 0 ? 1 : (DIR == 1 ? (int64_t)g.nc1 : (int64_t)g.nc1 * g.nc2);
-  const int64_t c = cidx(g, k, j, i);   // cell on the right of the face
+  const int64_t st = DIR == 0 ? 1 : (DIR == 1 ? d.nc1 : d.nc1 * d.nc2);
+  const int64_t c = d.cell(k, j, i);   // cell on the right of the face
   const int f = DIR == 0 ? i : (DIR == 1 ? j : k);
   T wl[7], wr[7];
   if (ORDER == 1) {
@@ -177,8 +209,9 @@ k_flux(Geom g, StagePtrs<T> p, Box bx, Phys ph) {
   wli[IPR] = wl[IPR];
   wri[IDN] = wr[IDN]; wri[IVX] = wr[ivx]; wri[IVY] = wr[ivy]; wri[IVZ] = wr[ivz];
   wri[IPR] = wr[IPR];
-  const int64_t nf = fsize<DIR>(g);
-  const int64_t fi = fidx<DIR>(g, k, j, i);
+  constexpr int64_t S = SNC;
+  const int64_t nf = SNC ? S * S * (S + 1) : fsize<DIR>(g);
+  const int64_t fi = DIR == 0 ? d.f1(k, j, i) : (DIR == 1 ? d.f2(k, j, i) : d.cell(k, j, i));
   T* __restrict__ out = p.flx[DIR] + (int64_t)b * NF * nf;
   const T gam = ph_gamma<T>(ph);
   if constexpr (MHD) {
@@ -217,10 +250,11 @@ k_flux(Geom g, StagePtrs<T> p, Box bx, Phys ph) {
 
 // Riemann solve of one face from reconstructed states in the unrotated order, storing the
 // flux (and for MHD the face EMFs and CT weight) like k_flux.
-template <typename T, int DIR, int SOLVER, bool MHD>
+template <typename T, int DIR, int SOLVER, bool MHD, int SNC = 0>
 __device__ __forceinline__ void face_solve(const Geom& g, const StagePtrs<T>& p, const Phys& ph,
                                            int b, int64_t fi, const T* wl, const T* wr,
                                            int k, int j, int i) {
+  constexpr int64_t S = SNC;
   constexpr int NF = MHD ? 8 : 5;
   constexpr int ivx = IVX + DIR, ivy = IVX + (DIR + 1) % 3, ivz = IVX + (DIR + 2) % 3;
   T wli[7], wri[7], fx[7];
@@ -228,7 +262,7 @@ __device__ __forceinline__ void face_solve(const Geom& g, const StagePtrs<T>& p,
   wli[IPR] = wl[IPR];
   wri[IDN] = wr[IDN]; wri[IVX] = wr[ivx]; wri[IVY] = wr[ivy]; wri[IVZ] = wr[ivz];
   wri[IPR] = wr[IPR];
-  const int64_t nf = fsize<DIR>(g);
+  const int64_t nf = SNC ? S * S * (S + 1) : fsize<DIR>(g);
   T* __restrict__ out = p.flx[DIR] + (int64_t)b * NF * nf;
   const T gam = ph_gamma<T>(ph);
   if constexpr (MHD) {
@@ -332,7 +366,7 @@ k_flux_x1_ppm(Geom g, StagePtrs<T> p, Box bx, Phys ph, int rows) {
 // left state of its upper face -- the same row-by-row reuse as the reference's
 // wl_/wlb_ swap in hydro/calculate_fluxes.cpp:174-212 and :278-316.
 // The box describes the transverse pencil set (i, and k or j) and the face range (nk).
-template <typename T, int DIR, int ORDER, int SOLVER, bool MHD>
+template <typename T, int DIR, int ORDER, int SOLVER, bool MHD, int SNC = 0>
 __global__ void __launch_bounds__(128)
 k_flux_march(Geom g, StagePtrs<T> p, Box bx, Phys ph, int fs, int fe) {
   static_assert(DIR == 1 || DIR == 2, "marching sweeps are transverse to i");
@@ -357,16 +391,17 @@ k_flux_march(Geom g, StagePtrs<T> p, Box bx, Phys ph, int fs, int fe) {
     fe = s1;
   }
   constexpr int NW = MHD ? 7 : 5;
-  const int64_t nc = g.ncell;
+  const BlockDims<SNC> d(g);
+  const int64_t nc = d.ncell;
   const T* __restrict__ w = p.w + (int64_t)b * NHYD * nc;
   const T* __restrict__ bcc = MHD ? p.bcc + (int64_t)b * 3 * nc : nullptr;
-  const int64_t st = DIR == 1 ? (int64_t)g.nc1 : (int64_t)g.nc1 * g.nc2;
+  const int64_t st = DIR == 1 ? d.nc1 : d.nc1 * d.nc2;
   // cell index of pencil position f
   auto cell_at = [&](int f) -> int64_t {
-    return DIR == 1 ? cidx(g, a, f, i) : cidx(g, f, a, i);
+    return DIR == 1 ? d.cell(a, f, i) : d.cell(f, a, i);
   };
   auto face_at = [&](int f) -> int64_t {
-    return DIR == 1 ? f2idx(g, a, f, i) : f3idx(g, f, a, i);
+    return DIR == 1 ? d.f2(a, f, i) : d.cell(f, a, i);
   };
   const T* cf = p.coef + ((int64_t)b * 3 + DIR) * 2 * g.ncmax;
   T cm1[7], c0[7], cp1[7], wlnext[7], wr[7];
@@ -378,7 +413,7 @@ k_flux_march(Geom g, StagePtrs<T> p, Box bx, Phys ph, int fs, int fe) {
       int64_t cc = c + st;
 #pragma unroll
       for (int n = 0; n < NW; ++n) wr[n] = wave_var<T, DIR>(w, bcc, nc, n, cc);
-      face_solve<T, DIR, SOLVER, MHD>(g, p, ph, b, face_at(f), wlnext, wr, DIR == 1 ? a : f,
+      face_solve<T, DIR, SOLVER, MHD, SNC>(g, p, ph, b, face_at(f), wlnext, wr, DIR == 1 ? a : f,
                                       DIR == 1 ? f : a, i);
 #pragma unroll
       for (int n = 0; n < NW; ++n) wlnext[n] = wr[n];
@@ -414,7 +449,7 @@ k_flux_march(Geom g, StagePtrs<T> p, Box bx, Phys ph, int fs, int fe) {
       }
       cm1[IDN] = (cm1[IDN] > df) ? cm1[IDN] : df; cm1[IPR] = (cm1[IPR] > pf) ? cm1[IPR] : pf;
       wr[IDN] = (wr[IDN] > df) ? wr[IDN] : df; wr[IPR] = (wr[IPR] > pf) ? wr[IPR] : pf;
-      face_solve<T, DIR, SOLVER, MHD>(g, p, ph, b, face_at(f), cm1, wr, DIR == 1 ? a : f,
+      face_solve<T, DIR, SOLVER, MHD, SNC>(g, p, ph, b, face_at(f), cm1, wr, DIR == 1 ? a : f,
                                       DIR == 1 ? f : a, i);
     }
     return;
@@ -462,7 +497,7 @@ k_flux_march(Geom g, StagePtrs<T> p, Box bx, Phys ph, int fs, int fe) {
 #pragma unroll
       for (int n = 0; n < NW; ++n) ahead[n] = wave_var<T, DIR>(w, bcc, nc, n, c + 2 * st);
     }
-    face_solve<T, DIR, SOLVER, MHD>(g, p, ph, b, face_at(f), cm1, wr, DIR == 1 ? a : f,
+    face_solve<T, DIR, SOLVER, MHD, SNC>(g, p, ph, b, face_at(f), cm1, wr, DIR == 1 ? a : f,
                                     DIR == 1 ? f : a, i);
     c += st;
   }
@@ -914,23 +949,24 @@ __device__ __forceinline__ float pair_diff(float2 a, float2 b) {
 // potential differences times the stage-start density, energy from this stage's mass
 // fluxes. phi2 holds the potential as FP32 pairs hi + lo (one ghost layer), so the
 // differences take no FP64 instructions.
-template <bool MHD, bool DT, bool SG>
+template <bool MHD, bool DT, bool SG, int SNC>
 __device__ __forceinline__ float update_c2p_cell(const Geom& g, const StagePtrs<float>& p,
                                                  int i, int j, int k, int b, const StageW& sw,
                                                  const Phys& ph, const StateBufs& sb,
                                                  const float2* __restrict__ phi2) {
   const MixedGeo mg = p.mg[b];
   const float wf = __fmul_rn(sw.betaf, __ldg(p.dtT));
-  const int64_t nc = g.ncell;
-  const int64_t c = cidx(g, k, j, i);
+  const BlockDims<SNC> d(g);
+  const int64_t nc = d.ncell;
+  const int64_t c = d.cell(k, j, i);
   const double* __restrict__ uin = sb.u_in + (int64_t)b * NHYD * nc;
   double* __restrict__ uout = sb.u_out + (int64_t)b * NHYD * nc;
   constexpr int NF = MHD ? 8 : 5;
-  const float* __restrict__ F1 = p.flx[0] + (int64_t)b * NF * g.nf1;
-  const float* __restrict__ F2 = p.flx[1] + (int64_t)b * NF * g.nf2;
-  const float* __restrict__ F3 = p.flx[2] + (int64_t)b * NF * g.nf3;
-  const int64_t q1 = f1idx(g, k, j, i), q2 = f2idx(g, k, j, i), q3 = f3idx(g, k, j, i);
-  const int64_t s2 = g.nc1, s3 = (int64_t)g.nc1 * g.nc2;
+  const float* __restrict__ F1 = p.flx[0] + (int64_t)b * NF * d.nf1;
+  const float* __restrict__ F2 = p.flx[1] + (int64_t)b * NF * d.nf2;
+  const float* __restrict__ F3 = p.flx[2] + (int64_t)b * NF * d.nf3;
+  const int64_t q1 = d.f1(k, j, i), q2 = d.f2(k, j, i), q3 = c;
+  const int64_t s2 = d.nc1, s3 = d.nc1 * d.nc2;
   const float cw1 = __fmul_rn(wf, mg.idx[0]), cw2 = __fmul_rn(wf, mg.idx[1]),
               cw3 = __fmul_rn(wf, mg.idx[2]);
   float* __restrict__ w = p.w + (int64_t)b * NHYD * nc;
@@ -943,26 +979,26 @@ __device__ __forceinline__ float update_c2p_cell(const Geom& g, const StagePtrs<
     const float2* __restrict__ pp = phi2 + (int64_t)b * nc;
     const float2 pc = __ldg(pp + c);
     const int64_t sd[3] = {1, s2, s3};
-    const float cw[3] = {cw1, cw2, cw3};
+    const float cwd[3] = {cw1, cw2, cw3};
     const float* __restrict__ Fd[3] = {F1 + q1, F2 + q2, F3 + q3};
 #pragma unroll
-    for (int d = 0; d < 3; ++d) {
-      const float dl = pair_diff(pc, __ldg(pp + c - sd[d]));
-      const float dr = pair_diff(__ldg(pp + c + sd[d]), pc);
-      sgs[1 + d] = cw[d] * rho * (0.5f * (dl + dr));
-      sgs[4] += cw[d] * (0.5f * (__ldg(Fd[d]) * dl + __ldg(Fd[d] + sd[d]) * dr));
+    for (int a = 0; a < 3; ++a) {
+      const float dl = pair_diff(pc, __ldg(pp + c - sd[a]));
+      const float dr = pair_diff(__ldg(pp + c + sd[a]), pc);
+      sgs[1 + a] = cwd[a] * rho * (0.5f * (dl + dr));
+      sgs[4] += cwd[a] * (0.5f * (__ldg(Fd[a]) * dl + __ldg(Fd[a] + sd[a]) * dr));
     }
   }
   float fx[NHYD][6];
   double uo[NHYD];
 #pragma unroll
   for (int n = 0; n < NHYD; ++n) {
-    fx[n][0] = __ldg(F1 + n * g.nf1 + q1 + 1);
-    fx[n][1] = __ldg(F1 + n * g.nf1 + q1);
-    fx[n][2] = __ldg(F2 + n * g.nf2 + q2 + s2);
-    fx[n][3] = __ldg(F2 + n * g.nf2 + q2);
-    fx[n][4] = __ldg(F3 + n * g.nf3 + q3 + s3);
-    fx[n][5] = __ldg(F3 + n * g.nf3 + q3);
+    fx[n][0] = __ldg(F1 + n * d.nf1 + q1 + 1);
+    fx[n][1] = __ldg(F1 + n * d.nf1 + q1);
+    fx[n][2] = __ldg(F2 + n * d.nf2 + q2 + s2);
+    fx[n][3] = __ldg(F2 + n * d.nf2 + q2);
+    fx[n][4] = __ldg(F3 + n * d.nf3 + q3 + s3);
+    fx[n][5] = __ldg(F3 + n * d.nf3 + q3);
     uo[n] = __ldg(uin + n * nc + c);
   }
   // faces (lower, upper) per direction, base values and edge EMFs
@@ -970,24 +1006,24 @@ __device__ __forceinline__ float update_c2p_cell(const Geom& g, const StagePtrs<
   float E1[2][2], E2[2][2], E3[2][2];  // E1[dk][dj], E2[dk][di], E3[dj][di]
   int64_t fl[3] = {0, 0, 0}, fu[3] = {0, 0, 0};
   if constexpr (MHD) {
-    fl[0] = (int64_t)b * g.nf1 + q1;      fu[0] = fl[0] + 1;
-    fl[1] = (int64_t)b * g.nf2 + q2;      fu[1] = fl[1] + g.nc1;
-    fl[2] = (int64_t)b * g.nf3 + q3;      fu[2] = fl[2] + (int64_t)g.nc1 * g.nc2;
+    fl[0] = (int64_t)b * d.nf1 + q1;      fu[0] = fl[0] + 1;
+    fl[1] = (int64_t)b * d.nf2 + q2;      fu[1] = fl[1] + d.nc1;
+    fl[2] = (int64_t)b * d.nf3 + q3;      fu[2] = fl[2] + d.nc1 * d.nc2;
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
       bl[d] = __ldg(sb.b_in[d] + fl[d]);
       bu[d] = __ldg(sb.b_in[d] + fu[d]);
     }
-    const float* __restrict__ Ea = p.edge + (int64_t)b * 3 * g.ne;
-    const int64_t e = eidx(g, k, j, i);
-    const int64_t ej = (int64_t)g.nc1 + 1, ek = ((int64_t)g.nc1 + 1) * (g.nc2 + 1);
+    const float* __restrict__ Ea = p.edge + (int64_t)b * 3 * d.ne;
+    const int64_t e = d.edge(k, j, i);
+    const int64_t ej = d.nc1 + 1, ek = (d.nc1 + 1) * (d.nc2 + 1);
 #pragma unroll
     for (int x = 0; x < 2; ++x)
 #pragma unroll
       for (int y = 0; y < 2; ++y) {
         E1[x][y] = __ldg(Ea + e + x * ek + y * ej);
-        E2[x][y] = __ldg(Ea + g.ne + e + x * ek + y);
-        E3[x][y] = __ldg(Ea + 2 * g.ne + e + x * ej + y);
+        E2[x][y] = __ldg(Ea + d.ne + e + x * ek + y);
+        E3[x][y] = __ldg(Ea + 2 * d.ne + e + x * ej + y);
       }
   }
   // conserved update (base = the state at the start of the cycle)
@@ -1103,14 +1139,14 @@ __device__ __forceinline__ float update_c2p_cell(const Geom& g, const StagePtrs<
   return 3.402823466e38f;
 }
 
-template <bool MHD, bool DT, bool SG>
+template <bool MHD, bool DT, bool SG, int SNC>
 __global__ void __launch_bounds__(128, 8)
 k_update_c2p(Geom g, StagePtrs<float> p, Box bx, StageW sw, Phys ph, StateBufs sb,
              unsigned long long* dtmin, const float2* __restrict__ phi2) {
   int i, j, k, b;
   const bool active = box_coords(bx, i, j, k, b);
   float mindt = 3.402823466e38f;
-  if (active) mindt = update_c2p_cell<MHD, DT, SG>(g, p, i, j, k, b, sw, ph, sb, phi2);
+  if (active) mindt = update_c2p_cell<MHD, DT, SG, SNC>(g, p, i, j, k, b, sw, ph, sb, phi2);
   if constexpr (DT) {  // block minimum, then one 64-bit atomicMin (as k_block_dt)
     for (int o = 16; o > 0; o >>= 1) mindt = mn(mindt, __shfl_xor_sync(0xffffffffu, mindt, o));
     __shared__ float red[32];
