@@ -869,16 +869,16 @@ def main():
     k_achieved = BYTES_PER_CELL_STAGE * zones / t_upd / 1e9
     k_traffic = None
     kpath = os.path.join(ROOT, "profiles", "single_pass_stage_ncu_192.md"
-                         if kname == "k_single_pass" else "update_c2p_fused_ncu_192.md")
+                         if kname == "k_single_pass" else "traffic_ot192_mhd_cycle.md")
     if os.path.exists(kpath):
         with open(kpath) as f:
             for ln in f:
                 if ln.startswith("dram_bytes_per_cell:"):
                     k_traffic = float(ln.split(":")[1]) * zones
-    # DRAM bytes of one cycle from the ncu summary (bytes per zone-cycle measured at 128^3,
+    # DRAM bytes of one cycle from the ncu summary (bytes per zone-cycle measured at 192^3,
     # scaled by the cells of this run)
     traffic = None
-    tpath = os.path.join(ROOT, "profiles", "traffic_ot_mhd_cycle_128.md")
+    tpath = os.path.join(ROOT, "profiles", "traffic_ot192_mhd_cycle.md")
     if os.path.exists(tpath):
         with open(tpath) as f:
             for ln in f:
@@ -930,7 +930,7 @@ def main():
                            "frac": achieved / peak, "traffic": traffic,
                            "note": "one launch = one captured VL2 cycle (graph); algorithmic "
                                    "bytes 384 B/zone-cycle; traffic = ncu DRAM bytes per cycle "
-                                   "(128^3 capture scaled to the cells)"},
+                                   "(192^3 capture scaled to the cells)"},
         "cycle_breakdown_ms": {k: float(np.median(v)) for k, v in groups.items()},
         "cpu_baseline": cpu,
         "e2e": e2e,
