@@ -332,7 +332,9 @@ int athg_history(athg_ctx* ctx, double* out, int* count);
  * one refinement level tiling mg's nx^3 root grid (the same mesh). The potential of
  * each block, with one ghost layer, downloads as ATHG_VAR_PHI. mg must outlive the
  * coupling; pass mg = NULL to detach. Solves with a threshold or a multipole boundary
- * synchronise with the host, so athg_cycles then runs the stages without a graph. */
+ * synchronise with the host, so athg_cycles then runs the stages without a graph. In
+ * mixed precision with VL2 the source term runs inside the fused update (the potential
+ * read as FP32 pairs), like the rest of the fused stage. */
 int athg_attach_gravity(athg_ctx* ctx, athg_mg* mg, double four_pi_G);
 
 /* ---- CFL time step of one caller-owned block, with no device allocation ------------
