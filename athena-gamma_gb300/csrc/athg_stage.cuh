@@ -1139,8 +1139,11 @@ __device__ __forceinline__ float update_c2p_cell(const Geom& g, const StagePtrs<
   return 3.402823466e38f;
 }
 
+// Seven blocks of 128 per SM: up to 73 registers a thread. On a GB300 at 256^3 that ran
+// 1.027 / 1.069 ms per launch (without / with the time step) against 1.097 / 1.152 ms with
+// eight blocks and 64 registers, where the kernel spilled.
 template <bool MHD, bool DT, bool SG, int SNC>
-__global__ void __launch_bounds__(128, 8)
+__global__ void __launch_bounds__(128, 7)
 k_update_c2p(Geom g, StagePtrs<float> p, Box bx, StageW sw, Phys ph, StateBufs sb,
              unsigned long long* dtmin, const float2* __restrict__ phi2) {
   int i, j, k, b;
