@@ -129,3 +129,31 @@ def test_fused_mixed_sg_tracks_fp64(mhd, threshold):
     for k, e in err["fused"].items():
         assert e < 5e-6, (k, err)
         assert e <= 2.0 * err["unfused"][k] + 1e-9, (k, err)
+
+
+def test_fixed_size_sg_matches_general():
+    """Self-gravity on 64^3 blocks with two ghost layers takes the fixed-size instantiations
+    of the sweeps and of the fused update with the source term; 32^3 blocks take the general
+    ones. One 128^3 mesh run both ways for three cycles agrees to round-off (the multigrid's
+    sums, parallel reductions, differ in their last bits between runs)."""
+    import oracle_lib as ol
+    n = 128
+    u, b1, b2, b3 = ol.smooth_random_state((n, n, n), True, seed=37, amp=0.3)
+    out = {}
+    for mb in ((64, 64, 64), (32, 32, 32)):
+        sim = athg.Sim((n, n, n), mb, mhd=True, solver="hlld", precision="mixed", cfl=0.4,
+                       tlim=100.0)
+        mg = athg.Multigrid(n, domain=((0.0, 1.0),) * 3, bc="periodic", mode="FMG",
+                            threshold=-1.0, niteration=2, precision="fp64")
+        sim.attach_gravity(mg, 4.0)
+        sim.load_interior(u, b1, b2, b3)
+        sim.initialize()
+        sim.cycles(3)
+        out[mb] = sim.interior()
+        sim.attach_gravity(None, 0.0)
+        sim.close()
+        mg.close()
+    a, c = out[(64, 64, 64)], out[(32, 32, 32)]
+    for k in a:
+        err = np.abs(a[k] - c[k]).max() / np.abs(c[k]).max()
+        assert err < 1e-10, (k, err)
