@@ -332,7 +332,23 @@ __device__ __forceinline__ dfl ps(const float2* p, int64_t q) {  // pair load
   return dfl(v.x, v.y);
 }
 
-template <bool MHD>
+// The register step of MeshBlock::WeightedAve (r = delta u, or r += delta u), written to
+// the register and returned. COPY (a first stage with delta 1): 0 + 1 * u, a copy but for
+// -0 becoming +0, done on the integer pipe with that same result; otherwise FP64.
+template <bool COPY>
+__device__ __forceinline__ double reg_update(const StageW& sw, double uo, double* reg) {
+  if constexpr (COPY) {
+    const double r = (bits_d(uo) << 1) == 0 ? 0.0 : uo;
+    *reg = r;
+    return r;
+  } else {
+    double r = sw.zero_reg ? 0.0 : *reg;
+    if (sw.delta != 0.0) { r += sw.delta * uo; *reg = r; }
+    return r;
+  }
+}
+
+template <bool MHD, bool COPY>
 __global__ void __launch_bounds__(kThreads) k_update_df(Geom g, StagePtrs<double> p, Box bx,
                                                          StageW sw) {
   int i, j, k, b;
@@ -356,8 +372,7 @@ __global__ void __launch_bounds__(kThreads) k_update_df(Geom g, StagePtrs<double
 #pragma unroll
     for (int n = 0; n < NHYD; ++n) {
       const double uo = u[n * nc + c];
-      double r = sw.zero_reg ? 0.0 : u1[n * nc + c];
-      if (sw.delta != 0.0) { r += sw.delta * uo; u1[n * nc + c] = r; }
+      const double r = reg_update<COPY>(sw, uo, u1 + n * nc + c);
       const double base = sw.swap ? r : sw.g1 * uo + sw.g2 * r;
       const dfl inc = (c1 * (ps(F1, n * g.nf1 + 1) - ps(F1, n * g.nf1)) +
                        c2 * (ps(F2, n * g.nf2 + s2) - ps(F2, n * g.nf2))) +
@@ -374,8 +389,7 @@ __global__ void __launch_bounds__(kThreads) k_update_df(Geom g, StagePtrs<double
     const int64_t ej = (int64_t)g.nc1 + 1, ek = ((int64_t)g.nc1 + 1) * (g.nc2 + 1);
     auto face = [&](double* bb, double* rr, int64_t q, dfl inc) {
       const double bo = bb[q];
-      double r = sw.zero_reg ? 0.0 : rr[q];
-      if (sw.delta != 0.0) { r += sw.delta * bo; rr[q] = r; }
+      const double r = reg_update<COPY>(sw, bo, rr + q);
       const double v = sw.swap ? r : sw.g1 * bo + sw.g2 * r;
       bb[q] = (v + f2d_int(inc.hi)) + f2d_int(inc.lo);
     };
@@ -578,8 +592,14 @@ void df_update(const Geom& g, const StagePtrs<double>& p, bool mhd, const StageW
                cudaStream_t st) {
   const Box b = mhd ? box_of(g.is, g.ie + 1, g.js, g.je + 1, g.ks, g.ke + 1)
                     : box_of(g.is, g.ie, g.js, g.je, g.ks, g.ke);
-  if (mhd) k_update_df<true><<<grid_of(b, g.nb), kThreads, 0, st>>>(g, p, b, sw);
-  else k_update_df<false><<<grid_of(b, g.nb), kThreads, 0, st>>>(g, p, b, sw);
+  const bool copy = sw.zero_reg && sw.delta == 1.0;  // a first stage's register copy
+  if (mhd) {
+    if (copy) k_update_df<true, true><<<grid_of(b, g.nb), kThreads, 0, st>>>(g, p, b, sw);
+    else k_update_df<true, false><<<grid_of(b, g.nb), kThreads, 0, st>>>(g, p, b, sw);
+  } else {
+    if (copy) k_update_df<false, true><<<grid_of(b, g.nb), kThreads, 0, st>>>(g, p, b, sw);
+    else k_update_df<false, false><<<grid_of(b, g.nb), kThreads, 0, st>>>(g, p, b, sw);
+  }
 }
 
 void df_c2p(const Geom& g, const StagePtrs<double>& p, bool mhd, const Phys& ph, float2* wp,
