@@ -363,20 +363,34 @@ __global__ void __launch_bounds__(kThreads) k_update_df(Geom g, StagePtrs<double
     double* __restrict__ u = p.u + (int64_t)b * NHYD * nc;
     double* __restrict__ u1 = p.u1 + (int64_t)b * NHYD * nc;
     const int64_t c = cidx(g, k, j, i);
-    const float2* F1 = reinterpret_cast<const float2*>(p.flx[0] + (int64_t)b * NF * g.nf1) +
-                       f1idx(g, k, j, i);
-    const float2* F2 = reinterpret_cast<const float2*>(p.flx[1] + (int64_t)b * NF * g.nf2) +
-                       f2idx(g, k, j, i);
-    const float2* F3 = reinterpret_cast<const float2*>(p.flx[2] + (int64_t)b * NF * g.nf3) + c;
+    const float2* __restrict__ F1 =
+        reinterpret_cast<const float2*>(p.flx[0] + (int64_t)b * NF * g.nf1) + f1idx(g, k, j, i);
+    const float2* __restrict__ F2 =
+        reinterpret_cast<const float2*>(p.flx[1] + (int64_t)b * NF * g.nf2) + f2idx(g, k, j, i);
+    const float2* __restrict__ F3 =
+        reinterpret_cast<const float2*>(p.flx[2] + (int64_t)b * NF * g.nf3) + c;
     const int64_t s2 = g.nc1, s3 = (int64_t)g.nc1 * g.nc2;
+    // every flux pair and state value loaded before the first store, so a thread keeps
+    // all of its loads in flight at once
+    float2 f[NHYD][6];
+    double uo[NHYD];
 #pragma unroll
     for (int n = 0; n < NHYD; ++n) {
-      const double uo = u[n * nc + c];
-      const double r = reg_update<COPY>(sw, uo, u1 + n * nc + c);
-      const double base = sw.swap ? r : sw.g1 * uo + sw.g2 * r;
-      const dfl inc = (c1 * (ps(F1, n * g.nf1 + 1) - ps(F1, n * g.nf1)) +
-                       c2 * (ps(F2, n * g.nf2 + s2) - ps(F2, n * g.nf2))) +
-                      c3 * (ps(F3, n * g.nf3 + s3) - ps(F3, n * g.nf3));
+      f[n][0] = __ldg(F1 + n * g.nf1 + 1);
+      f[n][1] = __ldg(F1 + n * g.nf1);
+      f[n][2] = __ldg(F2 + n * g.nf2 + s2);
+      f[n][3] = __ldg(F2 + n * g.nf2);
+      f[n][4] = __ldg(F3 + n * g.nf3 + s3);
+      f[n][5] = __ldg(F3 + n * g.nf3);
+      uo[n] = u[n * nc + c];
+    }
+    auto pr = [](float2 v) { return dfl(v.x, v.y); };
+#pragma unroll
+    for (int n = 0; n < NHYD; ++n) {
+      const double r = reg_update<COPY>(sw, uo[n], u1 + n * nc + c);
+      const double base = sw.swap ? r : sw.g1 * uo[n] + sw.g2 * r;
+      const dfl inc = (c1 * (pr(f[n][0]) - pr(f[n][1])) + c2 * (pr(f[n][2]) - pr(f[n][3]))) +
+                      c3 * (pr(f[n][4]) - pr(f[n][5]));
       u[n * nc + c] = (base - f2d_int(inc.hi)) - f2d_int(inc.lo);
     }
   }
