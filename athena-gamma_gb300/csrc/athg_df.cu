@@ -432,6 +432,9 @@ __global__ void __launch_bounds__(256) k_c2p_df(Geom g, StagePtrs<double> p, Box
   double* __restrict__ u = p.u + (int64_t)b * NHYD * nc;
   double* __restrict__ w = p.w + (int64_t)b * NHYD * nc;
   float2* __restrict__ wq = wpairs + (int64_t)b * NV * nc;
+  // the conserved state first: its loads are issued before any store of this thread
+  const double u0 = u[c], u1v = u[nc + c], u2v = u[2 * nc + c], u3v = u[3 * nc + c],
+               u4v = u[4 * nc + c];
   dfl pb(0.0f, 0.0f);
   if constexpr (MHD) {
     const double* b1 = p.b1 + (int64_t)b * g.nf1;
@@ -450,16 +453,15 @@ __global__ void __launch_bounds__(256) k_c2p_df(Geom g, StagePtrs<double> p, Box
     }
     pb = half * (bc[0] * bc[0] + bc[1] * bc[1] + bc[2] * bc[2]);
   }
-  double ud = u[c];
+  double ud = u0;
   const uint64_t ub = bits_d(ud);
   if (!((ub >> 63) == 0 && ub > bits_d(ph.dfloor) && ub <= 0x7ff0000000000000ull)) ud = ph.dfloor;
   u[c] = ud;
-  const dfl dd = df_of(ud), m1 = df_of(u[nc + c]), m2 = df_of(u[2 * nc + c]),
-            m3 = df_of(u[3 * nc + c]);
+  const dfl dd = df_of(ud), m1 = df_of(u1v), m2 = df_of(u2v), m3 = df_of(u3v);
   const dfl di = dfl(1.0f, 0.0f) / dd;
   const dfl ek = dfl(0.5f, 0.0f) * di * (m1 * m1 + m2 * m2 + m3 * m3);
   const dfl gm1(ph.gm1f.hi, ph.gm1f.lo), pfl(ph.pfloorf.hi, ph.pfloorf.lo);
-  dfl wp = gm1 * ((df_of(u[4 * nc + c]) - ek) - pb);
+  dfl wp = gm1 * ((df_of(u4v) - ek) - pb);
   const bool floored = !(wp > pfl);
   if (floored) {
     u[4 * nc + c] = dbl((df_of(ph.pfloor / ph.gm1) + ek) + pb);
