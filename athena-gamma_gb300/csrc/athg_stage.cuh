@@ -828,6 +828,9 @@ __global__ void __launch_bounds__(256) k_c2p(Geom g, StagePtrs<T> p, Box bx, Phy
     const int64_t c = cidx(g, k, j, i);
     double* __restrict__ u = p.u + (int64_t)b * NHYD * nc;
     float* __restrict__ w = p.w + (int64_t)b * NHYD * nc;
+    // the conserved state first: its loads are issued before any store of this thread
+    double ud = u[c];
+    const double m1 = u[nc + c], m2 = u[2 * nc + c], m3 = u[3 * nc + c], ue = u[4 * nc + c];
     ff ss = {0.0f, 0.0f};  // (2 Bcc)^2
     if constexpr (MHD) {
       const double* __restrict__ b1 = p.b1 + (int64_t)b * g.nf1;
@@ -850,8 +853,6 @@ __global__ void __launch_bounds__(256) k_c2p(Geom g, StagePtrs<T> p, Box bx, Phy
       p.bfw[2][(int64_t)b * g.nf3 + q3] = f3.hi;
       ss = ff_add(ff_add(ff_sqr(s1), ff_sqr(s2)), ff_sqr(s3));
     }
-    double ud = u[c];
-    const double m1 = u[nc + c], m2 = u[2 * nc + c], m3 = u[3 * nc + c], ue = u[4 * nc + c];
     // ud > dfloor on the bit patterns (dfloor > 0; negative, zero and NaN densities floor)
     const uint64_t ub = bits_d(ud);
     if (!((ub >> 63) == 0 && ub > bits_d(ph.dfloor) && ub <= 0x7ff0000000000000ull)) {
