@@ -565,12 +565,15 @@ __device__ void block_add(double (&v)[NV], double* out) {
   }
 }
 
+// the mean from the level sum, once (red[1] = red[0] * scale), so the passes that subtract
+// it take one FP64 instruction per cell instead of two
+__global__ void k_mean(double* red, double scale) { red[1] = red[0] * scale; }
+
 template <typename T>
-__global__ void k_sub_const(T* a, long long cnt, const double* tot, double scale) {
+__global__ void k_sub_const(T* a, long long cnt, const double* ave) {
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= cnt) return;
-  const double ave = (*tot) * scale;
-  a[t] -= (T)ave;
+  a[t] -= (T)(*ave);
 }
 
 // Column sums: one thread per (i, j) column and run of kColK cells along k, then one block
@@ -590,10 +593,19 @@ __global__ void k_sum(const T* a, int n, double* out) {
     const long long sk = (long long)(n + 2) * (n + 2);
     const T* p = a + ix(n + 2, k0, j, i);
     double acc = 0.0;
-    // FP32 values widen on the integer pipe (f2d_int): only the addition is an FP64 instruction
-    for (int k = k0; k <= k1; ++k, p += sk) {
-      if constexpr (sizeof(T) == 4) acc += athg::f2d_int(*p);
-      else acc += (double)*p;
+    if constexpr (sizeof(T) == 4) {
+      // FP32 values: the column as an unevaluated pair hi + lo of TwoSums (no FP64
+      // instruction per cell), widened on the integer pipe and added once
+      float hi = 0.0f, lo = 0.0f;
+      for (int k = k0; k <= k1; ++k, p += sk) {
+        float sum, err;
+        athg::two_sum(hi, *p, sum, err);
+        hi = sum;
+        lo += err;
+      }
+      acc = athg::f2d_int(hi) + athg::f2d_int(lo);
+    } else {
+      for (int k = k0; k <= k1; ++k, p += sk) acc += (double)*p;
     }
     v[0] = acc;
   }
@@ -676,19 +688,17 @@ __global__ void k_narrow(const double* a, float* b, long long cnt) {
   if (t < cnt) b[t] = athg::d2f_int(a[t]);
 }
 // the mean subtraction of the FP64 source (k_sub_const) and its narrowing in one pass
-__global__ void k_sub_narrow(double* a, float* b, long long cnt, const double* tot,
-                             double scale) {
+__global__ void k_sub_narrow(double* a, float* b, long long cnt, const double* ave) {
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= cnt) return;
-  const double v = a[t] - (*tot) * scale;
+  const double v = a[t] - *ave;
   a[t] = v;
   b[t] = athg::d2f_int(v);
 }
 // the widening of the FP32 FMG solution and its mean subtraction (k_sub_const) in one pass
-__global__ void k_widen_sub(const float* a, double* b, long long cnt, const double* tot,
-                            double scale) {
+__global__ void k_widen_sub(const float* a, double* b, long long cnt, const double* ave) {
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t < cnt) b[t] = athg::f2d_int(a[t]) - (*tot) * scale;
+  if (t < cnt) b[t] = athg::f2d_int(a[t]) - *ave;
 }
 
 // multipole moments (and the centre of mass) of the finest source, FP64, as column sums (x
@@ -1012,25 +1022,25 @@ int vcycle(athg_mg* m, Hier<T>& h, int top, bool fas, bool homog, bool subtract,
   return ATHG_OK;
 }
 
-// the sum of level L's interior into m->red; *scale turns it into the mean: total = sum *
-// dx^3 (Multigrid::CalculateTotal), average = total / volume
+// the mean of level L's interior into m->red[1] (the sum in m->red[0]): total = sum * dx^3
+// (Multigrid::CalculateTotal), average = total / volume
 template <typename T>
-int level_sum(athg_mg* m, Hier<T>& h, const T* a, int L, double* scale) {
+int level_mean(athg_mg* m, Hier<T>& h, const T* a, int L) {
   const int n = h.n[L];
   MCK(cudaMemsetAsync(m->red, 0, sizeof(double), m->st));
   k_sum<T><<<nblk((long long)n * n * col_chunks(n)), TPB, 0, m->st>>>(a, n, m->red);
   MCKL();
   const double dxl = h.dx[L];
-  *scale = dxl * dxl * dxl / m->vol;
+  k_mean<<<1, 1, 0, m->st>>>(m->red, dxl * dxl * dxl / m->vol);
+  MCKL();
   return ATHG_OK;
 }
 
 template <typename T>
 int subtract_mean(athg_mg* m, Hier<T>& h, T* a, int L) {
-  double scale;
-  RC(level_sum(m, h, a, L, &scale));
-  k_sub_const<T><<<nblk((long long)h.cells(L)), TPB, 0, m->st>>>(a, (long long)h.cells(L), m->red,
-                                                                scale);
+  RC(level_mean(m, h, a, L));
+  k_sub_const<T><<<nblk((long long)h.cells(L)), TPB, 0, m->st>>>(a, (long long)h.cells(L),
+                                                                m->red + 1);
   MCKL();
   return ATHG_OK;
 }
@@ -1346,9 +1356,8 @@ int mg_solve(athg_mg* m, bool want_norm, int* iterations, double* defect_norm) {
   // mixed FMG: the mean subtractions of the source and of the FMG solution ride on the
   // narrowing and widening passes (k_sub_narrow, k_widen_sub)
   const bool mixed_fmg = m->cfg.mode == ATHG_MG_FMG && m->cfg.precision == ATHG_MIXED;
-  double scale = 0.0;
   if (m->subtract) {
-    if (mixed_fmg) RC(level_sum(m, H, H.src[top], top, &scale));
+    if (mixed_fmg) RC(level_mean(m, H, H.src[top], top));
     else RC(subtract_mean(m, H, H.src[top], top));
   }
   if (m->any_mp) RC(multipole_setup(m));
@@ -1357,15 +1366,15 @@ int mg_solve(athg_mg* m, bool want_norm, int* iterations, double* defect_norm) {
       Hier<float>& h = m->h32;
       const long long c = (long long)h.cells(top);
       if (m->subtract) {
-        k_sub_narrow<<<nblk(c), TPB, 0, m->st>>>(H.src[top], h.src[top], c, m->red, scale);
+        k_sub_narrow<<<nblk(c), TPB, 0, m->st>>>(H.src[top], h.src[top], c, m->red + 1);
       } else {
         k_narrow<<<nblk(c), TPB, 0, m->st>>>(H.src[top], h.src[top], c);
       }
       MCKL();
       RC(fmg(m, h, m->fas, m->subtract, m->coffset32));
       if (m->subtract) {
-        RC(level_sum(m, h, h.u[top], top, &scale));
-        k_widen_sub<<<nblk(c), TPB, 0, m->st>>>(h.u[top], H.u[top], c, m->red, scale);
+        RC(level_mean(m, h, h.u[top], top));
+        k_widen_sub<<<nblk(c), TPB, 0, m->st>>>(h.u[top], H.u[top], c, m->red + 1);
       } else {
         k_widen<<<nblk(c), TPB, 0, m->st>>>(h.u[top], H.u[top], c);
       }
